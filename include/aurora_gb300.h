@@ -1,0 +1,270 @@
+/*
+ * aurora_gb300 — C ABI of the GB300-native (sm_103a) rendering hot path.
+ *
+ * The entry points replace the free functions the Aurora renderer binds in
+ * src/kernels/kernels.h:27-64 (Nadrin/aurora). Each declaration below names the
+ * reference function it stands in for. Everything crossing this boundary is a
+ * plain C type: POD structs, raw pointers and sizes. No C++ or torch types.
+ *
+ * Conventions
+ *  - Every function returns aur_status. AUR_OK is 0. On failure a message for
+ *    the calling thread is available from aur_last_error().
+ *  - An aur_ctx owns one CUDA device and one stream. Calls on one context must
+ *    not race each other; distinct contexts are independent.
+ *  - Pointers documented as "device" must be device-accessible memory of the
+ *    context's device; "host" pointers are ordinary (preferably pinned) host
+ *    memory. Library-owned objects (aur_nmh, aur_scene) are freed by their
+ *    destroy function and never free caller memory (unlike cudaRebuildNMH,
+ *    which frees and replaces the caller's Geometry, rebuilder.cu:444-445).
+ *  - Triangle soups use the reference layout (data/geometry.h:13-55,
+ *    kernels/lib/primitive.cuh:288-293): vertices are 9 floats per triangle
+ *    ordered [x1 x2 x3 y1 y2 y3 z1 z2 z3]; normals are 9 floats per triangle
+ *    ordered [n1.xyz n2.xyz n3.xyz]; shader ids are 1-based uint16 (0 selects
+ *    shader 0, util/array.h:12-18).
+ */
+#ifndef AURORA_GB300_H
+#define AURORA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+
+typedef enum aur_status {
+    AUR_OK = 0,
+    AUR_ERR_INVALID = 1,     /* bad argument, size or pointer */
+    AUR_ERR_OOM = 2,         /* device allocation failed (reference: MS::kInsufficientMemory) */
+    AUR_ERR_CUDA = 3,        /* CUDA runtime error; the message holds cudaGetErrorString */
+    AUR_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+    AUR_ERR_OVERFLOW = 5,    /* a fixed-capacity device stack or queue would overflow */
+    AUR_ERR_UNSUPPORTED = 6, /* feature outside this library's scope (textures) */
+    AUR_ERR_NO_DEVICE = 7    /* no CUDA device, or the device is not sm_103 */
+} aur_status;
+
+/* Message describing the last failure on the calling thread ("" if none). */
+const char* aur_last_error(void);
+/* Library version string. */
+const char* aur_version(void);
+
+/* ------------------------------------------------------------ shared types */
+
+typedef struct aur_float3 { float x, y, z; } aur_float3;
+
+/* Ray for the traversal entry points: origin + tmax, direction + padding.
+ * Reference: util/ray.h:13-49 (pos, dir, t). 32 bytes, 16-byte aligned. */
+typedef struct aur_ray {
+    float ox, oy, oz, tmax;
+    float dx, dy, dz, pad;
+} aur_ray;
+
+/* Closest-hit result (util/hitpoint.h: u, v, triangleID; ray.t).
+ * prim is the ORIGINAL triangle index (before NMH reordering), AUR_NO_HIT on a
+ * miss, in which case t = tmax and u = v = 0. */
+typedef struct aur_hit { float t, u, v; uint32_t prim; } aur_hit;
+#define AUR_NO_HIT 0xFFFFFFFFu
+
+/* util/shader.h:10-33. type: 0 Lambert, 1 Phong (shaded as Lambert,
+ * kernels/lib/bsdf.cuh:202-210). texture must be 0 (textures are out of scope). */
+typedef struct aur_shader {
+    int32_t type;
+    aur_float3 diffuse_color;
+    aur_float3 emission_color;
+    aur_float3 specular_color;
+    aur_float3 reflection_color;
+    float diffuse;
+    float emission;
+    float exponent;
+    float reflectivity;
+    float translucence;
+    float refractive_index;
+    uint32_t texture;
+} aur_shader;
+
+enum { AUR_SHADER_LAMBERT = 0, AUR_SHADER_PHONG = 1 };
+
+/* util/light.h:12-42. For an area light, position is the quad corner v1 and
+ * e1, e2 its edges (core/scene.cpp:435-448); direction is the emitting normal.
+ * samples >= 1 shadow samples per shading point (numShadowSamples). */
+typedef struct aur_light {
+    int32_t type;
+    float intensity;
+    float ambient;
+    float area;
+    int32_t samples;
+    aur_float3 position;
+    aur_float3 color;
+    aur_float3 direction;
+    aur_float3 e1, e2;
+} aur_light;
+
+enum { AUR_LIGHT_AMBIENT = 0, AUR_LIGHT_POINT = 1, AUR_LIGHT_DIRECTIONAL = 2, AUR_LIGHT_AREA = 3 };
+
+/* util/camera.h:12-36 (pinhole; tanfov = tanf(port field of view)). */
+typedef struct aur_camera {
+    aur_float3 position;
+    aur_float3 forward;
+    aur_float3 right;
+    aur_float3 up;
+    float tanfov_x, tanfov_y;
+    float aspect;
+} aur_camera;
+
+/* Integrator selection.
+ *  AUR_MODE_REFERENCE: exactly the reference integrator
+ *    (kernels/monteCarloRaytracer.cu:23-113): emission + direct lighting at
+ *    each hit, specular reflection/refraction rays, no diffuse bounce.
+ *  AUR_MODE_PATH: the same, plus a cosine-sampled diffuse bounce
+ *    (BSDF::samplef, kernels/lib/bsdf.cuh:222-236) at every non-specular hit
+ *    while depth <= max_depth, with RGB path throughput. */
+enum { AUR_MODE_REFERENCE = 0, AUR_MODE_PATH = 1 };
+
+/* Per-render parameters (Dim(width,height,samples), MAX_DEPTH, RNG seed). */
+typedef struct aur_render_params {
+    uint32_t width, height;
+    uint32_t spp;            /* samples per pixel; sub-pixel grid of (short)sqrtf(spp) */
+    uint32_t max_depth;      /* MAX_DEPTH (monteCarloRaytracer.cu:20); <= AUR_MAX_DEPTH */
+    uint32_t seed;           /* counter-based RNG key (replaces curand_init seed) */
+    uint32_t mode;           /* AUR_MODE_* */
+    uint32_t sample_begin;   /* render samples [sample_begin, sample_end) of spp; */
+    uint32_t sample_end;     /*   sample_end == 0 means spp */
+    uint32_t scene_id;       /* second RNG key word: independent streams per scene */
+} aur_render_params;
+
+#define AUR_MAX_DEPTH 16u
+
+/* The reference Ray / HitPoint structs for the renderer-helper entry points
+ * (util/ray.h:13-49, util/hitpoint.h:10-23). Layout is part of the ABI. */
+typedef struct aur_path_ray {
+    aur_float3 pos;
+    aur_float3 dir;
+    float t;
+    float weight;
+    float eta;
+} aur_path_ray;
+
+typedef struct aur_hitpoint {
+    aur_float3 color;
+    aur_float3 position;
+    aur_float3 wo;
+    float u, v;
+    int32_t triangle_id;      /* NMH position of the last hit, -1 if none */
+} aur_hitpoint;
+
+/* ----------------------------------------------------------------- context */
+
+typedef struct aur_ctx aur_ctx;
+
+/* Creates a context on CUDA device `device` with its own non-blocking stream.
+ * Replaces Engine::initialize's cudaSetDevice (core/engine.cpp:33-47). */
+aur_status aur_ctx_create(int device, aur_ctx** out);
+aur_status aur_ctx_destroy(aur_ctx* ctx);
+/* Uses `cuda_stream` (a cudaStream_t) for all later work; NULL restores the
+ * context's own stream. */
+aur_status aur_ctx_set_stream(aur_ctx* ctx, void* cuda_stream);
+/* Returns the cudaStream_t the context launches on. */
+aur_status aur_ctx_get_stream(aur_ctx* ctx, void** cuda_stream);
+aur_status aur_ctx_synchronize(aur_ctx* ctx);
+/* Number of SMs of the context's device. */
+aur_status aur_ctx_sm_count(aur_ctx* ctx, int* sm_count);
+
+/* --------------------------------------------------------------------- NMH */
+
+typedef struct aur_nmh aur_nmh;
+
+/* Builds the NMH (implicit pair-heap) over `count` triangles.
+ * Replaces cudaRebuildNMH(Geometry&) (kernels/rebuilder.cu:311-450).
+ * vertices: device, count*9 floats, reference layout. An odd count is padded
+ * by duplicating the last triangle (Geometry::padToEven, data/geometry.cpp:164-176);
+ * the duplicate gets prim id `count`. Ties in every ordering are broken by the
+ * lower original prim id, which makes the result deterministic where the
+ * reference's atomicCAS swap (rebuilder.cu:93-125) is not. */
+aur_status aur_nmh_build(aur_ctx* ctx, const float* vertices, uint32_t count, aur_nmh** out);
+aur_status aur_nmh_destroy(aur_nmh* nmh);
+/* Triangle count after padding and number of heap levels (log2i(count/2)+1). */
+aur_status aur_nmh_info(const aur_nmh* nmh, uint32_t* count, uint32_t* levels);
+/* Copies the topology to host memory: perm[i] = original prim id at NMH
+ * position i (count entries); vertices (nullable) = count*9 floats of the
+ * permuted soup in the reference layout (applyIndices, rebuilder.cu:217-245). */
+aur_status aur_nmh_export(aur_ctx* ctx, const aur_nmh* nmh, uint32_t* perm, float* vertices);
+/* Device pointer to the perm array (count uint32) owned by the NMH. */
+aur_status aur_nmh_perm_device(const aur_nmh* nmh, const uint32_t** perm);
+
+/* --------------------------------------------------------------- traversal */
+
+/* Closest hit for n rays (intersect(), kernels/lib/intersect.cuh:95-152).
+ * rays, hits: device. Ties in t go to the lower original prim id. */
+aur_status aur_trace_closest(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits);
+/* Any hit (shadow ray, intersectAny(), intersect.cuh:36-86): occluder[i] is
+ * the original prim id of the first hit found in traversal order with
+ * Epsilon < t < tmax, or AUR_NO_HIT. rays, occluder: device. */
+aur_status aur_trace_any(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, uint32_t* occluder);
+/* Same as above with HOST buffers: copies are chunked and overlapped with the
+ * traversal on the context's stream plus two internal copy streams. */
+aur_status aur_trace_closest_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits);
+aur_status aur_trace_any_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, uint32_t* occluder);
+/* Counts traversal work for n device rays: node_visits[0] = nodes fetched by
+ * closest hit, node_visits[1] = by any hit (a node is fetched when popped with
+ * index < count, intersect.cuh:103-111). Used for roofline accounting. */
+aur_status aur_trace_count_visits(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n,
+                                  unsigned long long node_visits[2]);
+
+/* ------------------------------------------------------------------- scene */
+
+typedef struct aur_scene aur_scene;
+
+/* Uploads a triangle soup with its materials and lights and builds its NMH
+ * (Scene::update / updateMeshes, core/scene.cpp:144-299). Host pointers.
+ * normals: nullable (face normals are used); shader_ids: nullable (all 0). */
+aur_status aur_scene_create(aur_ctx* ctx, const float* vertices, const float* normals,
+                            const uint16_t* shader_ids, uint32_t count,
+                            const aur_shader* shaders, uint32_t num_shaders,
+                            const aur_light* lights, uint32_t num_lights, aur_scene** out);
+aur_status aur_scene_destroy(aur_scene* scene);
+aur_status aur_scene_nmh(const aur_scene* scene, const aur_nmh** nmh);
+/* Replaces the shader / light tables (same counts as at creation). Host pointers. */
+aur_status aur_scene_set_shaders(aur_ctx* ctx, aur_scene* scene, const aur_shader* shaders, uint32_t num_shaders);
+aur_status aur_scene_set_lights(aur_ctx* ctx, aur_scene* scene, const aur_light* lights, uint32_t num_lights);
+
+/* --------------------------------------------------------------- rendering */
+
+/* Camera::Camera (util/camera.h:15-28): forward = normalize(direction),
+ * right = cross(forward, (0,1,0)), up = cross(right, forward),
+ * tanfov = tanf(fov). Host-only helper. */
+aur_status aur_camera_make(aur_float3 position, aur_float3 direction, float fov_x, float fov_y,
+                           float aspect, aur_camera* out);
+
+/* Renders params->width x params->height pixels, samples
+ * [sample_begin, sample_end) of params->spp, and ADDS them into accum
+ * (device float4 per pixel, RGBA, alpha = coverage) with weight 1/spp.
+ * Fused form of the reference per-sample loop (monteCarloRaytracer.cpp:81-120):
+ * generateRays + cudaRaytraceMonteCarlo + drawPixels. */
+aur_status aur_render(aur_ctx* ctx, const aur_scene* scene, const aur_camera* camera,
+                      const aur_render_params* params, float* accum);
+
+/* Renderer helpers, one per reference kernel wrapper. */
+/* cudaGenerateRays (kernels/utility.cu:79-94). rays, hits: device, width*height. */
+aur_status aur_generate_rays(aur_ctx* ctx, uint32_t width, uint32_t height, uint32_t sample_id,
+                             uint32_t samples, const aur_camera* camera,
+                             aur_path_ray* rays, aur_hitpoint* hits);
+/* cudaRaytraceMonteCarlo (monteCarloRaytracer.cu:115-124) on rays
+ * [offset, offset+num_rays). The RNG is keyed by (params->seed,
+ * params->scene_id, ray index as pixel, sample_id). */
+aur_status aur_raytrace_monte_carlo(aur_ctx* ctx, const aur_scene* scene, const aur_render_params* params,
+                                    uint32_t sample_id, uint32_t offset, uint32_t num_rays,
+                                    aur_path_ray* rays, aur_hitpoint* hits);
+/* cudaDrawPixels (kernels/utility.cu:199-229): accum[p] += (color*weight, weight)
+ * where hits[p].triangle_id != -1. */
+aur_status aur_draw_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float weight,
+                           const aur_hitpoint* hits, float* accum);
+/* Renderer::clearPixels (core/renderer.cpp:33-36). */
+aur_status aur_clear_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float* accum);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AURORA_GB300_H */

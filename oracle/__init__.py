@@ -1,0 +1,202 @@
+"""ctypes front end of the oracle (test infrastructure only).
+
+The oracle is the CPU restatement of the reference algorithms in
+aur_oracle.cpp. Only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline use it, and only as the checker or the timed CPU baseline; the
+product library never loads it. ref_* functions call the reference's own
+traversal code compiled through ref_shim/ (oracle/_ref), available only where
+the reference source tree was present at build time.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from aurora_gb300 import types as T
+
+from .build import ORACLE_SO, REF_SO, build_oracle, build_ref
+
+_lib = None
+_ref = None
+P = ctypes.c_void_p
+U32 = ctypes.c_uint32
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else ctypes.c_void_p(0)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build_oracle()
+        L = ctypes.CDLL(ORACLE_SO)
+        L.orc_philox4x32_10.argtypes = [P, P, P]
+        L.orc_sincos.argtypes = [P, U32, P, P]
+        L.orc_calc_partition.argtypes = [U32, P, P]
+        L.orc_nmh_build.argtypes = [P, U32, P]
+        L.orc_nmh_build.restype = ctypes.c_int
+        L.orc_gather9.argtypes = [P, P, U32, P]
+        L.orc_trace_closest.argtypes = [P, U32, P, P, U32, P, P, ctypes.c_int]
+        L.orc_trace_closest.restype = ctypes.c_uint64
+        L.orc_trace_any.argtypes = [P, U32, P, P, U32, P, P, ctypes.c_int]
+        L.orc_trace_any.restype = ctypes.c_uint64
+        L.orc_brute_closest.argtypes = [P, U32, P, U32, P, ctypes.c_int]
+        L.orc_camera_make.argtypes = [P, P, ctypes.c_float, ctypes.c_float, ctypes.c_float, P]
+        L.orc_generate_rays.argtypes = [P, U32, U32, U32, U32, P]
+        L.orc_render.argtypes = [P, P, P, P, U32, P, U32, P, U32, P, P, P, ctypes.c_int]
+        L.orc_render.restype = ctypes.c_uint64
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's own traversal compiled as host C++, or None."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO):
+            build_ref()
+        if not os.path.exists(REF_SO):
+            return None
+        L = ctypes.CDLL(REF_SO)
+        L.ref_trace_closest.argtypes = [P, U32, P, U32, P, P]
+        L.ref_trace_any.argtypes = [P, U32, P, U32, P]
+        _ref = L
+    return _ref
+
+
+def nthreads_default():
+    return max(1, os.cpu_count() or 1)
+
+
+def philox(ctr, key):
+    c = np.asarray(ctr, np.uint32); k = np.asarray(key, np.uint32); o = np.zeros(4, np.uint32)
+    lib().orc_philox4x32_10(_ptr(c), _ptr(k), _ptr(o))
+    return o
+
+
+def sincos(x):
+    x = np.ascontiguousarray(x, np.float32); s = np.empty_like(x); c = np.empty_like(x)
+    lib().orc_sincos(_ptr(x), x.size, _ptr(s), _ptr(c))
+    return s, c
+
+
+def calc_partition(N):
+    L = np.zeros(1, np.uint32); R = np.zeros(1, np.uint32)
+    lib().orc_calc_partition(N, _ptr(L), _ptr(R))
+    return int(L[0]), int(R[0])
+
+
+def pad_even(vertices):
+    """Geometry::padToEven: an odd soup gets a copy of its last triangle."""
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 9)
+    if v.shape[0] % 2:
+        v = np.concatenate([v, v[-1:]])
+    return v
+
+
+def nmh_build(vertices):
+    """Canonical NMH build. Returns (perm, levels) for the even-padded soup."""
+    v = pad_even(vertices)
+    perm = np.zeros(v.shape[0], np.uint32)
+    lv = lib().orc_nmh_build(_ptr(v), v.shape[0], _ptr(perm))
+    if lv < 0:
+        raise RuntimeError("orc_nmh_build failed: %d" % lv)
+    return perm, lv
+
+
+def gather9(src, perm):
+    src = np.ascontiguousarray(src, np.float32).reshape(-1, 9)
+    out = np.empty((perm.shape[0], 9), np.float32)
+    lib().orc_gather9(_ptr(src), _ptr(perm), perm.shape[0], _ptr(out))
+    return out
+
+
+def trace_closest(V_nmh, perm, rays, nthreads=None):
+    V = np.ascontiguousarray(V_nmh, np.float32); rays = np.ascontiguousarray(rays, T.ray_dtype)
+    hits = np.zeros(rays.shape[0], T.hit_dtype); vis = np.zeros(rays.shape[0], np.uint32)
+    tot = lib().orc_trace_closest(_ptr(V), V.shape[0], _ptr(perm), _ptr(rays), rays.shape[0], _ptr(hits),
+                                  _ptr(vis), nthreads or nthreads_default())
+    return hits, vis, int(tot)
+
+
+def trace_any(V_nmh, perm, rays, nthreads=None):
+    V = np.ascontiguousarray(V_nmh, np.float32); rays = np.ascontiguousarray(rays, T.ray_dtype)
+    occ = np.zeros(rays.shape[0], np.uint32); vis = np.zeros(rays.shape[0], np.uint32)
+    tot = lib().orc_trace_any(_ptr(V), V.shape[0], _ptr(perm), _ptr(rays), rays.shape[0], _ptr(occ),
+                              _ptr(vis), nthreads or nthreads_default())
+    return occ, vis, int(tot)
+
+
+def brute_closest(vertices, rays, nthreads=None):
+    V = np.ascontiguousarray(vertices, np.float32); rays = np.ascontiguousarray(rays, T.ray_dtype)
+    hits = np.zeros(rays.shape[0], T.hit_dtype)
+    lib().orc_brute_closest(_ptr(V), V.shape[0], _ptr(rays), rays.shape[0], _ptr(hits),
+                            nthreads or nthreads_default())
+    return hits
+
+
+def camera_make(pos, direction, fovx, fovy, aspect=1.0):
+    p = np.asarray(pos, np.float32); d = np.asarray(direction, np.float32); c = np.zeros((), T.camera_dtype)
+    lib().orc_camera_make(_ptr(p), _ptr(d), fovx, fovy, aspect, _ptr(c))
+    return c
+
+
+def generate_rays(camera, W, H, sample, samples):
+    cam = np.asarray(camera, T.camera_dtype).reshape(())
+    rays = np.zeros(W * H, T.path_ray_dtype)
+    lib().orc_generate_rays(_ptr(cam), W, H, sample, samples, _ptr(rays))
+    return rays
+
+
+class NmhScene:
+    """A scene reordered into NMH order, as the renderer consumes it."""
+
+    def __init__(self, scene, perm=None):
+        V = pad_even(scene.vertices)
+        N = pad_even(scene.normals)
+        S = scene.shader_ids
+        if S.shape[0] % 2:
+            S = np.concatenate([S, S[-1:]])
+        if perm is None:
+            perm, _ = nmh_build(V)
+        self.perm = np.ascontiguousarray(perm, np.uint32)
+        self.V = gather9(V, self.perm)
+        self.N = gather9(N, self.perm)
+        self.S = np.ascontiguousarray(S[self.perm], np.uint16)
+        self.shaders = np.ascontiguousarray(scene.shaders, T.shader_dtype)
+        self.lights = np.ascontiguousarray(scene.lights, T.light_dtype)
+        self.camera = np.asarray(scene.camera, T.camera_dtype).reshape(())
+
+
+def render(nscene, params, camera=None, accum=None, nthreads=None):
+    """Adds the requested samples into accum (H, W, 4) float32 and returns
+    (accum, node fetches)."""
+    p = np.asarray(params, T.params_dtype).reshape(())
+    W, H = int(p["width"]), int(p["height"])
+    if accum is None:
+        accum = np.zeros((H, W, 4), np.float32)
+    cam = np.asarray(nscene.camera if camera is None else camera, T.camera_dtype).reshape(())
+    tot = lib().orc_render(_ptr(nscene.V), _ptr(nscene.N), _ptr(nscene.S), _ptr(nscene.perm),
+                           nscene.V.shape[0], _ptr(nscene.shaders), nscene.shaders.shape[0],
+                           _ptr(nscene.lights), nscene.lights.shape[0], _ptr(cam), _ptr(p), _ptr(accum),
+                           nthreads or nthreads_default())
+    return accum, int(tot)
+
+
+def ref_trace_closest(V_nmh, rays):
+    """Reference intersect(): (t, u, v) float32 (n,3) and NMH position (n,)."""
+    L = ref_lib()
+    V = np.ascontiguousarray(V_nmh, np.float32); rays = np.ascontiguousarray(rays, T.ray_dtype)
+    tuv = np.zeros((rays.shape[0], 3), np.float32); ids = np.zeros(rays.shape[0], np.int32)
+    L.ref_trace_closest(_ptr(V), V.shape[0], _ptr(rays), rays.shape[0], _ptr(tuv), _ptr(ids))
+    return tuv, ids
+
+
+def ref_trace_any(V_nmh, rays):
+    L = ref_lib()
+    V = np.ascontiguousarray(V_nmh, np.float32); rays = np.ascontiguousarray(rays, T.ray_dtype)
+    ids = np.zeros(rays.shape[0], np.int32)
+    L.ref_trace_any(_ptr(V), V.shape[0], _ptr(rays), rays.shape[0], _ptr(ids))
+    return ids

@@ -1,0 +1,841 @@
+/*
+ * aur_oracle.cpp — CPU restatement of the Aurora rendering hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This file is the checker the CUDA kernels in
+ * aurora_gb300/csrc are compared against, and the timed CPU baseline of the
+ * benchmark. It is never linked into, loaded by or called from the product
+ * library.
+ *
+ * Every function restates the algorithm of the Nadrin/aurora source file cited
+ * beside it, in the same floating-point operation order, compiled with
+ * -ffp-contract=off so that no multiply-add is fused. Where the reference is
+ * racy or unspecified the deterministic rule marked [canon] is used instead:
+ *   - NMH build: every ordering ties by the lower original prim id; the
+ *     max-key swap ties by the lower prim id (the reference's atomicCAS loop,
+ *     kernels/rebuilder.cu:93-125, is nondeterministic on ties).
+ *   - Closest hit: equal t goes to the lower original prim id (the reference
+ *     keeps the first tested, intersect.cuh:123-136).
+ *   - RNG: a counter-based Philox4x32-10 keyed by (seed, scene, pixel, sample,
+ *     ray, slot) replaces per-pixel cuRAND XORWOW state (utility.cu:182-197);
+ *     the two area-light uniforms are drawn in a fixed order.
+ *   - normalize(v) = v * (1/sqrtf(dot(v,v))), the reference's host definition
+ *     of rsqrtf (util/math.h:45-46), so CPU and GPU round identically.
+ *   - sin/cos are this project's own (Cody-Waite reduction + Taylor series).
+ */
+#include "../include/aurora_gb300.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// util/math.h:17-21
+const float kInfinity = 1000000.0f;
+const float kEpsilon = 0.0000001f;
+const float kPi = 3.1415926536f;
+const float kInvPi = 0.3183098862f;
+
+struct F2 { float x, y; };
+struct F3 { float x, y, z; };
+
+inline F3 mk3(float x, float y, float z) { F3 r; r.x = x; r.y = y; r.z = z; return r; }
+inline F3 mk3(float v) { return mk3(v, v, v); }
+inline F3 from(const aur_float3& a) { return mk3(a.x, a.y, a.z); }
+// util/math.h:92-185, component-wise, left to right
+inline F3 operator-(const F3& a) { return mk3(-a.x, -a.y, -a.z); }
+inline F3 operator+(const F3& a, const F3& b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline F3 operator-(const F3& a, const F3& b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline F3 operator*(const F3& a, float b) { return mk3(a.x * b, a.y * b, a.z * b); }
+inline F3 operator*(float a, const F3& b) { return mk3(a * b.x, a * b.y, a * b.z); }
+inline F3 operator*(const F3& a, const F3& b) { return mk3(a.x * b.x, a.y * b.y, a.z * b.z); }
+inline F3 operator/(const F3& a, float b) { return mk3(a.x / b, a.y / b, a.z / b); }
+// util/math.h:190-191
+inline float dot(const F3& a, const F3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// util/math.h:196-197
+inline float length(const F3& v) { return sqrtf(dot(v, v)); }
+// util/math.h:210-211 with rsqrtf = 1/sqrtf (util/math.h:45-46)
+inline F3 normalize(const F3& v) { return v * (1.0f / sqrtf(dot(v, v))); }
+// util/math.h:222-224
+inline F3 bclerp(const F3& a, const F3& b, const F3& c, float u, float v) {
+    return (1.0f - u - v) * a + u * b + v * c;
+}
+// util/math.h:227-228
+inline F3 cross(const F3& a, const F3& b) {
+    return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+// util/math.h:231-232
+inline F3 reflect(const F3& i, const F3& n) { return i - 2.0f * n * dot(n, i); }
+// util/math.h:235-246
+inline bool refract(F3& r, const F3& i, const F3& n, float eta1, float eta2) {
+    const float eta = eta1 / eta2;
+    const float cosi = dot(n, i);
+    const float sint = eta * eta * (1.0f - cosi * cosi);
+    if (sint > 1.0f) return false;
+    r = eta * i - (eta + sqrtf(1.0f - sint)) * n;
+    return true;
+}
+// util/math.h:86-87
+inline bool zero(const F3& v) { return v.x < kEpsilon && v.y < kEpsilon && v.z < kEpsilon; }
+inline float comp(const F3& v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
+
+// util/math.h:253-261
+inline uint32_t log2i(uint32_t x) {
+    uint32_t r = (uint32_t)(-1);
+    while (x) { x >>= 1; r++; }
+    return r;
+}
+// util/math.h:264-272
+inline uint32_t exp2i(uint32_t x) {
+    if (x == 0) return 1;
+    uint32_t r = 2;
+    while (--x) r *= 2;
+    return r;
+}
+
+// ------------------------------------------------------------------ RNG
+// Philox4x32-10, J. K. Salmon, M. A. Moraes, R. O. Dror, D. E. Shaw,
+// "Parallel random numbers: as easy as 1, 2, 3", SC'11. Round function and
+// constants as published there.
+struct U4 { uint32_t x, y, z, w; };
+
+inline U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c.x;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c.z;
+        U4 n;
+        n.x = (uint32_t)(p1 >> 32) ^ c.y ^ k0;
+        n.y = (uint32_t)p1;
+        n.z = (uint32_t)(p0 >> 32) ^ c.w ^ k1;
+        n.w = (uint32_t)p0;
+        c = n;
+    }
+    return c;
+}
+
+// Uniform in (0, 1], the range of curand_uniform: ((x >> 8) + 1) * 2^-24.
+inline float u01(uint32_t x) { return (float)((x >> 8) + 1u) * (1.0f / 16777216.0f); }
+
+struct RngKey { uint32_t seed, scene; };
+// slot 0: BSDF sample; slot 1 + (light << 16) + j: j-th sample of light `light`.
+inline void draw2(const RngKey& k, uint32_t pixel, uint32_t sample, uint32_t ray, uint32_t slot,
+                  float& u1, float& u2) {
+    U4 c; c.x = pixel; c.y = sample; c.z = ray; c.w = slot;
+    const U4 r = philox4x32_10(c, k.seed, k.scene);
+    u1 = u01(r.x);
+    u2 = u01(r.y);
+}
+
+// ------------------------------------------------------------ sin / cos
+// Own implementation: Cody-Waite reduction by pi/2 into [-pi/4, pi/4], then
+// Taylor polynomials (sin to x^11, cos to x^12) evaluated by Horner's rule
+// with separately rounded multiplies and adds.
+inline void own_sincos(float x, float& s, float& c) {
+    const float kTwoOverPi = 0.636619747f;
+    const float kPio2Hi = 1.5707950592041016f;  // pi/2 = hi + lo; hi has 4 low zero bits,
+    const float kPio2Lo = 1.2675908465098473e-06f;  // so q*hi is exact for |q| <= 8
+    const float q = rintf(x * kTwoOverPi);
+    const float r = (x - q * kPio2Hi) - q * kPio2Lo;
+    const float r2 = r * r;
+    float ps = -2.50521084e-08f;               // -1/11!
+    ps = ps * r2 + 2.75573192e-06f;            //  1/9!
+    ps = ps * r2 + -1.98412698e-04f;           // -1/7!
+    ps = ps * r2 + 8.33333333e-03f;            //  1/5!
+    ps = ps * r2 + -1.66666667e-01f;           // -1/3!
+    const float sr = r + (r * r2) * ps;
+    float pc = 2.08767570e-09f;                //  1/12!
+    pc = pc * r2 + -2.75573192e-07f;           // -1/10!
+    pc = pc * r2 + 2.48015873e-05f;            //  1/8!
+    pc = pc * r2 + -1.38888889e-03f;           // -1/6!
+    pc = pc * r2 + 4.16666667e-02f;            //  1/4!
+    pc = pc * r2 + -0.5f;                      // -1/2!
+    const float cr = 1.0f + r2 * pc;
+    const int qi = ((int)q) & 3;
+    if (qi == 0) { s = sr; c = cr; }
+    else if (qi == 1) { s = cr; c = -sr; }
+    else if (qi == 2) { s = -sr; c = -cr; }
+    else { s = -cr; c = sr; }
+}
+
+// -------------------------------------------------------------- sampling
+// kernels/lib/sampling.cuh:51-73
+inline F2 sampleDiskConcentric(float u1, float u2) {
+    const float x = 2.0f * u1 - 1.0f;
+    const float y = 2.0f * u2 - 1.0f;
+    float r, theta;
+    if (x >= -y) {
+        if (x > y) { r = x; theta = kPi / 4.0f * (y / x); }
+        else { r = y; theta = kPi / 4.0f * (2.0f - x / y); }
+    } else {
+        if (x < y) { r = -x; theta = kPi / 4.0f * (4.0f + y / x); }
+        else {
+            r = -y;
+            if (y != 0.0f) theta = kPi / 4.0f * (6.0f - x / y);
+            else theta = 0.0f;
+        }
+    }
+    float s, c;
+    own_sincos(theta, s, c);
+    F2 d; d.x = r * c; d.y = r * s;
+    return d;
+}
+// kernels/lib/sampling.cuh:76-82
+inline F3 sampleHemisphereCosine(float u1, float u2) {
+    const F2 d = sampleDiskConcentric(u1, u2);
+    return mk3(d.x, d.y, sqrtf(fmaxf(0.0f, 1.0f - d.x * d.x - d.y * d.y)));
+}
+// kernels/lib/common.cuh:340-354
+inline F3 worldToLocal(const F3& v, const F3& N, const F3& S, const F3& T) {
+    return mk3(v.x * S.x + v.y * S.y + v.z * S.z, v.x * T.x + v.y * T.y + v.z * T.z,
+               v.x * N.x + v.y * N.y + v.z * N.z);
+}
+inline F3 localToWorld(const F3& v, const F3& N, const F3& S, const F3& T) {
+    return mk3(S.x * v.x + T.x * v.y + N.x * v.z, S.y * v.x + T.y * v.y + N.y * v.z,
+               S.z * v.x + T.z * v.y + N.z * v.z);
+}
+
+// ------------------------------------------------------------ traversal
+struct Ray {
+    F3 pos, dir;
+    float t, weight, eta;
+    F3 thr;          // RGB path throughput (path mode); (weight,weight,weight) otherwise
+};
+
+// kernels/lib/ray.cuh:198-223 (Moller-Trumbore with back-face culling)
+inline bool intersectTri(const Ray& ray, const float* v, float& u, float& vv, float& t) {
+    const F3 v1 = mk3(v[0], v[3], v[6]);
+    const F3 v2 = mk3(v[1], v[4], v[7]);
+    const F3 v3 = mk3(v[2], v[5], v[8]);
+    const F3 e1 = v2 - v1;
+    const F3 e2 = v3 - v1;
+    const F3 P = cross(ray.dir, e2);
+    const float det = dot(e1, P);
+    if (det < kEpsilon) return false;
+    const float invdet = 1.0f / det;
+    const F3 T = ray.pos - v1;
+    u = dot(T, P) * invdet;
+    if (u < 0.0f || u > 1.0f) return false;
+    const F3 Q = cross(T, e1);
+    vv = dot(ray.dir, Q) * invdet;
+    if (vv < 0.0f || u + vv > 1.0f) return false;
+    t = dot(e2, Q) * invdet;
+    return true;
+}
+
+// kernels/lib/ray.cuh:225-237; device min/max of floats are fminf/fmaxf
+inline bool intersectSlab(const Ray& ray, float s0, float s1, int axis, F2& range) {
+    const float p = comp(ray.pos, axis);
+    const float d = comp(ray.dir, axis);
+    const float dx = (s0 - p) / d;
+    const float dy = (s1 - p) / d;
+    range.x = fmaxf(fminf(dx, dy), range.x);
+    range.y = fminf(fmaxf(dx, dy), range.y);
+    return (range.x <= range.y) && (range.x <= ray.t);
+}
+
+inline float vmin(const float* v, int a) { return fminf(fminf(v[3 * a], v[3 * a + 1]), v[3 * a + 2]); }
+inline float vmax(const float* v, int a) { return fmaxf(fmaxf(v[3 * a], v[3 * a + 1]), v[3 * a + 2]); }
+
+struct TState { uint32_t index; int axis; F2 range; };
+
+// kernels/lib/intersect.cuh:95-152 (closest hit), [canon] tie on t -> lower perm id.
+// Returns the NMH position of the hit (or -1). ray.t is updated.
+inline int64_t traceClosest(const float* V, uint32_t count, const uint32_t* perm, Ray& ray,
+                            float& hu, float& hv, uint64_t* visits) {
+    int64_t hit = -1;
+    TState stack[64];
+    int sp = 0;
+    TState s0; s0.index = 0; s0.axis = 0; s0.range.x = kEpsilon; s0.range.y = kInfinity;
+    stack[sp++] = s0;
+    while (sp > 0) {
+        TState st = stack[--sp];
+        if (st.index >= count) continue;
+        if (visits) ++*visits;
+        const float* v1 = V + (size_t)st.index * 9;
+        const float* v2 = V + (size_t)(st.index + 1) * 9;
+        const float s0x = fminf(vmin(v1, st.axis), vmin(v2, st.axis));
+        const float s0y = fmaxf(vmax(v1, st.axis), vmax(v2, st.axis));
+        if (!intersectSlab(ray, s0x, s0y, st.axis, st.range)) continue;
+        for (uint32_t k = 0; k < 2; ++k) {
+            float u, v, t;
+            const uint32_t idx = st.index + k;
+            if (intersectTri(ray, V + (size_t)idx * 9, u, v, t) && t > kEpsilon) {
+                bool take = t < ray.t;
+                if (!take && t == ray.t && hit >= 0 && perm && perm[idx] < perm[(size_t)hit]) take = true;
+                if (take) { ray.t = t; hu = u; hv = v; hit = idx; }
+            }
+        }
+        const int axis = (st.axis + 1) % 3;
+        uint32_t L = 2 * st.index + 2, R = 2 * st.index + 4;
+        if (comp(ray.dir, axis) < 0.0f) std::swap(L, R);
+        TState a; a.index = R; a.axis = axis; a.range = st.range;
+        TState b; b.index = L; b.axis = axis; b.range = st.range;
+        stack[sp++] = a;
+        stack[sp++] = b;
+    }
+    return hit;
+}
+
+// kernels/lib/intersect.cuh:36-86 (any hit). Returns NMH position or -1.
+inline int64_t traceAny(const float* V, uint32_t count, const Ray& ray, uint64_t* visits) {
+    TState stack[64];
+    int sp = 0;
+    TState s0; s0.index = 0; s0.axis = 0; s0.range.x = kEpsilon; s0.range.y = kInfinity;
+    stack[sp++] = s0;
+    while (sp > 0) {
+        TState st = stack[--sp];
+        if (st.index >= count) continue;
+        if (visits) ++*visits;
+        const float* v1 = V + (size_t)st.index * 9;
+        const float* v2 = V + (size_t)(st.index + 1) * 9;
+        const float s0x = fminf(vmin(v1, st.axis), vmin(v2, st.axis));
+        const float s0y = fmaxf(vmax(v1, st.axis), vmax(v2, st.axis));
+        if (!intersectSlab(ray, s0x, s0y, st.axis, st.range)) continue;
+        float u, v, t;
+        if (intersectTri(ray, v1, u, v, t) && t > kEpsilon && t < ray.t) return st.index;
+        if (intersectTri(ray, v2, u, v, t) && t > kEpsilon && t < ray.t) return st.index + 1;
+        const int axis = (st.axis + 1) % 3;
+        uint32_t L = 2 * st.index + 2, R = 2 * st.index + 4;
+        if (comp(ray.dir, axis) < 0.0f) std::swap(L, R);
+        TState a; a.index = R; a.axis = axis; a.range = st.range;
+        TState b; b.index = L; b.axis = axis; b.range = st.range;
+        stack[sp++] = a;
+        stack[sp++] = b;
+    }
+    return -1;
+}
+
+template <class F>
+void parallel_for(uint32_t n, int nthreads, F f) {
+    if (nthreads <= 1 || n < 256) { for (uint32_t i = 0; i < n; ++i) f(i, 0); return; }
+    std::atomic<uint32_t> next(0);
+    std::vector<std::thread> th;
+    for (int w = 0; w < nthreads; ++w) {
+        th.emplace_back([&, w]() {
+            for (;;) {
+                const uint32_t b = next.fetch_add(64);
+                if (b >= n) break;
+                const uint32_t e = std::min(n, b + 64);
+                for (uint32_t i = b; i < e; ++i) f(i, w);
+            }
+        });
+    }
+    for (auto& t : th) t.join();
+}
+
+inline Ray rayFrom(const aur_ray& r) {
+    Ray ray;
+    ray.pos = mk3(r.ox, r.oy, r.oz);
+    ray.dir = mk3(r.dx, r.dy, r.dz);
+    ray.t = r.tmax;
+    ray.weight = 1.0f;
+    ray.eta = 1.0f;
+    ray.thr = mk3(1.0f);
+    return ray;
+}
+
+// ------------------------------------------------------------ NMH build
+// kernels/rebuilder.cu:40-50
+inline void calcPartition(uint32_t N, uint32_t& L, uint32_t& R) {
+    const uint32_t n = N / 2;
+    const uint32_t H = log2i(n);
+    const uint32_t s = exp2i(H - 1) - 1;
+    const uint32_t S = exp2i(H) - 1;
+    const int o = int((n - 1) - s - S);
+    const uint32_t O = (uint32_t)(o > 0 ? o : 0);
+    R = 2 * (s + O);
+    L = 2 * (n - 1) - R;
+}
+
+struct Bounds { std::vector<float> mn[3], mx[3]; };
+
+// kernels/rebuilder.cu:72-91
+void triangleBounds(const float* V, uint32_t n, Bounds& b) {
+    for (int a = 0; a < 3; ++a) { b.mn[a].resize(n); b.mx[a].resize(n); }
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* v = V + (size_t)i * 9;
+        for (int a = 0; a < 3; ++a) { b.mn[a][i] = vmin(v, a); b.mx[a][i] = vmax(v, a); }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+// Philox known-answer hook for tests.
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    U4 c; c.x = ctr[0]; c.y = ctr[1]; c.z = ctr[2]; c.w = ctr[3];
+    const U4 r = philox4x32_10(c, key[0], key[1]);
+    out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = r.w;
+}
+
+void orc_sincos(const float* x, uint32_t n, float* s, float* c) {
+    for (uint32_t i = 0; i < n; ++i) own_sincos(x[i], s[i], c[i]);
+}
+
+void orc_calc_partition(uint32_t N, uint32_t* L, uint32_t* R) { calcPartition(N, *L, *R); }
+
+/*
+ * NMH build, [canon] restatement of cudaRebuildNMH (kernels/rebuilder.cu:311-450).
+ * Node k holds triangles at positions 2k, 2k+1; its children are nodes 2k+1,
+ * 2k+2 (intersect.cuh:139-140). Level d uses axis d mod 3. For a node with
+ * member set S at level d (axis a):
+ *   - sort S by (min-key on a, prim id) (sortTriangles, :262-289);
+ *   - pair[0] = first; pair[1] = largest max-key on a among the rest, ties to
+ *     the lower prim id (swapMaxTriangleTPS/TPT, :93-151);
+ *   - the remainder, ordered by (min-key on axis a+1, prim id) as the next
+ *     level's sort does, gives its first numL to the left child and the rest
+ *     to the right (calcPartition + emitSplits, :40-50, :189-215).
+ * The final level's sort (:381-385) leaves every pair ordered by
+ * (min-key on the last level's axis, prim id).
+ * vertices: n*9 (n even). perm_out[i] = original id at NMH position i.
+ * Returns the number of levels, or -1 on an invalid count.
+ */
+int orc_nmh_build(const float* vertices, uint32_t n, uint32_t* perm_out) {
+    if (n == 0) return 0;
+    if (n % 2) return -1;
+    const uint32_t nodes = n / 2;
+    const uint32_t levels = log2i(nodes) + 1;
+    Bounds b;
+    triangleBounds(vertices, n, b);
+    std::vector<std::vector<uint32_t>> members(nodes);
+    std::vector<uint32_t> all(n);
+    for (uint32_t i = 0; i < n; ++i) all[i] = i;
+    members[0] = all;
+    auto byMin = [&](int a) {
+        return [&b, a](uint32_t p, uint32_t q) {
+            const float kp = b.mn[a][p], kq = b.mn[a][q];
+            if (kp != kq) return kp < kq;
+            return p < q;
+        };
+    };
+    std::vector<uint32_t> pair0(nodes), pair1(nodes);
+    for (uint32_t k = 0; k < nodes; ++k) {
+        const uint32_t level = log2i(k + 1);
+        const int a = (int)(level % 3);
+        std::vector<uint32_t>& S = members[k];
+        std::sort(S.begin(), S.end(), byMin(a));
+        pair0[k] = S[0];
+        if (S.size() == 2) { pair1[k] = S[1]; continue; }
+        size_t best = 1;
+        for (size_t i = 2; i < S.size(); ++i) {
+            const float kv = b.mx[a][S[i]], kb = b.mx[a][S[best]];
+            if (kv > kb || (kv == kb && S[i] < S[best])) best = i;
+        }
+        pair1[k] = S[best];
+        std::vector<uint32_t> rest;
+        rest.reserve(S.size() - 2);
+        for (size_t i = 1; i < S.size(); ++i) if (i != best) rest.push_back(S[i]);
+        std::sort(rest.begin(), rest.end(), byMin((a + 1) % 3));
+        uint32_t numL, numR;
+        calcPartition((uint32_t)S.size(), numL, numR);
+        if (numL + numR != rest.size()) return -2;
+        const uint32_t cl = 2 * k + 1, cr = 2 * k + 2;
+        if ((numL > 0) != (cl < nodes) || (numR > 0) != (cr < nodes)) return -3;
+        if (numL) members[cl].assign(rest.begin(), rest.begin() + numL);
+        if (numR) members[cr].assign(rest.begin() + numL, rest.end());
+        std::vector<uint32_t>().swap(S);
+    }
+    const int al = (int)((levels - 1) % 3);
+    auto less = byMin(al);
+    for (uint32_t k = 0; k < nodes; ++k) {
+        uint32_t p = pair0[k], q = pair1[k];
+        if (less(q, p)) std::swap(p, q);
+        perm_out[2 * k] = p;
+        perm_out[2 * k + 1] = q;
+    }
+    return (int)levels;
+}
+
+/* applyIndices (rebuilder.cu:217-245) for 9-float attributes. */
+void orc_gather9(const float* src, const uint32_t* perm, uint32_t n, float* dst) {
+    for (uint32_t i = 0; i < n; ++i) std::memcpy(dst + (size_t)i * 9, src + (size_t)perm[i] * 9, 36);
+}
+
+/*
+ * Closest hit over an NMH-ordered soup (intersect.cuh:95-152), [canon] ties.
+ * V: count*9 NMH-ordered vertices; perm: NMH position -> original id.
+ * hits[i].prim = original id or AUR_NO_HIT. visits (nullable): per-ray node
+ * fetch counts. Returns total node fetches.
+ */
+uint64_t orc_trace_closest(const float* V, uint32_t count, const uint32_t* perm, const aur_ray* rays,
+                           uint32_t n, aur_hit* hits, uint32_t* visits, int nthreads) {
+    std::vector<uint64_t> tot((size_t)std::max(1, nthreads), 0);
+    parallel_for(n, nthreads, [&](uint32_t i, int w) {
+        Ray ray = rayFrom(rays[i]);
+        float u = 0.0f, v = 0.0f;
+        uint64_t vis = 0;
+        const int64_t h = traceClosest(V, count, perm, ray, u, v, &vis);
+        aur_hit out;
+        if (h >= 0) { out.t = ray.t; out.u = u; out.v = v; out.prim = perm[h]; }
+        else { out.t = rays[i].tmax; out.u = 0.0f; out.v = 0.0f; out.prim = AUR_NO_HIT; }
+        hits[i] = out;
+        if (visits) visits[i] = (uint32_t)vis;
+        tot[(size_t)w] += vis;
+    });
+    uint64_t s = 0;
+    for (uint64_t x : tot) s += x;
+    return s;
+}
+
+/* Any hit (intersect.cuh:36-86): occluder[i] = original id or AUR_NO_HIT. */
+uint64_t orc_trace_any(const float* V, uint32_t count, const uint32_t* perm, const aur_ray* rays,
+                       uint32_t n, uint32_t* occluder, uint32_t* visits, int nthreads) {
+    std::vector<uint64_t> tot((size_t)std::max(1, nthreads), 0);
+    parallel_for(n, nthreads, [&](uint32_t i, int w) {
+        const Ray ray = rayFrom(rays[i]);
+        uint64_t vis = 0;
+        const int64_t h = traceAny(V, count, ray, &vis);
+        occluder[i] = h >= 0 ? perm[h] : AUR_NO_HIT;
+        if (visits) visits[i] = (uint32_t)vis;
+        tot[(size_t)w] += vis;
+    });
+    uint64_t s = 0;
+    for (uint64_t x : tot) s += x;
+    return s;
+}
+
+/*
+ * Brute-force closest hit over an ORIGINAL-order soup: the algorithm-
+ * independent check of traversal. Same triangle test and acceptance
+ * (Epsilon < t < tmax), minimum (t, prim id).
+ */
+void orc_brute_closest(const float* V, uint32_t count, const aur_ray* rays, uint32_t n, aur_hit* hits,
+                       int nthreads) {
+    parallel_for(n, nthreads, [&](uint32_t i, int) {
+        Ray ray = rayFrom(rays[i]);
+        aur_hit out; out.t = rays[i].tmax; out.u = 0.0f; out.v = 0.0f; out.prim = AUR_NO_HIT;
+        for (uint32_t k = 0; k < count; ++k) {
+            float u, v, t;
+            if (intersectTri(ray, V + (size_t)k * 9, u, v, t) && t > kEpsilon && t < ray.t) {
+                ray.t = t; out.t = t; out.u = u; out.v = v; out.prim = k;
+            }
+        }
+        hits[i] = out;
+    });
+}
+
+}  // extern "C"
+
+// ============================================================ integrator
+namespace {
+
+struct Scene {
+    const float* V;            // NMH-ordered vertices, count*9
+    const float* N;            // NMH-ordered normals, count*9
+    const uint16_t* S;         // NMH-ordered shader ids (1-based)
+    const uint32_t* perm;
+    uint32_t count;
+    const aur_shader* shaders;
+    uint32_t nshaders;
+    const aur_light* lights;
+    uint32_t nlights;
+};
+
+struct BSDF { F3 N, S, T, color1; };
+
+// kernels/utility.cu:136-167 (per-vertex tangent/bitangent), evaluated at
+// shading time from the stored normals.
+inline void vertexTB(const F3& n, F3& t, F3& b) {
+    const F3 up = mk3(0.0f, 1.0f, 0.0f), fwd = mk3(0.0f, 0.0f, 1.0f);
+    t = cross(n, up);
+    if (length(t) < kEpsilon) t = cross(n, fwd);
+    b = cross(n, t);
+}
+
+// kernels/lib/common.cuh:314-327 + shader.cuh:243-262
+inline BSDF getBSDF(const Scene& sc, const aur_shader& sh, uint32_t idx, float u, float v) {
+    const float* nv = sc.N + (size_t)idx * 9;
+    const F3 n1 = mk3(nv[0], nv[1], nv[2]), n2 = mk3(nv[3], nv[4], nv[5]), n3 = mk3(nv[6], nv[7], nv[8]);
+    F3 t1, t2, t3, b1, b2, b3;
+    vertexTB(n1, t1, b1);
+    vertexTB(n2, t2, b2);
+    vertexTB(n3, t3, b3);
+    BSDF bs;
+    bs.N = normalize(bclerp(n1, n2, n3, u, v));
+    bs.S = normalize(bclerp(t1, t2, t3, u, v));
+    bs.T = normalize(bclerp(b1, b2, b3, u, v));
+    bs.color1 = from(sh.diffuse_color) * sh.diffuse;
+    return bs;
+}
+
+inline F3 bsdfF(const BSDF& b) { return b.color1 * kInvPi; }   // bsdf.cuh:202-210
+
+struct PixelCtx { RngKey key; uint32_t pixel, sample, ray; };
+
+// light.cuh:228-259; the area case draws u1 then u2 from one Philox block.
+inline F3 sampleL(const aur_light& L, const PixelCtx* pc, uint32_t slot, Ray& ray, float& pdf) {
+    const F3 color = from(L.color);
+    switch (L.type) {
+    case AUR_LIGHT_AMBIENT:
+        ray.dir = from(L.position) - ray.pos;
+        ray.t = length(ray.dir);
+        ray.dir = ray.dir / ray.t;
+        pdf = 1.0f;
+        return (color * L.intensity) * (1.0f - L.ambient);
+    case AUR_LIGHT_POINT:
+        ray.dir = from(L.position) - ray.pos;
+        ray.t = length(ray.dir);
+        ray.dir = ray.dir / ray.t;
+        pdf = 1.0f;
+        return (color * L.intensity) / (ray.t * ray.t);
+    case AUR_LIGHT_DIRECTIONAL:
+        ray.dir = -from(L.direction);
+        ray.t = kInfinity;
+        pdf = 1.0f;
+        return color * L.intensity;
+    default: {
+        float u1, u2;
+        draw2(pc->key, pc->pixel, pc->sample, pc->ray, slot, u1, u2);
+        const F3 P = from(L.position) + ((from(L.e1) * u1) + (from(L.e2) * u2));   // sampling.cuh:148-152
+        ray.dir = P - ray.pos;
+        ray.t = length(ray.dir);
+        ray.dir = ray.dir / ray.t;
+        pdf = 1.0f / fabsf(dot(from(L.direction), -ray.dir));                       // light.cuh:282-293
+        return (color * L.intensity) * fmaxf(0.0f, dot(from(L.direction), -ray.dir));
+    }
+    }
+}
+
+inline Ray pointRay(const F3& p) {
+    Ray r; r.pos = p; r.dir = mk3(0.0f); r.t = kInfinity; r.weight = 1.0f; r.eta = 1.0f; r.thr = mk3(1.0f);
+    return r;
+}
+
+// radiance.cuh:13-16
+inline F3 ambientRadiance(const aur_light& L, const BSDF& b) {
+    return bsdfF(b) * ((from(L.color) * L.intensity) * L.ambient);
+}
+
+// radiance.cuh:18-33 (no offset of the shadow ray)
+inline F3 directDelta(const Scene& sc, const aur_light& L, const BSDF& b, const F3& pos, uint64_t* vis) {
+    Ray wi = pointRay(pos);
+    float pdf;
+    const F3 Li = sampleL(L, nullptr, 0, wi, pdf);
+    if (pdf > 0.0f && !zero(Li)) {
+        const F3 f = bsdfF(b);
+        if (!zero(f) && traceAny(sc.V, sc.count, wi, vis) < 0)
+            return f * Li * fmaxf(0.0f, dot(wi.dir, b.N));
+    }
+    return mk3(0.0f);
+}
+
+// radiance.cuh:35-80 (light-sampling half; the #if 0 BSDF half stays off)
+inline F3 directArea(const Scene& sc, const aur_light& L, uint32_t li, const BSDF& b, const F3& pos,
+                     const PixelCtx& pc, uint64_t* vis) {
+    F3 acc = mk3(0.0f);
+    for (int32_t i = 0; i < L.samples; ++i) {
+        F3 Ls = mk3(0.0f);
+        Ray wi = pointRay(pos);
+        float lightPdf;
+        const F3 Li = sampleL(L, &pc, 1u + (li << 16) + (uint32_t)i, wi, lightPdf);
+        // Ray::offset (ray.cuh:184-191)
+        wi.pos.x += kEpsilon * wi.dir.x;
+        wi.pos.y += kEpsilon * wi.dir.y;
+        wi.pos.z += kEpsilon * wi.dir.z;
+        wi.t += kEpsilon;
+        if (lightPdf > 0.0f && !zero(Li)) {
+            const F3 f = bsdfF(b);
+            if (!zero(f) && traceAny(sc.V, sc.count, wi, vis) < 0)
+                Ls = Ls + f * Li * fmaxf(0.0f, dot(wi.dir, b.N));
+        }
+        acc = acc + Ls;
+    }
+    const float ns = (float)L.samples;
+    return mk3(acc.x / ns, acc.y / ns, acc.z / ns);
+}
+
+// utility.cu:18-77: camera ray for pixel (x, y), sample s of `samples`.
+inline Ray cameraRay(const aur_camera& cam, uint32_t W, uint32_t H, uint32_t x, uint32_t y, uint32_t s,
+                     uint32_t samples) {
+    F2 pixel;
+    if (samples == 1) {
+        pixel.x = float(x) / float(W) - 0.5f;
+        pixel.y = float(y) / float(H) - 0.5f;
+    } else {
+        const short sw = (short)sqrtf((float)samples);
+        const short sx = (short)(s % (uint32_t)sw), sy = (short)(s / (uint32_t)sw);
+        const float dx = 1.0f / float(W), dy = 1.0f / float(H);
+        const float sdx = dx / sw, sdy = dy / sw;
+        pixel.x = x * dx - 0.5f + (sx * sdx);
+        pixel.y = y * dy - 0.5f + (sy * sdy);
+    }
+    Ray r;
+    r.pos = from(cam.position);
+    r.t = kInfinity;
+    r.weight = 1.0f;
+    r.eta = 1.0f;
+    r.thr = mk3(1.0f);
+    r.dir = normalize(pixel.x * from(cam.right) * cam.tanfov_x + pixel.y * from(cam.up) * cam.tanfov_y +
+                      from(cam.forward));
+    return r;
+}
+
+struct SampleOut { F3 color; bool hit; };
+
+// monteCarloRaytracer.cu:23-113 for one camera ray; mode adds the path bounce.
+SampleOut integrate(const Scene& sc, const aur_render_params& p, const Ray& primary, const PixelCtx& pc0,
+                    uint64_t* vis) {
+    Ray stack[AUR_MAX_DEPTH + 2];
+    int sp = 0;
+    stack[sp++] = primary;
+    int depth = 0;
+    F3 color = mk3(0.0f);
+    bool anyHit = false;
+    uint32_t rayIndex = 0;
+    const int maxDepth = (int)p.max_depth;
+    while (depth <= maxDepth && sp > 0) {
+        Ray ray = stack[--sp];
+        PixelCtx pc = pc0;
+        pc.ray = rayIndex++;
+        float u = 0.0f, v = 0.0f;
+        const int64_t h = traceClosest(sc.V, sc.count, sc.perm, ray, u, v, vis);
+        if (h < 0) continue;
+        anyHit = true;
+        const uint32_t tri = (uint32_t)h;
+        const F3 position = ray.pos + (ray.dir * ray.t);
+        const F3 wo = -ray.dir;
+        const uint32_t sid = sc.S[tri];
+        const aur_shader& sh = sc.shaders[sid > 0 ? sid - 1 : 0];   // getSafeID, util/array.h:16-17
+        const BSDF b = getBSDF(sc, sh, tri, u, v);
+        F3 Li = from(sh.emission_color);
+        for (uint32_t i = 0; i < sc.nlights; ++i) {
+            const aur_light& L = sc.lights[i];
+            if (L.type == AUR_LIGHT_AMBIENT) Li = Li + ambientRadiance(L, b);
+            if (L.type != AUR_LIGHT_AREA) Li = Li + directDelta(sc, L, b, position, vis);
+            else Li = Li + directArea(sc, L, i, b, position, pc, vis);
+        }
+        const bool specular = sh.reflectivity > 0.0f || sh.translucence > 0.0f;
+        if (specular) depth++;
+        if (depth <= maxDepth && sh.reflectivity > 0.0f) {
+            Ray nr = pointRay(position);
+            nr.dir = reflect(ray.dir, b.N);
+            nr.weight = sh.reflectivity;
+            nr.eta = ray.eta;
+            nr.thr = p.mode == AUR_MODE_PATH ? ray.thr * sh.reflectivity : mk3(nr.weight);
+            ray.weight *= (1.0f - sh.reflectivity);
+            ray.thr = p.mode == AUR_MODE_PATH ? ray.thr * (1.0f - sh.reflectivity) : mk3(ray.weight);
+            stack[sp++] = nr;
+        }
+        if (depth <= maxDepth && sh.translucence > 0.0f) {
+            F3 rN = b.N;
+            float etai = ray.eta, etat = sh.refractive_index;
+            if (dot(rN, wo) < 0.0f) { rN = -rN; etai = sh.refractive_index; etat = 1.0f; }
+            F3 tdir;
+            if (refract(tdir, ray.dir, rN, etai, etat)) {
+                Ray nr = pointRay(position);
+                nr.dir = tdir;
+                nr.weight = sh.translucence;
+                nr.eta = etat;
+                nr.thr = p.mode == AUR_MODE_PATH ? ray.thr * sh.translucence : mk3(nr.weight);
+                ray.weight *= (1.0f - sh.translucence);
+                ray.thr = p.mode == AUR_MODE_PATH ? ray.thr * (1.0f - sh.translucence) : mk3(ray.weight);
+                stack[sp++] = nr;
+            }
+        }
+        if (p.mode == AUR_MODE_PATH && !specular) {
+            depth++;
+            if (depth <= maxDepth) {
+                // BSDF::samplef (bsdf.cuh:222-236)
+                float u1, u2;
+                draw2(pc.key, pc.pixel, pc.sample, pc.ray, 0u, u1, u2);
+                const F3 lwo = worldToLocal(wo, b.N, b.S, b.T);
+                F3 lwi = sampleHemisphereCosine(u1, u2);
+                if (lwo.z < 0.0f) lwi.z *= -1.0f;
+                const float pdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
+                const F3 f = bsdfF(b);
+                const F3 wi = localToWorld(lwi, b.N, b.S, b.T);
+                if (pdf > 0.0f && !zero(f)) {
+                    Ray nr = pointRay(position);
+                    nr.dir = wi;
+                    nr.eta = ray.eta;
+                    nr.thr = ray.thr * (f * (fabsf(dot(wi, b.N)) / pdf));
+                    stack[sp++] = nr;
+                }
+            }
+        }
+        color = color + Li * ray.thr;
+    }
+    SampleOut o; o.color = color; o.hit = anyHit;
+    return o;
+}
+
+}  // namespace
+
+extern "C" {
+
+/* Camera::Camera (util/camera.h:15-28); tanf on the host. */
+void orc_camera_make(const float pos[3], const float dir[3], float fovx, float fovy, float aspect,
+                     aur_camera* out) {
+    const F3 up0 = mk3(0.0f, 1.0f, 0.0f);
+    const F3 fwd = normalize(mk3(dir[0], dir[1], dir[2]));
+    const F3 right = cross(fwd, up0);
+    const F3 up = cross(right, fwd);
+    out->position.x = pos[0]; out->position.y = pos[1]; out->position.z = pos[2];
+    out->forward.x = fwd.x; out->forward.y = fwd.y; out->forward.z = fwd.z;
+    out->right.x = right.x; out->right.y = right.y; out->right.z = right.z;
+    out->up.x = up.x; out->up.y = up.y; out->up.z = up.z;
+    out->tanfov_x = tanf(fovx);
+    out->tanfov_y = tanf(fovy);
+    out->aspect = aspect;
+}
+
+/* Camera rays for one sample (utility.cu:45-94), reference Ray layout. */
+void orc_generate_rays(const aur_camera* cam, uint32_t W, uint32_t H, uint32_t sample, uint32_t samples,
+                       aur_path_ray* rays) {
+    for (uint32_t y = 0; y < H; ++y)
+        for (uint32_t x = 0; x < W; ++x) {
+            const Ray r = cameraRay(*cam, W, H, x, y, sample, samples);
+            aur_path_ray& o = rays[(size_t)y * W + x];
+            o.pos.x = r.pos.x; o.pos.y = r.pos.y; o.pos.z = r.pos.z;
+            o.dir.x = r.dir.x; o.dir.y = r.dir.y; o.dir.z = r.dir.z;
+            o.t = r.t; o.weight = r.weight; o.eta = r.eta;
+        }
+}
+
+/*
+ * Renders samples [sample_begin, sample_end) of p->spp per pixel and adds
+ * them into accum (W*H*4 floats) in sample order, exactly as
+ * cudaDrawPixels does (utility.cu:199-219): rgb += color*(1/spp) and
+ * alpha += 1/spp for samples whose camera ray hit something.
+ * Scene arrays are NMH-ordered (perm: NMH position -> original id).
+ * Returns the number of node fetches (closest + any).
+ */
+uint64_t orc_render(const float* V, const float* N, const uint16_t* S, const uint32_t* perm, uint32_t count,
+                    const aur_shader* shaders, uint32_t nshaders, const aur_light* lights, uint32_t nlights,
+                    const aur_camera* cam, const aur_render_params* p, float* accum, int nthreads) {
+    Scene sc;
+    sc.V = V; sc.N = N; sc.S = S; sc.perm = perm; sc.count = count;
+    sc.shaders = shaders; sc.nshaders = nshaders; sc.lights = lights; sc.nlights = nlights;
+    const uint32_t W = p->width, H = p->height;
+    const uint32_t s0 = p->sample_begin, s1 = p->sample_end ? p->sample_end : p->spp;
+    const float weight = 1.0f / (float)p->spp;
+    std::vector<uint64_t> tot((size_t)std::max(1, nthreads), 0);
+    parallel_for(W * H, nthreads, [&](uint32_t pix, int w) {
+        const uint32_t x = pix % W, y = pix / W;
+        float* px = accum + (size_t)pix * 4;
+        for (uint32_t s = s0; s < s1; ++s) {
+            const Ray r = cameraRay(*cam, W, H, x, y, s, p->spp);
+            PixelCtx pc;
+            pc.key.seed = p->seed; pc.key.scene = p->scene_id;
+            pc.pixel = pix; pc.sample = s; pc.ray = 0;
+            const SampleOut o = integrate(sc, *p, r, pc, &tot[(size_t)w]);
+            if (o.hit) {
+                px[0] += o.color.x * weight;
+                px[1] += o.color.y * weight;
+                px[2] += o.color.z * weight;
+                px[3] += weight;
+            }
+        }
+    });
+    uint64_t s = 0;
+    for (uint64_t x : tot) s += x;
+    return s;
+}
+
+}  // extern "C"
