@@ -1,0 +1,294 @@
+"""ctypes front end of libaurora_gb300.so (the C ABI of include/aurora_gb300.h).
+
+Device memory and the launch stream come from torch: a Context launches on
+torch's current CUDA stream, so its work is ordered with torch's own. Every
+call raises AuroraError when the library returns a non-zero status. Nothing
+here computes on the CPU: the CUDA library must be built (build.py) and a
+GPU present, otherwise loading fails loudly.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import types as T
+from .build import LIB
+
+_lib = None
+P = ctypes.c_void_p
+U32 = ctypes.c_uint32
+
+
+class AuroraError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("aurora_gb300 status %d: %s" % (status, message))
+        self.status = status
+
+
+SIGNATURES = {
+    "aur_last_error": ([], ctypes.c_char_p),
+    "aur_version": ([], ctypes.c_char_p),
+    "aur_ctx_create": ([ctypes.c_int, P], ctypes.c_int),
+    "aur_ctx_destroy": ([P], ctypes.c_int),
+    "aur_ctx_set_stream": ([P, P], ctypes.c_int),
+    "aur_ctx_get_stream": ([P, P], ctypes.c_int),
+    "aur_ctx_synchronize": ([P], ctypes.c_int),
+    "aur_ctx_sm_count": ([P, P], ctypes.c_int),
+    "aur_nmh_build": ([P, P, U32, P], ctypes.c_int),
+    "aur_nmh_destroy": ([P], ctypes.c_int),
+    "aur_nmh_info": ([P, P, P], ctypes.c_int),
+    "aur_nmh_export": ([P, P, P, P], ctypes.c_int),
+    "aur_nmh_perm_device": ([P, P], ctypes.c_int),
+    "aur_trace_closest": ([P, P, P, U32, P], ctypes.c_int),
+    "aur_trace_any": ([P, P, P, U32, P], ctypes.c_int),
+    "aur_trace_closest_host": ([P, P, P, U32, P], ctypes.c_int),
+    "aur_trace_any_host": ([P, P, P, U32, P], ctypes.c_int),
+    "aur_trace_count_visits": ([P, P, P, U32, P], ctypes.c_int),
+    "aur_scene_create": ([P, P, P, P, U32, P, U32, P, U32, P], ctypes.c_int),
+    "aur_scene_destroy": ([P], ctypes.c_int),
+    "aur_scene_nmh": ([P, P], ctypes.c_int),
+    "aur_scene_set_shaders": ([P, P, P, U32], ctypes.c_int),
+    "aur_scene_set_lights": ([P, P, P, U32], ctypes.c_int),
+    "aur_camera_make": None,  # struct-by-value arguments; not bound
+    "aur_render": ([P, P, P, P, P], ctypes.c_int),
+    "aur_generate_rays": ([P, U32, U32, U32, U32, P, P, P], ctypes.c_int),
+    "aur_raytrace_monte_carlo": ([P, P, P, U32, U32, U32, P, P], ctypes.c_int),
+    "aur_draw_pixels": ([P, U32, U32, ctypes.c_float, P, P], ctypes.c_int),
+    "aur_clear_pixels": ([P, U32, U32, P], ctypes.c_int),
+    "aur_debug_nmh_layout": ([U32, U32, P], ctypes.c_int),
+}
+
+
+def lib():
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise RuntimeError("libaurora_gb300.so is not built (run aurora_gb300.build.build())")
+        L = ctypes.CDLL(LIB)
+        for name, sig in SIGNATURES.items():
+            fn = getattr(L, name)
+            if sig is not None:
+                fn.argtypes, fn.restype = sig
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status != 0:
+        raise AuroraError(status, lib().aur_last_error().decode())
+
+
+def _ptr(x):
+    """Address of a numpy array / torch tensor / None."""
+    if x is None:
+        return P(0)
+    if isinstance(x, np.ndarray):
+        return P(x.ctypes.data)
+    return P(x.data_ptr())
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class Context:
+    """aur_ctx on one device, launching on torch's current stream."""
+
+    def __init__(self, device=0):
+        torch = _torch()
+        self.device = device
+        h = P()
+        check(lib().aur_ctx_create(device, ctypes.byref(h)))
+        self.handle = h
+        torch.cuda.set_device(device)
+        self.use_torch_stream()
+
+    def use_torch_stream(self):
+        torch = _torch()
+        h = torch.cuda.current_stream(self.device).cuda_stream
+        # torch's default stream is the legacy default stream, handle 0; the
+        # ABI reads NULL as "the context's own stream", so name it explicitly
+        # as cudaStreamLegacy ((cudaStream_t)0x1).
+        check(lib().aur_ctx_set_stream(self.handle, P(h if h else 1)))
+
+    def synchronize(self):
+        check(lib().aur_ctx_synchronize(self.handle))
+
+    def sm_count(self):
+        v = ctypes.c_int()
+        check(lib().aur_ctx_sm_count(self.handle, ctypes.byref(v)))
+        return v.value
+
+    def close(self):
+        if self.handle:
+            lib().aur_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Nmh:
+    """aur_nmh built from a device tensor of count*9 float32 vertices."""
+
+    def __init__(self, ctx, vertices_dev, count=None, handle=None):
+        self.ctx = ctx
+        self.owned = handle is None
+        if handle is None:
+            count = vertices_dev.numel() // 9 if count is None else count
+            h = P()
+            check(lib().aur_nmh_build(ctx.handle, _ptr(vertices_dev), count, ctypes.byref(h)))
+            handle = h
+        self.handle = handle
+
+    def info(self):
+        c, lv = U32(), U32()
+        check(lib().aur_nmh_info(self.handle, ctypes.byref(c), ctypes.byref(lv)))
+        return c.value, lv.value
+
+    def export(self, with_vertices=True):
+        count, _ = self.info()
+        perm = np.zeros(count, np.uint32)
+        verts = np.zeros((count, 9), np.float32) if with_vertices else None
+        check(lib().aur_nmh_export(self.ctx.handle, self.handle, _ptr(perm), _ptr(verts)))
+        return perm, verts
+
+    def close(self):
+        if self.handle and self.owned:
+            lib().aur_nmh_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def rays_tensor(rays_np, device="cuda"):
+    """numpy ray_dtype records -> (n, 8) float32 device tensor (same bytes)."""
+    torch = _torch()
+    a = np.ascontiguousarray(rays_np, T.ray_dtype).view(np.float32).reshape(-1, 8)
+    return torch.from_numpy(a).to(device)
+
+
+def trace_closest(ctx, nmh, rays_dev, hits_dev=None):
+    torch = _torch()
+    n = rays_dev.shape[0]
+    if hits_dev is None:
+        hits_dev = torch.empty((n, 4), dtype=torch.float32, device=rays_dev.device)
+    check(lib().aur_trace_closest(ctx.handle, nmh.handle, _ptr(rays_dev), n, _ptr(hits_dev)))
+    return hits_dev
+
+
+def trace_any(ctx, nmh, rays_dev, occ_dev=None):
+    torch = _torch()
+    n = rays_dev.shape[0]
+    if occ_dev is None:
+        occ_dev = torch.empty((n,), dtype=torch.int32, device=rays_dev.device)
+    check(lib().aur_trace_any(ctx.handle, nmh.handle, _ptr(rays_dev), n, _ptr(occ_dev)))
+    return occ_dev
+
+
+def hits_to_numpy(hits_dev):
+    return hits_dev.cpu().numpy().view(T.hit_dtype).reshape(-1)
+
+
+def trace_closest_host(ctx, nmh, rays_host, hits_host):
+    check(lib().aur_trace_closest_host(ctx.handle, nmh.handle, _ptr(rays_host), rays_host.shape[0], _ptr(hits_host)))
+    return hits_host
+
+
+def trace_any_host(ctx, nmh, rays_host, occ_host):
+    check(lib().aur_trace_any_host(ctx.handle, nmh.handle, _ptr(rays_host), rays_host.shape[0], _ptr(occ_host)))
+    return occ_host
+
+
+def count_visits(ctx, nmh, rays_dev):
+    out = (ctypes.c_ulonglong * 2)()
+    check(lib().aur_trace_count_visits(ctx.handle, nmh.handle, _ptr(rays_dev), rays_dev.shape[0], out))
+    return int(out[0]), int(out[1])
+
+
+class Scene:
+    """aur_scene from a scenes.SceneData (host arrays)."""
+
+    def __init__(self, ctx, sd):
+        self.ctx = ctx
+        self.data = sd
+        h = P()
+        check(lib().aur_scene_create(ctx.handle, _ptr(sd.vertices), _ptr(sd.normals), _ptr(sd.shader_ids), sd.count,
+                                     _ptr(sd.shaders), sd.shaders.shape[0], _ptr(sd.lights), sd.lights.shape[0],
+                                     ctypes.byref(h)))
+        self.handle = h
+        nh = P()
+        check(lib().aur_scene_nmh(self.handle, ctypes.byref(nh)))
+        self.nmh = Nmh(ctx, None, handle=nh)
+
+    def set_shaders(self, shaders):
+        shaders = np.ascontiguousarray(shaders, T.shader_dtype)
+        check(lib().aur_scene_set_shaders(self.ctx.handle, self.handle, _ptr(shaders), shaders.shape[0]))
+
+    def set_lights(self, lights):
+        lights = np.ascontiguousarray(lights, T.light_dtype)
+        check(lib().aur_scene_set_lights(self.ctx.handle, self.handle, _ptr(lights), lights.shape[0]))
+
+    def render(self, params, camera=None, accum=None):
+        """Adds the samples of `params` into accum (H, W, 4) float32 device tensor."""
+        torch = _torch()
+        p = np.asarray(params, T.params_dtype).reshape(())
+        if accum is None:
+            accum = torch.zeros((int(p["height"]), int(p["width"]), 4), dtype=torch.float32, device="cuda")
+        cam = np.asarray(self.data.camera if camera is None else camera, T.camera_dtype).reshape(())
+        check(lib().aur_render(self.ctx.handle, self.handle, _ptr(cam), _ptr(p), _ptr(accum)))
+        return accum
+
+    def close(self):
+        if self.handle:
+            self.nmh.handle = None
+            lib().aur_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def generate_rays(ctx, W, H, sample, samples, camera, rays_dev, hits_dev):
+    cam = np.asarray(camera, T.camera_dtype).reshape(())
+    check(lib().aur_generate_rays(ctx.handle, W, H, sample, samples, _ptr(cam), _ptr(rays_dev), _ptr(hits_dev)))
+
+
+def raytrace_monte_carlo(ctx, scene, params, sample, offset, num, rays_dev, hits_dev):
+    p = np.asarray(params, T.params_dtype).reshape(())
+    check(lib().aur_raytrace_monte_carlo(ctx.handle, scene.handle, _ptr(p), sample, offset, num, _ptr(rays_dev),
+                                         _ptr(hits_dev)))
+
+
+def draw_pixels(ctx, W, H, weight, hits_dev, accum_dev):
+    check(lib().aur_draw_pixels(ctx.handle, W, H, weight, _ptr(hits_dev), _ptr(accum_dev)))
+
+
+def clear_pixels(ctx, W, H, accum_dev):
+    check(lib().aur_clear_pixels(ctx.handle, W, H, _ptr(accum_dev)))
+
+
+def debug_nmh_layout(n, k):
+    out = np.zeros(3, np.uint32)
+    check(lib().aur_debug_nmh_layout(n, k, _ptr(out)))
+    return tuple(int(x) for x in out)
+
+
+def exported_symbols():
+    """Names declared in include/aurora_gb300.h (parsed from the header)."""
+    import re
+    hdr = os.path.join(os.path.dirname(LIB), "..", "..", "include", "aurora_gb300.h")
+    text = open(hdr).read()
+    return sorted(set(re.findall(r"^\s*(?:aur_status|const char\*)\s+(aur_\w+)\s*\(", text, re.M)))

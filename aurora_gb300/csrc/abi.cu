@@ -1,0 +1,346 @@
+// abi.cu — contexts, errors, NMH and scene objects of the C ABI.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "aur_internal.h"
+#include "aur_math.cuh"
+
+namespace aur {
+
+namespace {
+thread_local char g_error[512] = "";
+}
+
+aur_status fail(aur_status st, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_error, sizeof(g_error), fmt, ap);
+    va_end(ap);
+    return st;
+}
+
+aur_status cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+    const aur_status st = (e == cudaErrorMemoryAllocation) ? AUR_ERR_OOM
+                          : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? AUR_ERR_NO_DEVICE
+                                                                                          : AUR_ERR_CUDA;
+    const char* base = strrchr(file, '/');
+    return fail(st, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), base ? base + 1 : file, line);
+}
+
+void clear_error() { g_error[0] = 0; }
+
+namespace {
+
+// Reorders per-triangle attributes into NMH order; odd inputs read their
+// padding duplicate from the last triangle.
+__global__ void k_permute_attrs(const uint32_t* __restrict__ perm, uint32_t N, uint32_t count_in,
+                                const float* __restrict__ nin, const uint16_t* __restrict__ sin,
+                                float* __restrict__ nout, uint16_t* __restrict__ sout) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    uint32_t src = perm[i];
+    if (src >= count_in) src = count_in - 1;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) nout[(size_t)i * 9 + q] = nin[(size_t)src * 9 + q];
+    sout[i] = sin[src];
+}
+
+}  // namespace
+}  // namespace aur
+
+using namespace aur;
+
+extern "C" {
+
+const char* aur_last_error(void) { return g_error; }
+
+const char* aur_version(void) { return "aurora_gb300 0.1 (sm_103a)"; }
+
+aur_status aur_ctx_create(int device, aur_ctx** out) {
+    clear_error();
+    AUR_CHECK(out, AUR_ERR_INVALID, "aur_ctx_create: null output");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(AUR_ERR_NO_DEVICE, "aur_ctx_create: no CUDA device (%s)", cudaGetErrorString(e));
+    }
+    AUR_CHECK(device >= 0 && device < ndev, AUR_ERR_INVALID, "aur_ctx_create: device %d of %d", device, ndev);
+    cudaDeviceProp prop;
+    AUR_CUDA(cudaGetDeviceProperties(&prop, device));
+    AUR_CHECK(prop.major == 10 && prop.minor == 3, AUR_ERR_NO_DEVICE,
+              "aur_ctx_create: device %d is sm_%d%d; this build targets sm_103a", device, prop.major, prop.minor);
+    AUR_CUDA(cudaSetDevice(device));
+    aur_ctx* c = new aur_ctx();
+    c->device = device;
+    c->sm_count = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&c->d_flags, 256) != cudaSuccess || cudaMemset(c->d_flags, 0, 256) != cudaSuccess) {
+        e = cudaGetLastError();
+        aur_ctx_destroy(c);
+        return cuda_fail(e, "aur_ctx_create", __FILE__, __LINE__);
+    }
+    for (auto& ev : c->ev) {
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+            e = cudaGetLastError();
+            aur_ctx_destroy(c);
+            return cuda_fail(e, "aur_ctx_create events", __FILE__, __LINE__);
+        }
+    }
+    c->stream = c->own_stream;
+    *out = c;
+    return AUR_OK;
+}
+
+aur_status aur_ctx_destroy(aur_ctx* ctx) {
+    if (!ctx) return AUR_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+    for (auto& s : ctx->pipe) cudaFree(s.ptr);
+    for (auto& s : ctx->out) cudaFree(s.ptr);
+    for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
+    cudaFree(ctx->d_flags);
+    if (ctx->copy_in) cudaStreamDestroy(ctx->copy_in);
+    if (ctx->copy_out) cudaStreamDestroy(ctx->copy_out);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return AUR_OK;
+}
+
+aur_status aur_ctx_set_stream(aur_ctx* ctx, void* cuda_stream) {
+    AUR_CHECK(ctx, AUR_ERR_INVALID, "aur_ctx_set_stream: null context");
+    ctx->stream = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own_stream;
+    return AUR_OK;
+}
+
+aur_status aur_ctx_get_stream(aur_ctx* ctx, void** cuda_stream) {
+    AUR_CHECK(ctx && cuda_stream, AUR_ERR_INVALID, "aur_ctx_get_stream: null argument");
+    *cuda_stream = (void*)ctx->stream;
+    return AUR_OK;
+}
+
+aur_status aur_ctx_synchronize(aur_ctx* ctx) {
+    AUR_CHECK(ctx, AUR_ERR_INVALID, "aur_ctx_synchronize: null context");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    uint32_t flags = 0;
+    AUR_CUDA(cudaMemcpy(&flags, ctx->d_flags, 4, cudaMemcpyDeviceToHost));
+    if (flags) {
+        cudaMemset(ctx->d_flags, 0, 4);
+        return fail(AUR_ERR_OVERFLOW, "a device-side stack would have overflowed (flags 0x%x)", flags);
+    }
+    return AUR_OK;
+}
+
+aur_status aur_ctx_sm_count(aur_ctx* ctx, int* sm_count) {
+    AUR_CHECK(ctx && sm_count, AUR_ERR_INVALID, "aur_ctx_sm_count: null argument");
+    *sm_count = ctx->sm_count;
+    return AUR_OK;
+}
+
+// ------------------------------------------------------------------ NMH
+
+aur_status aur_nmh_build(aur_ctx* ctx, const float* vertices, uint32_t count, aur_nmh** out) {
+    clear_error();
+    return nmh_build_impl(ctx, vertices, count, out);
+}
+
+aur_status aur_nmh_destroy(aur_nmh* nmh) {
+    if (!nmh) return AUR_OK;
+    cudaSetDevice(nmh->device);
+    cudaFree(nmh->node_recs);
+    cudaFree(nmh->perm);
+    cudaFree(nmh->verts);
+    delete nmh;
+    return AUR_OK;
+}
+
+aur_status aur_nmh_info(const aur_nmh* nmh, uint32_t* count, uint32_t* levels) {
+    AUR_CHECK(nmh, AUR_ERR_INVALID, "aur_nmh_info: null NMH");
+    if (count) *count = nmh->count;
+    if (levels) *levels = nmh->levels;
+    return AUR_OK;
+}
+
+aur_status aur_nmh_export(aur_ctx* ctx, const aur_nmh* nmh, uint32_t* perm, float* vertices) {
+    AUR_CHECK(ctx && nmh, AUR_ERR_INVALID, "aur_nmh_export: null context or NMH");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    if (nmh->count == 0) return AUR_OK;
+    if (perm)
+        AUR_CUDA(cudaMemcpyAsync(perm, nmh->perm, (size_t)nmh->count * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (vertices)
+        AUR_CUDA(cudaMemcpyAsync(vertices, nmh->verts, (size_t)nmh->count * 36, cudaMemcpyDeviceToHost, ctx->stream));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    return AUR_OK;
+}
+
+aur_status aur_nmh_perm_device(const aur_nmh* nmh, const uint32_t** perm) {
+    AUR_CHECK(nmh && perm, AUR_ERR_INVALID, "aur_nmh_perm_device: null argument");
+    *perm = nmh->perm;
+    return AUR_OK;
+}
+
+// ---------------------------------------------------------------- scene
+
+static aur_status validate_materials(const aur_shader* shaders, uint32_t ns, const aur_light* lights, uint32_t nl) {
+    AUR_CHECK(ns >= 1 && shaders, AUR_ERR_INVALID, "scene: at least one shader is required (id 0 selects shader 0)");
+    AUR_CHECK(nl == 0 || lights, AUR_ERR_INVALID, "scene: null light table");
+    for (uint32_t i = 0; i < ns; ++i) {
+        AUR_CHECK(shaders[i].texture == 0, AUR_ERR_UNSUPPORTED, "scene: shader %u uses a texture; textures are out of scope",
+                  i);
+        AUR_CHECK(shaders[i].type == AUR_SHADER_LAMBERT || shaders[i].type == AUR_SHADER_PHONG, AUR_ERR_INVALID,
+                  "scene: shader %u has unknown type %d", i, shaders[i].type);
+    }
+    for (uint32_t i = 0; i < nl; ++i) {
+        AUR_CHECK(lights[i].type >= AUR_LIGHT_AMBIENT && lights[i].type <= AUR_LIGHT_AREA, AUR_ERR_INVALID,
+                  "scene: light %u has unknown type %d", i, lights[i].type);
+        AUR_CHECK(lights[i].type != AUR_LIGHT_AREA || lights[i].samples >= 1, AUR_ERR_INVALID,
+                  "scene: area light %u needs samples >= 1", i);
+    }
+    return AUR_OK;
+}
+
+aur_status aur_scene_create(aur_ctx* ctx, const float* vertices, const float* normals, const uint16_t* shader_ids,
+                            uint32_t count, const aur_shader* shaders, uint32_t num_shaders, const aur_light* lights,
+                            uint32_t num_lights, aur_scene** out) {
+    clear_error();
+    AUR_CHECK(ctx && out, AUR_ERR_INVALID, "aur_scene_create: null context or output");
+    AUR_CHECK(count == 0 || vertices, AUR_ERR_INVALID, "aur_scene_create: null vertices");
+    AUR_CHECK(count < kMaxTriangles, AUR_ERR_INVALID, "aur_scene_create: too many triangles (%u)", count);
+    aur_status st = validate_materials(shaders, num_shaders, lights, num_lights);
+    if (st != AUR_OK) return st;
+    if (shader_ids)
+        for (uint32_t i = 0; i < count; ++i)
+            AUR_CHECK(shader_ids[i] <= num_shaders, AUR_ERR_INVALID, "aur_scene_create: triangle %u has shader id %u > %u",
+                      i, shader_ids[i], num_shaders);
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    aur_scene* sc = new aur_scene();
+    auto bail = [&](aur_status e) {
+        aur_scene_destroy(sc);
+        return e;
+    };
+    // host-side normals when absent: the face normal at all three vertices
+    std::vector<float> fn;
+    if (!normals && count) {
+        fn.resize((size_t)count * 9);
+        for (uint32_t i = 0; i < count; ++i) {
+            const float* v = vertices + (size_t)i * 9;
+            const f3 p1 = mk3(v[0], v[3], v[6]), p2 = mk3(v[1], v[4], v[7]), p3 = mk3(v[2], v[5], v[8]);
+            f3 n = cross(p2 - p1, p3 - p1);
+            const float l = length(n);
+            n = l > 0.0f ? n / l : mk3(0.0f, 1.0f, 0.0f);
+            for (int q = 0; q < 3; ++q) { fn[(size_t)i * 9 + 3 * q] = n.x; fn[(size_t)i * 9 + 3 * q + 1] = n.y; fn[(size_t)i * 9 + 3 * q + 2] = n.z; }
+        }
+        normals = fn.data();
+    }
+    std::vector<uint16_t> zeros;
+    if (!shader_ids && count) { zeros.assign(count, 0); shader_ids = zeros.data(); }
+    float* dv = nullptr; float* dn = nullptr; uint16_t* ds = nullptr;
+    if (count) {
+        if (cudaMallocAsync(&dv, (size_t)count * 36, s) != cudaSuccess || cudaMallocAsync(&dn, (size_t)count * 36, s) != cudaSuccess ||
+            cudaMallocAsync(&ds, (size_t)count * 2, s) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFreeAsync(dv, s); cudaFreeAsync(dn, s); cudaFreeAsync(ds, s);
+            return bail(fail(AUR_ERR_OOM, "aur_scene_create: out of device memory"));
+        }
+        cudaMemcpyAsync(dv, vertices, (size_t)count * 36, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(dn, normals, (size_t)count * 36, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(ds, shader_ids, (size_t)count * 2, cudaMemcpyHostToDevice, s);
+    }
+    st = nmh_build_impl(ctx, dv, count, &sc->nmh);
+    if (st != AUR_OK) {
+        cudaFreeAsync(dv, s); cudaFreeAsync(dn, s); cudaFreeAsync(ds, s);
+        return bail(st);
+    }
+    const uint32_t N = sc->nmh->count;
+    if (N) {
+        if (cudaMalloc(&sc->normals, (size_t)N * 36) != cudaSuccess || cudaMalloc(&sc->shader_ids, (size_t)N * 2) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFreeAsync(dv, s); cudaFreeAsync(dn, s); cudaFreeAsync(ds, s);
+            return bail(fail(AUR_ERR_OOM, "aur_scene_create: out of device memory"));
+        }
+        k_permute_attrs<<<(N + 255) / 256, 256, 0, s>>>(sc->nmh->perm, N, count, dn, ds, sc->normals, sc->shader_ids);
+    }
+    cudaFreeAsync(dv, s); cudaFreeAsync(dn, s); cudaFreeAsync(ds, s);
+    if (cudaMalloc(&sc->shaders, sizeof(aur_shader) * num_shaders) != cudaSuccess ||
+        (num_lights && cudaMalloc(&sc->lights, sizeof(aur_light) * num_lights) != cudaSuccess)) {
+        cudaGetLastError();
+        return bail(fail(AUR_ERR_OOM, "aur_scene_create: out of device memory"));
+    }
+    sc->num_shaders = num_shaders;
+    sc->num_lights = num_lights;
+    cudaMemcpyAsync(sc->shaders, shaders, sizeof(aur_shader) * num_shaders, cudaMemcpyHostToDevice, s);
+    if (num_lights) cudaMemcpyAsync(sc->lights, lights, sizeof(aur_light) * num_lights, cudaMemcpyHostToDevice, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "aur_scene_create", __FILE__, __LINE__));
+    *out = sc;
+    return AUR_OK;
+}
+
+aur_status aur_scene_destroy(aur_scene* sc) {
+    if (!sc) return AUR_OK;
+    if (sc->nmh) cudaSetDevice(sc->nmh->device);
+    cudaFree(sc->normals);
+    cudaFree(sc->shader_ids);
+    cudaFree(sc->shaders);
+    cudaFree(sc->lights);
+    aur_nmh_destroy(sc->nmh);
+    delete sc;
+    return AUR_OK;
+}
+
+aur_status aur_scene_nmh(const aur_scene* sc, const aur_nmh** nmh) {
+    AUR_CHECK(sc && nmh, AUR_ERR_INVALID, "aur_scene_nmh: null argument");
+    *nmh = sc->nmh;
+    return AUR_OK;
+}
+
+aur_status aur_scene_set_shaders(aur_ctx* ctx, aur_scene* sc, const aur_shader* shaders, uint32_t n) {
+    AUR_CHECK(ctx && sc, AUR_ERR_INVALID, "aur_scene_set_shaders: null argument");
+    AUR_CHECK(n == sc->num_shaders, AUR_ERR_INVALID, "aur_scene_set_shaders: %u shaders, scene has %u", n,
+              sc->num_shaders);
+    aur_status st = validate_materials(shaders, n, nullptr, 0);
+    if (st != AUR_OK) return st;
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    AUR_CUDA(cudaMemcpyAsync(sc->shaders, shaders, sizeof(aur_shader) * n, cudaMemcpyHostToDevice, ctx->stream));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    return AUR_OK;
+}
+
+aur_status aur_scene_set_lights(aur_ctx* ctx, aur_scene* sc, const aur_light* lights, uint32_t n) {
+    AUR_CHECK(ctx && sc, AUR_ERR_INVALID, "aur_scene_set_lights: null argument");
+    AUR_CHECK(n == sc->num_lights, AUR_ERR_INVALID, "aur_scene_set_lights: %u lights, scene has %u", n, sc->num_lights);
+    for (uint32_t i = 0; i < n; ++i)
+        AUR_CHECK(lights[i].type != AUR_LIGHT_AREA || lights[i].samples >= 1, AUR_ERR_INVALID,
+                  "aur_scene_set_lights: area light %u needs samples >= 1", i);
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    if (n) AUR_CUDA(cudaMemcpyAsync(sc->lights, lights, sizeof(aur_light) * n, cudaMemcpyHostToDevice, ctx->stream));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    return AUR_OK;
+}
+
+aur_status aur_camera_make(aur_float3 position, aur_float3 direction, float fov_x, float fov_y, float aspect,
+                           aur_camera* out) {
+    AUR_CHECK(out, AUR_ERR_INVALID, "aur_camera_make: null output");
+    const f3 fwd = normalize(from(direction));
+    const f3 right = cross(fwd, mk3(0.0f, 1.0f, 0.0f));
+    const f3 up = cross(right, fwd);
+    out->position = position;
+    out->forward = to(fwd);
+    out->right = to(right);
+    out->up = to(up);
+    out->tanfov_x = tanf(fov_x);
+    out->tanfov_y = tanf(fov_y);
+    out->aspect = aspect;
+    return AUR_OK;
+}
+
+}  // extern "C"

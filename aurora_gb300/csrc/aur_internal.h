@@ -1,0 +1,82 @@
+// aur_internal.h — library-internal objects and error plumbing.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/aurora_gb300.h"
+
+namespace aur {
+
+// Thread-local error message; returns `st` for tail calls.
+aur_status fail(aur_status st, const char* fmt, ...);
+aur_status cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+void clear_error();
+
+#define AUR_CUDA(call)                                                                    \
+    do {                                                                                  \
+        cudaError_t aur_e_ = (call);                                                      \
+        if (aur_e_ != cudaSuccess) return ::aur::cuda_fail(aur_e_, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define AUR_CHECK(cond, st, ...)                                  \
+    do {                                                          \
+        if (!(cond)) return ::aur::fail((st), __VA_ARGS__);       \
+    } while (0)
+
+// Grow-only device scratch owned by a context (stream-ordered allocation).
+struct Scratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+// Largest triangle count: node indices carry the axis in their top 2 bits.
+constexpr uint32_t kMaxTriangles = 1u << 30;
+// Traversal stack entries per thread (one per heap level; 2^30 triangles
+// give 30 levels).
+constexpr int kStackDepth = 32;
+
+}  // namespace aur
+
+struct aur_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;       // launch stream (own or caller's)
+    cudaStream_t copy_in = nullptr;      // host-buffer pipelines
+    cudaStream_t copy_out = nullptr;
+    uint32_t* d_flags = nullptr;         // small device scratch: counters, error flags
+    aur::Scratch pipe[2];                // double-buffered device chunks for *_host calls
+    aur::Scratch out[2];
+    cudaEvent_t ev[8] = {};
+};
+
+struct aur_nmh {
+    int device = 0;
+    uint32_t count = 0;       // triangles after even padding
+    uint32_t input_count = 0; // triangles as given
+    uint32_t levels = 0;
+    uint32_t nodes = 0;       // count / 2
+    float4* node_recs = nullptr;  // nodes * 5 float4 (slab, 2 x (v1, e1, e2))
+    uint32_t* perm = nullptr;     // NMH position -> original prim id
+    float* verts = nullptr;       // count * 9, NMH order, reference layout
+};
+
+struct aur_scene {
+    aur_nmh* nmh = nullptr;
+    float* normals = nullptr;         // count * 9, NMH order
+    uint16_t* shader_ids = nullptr;   // count, NMH order
+    aur_shader* shaders = nullptr;
+    uint32_t num_shaders = 0;
+    aur_light* lights = nullptr;
+    uint32_t num_lights = 0;
+};
+
+namespace aur {
+
+aur_status nmh_build_impl(aur_ctx* ctx, const float* vertices, uint32_t count, aur_nmh** out);
+aur_status launch_trace(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits,
+                        uint32_t* occluder, unsigned long long* visit_counter, cudaStream_t stream);
+
+}  // namespace aur

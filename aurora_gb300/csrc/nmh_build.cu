@@ -1,0 +1,709 @@
+// nmh_build.cu — GPU build of the NMH implicit pair-heap.
+//
+// Replaces cudaRebuildNMH (kernels/rebuilder.cu:311-450). The reference
+// re-sorts all triangles twice per level with Thrust (sortTriangles, :262-289)
+// and reads the split count back to the host every level (:255). Here:
+//   1. per-triangle bounds and order-preserving integer keys (:72-91);
+//   2. one stable LSD radix sort per axis of (min-key, prim id) — three
+//      presorted lists;
+//   3. per level, all on the device with closed-form segment offsets:
+//      a. segmented arg-max of the max-key over the current axis' list gives
+//         pair[1]; the first element of each segment is pair[0] (:93-151);
+//      b. the next axis' list is compacted (pairs removed); its position
+//         within the remainder decides left/right (calcPartition sizes,
+//         :40-50, :189-215);
+//      c. the other two lists are stably partitioned left/right.
+//      Stable partitions are warp-ballot scans over 4096-element tiles.
+//   4. each pair is ordered by the last level's axis key (the reference's
+//      final sort, :381-385), then vertices are gathered into NMH order
+//      (applyIndices, :217-245) and traversal node records are written.
+// Every ordering ties by the lower original prim id.
+#include <cstdio>
+
+#include "aur_internal.h"
+#include "aur_math.cuh"
+
+namespace aur {
+namespace {
+
+constexpr uint32_t kDone = 0xFFFFFFFFu;
+constexpr int kThreads = 256;
+constexpr int kTileItems = 16;                       // per thread, scan tiles
+constexpr uint32_t kTile = kThreads * kTileItems;     // 4096
+constexpr int kSortItems = 8;
+constexpr uint32_t kSortTile = kThreads * kSortItems; // 2048
+
+__device__ __forceinline__ uint32_t orderable(float f) {
+    if (f == 0.0f) f = 0.0f;  // -0 and +0 compare equal in the reference's float sorts
+    const uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__host__ __device__ __forceinline__ uint32_t level_of(uint32_t k) {
+#ifdef __CUDA_ARCH__
+    return 31u - (uint32_t)__clz(k + 1u);
+#else
+    return 31u - (uint32_t)__builtin_clz(k + 1u);
+#endif
+}
+
+// Nodes in the subtree of node k of a complete heap of n nodes.
+__host__ __device__ __forceinline__ uint64_t subtree_nodes(uint64_t k, uint64_t n) {
+    uint64_t s = 0;
+    for (uint64_t f = k, w = 1; f < n; f = 2 * f + 1, w <<= 1) s += (w < n - f) ? w : n - f;
+    return s;
+}
+
+// Triangle offset of node k's segment among the active triangles of its
+// level (L0 = first node of the level): twice the subtree sizes of the nodes
+// left of k on the level.
+__host__ __device__ __forceinline__ uint64_t segment_start(uint64_t k, uint64_t L0, uint64_t n) {
+    const uint64_t M = k - L0;
+    uint64_t s = 0;
+    for (uint64_t f = L0, w = 1; f < n; f = 2 * f + 1, w <<= 1) s += (M * w < n - f) ? M * w : n - f;
+    return 2 * s;
+}
+
+// Triangles that go to left children among the nodes left of k on its level:
+// sum over k' in [L0, k) of 2 * subtree_nodes(2k'+1).
+__host__ __device__ __forceinline__ uint64_t left_base(uint64_t k, uint64_t L0, uint64_t n) {
+    const uint64_t M = k - L0;
+    uint64_t s = 0;
+    for (uint64_t g = 2 * L0 + 1, w = 1; g < n; g = 2 * g + 1, w <<= 1) {
+        const uint64_t r = n - g, step = 2 * w;
+        uint64_t full = 0;
+        if (r >= w) { full = (r - w) / step + 1; if (full > M) full = M; }
+        s += full * w;
+        if (full < M && r > full * step) {
+            const uint64_t rem = r - full * step;
+            s += rem < w ? rem : w;
+        }
+    }
+    return 2 * s;
+}
+
+// ------------------------------------------------------------ kernels
+
+// Bounds and sort keys (computeTriangleBounds, rebuilder.cu:72-91). Position
+// i >= count_in is the even-padding duplicate of the last triangle.
+__global__ void k_bounds(const float* __restrict__ V, uint32_t N, size_t S, uint32_t count_in,
+                         float* __restrict__ mn, float* __restrict__ mx, uint32_t* __restrict__ keys,
+                         uint32_t* __restrict__ vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const uint32_t src = i < count_in ? i : count_in - 1;
+    const float* v = V + (size_t)src * 9;
+    float c[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) c[q] = v[q];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float lo = fminf(fminf(c[3 * a], c[3 * a + 1]), c[3 * a + 2]);
+        const float hi = fmaxf(fmaxf(c[3 * a], c[3 * a + 1]), c[3 * a + 2]);
+        mn[a * S + i] = lo;
+        mx[a * S + i] = hi;
+        keys[a * S + i] = orderable(lo);
+        vals[a * S + i] = i;
+    }
+}
+
+// Radix sort, pass histogram: hist[(axis*256 + digit) * nb + block].
+__global__ void k_radix_hist(const uint32_t* __restrict__ keys, uint32_t N, size_t S, int shift,
+                             uint32_t* __restrict__ hist, uint32_t nb) {
+    __shared__ uint32_t h[256];
+    const uint32_t axis = blockIdx.y;
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t* k = keys + axis * S;
+    const uint32_t base = blockIdx.x * kSortTile;
+#pragma unroll
+    for (int i = 0; i < kSortItems; ++i) {
+        const uint32_t idx = base + i * kThreads + threadIdx.x;
+        if (idx < N) atomicAdd(&h[(k[idx] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[((size_t)axis * 256 + threadIdx.x) * nb + blockIdx.x] = h[threadIdx.x];
+}
+
+// Block-wide exclusive scan of one value per thread (blockDim.x <= 1024).
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp, uint32_t& total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < nw ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nw) s_warp[lane] = w;
+    }
+    __syncthreads();
+    total = s_warp[nw - 1];
+    const uint32_t r = x - v + (warp > 0 ? s_warp[warp - 1] : 0);
+    __syncthreads();
+    return r;
+}
+
+// Exclusive scan of each (axis, digit) row of the histogram over blocks;
+// totals[axis*256 + digit] = row sum.
+__global__ void k_radix_scan_rows(uint32_t* __restrict__ hist, uint32_t nb, uint32_t* __restrict__ totals) {
+    __shared__ uint32_t s_warp[32];
+    const size_t row = (size_t)blockIdx.y * 256 + blockIdx.x;
+    uint32_t* h = hist + row * nb;
+    uint32_t carry = 0;
+    for (uint32_t b = 0; b < nb; b += blockDim.x) {
+        const uint32_t i = b + threadIdx.x;
+        const uint32_t v = i < nb ? h[i] : 0;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(v, s_warp, tot);
+        if (i < nb) h[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) totals[row] = carry;
+}
+
+// Stable scatter of one radix pass.
+__global__ void __launch_bounds__(kThreads) k_radix_scatter(const uint32_t* __restrict__ kin,
+                                                            const uint32_t* __restrict__ vin,
+                                                            uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                            uint32_t N, size_t S, int shift,
+                                                            const uint32_t* __restrict__ hist,
+                                                            const uint32_t* __restrict__ totals, uint32_t nb,
+                                                            uint32_t* __restrict__ err) {
+    __shared__ uint32_t s_off[256];
+    __shared__ uint32_t s_base[256];
+    __shared__ uint32_t s_wc[kThreads / 32][256];
+    __shared__ uint32_t s_warp[32];
+    const uint32_t axis = blockIdx.y;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    {
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(totals[axis * 256 + t], s_warp, tot);
+        s_off[t] = ex + hist[((size_t)axis * 256 + t) * nb + blockIdx.x];
+        s_base[t] = 0;
+    }
+    const uint32_t* ki = kin + axis * S;
+    const uint32_t* vi = vin + axis * S;
+    uint32_t* ko = kout + axis * S;
+    uint32_t* vo = vout + axis * S;
+    const uint32_t base = blockIdx.x * kSortTile;
+    for (int i = 0; i < kSortItems; ++i) {
+        const uint32_t idx = base + i * kThreads + t;
+        const bool valid = idx < N;
+        const uint32_t key = valid ? ki[idx] : 0xFFFFFFFFu;
+        const uint32_t val = valid ? vi[idx] : 0u;
+        const uint32_t d = valid ? ((key >> shift) & 255u) : 256u;
+#pragma unroll
+        for (int q = 0; q < 256 / 32; ++q) s_wc[warp][q * 32 + lane] = 0;
+        __syncthreads();
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t rank = __popc(peers & lanemask_lt());
+        if (valid && rank == 0) s_wc[warp][d] = __popc(peers);
+        __syncthreads();
+        {
+            uint32_t run = s_base[t];
+#pragma unroll
+            for (int w = 0; w < kThreads / 32; ++w) {
+                const uint32_t c = s_wc[w][t];
+                s_wc[w][t] = run;
+                run += c;
+            }
+            s_base[t] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t dst = s_off[d] + s_wc[warp][d] + rank;
+            if (dst < N) {
+                ko[dst] = key;
+                vo[dst] = val;
+            } else {
+                atomicOr(err, 4u);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Per-node layout table: segment start, left-child triangle count and
+// left base, for every node of the heap.
+__global__ void k_node_table(uint32_t n, uint32_t* __restrict__ nstart, uint32_t* __restrict__ nnuml,
+                             uint32_t* __restrict__ nlbase) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t L0 = (1u << level_of(k)) - 1u;
+    nstart[k] = (uint32_t)segment_start(k, L0, n);
+    nnuml[k] = (2u * k + 1u < n) ? (uint32_t)(2 * subtree_nodes(2u * k + 1u, n)) : 0u;
+    nlbase[k] = (uint32_t)left_base(k, L0, n);
+}
+
+// Segmented arg-max of (max-key, lowest prim id) over each node's segment,
+// excluding the segment's first element, which is recorded as pair[0]
+// (swapMaxTriangleTPS/TPT, rebuilder.cu:93-151). Each thread owns 16
+// consecutive list positions.
+__global__ void __launch_bounds__(kThreads) k_select(const uint32_t* __restrict__ list, uint32_t M,
+                                                     const float* __restrict__ mxa,
+                                                     const uint32_t* __restrict__ node_of,
+                                                     const uint32_t* __restrict__ nstart, uint32_t L0,
+                                                     unsigned long long* __restrict__ best,
+                                                     uint32_t* __restrict__ pair0) {
+    const uint32_t base = (blockIdx.x * kThreads + threadIdx.x) * kTileItems;
+    const int lane = threadIdx.x & 31;
+    uint32_t cur = kDone;
+    unsigned long long cur_key = 0;
+    bool first_run = true;
+    if (base < M) {
+        const int cnt = (M - base) < (uint32_t)kTileItems ? (int)(M - base) : kTileItems;
+        uint32_t pid[kTileItems];
+        if (cnt == kTileItems) {
+            const uint4* p = reinterpret_cast<const uint4*>(list + base);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint4 v = p[q];
+                pid[4 * q] = v.x; pid[4 * q + 1] = v.y; pid[4 * q + 2] = v.z; pid[4 * q + 3] = v.w;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < kTileItems; ++i) pid[i] = i < cnt ? list[base + i] : 0u;
+        }
+        uint32_t nd[kTileItems];
+#pragma unroll
+        for (int i = 0; i < kTileItems; ++i) nd[i] = i < cnt ? node_of[pid[i]] : kDone;
+#pragma unroll
+        for (int i = 0; i < kTileItems; ++i) {
+            if (i >= cnt) break;
+            const uint32_t k = nd[i];
+            unsigned long long key;
+            if (base + i == nstart[k]) {
+                pair0[k - L0] = pid[i];
+                key = 0ull;
+            } else {
+                key = ((unsigned long long)orderable(mxa[pid[i]]) << 32) | (unsigned long long)(0xFFFFFFFFu - pid[i]);
+            }
+            if (k != cur) {
+                if (cur != kDone) {
+                    if (first_run) atomicMax(&best[cur - L0], cur_key);
+                    else best[cur - L0] = cur_key;       // run wholly inside this thread's range
+                    first_run = false;
+                }
+                cur = k;
+                cur_key = key;
+            } else if (key > cur_key) {
+                cur_key = key;
+            }
+        }
+    }
+    // The last run may continue into the next lanes: segmented max across the
+    // warp (equal node ids are contiguous), heads publish.
+    uint32_t node = cur;
+    unsigned long long key = cur_key;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t on = __shfl_down_sync(0xffffffffu, node, o);
+        const unsigned long long ok = __shfl_down_sync(0xffffffffu, key, o);
+        if (lane + o < 32 && on == node && ok > key) key = ok;
+    }
+    const uint32_t prev = __shfl_up_sync(0xffffffffu, node, 1);
+    if (node != kDone && (lane == 0 || prev != node)) atomicMax(&best[node - L0], key);
+}
+
+// Writes each level node's pair into the heap and retires its triangles.
+__global__ void k_emit_pairs(uint32_t L0, uint32_t L1, unsigned long long* __restrict__ best,
+                             const uint32_t* __restrict__ pair0, uint32_t* __restrict__ heap,
+                             uint32_t* __restrict__ node_of) {
+    const uint32_t k = L0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= L1) return;
+    const uint32_t p0 = pair0[k - L0];
+    const uint32_t p1 = 0xFFFFFFFFu - (uint32_t)(best[k - L0] & 0xFFFFFFFFull);
+    best[k - L0] = 0ull;
+    heap[2 * k] = p0;
+    heap[2 * k + 1] = p1;
+    node_of[p0] = kDone;
+    node_of[p1] = kDone;
+}
+
+struct ListSet {
+    const uint32_t* in[2];
+    uint32_t* out[2];
+};
+
+// Flags of list position j: D = retired (pair), L = goes to a left child.
+template <bool kPart>
+__device__ __forceinline__ void flags_of(uint32_t nd, bool& D, bool& Lf) {
+    D = nd == kDone;
+    Lf = kPart && !D && (nd & 1u);
+}
+
+// Tile counts of (D, L) for list blockIdx.y.
+template <bool kPart>
+__global__ void __launch_bounds__(kThreads) k_tile_count(ListSet ls, uint32_t M, const uint32_t* __restrict__ node_of,
+                                                         uint2* __restrict__ cnt, uint32_t ntiles) {
+    __shared__ uint32_t s_d[kThreads / 32], s_l[kThreads / 32];
+    const uint32_t* list = ls.in[blockIdx.y];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t wbase = blockIdx.x * kTile + warp * 32 * kTileItems;
+    uint32_t cd = 0, cl = 0;
+#pragma unroll 4
+    for (int i = 0; i < kTileItems; ++i) {
+        const uint32_t j = wbase + i * 32 + lane;
+        bool D = false, Lf = false;
+        if (j < M) flags_of<kPart>(node_of[list[j]], D, Lf);
+        cd += __popc(__ballot_sync(0xffffffffu, D));
+        cl += __popc(__ballot_sync(0xffffffffu, Lf));
+    }
+    if (lane == 0) { s_d[warp] = cd; s_l[warp] = cl; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t d = 0, l = 0;
+        for (int w = 0; w < kThreads / 32; ++w) { d += s_d[w]; l += s_l[w]; }
+        cnt[(size_t)blockIdx.y * ntiles + blockIdx.x] = make_uint2(d, l);
+    }
+}
+
+// In-place exclusive scan of the tile counts of list blockIdx.x.
+__global__ void k_tile_scan(uint2* __restrict__ cnt, uint32_t ntiles) {
+    __shared__ uint32_t s_warp[32];
+    uint2* c = cnt + (size_t)blockIdx.x * ntiles;
+    uint32_t cd = 0, cl = 0;
+    for (uint32_t b = 0; b < ntiles; b += blockDim.x) {
+        const uint32_t i = b + threadIdx.x;
+        const uint2 v = i < ntiles ? c[i] : make_uint2(0, 0);
+        uint32_t td, tl;
+        const uint32_t ed = block_exclusive_scan(v.x, s_warp, td);
+        const uint32_t el = block_exclusive_scan(v.y, s_warp, tl);
+        if (i < ntiles) c[i] = make_uint2(cd + ed, cl + el);
+        cd += td;
+        cl += tl;
+    }
+}
+
+// Per-tile scan helper: for each of a warp's 16 items, exclusive global
+// counts of D and L flags before position j.
+template <bool kPart>
+struct TileScan {
+    uint32_t pid[kTileItems];
+    uint32_t nd[kTileItems];
+    uint32_t dmask[kTileItems], lmask[kTileItems];
+    uint32_t wd, wl;  // warp offsets within the tile + tile prefix
+};
+
+template <bool kPart>
+__device__ __forceinline__ void tile_scan(const uint32_t* __restrict__ list, uint32_t M,
+                                          const uint32_t* __restrict__ node_of, uint2 pre, TileScan<kPart>& s) {
+    __shared__ uint32_t s_d[kThreads / 32], s_l[kThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t wbase = blockIdx.x * kTile + warp * 32 * kTileItems;
+#pragma unroll
+    for (int i = 0; i < kTileItems; ++i) {
+        const uint32_t j = wbase + i * 32 + lane;
+        s.pid[i] = j < M ? list[j] : 0u;
+    }
+    uint32_t cd = 0, cl = 0;
+#pragma unroll
+    for (int i = 0; i < kTileItems; ++i) {
+        const uint32_t j = wbase + i * 32 + lane;
+        s.nd[i] = j < M ? node_of[s.pid[i]] : kDone;
+        bool D = false, Lf = false;
+        if (j < M) flags_of<kPart>(s.nd[i], D, Lf);
+        s.dmask[i] = __ballot_sync(0xffffffffu, D);
+        s.lmask[i] = __ballot_sync(0xffffffffu, Lf);
+        cd += __popc(s.dmask[i]);
+        cl += __popc(s.lmask[i]);
+    }
+    if (lane == 0) { s_d[warp] = cd; s_l[warp] = cl; }
+    __syncthreads();
+    uint32_t od = pre.x, ol = pre.y;
+    for (int w = 0; w < warp; ++w) { od += s_d[w]; ol += s_l[w]; }
+    s.wd = od;
+    s.wl = ol;
+}
+
+// Next-axis list: drop retired triangles, classify the rest left/right by
+// their rank in the remainder of their node (rpos < numL -> left child).
+__global__ void __launch_bounds__(kThreads) k_split_next(ListSet ls, uint32_t M, uint32_t* __restrict__ node_of,
+                                                         const uint32_t* __restrict__ nstart,
+                                                         const uint32_t* __restrict__ nnuml, uint32_t L0,
+                                                         const uint2* __restrict__ pre) {
+    TileScan<false> s;
+    tile_scan<false>(ls.in[0], M, node_of, pre[blockIdx.x], s);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t wbase = blockIdx.x * kTile + warp * 32 * kTileItems;
+    const uint32_t lt = lanemask_lt();
+    uint32_t gd = s.wd;
+    uint32_t* out = ls.out[0];
+#pragma unroll
+    for (int i = 0; i < kTileItems; ++i) {
+        const uint32_t j = wbase + i * 32 + lane;
+        const uint32_t GP = gd + __popc(s.dmask[i] & lt);
+        gd += __popc(s.dmask[i]);
+        if (j < M && s.nd[i] != kDone) {
+            const uint32_t k = s.nd[i];
+            const uint32_t rpos = (j - nstart[k]) - (GP - 2u * (k - L0));
+            node_of[s.pid[i]] = rpos < nnuml[k] ? 2u * k + 1u : 2u * k + 2u;
+            out[j - GP] = s.pid[i];
+        }
+    }
+}
+
+// The other two lists: stable partition into left then right child segments.
+__global__ void __launch_bounds__(kThreads) k_partition(ListSet ls, uint32_t M, const uint32_t* __restrict__ node_of,
+                                                        const uint32_t* __restrict__ nstart,
+                                                        const uint32_t* __restrict__ nnuml,
+                                                        const uint32_t* __restrict__ nlbase, uint32_t L0,
+                                                        const uint2* __restrict__ pre, uint32_t ntiles,
+                                                        uint32_t m_next, uint32_t* __restrict__ err) {
+    TileScan<true> s;
+    tile_scan<true>(ls.in[blockIdx.y], M, node_of, pre[(size_t)blockIdx.y * ntiles + blockIdx.x], s);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t wbase = blockIdx.x * kTile + warp * 32 * kTileItems;
+    const uint32_t lt = lanemask_lt();
+    uint32_t gd = s.wd, gl = s.wl;
+    uint32_t* out = ls.out[blockIdx.y];
+#pragma unroll
+    for (int i = 0; i < kTileItems; ++i) {
+        const uint32_t j = wbase + i * 32 + lane;
+        const uint32_t GP = gd + __popc(s.dmask[i] & lt);
+        const uint32_t GL = gl + __popc(s.lmask[i] & lt);
+        gd += __popc(s.dmask[i]);
+        gl += __popc(s.lmask[i]);
+        if (j < M && s.nd[i] != kDone) {
+            const uint32_t c = s.nd[i];
+            const uint32_t k = (c - 1u) >> 1;
+            const uint32_t lb = nlbase[k];
+            uint32_t dst;
+            if (c & 1u) {
+                dst = (nstart[k] - 2u * (k - L0)) + GL - lb;
+            } else {
+                const uint32_t GR = j - GL - GP;
+                dst = nnuml[k] + GR + lb;
+            }
+            if (dst < m_next) out[dst] = s.pid[i];
+            else atomicOr(err, 4u);
+        }
+    }
+}
+
+// Orders each pair by (min-key on the last level's axis, prim id).
+__global__ void k_pair_order(uint32_t n, const uint32_t* __restrict__ heap, const float* __restrict__ mn_last,
+                             uint32_t* __restrict__ perm) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t p = heap[2 * k], q = heap[2 * k + 1];
+    const float kp = mn_last[p], kq = mn_last[q];
+    if (kq < kp || (kq == kp && q < p)) { const uint32_t t = p; p = q; q = t; }
+    perm[2 * k] = p;
+    perm[2 * k + 1] = q;
+}
+
+// applyIndices (rebuilder.cu:217-245) for the vertices, plus the traversal
+// record of each node: slab of the pair on the node's axis
+// (intersect.cuh:106-111) and both triangles as (v1, e1, e2).
+__global__ void k_emit_nodes(const float* __restrict__ V, uint32_t count_in, const uint32_t* __restrict__ perm,
+                             uint32_t n, float* __restrict__ verts, float4* __restrict__ recs) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int a = (int)(level_of(k) % 3u);
+    float c[2][9];
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        const uint32_t pid = perm[2 * k + t];
+        const uint32_t src = pid < count_in ? pid : count_in - 1;
+        const float* v = V + (size_t)src * 9;
+        float* o = verts + (size_t)(2 * k + t) * 9;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) { c[t][q] = v[q]; o[q] = c[t][q]; }
+    }
+    const float lo = fminf(fminf(fminf(c[0][3 * a], c[0][3 * a + 1]), c[0][3 * a + 2]),
+                           fminf(fminf(c[1][3 * a], c[1][3 * a + 1]), c[1][3 * a + 2]));
+    const float hi = fmaxf(fmaxf(fmaxf(c[0][3 * a], c[0][3 * a + 1]), c[0][3 * a + 2]),
+                           fmaxf(fmaxf(c[1][3 * a], c[1][3 * a + 1]), c[1][3 * a + 2]));
+    float r[20];
+    r[0] = lo;
+    r[1] = hi;
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        // layout [x1 x2 x3 y1 y2 y3 z1 z2 z3]: v1 = (c0, c3, c6), v2 = (c1, c4, c7), v3 = (c2, c5, c8)
+        float* o = r + 2 + 9 * t;
+        o[0] = c[t][0]; o[1] = c[t][3]; o[2] = c[t][6];
+        o[3] = c[t][1] - c[t][0]; o[4] = c[t][4] - c[t][3]; o[5] = c[t][7] - c[t][6];
+        o[6] = c[t][2] - c[t][0]; o[7] = c[t][5] - c[t][3]; o[8] = c[t][8] - c[t][6];
+    }
+    float4* rec = recs + (size_t)k * 5;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) rec[q] = make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
+}
+
+inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+uint32_t log2i(uint32_t x) {
+    uint32_t r = (uint32_t)(-1);
+    while (x) { x >>= 1; r++; }
+    return r;
+}
+
+}  // namespace
+
+aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh** out) {
+    AUR_CHECK(ctx && out, AUR_ERR_INVALID, "aur_nmh_build: null context or output pointer");
+    AUR_CHECK(count == 0 || V, AUR_ERR_INVALID, "aur_nmh_build: null vertices for %u triangles", count);
+    AUR_CHECK(count < kMaxTriangles, AUR_ERR_INVALID, "aur_nmh_build: %u triangles exceed the limit of %u", count,
+              kMaxTriangles - 1);
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t N = count + (count & 1u);
+    const uint32_t n = N / 2;
+    aur_nmh* nmh = new aur_nmh();
+    nmh->device = ctx->device;
+    nmh->count = N;
+    nmh->input_count = count;
+    nmh->nodes = n;
+    nmh->levels = n ? log2i(n) + 1 : 0;
+    if (N == 0) { *out = nmh; return AUR_OK; }
+
+    auto cleanup = [&]() {
+        cudaFree(nmh->node_recs);
+        cudaFree(nmh->perm);
+        cudaFree(nmh->verts);
+        delete nmh;
+    };
+    if (cudaMalloc(&nmh->node_recs, (size_t)n * 5 * sizeof(float4)) != cudaSuccess ||
+        cudaMalloc(&nmh->perm, (size_t)N * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&nmh->verts, (size_t)N * 9 * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        cleanup();
+        return fail(AUR_ERR_OOM, "aur_nmh_build: out of device memory for %u triangles", N);
+    }
+
+    cudaStream_t st = ctx->stream;
+    const uint32_t nb = cdiv(N, kSortTile);
+    const uint32_t ntiles = cdiv(N, kTile);
+    // scratch layout (4-byte words unless noted)
+    size_t off = 0;
+    auto take = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
+    // per-axis arrays use a stride S that keeps every axis 256-byte aligned
+    const size_t S = ((size_t)N + 63) & ~(size_t)63;
+    const size_t o_mn = take(3 * S * 4), o_mx = take(3 * S * 4);
+    const size_t o_keys = take(3 * S * 4), o_vals = take(3 * S * 4);
+    const size_t o_k2 = take(3 * S * 4), o_v2 = take(3 * S * 4);
+    const size_t o_nodeof = take((size_t)N * 4), o_heap = take((size_t)N * 4);
+    const size_t o_pair0 = take((size_t)n * 4), o_best = take((size_t)n * 8);
+    const size_t o_ns = take((size_t)n * 4), o_nl = take((size_t)n * 4), o_nlb = take((size_t)n * 4);
+    const size_t o_tiles = take((size_t)2 * ntiles * sizeof(uint2));
+    const size_t o_hist = take((size_t)3 * 256 * nb * 4), o_tot = take((size_t)3 * 256 * 4);
+    char* base = nullptr;
+    if (cudaMallocAsync((void**)&base, off, st) != cudaSuccess) {
+        cudaGetLastError();
+        cleanup();
+        return fail(AUR_ERR_OOM, "aur_nmh_build: out of device memory for %zu bytes of scratch", off);
+    }
+    float* mn = (float*)(base + o_mn);
+    float* mx = (float*)(base + o_mx);
+    uint32_t* keys = (uint32_t*)(base + o_keys);
+    uint32_t* vals = (uint32_t*)(base + o_vals);
+    uint32_t* k2 = (uint32_t*)(base + o_k2);
+    uint32_t* v2 = (uint32_t*)(base + o_v2);
+    uint32_t* node_of = (uint32_t*)(base + o_nodeof);
+    uint32_t* heap = (uint32_t*)(base + o_heap);
+    uint32_t* pair0 = (uint32_t*)(base + o_pair0);
+    unsigned long long* best = (unsigned long long*)(base + o_best);
+    uint32_t* ns = (uint32_t*)(base + o_ns);
+    uint32_t* nl = (uint32_t*)(base + o_nl);
+    uint32_t* nlb = (uint32_t*)(base + o_nlb);
+    uint2* tiles = (uint2*)(base + o_tiles);
+    uint32_t* hist = (uint32_t*)(base + o_hist);
+    uint32_t* tot = (uint32_t*)(base + o_tot);
+
+    k_bounds<<<cdiv(N, 256), 256, 0, st>>>(V, N, S, count, mn, mx, keys, vals);
+    // three stable LSD radix sorts of (min-key, prim id); result in keys/vals
+    for (int pass = 0; pass < 4; ++pass) {
+        const int shift = pass * 8;
+        uint32_t* kin = (pass & 1) ? k2 : keys;
+        uint32_t* vin = (pass & 1) ? v2 : vals;
+        uint32_t* kout = (pass & 1) ? keys : k2;
+        uint32_t* vout = (pass & 1) ? vals : v2;
+        k_radix_hist<<<dim3(nb, 3), kThreads, 0, st>>>(kin, N, S, shift, hist, nb);
+        k_radix_scan_rows<<<dim3(256, 3), 1024, 0, st>>>(hist, nb, tot);
+        k_radix_scatter<<<dim3(nb, 3), kThreads, 0, st>>>(kin, vin, kout, vout, N, S, shift, hist, tot, nb,
+                                                          ctx->d_flags);
+    }
+    // lists: vals = sorted pids per axis (buffer A), v2 = buffer B
+    uint32_t* listA = vals;
+    uint32_t* listB = v2;
+    k_node_table<<<cdiv(n, 256), 256, 0, st>>>(n, ns, nl, nlb);
+    cudaMemsetAsync(node_of, 0, (size_t)N * 4, st);
+    cudaMemsetAsync(best, 0, (size_t)n * 8, st);
+
+    for (uint32_t lv = 0; lv < nmh->levels; ++lv) {
+        const uint32_t L0 = (1u << lv) - 1u;
+        const uint32_t L1 = ((2u << lv) - 1u) < n ? ((2u << lv) - 1u) : n;
+        const uint32_t M = N - 2u * L0;
+        const int a = (int)(lv % 3), b = (int)((lv + 1) % 3), c = (int)((lv + 2) % 3);
+        const uint32_t mt = cdiv(M, kTile);
+        k_select<<<cdiv(M, kTile), kThreads, 0, st>>>(listA + a * S, M, mx + a * S, node_of, ns, L0, best, pair0);
+        k_emit_pairs<<<cdiv(L1 - L0, 256), 256, 0, st>>>(L0, L1, best, pair0, heap, node_of);
+        if (lv + 1 == nmh->levels) break;
+        ListSet sb;
+        sb.in[0] = listA + b * S; sb.out[0] = listB + b * S;
+        sb.in[1] = nullptr; sb.out[1] = nullptr;
+        k_tile_count<false><<<dim3(mt, 1), kThreads, 0, st>>>(sb, M, node_of, tiles, mt);
+        k_tile_scan<<<1, 1024, 0, st>>>(tiles, mt);
+        k_split_next<<<mt, kThreads, 0, st>>>(sb, M, node_of, ns, nl, L0, tiles);
+        ListSet sac;
+        sac.in[0] = listA + a * S; sac.out[0] = listB + a * S;
+        sac.in[1] = listA + c * S; sac.out[1] = listB + c * S;
+        k_tile_count<true><<<dim3(mt, 2), kThreads, 0, st>>>(sac, M, node_of, tiles, mt);
+        k_tile_scan<<<2, 1024, 0, st>>>(tiles, mt);
+        k_partition<<<dim3(mt, 2), kThreads, 0, st>>>(sac, M, node_of, ns, nl, nlb, L0, tiles, mt,
+                                                      M - 2u * (L1 - L0), ctx->d_flags);
+        uint32_t* t = listA; listA = listB; listB = t;
+    }
+    const int al = (int)((nmh->levels - 1) % 3);
+    k_pair_order<<<cdiv(n, 256), 256, 0, st>>>(n, heap, mn + al * S, nmh->perm);
+    k_emit_nodes<<<cdiv(n, 128), 128, 0, st>>>(V, count, nmh->perm, n, nmh->verts, nmh->node_recs);
+    cudaFreeAsync(base, st);
+    cudaError_t e = cudaGetLastError();
+    uint32_t flags = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flags, ctx->d_flags, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cleanup();
+        return cuda_fail(e, "aur_nmh_build kernels", __FILE__, __LINE__);
+    }
+    if (flags & 4u) {
+        cudaMemsetAsync(ctx->d_flags, 0, 4, st);
+        cleanup();
+        return fail(AUR_ERR_CUDA, "aur_nmh_build: internal partition check failed (flags 0x%x)", flags);
+    }
+    *out = nmh;
+    return AUR_OK;
+}
+
+}  // namespace aur
+
+extern "C" {
+
+/* Layout helper exposed for host-side tests of the closed forms:
+ * out[0] = segment start, out[1] = left-child triangles, out[2] = left base
+ * of node k in a heap of n nodes. Pure host code, no device needed. */
+aur_status aur_debug_nmh_layout(uint32_t n, uint32_t k, uint32_t out[3]) {
+    if (!out || k >= n) return aur::fail(AUR_ERR_INVALID, "aur_debug_nmh_layout: k >= n");
+    const uint32_t L0 = (1u << aur::level_of(k)) - 1u;
+    out[0] = (uint32_t)aur::segment_start(k, L0, n);
+    out[1] = (2u * k + 1u < n) ? (uint32_t)(2 * aur::subtree_nodes(2u * k + 1u, n)) : 0u;
+    out[2] = (uint32_t)aur::left_base(k, L0, n);
+    return AUR_OK;
+}
+
+}  // extern "C"

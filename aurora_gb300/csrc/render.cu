@@ -1,0 +1,245 @@
+// render.cu — the plain GPU path tracer and the renderer-helper entry points.
+//
+// The reference renders sample by sample from the host: generateRays, then
+// cudaRaytraceMonteCarlo on 65,536-ray tiles with a device sync per tile,
+// then drawPixels (render/monteCarloRaytracer.cpp:81-120). aur_render fuses
+// ray generation and integration into one kernel over (sample, pixel) pairs
+// of a batch of samples, writes each sample's colour, and a second kernel adds
+// the samples to the frame in sample order — the same additions in the same
+// order as drawPixels, independent of the thread schedule.
+#include <algorithm>
+
+#include "aur_integrate.cuh"
+#include "aur_internal.h"
+
+namespace aur {
+namespace {
+
+constexpr int kRenderThreads = 128;
+
+inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+__device__ __forceinline__ StackRef stack_ref(uint32_t* smem, int cap) {
+    StackRef s;
+    s.idx = smem + threadIdx.x;
+    s.lo = reinterpret_cast<float*>(smem + cap * blockDim.x) + threadIdx.x;
+    s.hi = reinterpret_cast<float*>(smem + 2 * cap * blockDim.x) + threadIdx.x;
+    s.stride = blockDim.x;
+    s.cap = cap;
+    return s;
+}
+
+// colors[b * P + p] = (rgb, hit) of sample s0 + b at pixel p.
+__global__ void __launch_bounds__(kRenderThreads) k_render_samples(SceneView sc, aur_camera cam, aur_render_params p,
+                                                                   uint32_t s0, uint32_t nb, float4* __restrict__ colors,
+                                                                   uint32_t* __restrict__ err, int cap) {
+    extern __shared__ uint32_t smem[];
+    const StackRef stk = stack_ref(smem, cap);
+    const uint64_t P = (uint64_t)p.width * p.height;
+    const uint64_t t = (uint64_t)blockIdx.x * kRenderThreads + threadIdx.x;
+    if (t >= P * nb) return;
+    const uint32_t pix = (uint32_t)(t % P);
+    const uint32_t s = s0 + (uint32_t)(t / P);
+    const PathRay r = camera_ray(cam, p.width, p.height, pix % p.width, pix / p.width, s, p.spp);
+    uint32_t visits = 0;
+    const SampleResult res = integrate(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err);
+    colors[t] = make_float4(res.color.x, res.color.y, res.color.z, res.any_hit ? 1.0f : 0.0f);
+}
+
+// drawPixels (utility.cu:199-219) for nb consecutive samples, in order.
+__global__ void k_accumulate(const float4* __restrict__ colors, uint32_t P, uint32_t nb, float weight,
+                             float4* __restrict__ accum) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= P) return;
+    float4 a = accum[pix];
+    for (uint32_t b = 0; b < nb; ++b) {
+        const float4 c = colors[(size_t)b * P + pix];
+        if (c.w != 0.0f) {
+            a.x += c.x * weight;
+            a.y += c.y * weight;
+            a.z += c.z * weight;
+            a.w += weight;
+        }
+    }
+    accum[pix] = a;
+}
+
+// cudaGenerateRaysKernel(Multisample) (utility.cu:18-77)
+__global__ void k_generate_rays(uint32_t W, uint32_t H, uint32_t sample, uint32_t samples, aur_camera cam,
+                                aur_path_ray* __restrict__ rays, aur_hitpoint* __restrict__ hits) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= W * H) return;
+    const PathRay r = camera_ray(cam, W, H, pix % W, pix / W, sample, samples);
+    aur_path_ray o;
+    o.pos = to(r.pos);
+    o.dir = to(r.dir);
+    o.t = kInfinity;
+    o.weight = 1.0f;
+    o.eta = 1.0f;
+    rays[pix] = o;
+    hits[pix].color = to(mk3(0.0f));
+    hits[pix].triangle_id = -1;
+}
+
+// cudaRaytraceKernel (monteCarloRaytracer.cu:90-113) on caller-provided rays.
+__global__ void __launch_bounds__(kRenderThreads) k_raytrace_mc(SceneView sc, aur_render_params p, uint32_t sample,
+                                                                uint32_t offset, uint32_t num,
+                                                                const aur_path_ray* __restrict__ rays,
+                                                                aur_hitpoint* __restrict__ hits,
+                                                                uint32_t* __restrict__ err, int cap) {
+    extern __shared__ uint32_t smem[];
+    const StackRef stk = stack_ref(smem, cap);
+    const uint32_t t = blockIdx.x * kRenderThreads + threadIdx.x;
+    if (t >= num) return;
+    const uint32_t id = offset + t;
+    const aur_path_ray in = rays[id];
+    PathRay r;
+    r.pos = from(in.pos);
+    r.dir = from(in.dir);
+    r.weight = in.weight;
+    r.eta = in.eta;
+    r.thr = mk3(in.weight);
+    uint32_t visits = 0;
+    const SampleResult res = integrate(sc, p.max_depth, p.mode, p.seed, p.scene_id, id, sample, r, stk, visits, err);
+    aur_hitpoint h = hits[id];
+    h.color = to(from(h.color) + res.color);
+    if (res.any_hit) {
+        h.position = to(res.last_pos);
+        h.wo = to(res.last_wo);
+        h.u = res.last_u;
+        h.v = res.last_v;
+        h.triangle_id = (int32_t)res.last_tri;
+    }
+    hits[id] = h;
+}
+
+__global__ void k_draw_pixels(uint32_t P, float weight, const aur_hitpoint* __restrict__ hits,
+                              float4* __restrict__ accum) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= P) return;
+    const aur_hitpoint h = hits[pix];
+    if (h.triangle_id != -1) {
+        float4 a = accum[pix];
+        a.x += h.color.x * weight;
+        a.y += h.color.y * weight;
+        a.z += h.color.z * weight;
+        a.w += weight;
+        accum[pix] = a;
+    }
+}
+
+}  // namespace
+
+SceneView scene_view(const aur_scene* sc) {
+    SceneView v;
+    v.recs = sc->nmh->node_recs;
+    v.nodes = sc->nmh->nodes;
+    v.perm = sc->nmh->perm;
+    v.normals = sc->normals;
+    v.sids = sc->shader_ids;
+    v.shaders = sc->shaders;
+    v.lights = sc->lights;
+    v.num_lights = sc->num_lights;
+    return v;
+}
+
+aur_status check_params(const aur_render_params* p) {
+    AUR_CHECK(p, AUR_ERR_INVALID, "render: null parameters");
+    AUR_CHECK(p->width > 0 && p->height > 0 && (uint64_t)p->width * p->height < (1ull << 31), AUR_ERR_INVALID,
+              "render: bad frame size %ux%u", p->width, p->height);
+    AUR_CHECK(p->spp >= 1 && p->spp <= 65535, AUR_ERR_INVALID, "render: spp %u outside [1, 65535]", p->spp);
+    AUR_CHECK(p->max_depth <= AUR_MAX_DEPTH, AUR_ERR_INVALID, "render: max_depth %u > %u", p->max_depth,
+              AUR_MAX_DEPTH);
+    AUR_CHECK(p->mode == AUR_MODE_REFERENCE || p->mode == AUR_MODE_PATH, AUR_ERR_INVALID, "render: unknown mode %u",
+              p->mode);
+    const uint32_t end = p->sample_end ? p->sample_end : p->spp;
+    AUR_CHECK(p->sample_begin <= end && end <= p->spp, AUR_ERR_INVALID, "render: sample range [%u, %u) outside spp %u",
+              p->sample_begin, end, p->spp);
+    return AUR_OK;
+}
+
+int stack_cap(const aur_scene* sc) { return (int)sc->nmh->levels + 1; }
+
+}  // namespace aur
+
+using namespace aur;
+
+extern "C" {
+
+aur_status aur_render(aur_ctx* ctx, const aur_scene* scene, const aur_camera* camera, const aur_render_params* params,
+                      float* accum) {
+    clear_error();
+    AUR_CHECK(ctx && scene && camera && accum, AUR_ERR_INVALID, "aur_render: null argument");
+    aur_status st = check_params(params);
+    if (st != AUR_OK) return st;
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    const aur_render_params p = *params;
+    const uint32_t s0 = p.sample_begin, s1 = p.sample_end ? p.sample_end : p.spp;
+    if (s1 == s0) return AUR_OK;
+    const uint64_t P = (uint64_t)p.width * p.height;
+    const uint32_t batch = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(s1 - s0, (1ull << 24) / P));
+    float4* colors = nullptr;
+    AUR_CHECK(cudaMallocAsync(&colors, P * batch * sizeof(float4), ctx->stream) == cudaSuccess, AUR_ERR_OOM,
+              "aur_render: out of device memory");
+    const int cap = stack_cap(scene);
+    const size_t smem = (size_t)3 * cap * kRenderThreads * sizeof(uint32_t);
+    const SceneView sv = scene_view(scene);
+    const float weight = 1.0f / (float)p.spp;
+    for (uint32_t s = s0; s < s1; s += batch) {
+        const uint32_t nb = std::min(batch, s1 - s);
+        k_render_samples<<<cdiv(P * nb, kRenderThreads), kRenderThreads, smem, ctx->stream>>>(
+            sv, *camera, p, s, nb, colors, ctx->d_flags, cap);
+        k_accumulate<<<cdiv(P, 256), 256, 0, ctx->stream>>>(colors, (uint32_t)P, nb, weight, (float4*)accum);
+    }
+    cudaFreeAsync(colors, ctx->stream);
+    AUR_CUDA(cudaGetLastError());
+    return AUR_OK;
+}
+
+aur_status aur_generate_rays(aur_ctx* ctx, uint32_t width, uint32_t height, uint32_t sample_id, uint32_t samples,
+                             const aur_camera* camera, aur_path_ray* rays, aur_hitpoint* hits) {
+    AUR_CHECK(ctx && camera && rays && hits, AUR_ERR_INVALID, "aur_generate_rays: null argument");
+    AUR_CHECK(width && height && samples >= 1 && sample_id < samples, AUR_ERR_INVALID,
+              "aur_generate_rays: bad size or sample");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t P = width * height;
+    k_generate_rays<<<cdiv(P, 256), 256, 0, ctx->stream>>>(width, height, sample_id, samples, *camera, rays, hits);
+    AUR_CUDA(cudaGetLastError());
+    return AUR_OK;
+}
+
+aur_status aur_raytrace_monte_carlo(aur_ctx* ctx, const aur_scene* scene, const aur_render_params* params,
+                                    uint32_t sample_id, uint32_t offset, uint32_t num_rays, aur_path_ray* rays,
+                                    aur_hitpoint* hits) {
+    AUR_CHECK(ctx && scene && params && rays && hits, AUR_ERR_INVALID, "aur_raytrace_monte_carlo: null argument");
+    AUR_CHECK(params->max_depth <= AUR_MAX_DEPTH && params->mode <= AUR_MODE_PATH, AUR_ERR_INVALID,
+              "aur_raytrace_monte_carlo: bad parameters");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    if (num_rays == 0) return AUR_OK;
+    const int cap = stack_cap(scene);
+    const size_t smem = (size_t)3 * cap * kRenderThreads * sizeof(uint32_t);
+    k_raytrace_mc<<<cdiv(num_rays, kRenderThreads), kRenderThreads, smem, ctx->stream>>>(
+        scene_view(scene), *params, sample_id, offset, num_rays, rays, hits, ctx->d_flags, cap);
+    AUR_CUDA(cudaGetLastError());
+    return AUR_OK;
+}
+
+aur_status aur_draw_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float weight, const aur_hitpoint* hits,
+                           float* accum) {
+    AUR_CHECK(ctx && hits && accum, AUR_ERR_INVALID, "aur_draw_pixels: null argument");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t P = width * height;
+    if (P == 0) return AUR_OK;
+    k_draw_pixels<<<cdiv(P, 256), 256, 0, ctx->stream>>>(P, weight, hits, (float4*)accum);
+    AUR_CUDA(cudaGetLastError());
+    return AUR_OK;
+}
+
+aur_status aur_clear_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float* accum) {
+    AUR_CHECK(ctx && accum, AUR_ERR_INVALID, "aur_clear_pixels: null argument");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    AUR_CUDA(cudaMemsetAsync(accum, 0, (size_t)width * height * sizeof(float4), ctx->stream));
+    return AUR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,219 @@
+// trace.cu — closest-hit and any-hit traversal of the NMH pair-heap.
+//
+// Same visit order and arithmetic as intersect() / intersectAny()
+// (kernels/lib/intersect.cuh:36-152): depth-first, near child first by the
+// sign of the ray direction on the child's axis, range clipped cumulatively
+// by each node's slab (ray.cuh:225-237), Moller-Trumbore with culling
+// (ray.cuh:198-223). The node of the reference is 72 scattered bytes read
+// with 24 scalar loads; here it is an 80-byte record (slab + two triangles as
+// v1, e1, e2) read as one 16-byte load for the slab test and four more only
+// when the slab is hit. The traversal stack lives in shared memory: the
+// near child is visited next, only the far child is pushed, so the stack
+// never holds more entries than the heap has levels.
+#include "aur_internal.h"
+#include "aur_math.cuh"
+#include "aur_traverse.cuh"
+
+namespace aur {
+namespace {
+
+constexpr int kTraceThreads = 128;
+
+template <bool kAny, bool kCount>
+__global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restrict__ recs, uint32_t nodes,
+                                                         const uint32_t* __restrict__ perm,
+                                                         const float4* __restrict__ rays, uint32_t n,
+                                                         float4* __restrict__ hits, uint32_t* __restrict__ occ,
+                                                         unsigned long long* __restrict__ visit_counter,
+                                                         uint32_t* __restrict__ err, int cap) {
+    extern __shared__ uint32_t smem[];
+    const int tid = threadIdx.x;
+    StackRef stk;
+    stk.idx = smem + tid;
+    stk.lo = reinterpret_cast<float*>(smem + cap * kTraceThreads) + tid;
+    stk.hi = reinterpret_cast<float*>(smem + 2 * cap * kTraceThreads) + tid;
+    stk.stride = kTraceThreads;
+    stk.cap = cap;
+    const uint32_t i = blockIdx.x * kTraceThreads + tid;
+    uint32_t visits = 0;
+    if (i < n) {
+        const float4 r0 = rays[2 * (size_t)i];
+        const float4 r1 = rays[2 * (size_t)i + 1];
+        const f3 pos = mk3(r0.x, r0.y, r0.z);
+        const f3 dir = mk3(r1.x, r1.y, r1.z);
+        float best_t = r0.w, bu = 0.0f, bv = 0.0f;
+        const uint32_t best = traverse<kAny>(recs, nodes, perm, pos, dir, best_t, bu, bv, stk, visits, err);
+        if (kAny) {
+            occ[i] = best == kNoPrim ? AUR_NO_HIT : perm[best];
+        } else {
+            float4 h;
+            h.x = best == kNoPrim ? r0.w : best_t;
+            h.y = best == kNoPrim ? 0.0f : bu;
+            h.z = best == kNoPrim ? 0.0f : bv;
+            h.w = __uint_as_float(best == kNoPrim ? AUR_NO_HIT : perm[best]);
+            hits[i] = h;
+        }
+    }
+    if (kCount) {
+        unsigned long long v = visits;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((tid & 31) == 0 && v) atomicAdd(visit_counter, v);
+    }
+}
+
+inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+}  // namespace
+
+aur_status launch_trace(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits,
+                        uint32_t* occluder, unsigned long long* visit_counter, cudaStream_t stream) {
+    if (n == 0) return AUR_OK;
+    const int cap = (int)nmh->levels + 1;
+    const size_t smem = (size_t)3 * cap * kTraceThreads * sizeof(uint32_t);
+    const dim3 grid(cdiv(n, kTraceThreads));
+    const float4* r = reinterpret_cast<const float4*>(rays);
+    float4* h = reinterpret_cast<float4*>(hits);
+    uint32_t* err = ctx->d_flags;
+    if (visit_counter) {
+        if (occluder)
+            k_trace<true, true><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r, n,
+                                                                      nullptr, occluder, visit_counter, err, cap);
+        else
+            k_trace<false, true><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r, n,
+                                                                       h, nullptr, visit_counter, err, cap);
+    } else if (occluder) {
+        k_trace<true, false><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r, n,
+                                                                   nullptr, occluder, nullptr, err, cap);
+    } else {
+        k_trace<false, false><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r, n, h,
+                                                                    nullptr, nullptr, err, cap);
+    }
+    AUR_CUDA(cudaGetLastError());
+    return AUR_OK;
+}
+
+}  // namespace aur
+
+using namespace aur;
+
+namespace {
+
+aur_status check_trace_args(aur_ctx* ctx, const aur_nmh* nmh, const void* rays, uint32_t n, const void* out) {
+    AUR_CHECK(ctx && nmh, AUR_ERR_INVALID, "trace: null context or NMH");
+    AUR_CHECK(n == 0 || (rays && out), AUR_ERR_INVALID, "trace: null ray or result buffer for %u rays", n);
+    AUR_CHECK(nmh->device == ctx->device, AUR_ERR_INVALID, "trace: NMH lives on device %d, context on %d",
+              nmh->device, ctx->device);
+    AUR_CHECK(((uintptr_t)rays & 15) == 0 && ((uintptr_t)out & 3) == 0, AUR_ERR_INVALID,
+              "trace: rays must be 16-byte aligned");
+    return AUR_OK;
+}
+
+// Host-buffer pipeline: chunks alternate between two device slots; the H2D
+// copy of chunk c+1 and the D2H copy of chunk c-1 overlap the traversal of c.
+aur_status trace_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, void* out, bool any) {
+    aur_status st = check_trace_args(ctx, nmh, rays, n, out);
+    if (st != AUR_OK) return st;
+    if (n == 0) return AUR_OK;
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t chunk = 1u << 20;
+    const size_t out_sz = any ? sizeof(uint32_t) : sizeof(aur_hit);
+    for (int s = 0; s < 2; ++s) {
+        const size_t need_in = (size_t)chunk * sizeof(aur_ray), need_out = (size_t)chunk * out_sz;
+        if (ctx->pipe[s].bytes < need_in) {
+            cudaFree(ctx->pipe[s].ptr);
+            ctx->pipe[s].ptr = nullptr; ctx->pipe[s].bytes = 0;
+            AUR_CHECK(cudaMalloc(&ctx->pipe[s].ptr, need_in) == cudaSuccess, AUR_ERR_OOM, "trace_host: out of memory");
+            ctx->pipe[s].bytes = need_in;
+        }
+        if (ctx->out[s].bytes < need_out) {
+            cudaFree(ctx->out[s].ptr);
+            ctx->out[s].ptr = nullptr; ctx->out[s].bytes = 0;
+            AUR_CHECK(cudaMalloc(&ctx->out[s].ptr, need_out) == cudaSuccess, AUR_ERR_OOM, "trace_host: out of memory");
+            ctx->out[s].bytes = need_out;
+        }
+    }
+    cudaEvent_t* in_done = ctx->ev;
+    cudaEvent_t* comp_done = ctx->ev + 2;
+    cudaEvent_t* out_done = ctx->ev + 4;
+    // the copy streams start after work already queued on the launch stream
+    AUR_CUDA(cudaEventRecord(ctx->ev[6], ctx->stream));
+    AUR_CUDA(cudaStreamWaitEvent(ctx->copy_in, ctx->ev[6], 0));
+    bool used[2] = {false, false};
+    for (uint32_t c0 = 0, c = 0; c0 < n; c0 += chunk, ++c) {
+        const int s = (int)(c & 1);
+        const uint32_t m = (n - c0) < chunk ? (n - c0) : chunk;
+        if (used[s]) AUR_CUDA(cudaStreamWaitEvent(ctx->copy_in, out_done[s], 0));
+        AUR_CUDA(cudaMemcpyAsync(ctx->pipe[s].ptr, rays + c0, (size_t)m * sizeof(aur_ray), cudaMemcpyHostToDevice,
+                                 ctx->copy_in));
+        AUR_CUDA(cudaEventRecord(in_done[s], ctx->copy_in));
+        AUR_CUDA(cudaStreamWaitEvent(ctx->stream, in_done[s], 0));
+        st = launch_trace(ctx, nmh, (const aur_ray*)ctx->pipe[s].ptr, m, any ? nullptr : (aur_hit*)ctx->out[s].ptr,
+                          any ? (uint32_t*)ctx->out[s].ptr : nullptr, nullptr, ctx->stream);
+        if (st != AUR_OK) return st;
+        AUR_CUDA(cudaEventRecord(comp_done[s], ctx->stream));
+        AUR_CUDA(cudaStreamWaitEvent(ctx->copy_out, comp_done[s], 0));
+        AUR_CUDA(cudaMemcpyAsync((char*)out + (size_t)c0 * out_sz, ctx->out[s].ptr, (size_t)m * out_sz,
+                                 cudaMemcpyDeviceToHost, ctx->copy_out));
+        AUR_CUDA(cudaEventRecord(out_done[s], ctx->copy_out));
+        used[s] = true;
+    }
+    AUR_CUDA(cudaStreamSynchronize(ctx->copy_out));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    return AUR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+aur_status aur_trace_closest(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits) {
+    aur_status st = check_trace_args(ctx, nmh, rays, n, hits);
+    if (st != AUR_OK) return st;
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    return launch_trace(ctx, nmh, rays, n, hits, nullptr, nullptr, ctx->stream);
+}
+
+aur_status aur_trace_any(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, uint32_t* occluder) {
+    aur_status st = check_trace_args(ctx, nmh, rays, n, occluder);
+    if (st != AUR_OK) return st;
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    return launch_trace(ctx, nmh, rays, n, nullptr, occluder, nullptr, ctx->stream);
+}
+
+aur_status aur_trace_closest_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits) {
+    return trace_host(ctx, nmh, rays, n, hits, false);
+}
+
+aur_status aur_trace_any_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, uint32_t* occluder) {
+    return trace_host(ctx, nmh, rays, n, occluder, true);
+}
+
+aur_status aur_trace_count_visits(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n,
+                                  unsigned long long node_visits[2]) {
+    AUR_CHECK(node_visits, AUR_ERR_INVALID, "aur_trace_count_visits: null output");
+    aur_status st = check_trace_args(ctx, nmh, rays, n, rays);
+    if (st != AUR_OK) return st;
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    node_visits[0] = node_visits[1] = 0;
+    if (n == 0) return AUR_OK;
+    void* scratch = nullptr;
+    const size_t bytes = 256 + (size_t)n * sizeof(aur_hit);
+    AUR_CHECK(cudaMallocAsync(&scratch, bytes, ctx->stream) == cudaSuccess, AUR_ERR_OOM,
+              "aur_trace_count_visits: out of memory");
+    unsigned long long* cnt = (unsigned long long*)scratch;
+    aur_hit* hits = (aur_hit*)((char*)scratch + 256);
+    cudaMemsetAsync(cnt, 0, 16, ctx->stream);
+    st = launch_trace(ctx, nmh, rays, n, hits, nullptr, cnt, ctx->stream);
+    if (st == AUR_OK) st = launch_trace(ctx, nmh, rays, n, nullptr, (uint32_t*)hits, cnt + 1, ctx->stream);
+    unsigned long long host[2] = {0, 0};
+    cudaMemcpyAsync(host, cnt, 16, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaFreeAsync(scratch, ctx->stream);
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (st != AUR_OK) return st;
+    node_visits[0] = host[0];
+    node_visits[1] = host[1];
+    return AUR_OK;
+}
+
+}  // extern "C"

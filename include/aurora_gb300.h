@@ -163,7 +163,8 @@ typedef struct aur_ctx aur_ctx;
 aur_status aur_ctx_create(int device, aur_ctx** out);
 aur_status aur_ctx_destroy(aur_ctx* ctx);
 /* Uses `cuda_stream` (a cudaStream_t) for all later work; NULL restores the
- * context's own stream. */
+ * context's own stream. To launch on the legacy default stream pass
+ * cudaStreamLegacy ((cudaStream_t)0x1). */
 aur_status aur_ctx_set_stream(aur_ctx* ctx, void* cuda_stream);
 /* Returns the cudaStream_t the context launches on. */
 aur_status aur_ctx_get_stream(aur_ctx* ctx, void** cuda_stream);

@@ -1,0 +1,88 @@
+"""GPU integrator against the oracle: same counter RNG streams, per-pixel agreement."""
+import numpy as np
+import pytest
+
+import oracle
+from aurora_gb300 import api, scenes, types as T
+from helpers import load_golden
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-4   # per-pixel relative tolerance
+
+
+def _close(a, b):
+    return np.all(np.abs(a - b) <= REL * np.abs(b) + 1e-7)
+
+
+@pytest.mark.parametrize("mode", [T.MODE_REFERENCE, T.MODE_PATH])
+def test_cornell_render_matches_oracle(ctx, mode):
+    sd = scenes.cornell()
+    sc = api.Scene(ctx, sd)
+    p = T.render_params(64, 64, 16, 4, seed=0, mode=mode)
+    img = sc.render(p).cpu().numpy()
+    ref, _ = oracle.render(oracle.NmhScene(sd), p)
+    assert _close(img, ref)
+    assert np.array_equal(img, ref)      # same arithmetic, same order: bit-exact
+
+
+def test_cornell_sphere_render_matches_oracle(ctx):
+    sd = scenes.cornell_sphere(seed=1)
+    sc = api.Scene(ctx, sd)
+    p = T.render_params(48, 48, 4, 4, seed=3, mode=T.MODE_PATH)
+    img = sc.render(p).cpu().numpy()
+    ref, _ = oracle.render(oracle.NmhScene(sd), p)
+    assert _close(img, ref)
+
+
+def test_render_golden_regression(ctx):
+    g = load_golden("cornell")
+    sc = api.Scene(ctx, scenes.cornell())
+    for mode in (T.MODE_REFERENCE, T.MODE_PATH):
+        img = sc.render(T.render_params(32, 32, 4, 4, seed=0, mode=mode)).cpu().numpy()
+        assert _close(img, g["image_mode%d" % mode])
+
+
+def test_helper_entry_points_match_fused_render(ctx):
+    import torch
+    sd = scenes.cornell()
+    sc = api.Scene(ctx, sd)
+    W = H = 40
+    spp = 4
+    p = T.render_params(W, H, spp, 4, seed=2, mode=T.MODE_PATH)
+    fused = sc.render(p).cpu().numpy()
+    rays = torch.zeros((W * H, 9), dtype=torch.float32, device="cuda")
+    hits = torch.zeros((W * H, 12), dtype=torch.float32, device="cuda")
+    accum = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    api.clear_pixels(ctx, W, H, accum)
+    for s in range(spp):
+        api.generate_rays(ctx, W, H, s, spp, sd.camera, rays, hits)
+        for off in range(0, W * H, 512):                  # tiles, as the reference renders
+            api.raytrace_monte_carlo(ctx, sc, p, s, off, min(512, W * H - off), rays, hits)
+        api.draw_pixels(ctx, W, H, 1.0 / spp, hits, accum)
+    assert np.array_equal(accum.cpu().numpy(), fused)
+    prays = rays.cpu().numpy().view(T.path_ray_dtype).reshape(-1)
+    orays = oracle.generate_rays(sd.camera, W, H, spp - 1, spp)
+    assert np.array_equal(prays.view(np.uint32), orays.view(np.uint32))
+
+
+def test_sample_ranges_add_up(ctx):
+    sc = api.Scene(ctx, scenes.cornell())
+    full = sc.render(T.render_params(24, 24, 9, 3, seed=4)).cpu().numpy()
+    acc = sc.render(T.render_params(24, 24, 9, 3, seed=4, sample_begin=0, sample_end=5))
+    acc = sc.render(T.render_params(24, 24, 9, 3, seed=4, sample_begin=5, sample_end=9), accum=acc)
+    assert np.array_equal(acc.cpu().numpy(), full)
+
+
+def test_invalid_arguments_raise(ctx):
+    sd = scenes.cornell()
+    sc = api.Scene(ctx, sd)
+    with pytest.raises(api.AuroraError):
+        sc.render(T.render_params(8, 8, 0, 4))
+    with pytest.raises(api.AuroraError):
+        sc.render(T.render_params(8, 8, 4, 99))
+    bad = sd.shaders.copy()
+    bad["texture"][0] = 1
+    with pytest.raises(api.AuroraError) as e:
+        sc.set_shaders(bad)
+    assert e.value.status == 6

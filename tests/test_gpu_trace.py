@@ -1,0 +1,101 @@
+"""GPU closest-hit / any-hit traversal against the oracle and the reference goldens."""
+import numpy as np
+import pytest
+
+import oracle
+from aurora_gb300 import api, scenes, types as T
+from helpers import closest_vs_reference, hits_equal, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(ctx, V):
+    import torch
+    Vd = torch.from_numpy(np.ascontiguousarray(V, np.float32).reshape(-1)).cuda()
+    nmh = api.Nmh(ctx, Vd, count=V.shape[0])
+    perm, verts = nmh.export()
+    return nmh, perm, verts
+
+
+def _gpu_trace(ctx, nmh, rays):
+    rd = api.rays_tensor(rays)
+    hits = api.hits_to_numpy(api.trace_closest(ctx, nmh, rd))
+    occ = api.trace_any(ctx, nmh, rd).cpu().numpy().view(np.uint32)
+    return hits, occ
+
+
+@pytest.mark.parametrize("name", ["soup2048", "cornell"])
+def test_trace_matches_reference_golden(ctx, name):
+    g = load_golden(name)
+    nmh, perm, verts = _setup(ctx, g["vertices"])
+    hits, occ = _gpu_trace(ctx, nmh, g["rays"])
+    closest_vs_reference(hits, g["ref_tuv"], g["ref_prim"])
+    assert np.array_equal(occ, g["ref_any"])
+    ohits, _, _ = oracle.trace_closest(verts, perm, g["rays"])
+    assert hits_equal(hits, ohits)
+
+
+@pytest.mark.parametrize("n_tris,n_rays", [(1000, 1 << 14), (100000, 1 << 16), (1000000, 1 << 15)])
+def test_trace_matches_oracle(ctx, n_tris, n_rays):
+    V = scenes.random_soup(n_tris, seed=n_tris)
+    nmh, perm, verts = _setup(ctx, V)
+    rays = scenes.microbench_rays(n_rays, seed=3)
+    hits, occ = _gpu_trace(ctx, nmh, rays)
+    ohits, ovis, otot = oracle.trace_closest(verts, perm, rays)
+    oocc, avis, atot = oracle.trace_any(verts, perm, rays)
+    assert hits_equal(hits, ohits)
+    assert np.array_equal(occ, oocc)
+    assert (hits["prim"] != T.NO_HIT).mean() > (0.2 if n_tris >= 100000 else 0.005)
+    assert api.count_visits(ctx, nmh, api.rays_tensor(rays)) == (otot, atot)
+
+
+def test_trace_tie_rule_on_duplicates(ctx):
+    V = scenes.random_soup(4000, seed=5)
+    V[3000:3100] = V[100:200]           # coincident copies: exact ties in t
+    nmh, perm, verts = _setup(ctx, V)
+    rng = np.random.default_rng(0)
+    tri = np.concatenate([np.arange(100, 200), np.arange(3000, 3100)])
+    c = np.stack([V[tri, 0:3].mean(1), V[tri, 3:6].mean(1), V[tri, 6:9].mean(1)], 1)
+    o = c + rng.normal(size=c.shape) * 0.2
+    d = c - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros(len(tri), T.ray_dtype)
+    rays["ox"], rays["oy"], rays["oz"] = o.T
+    rays["dx"], rays["dy"], rays["dz"] = d.T
+    rays["tmax"] = 1e6
+    hits, _ = _gpu_trace(ctx, nmh, rays)
+    ohits, _, _ = oracle.trace_closest(verts, perm, rays)
+    assert hits_equal(hits, ohits)
+    # a ray that hits a coincident pair reports the lower id of the two
+    assert not np.any((hits["prim"] >= 3000) & (hits["prim"] < 3100))
+    assert np.isin(hits["prim"], np.arange(100, 200)).sum() > 50
+
+
+def test_trace_host_buffers_match_device(ctx):
+    V = scenes.random_soup(50000, seed=9)
+    nmh, perm, verts = _setup(ctx, V)
+    rays = scenes.microbench_rays((1 << 20) + 12345, seed=4)    # two pipeline chunks
+    hits_d, occ_d = _gpu_trace(ctx, nmh, rays)
+    hits_h = np.zeros(rays.shape[0], T.hit_dtype)
+    occ_h = np.zeros(rays.shape[0], np.uint32)
+    api.trace_closest_host(ctx, nmh, rays, hits_h)
+    api.trace_any_host(ctx, nmh, rays, occ_h)
+    assert hits_equal(hits_h, hits_d) and np.array_equal(occ_h, occ_d)
+
+
+def test_trace_edge_cases(ctx):
+    import torch
+    V = scenes.random_soup(3, seed=1)                 # odd count -> padded
+    nmh, perm, verts = _setup(ctx, V)
+    rays = scenes.microbench_rays(64, seed=2)
+    rays["tmax"][:8] = 1e-9                            # nothing closer than Epsilon
+    hits, occ = _gpu_trace(ctx, nmh, rays)
+    ohits, _, _ = oracle.trace_closest(verts, perm, rays)
+    assert hits_equal(hits, ohits)
+    assert np.all(hits["prim"][:8] == T.NO_HIT)
+    empty = api.Nmh(ctx, torch.zeros(0, device="cuda"), count=0)
+    h2, o2 = _gpu_trace(ctx, empty, rays)
+    assert np.all(h2["prim"] == T.NO_HIT) and np.all(o2 == T.NO_HIT)
+    assert np.array_equal(h2["t"], rays["tmax"])
+    z = api.trace_closest(ctx, nmh, api.rays_tensor(rays[:0]))
+    assert z.shape[0] == 0
