@@ -1,0 +1,337 @@
+"""Benchmark of the NMH traversal hot path on GB300.
+
+Workload (the traversal microbench): 1,000,000 triangles with centroids
+U[0,1]^3 and LogNormal(-4, 0.5) edges, 2^24 rays (half coherent pinhole rays
+of a 4096x4096 image, even rows; half random origin / uniform direction),
+tmax 1e6. One step = one closest-hit pass over all 2^24 device-resident rays;
+the metric is Mrays/s closest-hit. Inputs are seeded synthetic data.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {gb300,reference}]
+
+Prints one JSON line. `e2e` measures the same metric through the C ABI's
+host-buffer call (aur_trace_closest_host: rays copied in from pinned host
+memory and hits copied back inside the timed region). `roofline` divides the
+algorithmic bytes of a launch (28 B ray in + 16 B hit out + 72 B per node
+fetched, the reference's per-node read) by the kernel's CUDA-event duration.
+`cpu_baseline` times the oracle's C++ restatement of the reference traversal
+on a sample of the same rays on all host cores. With --gpus N > 1 (under
+torchrun) every rank runs an independent replica of the workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_TRIS = 1_000_000
+N_RAYS = 1 << 24
+RAY_IN_BYTES = 28      # origin, direction, tmax
+HIT_OUT_BYTES = 16     # t, u, v, prim
+NODE_BYTES = 72        # two triangles, as the reference fetches per visited node
+METRIC = "Mrays/s closest-hit"
+WORKLOAD = ("traversal microbench: 1M triangles (centroid U[0,1]^3, edges LogNormal(-4,0.5)), 2^24 rays "
+            "(half coherent pinhole 4096x4096 even rows, half random origin/direction), closest hit")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=1 << 22)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling cases only)")
+    ap.add_argument("--profile", action="store_true",
+                    help="small profiling case: one warm-up, one closest-hit and one any-hit launch")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(n_rays=N_RAYS):
+    from aurora_gb300 import scenes
+    V = scenes.random_soup(N_TRIS, seed=0)
+    rays = scenes.microbench_rays(n_rays, seed=1)
+    return V, rays
+
+
+def run_profile(args):
+    """One warm-up, then exactly one closest-hit and one any-hit launch."""
+    import torch
+    from aurora_gb300 import api, build as abuild
+    abuild.build()
+    ctx = api.Context(0)
+    V, rays = workload(args.rays)
+    nmh = api.Nmh(ctx, torch.from_numpy(V.reshape(-1)).cuda(), count=V.shape[0])
+    rays_d = api.rays_tensor(rays)
+    hits_d = api.trace_closest(ctx, nmh, rays_d)
+    torch.cuda.synchronize()
+    api.trace_closest(ctx, nmh, rays_d, hits_d)
+    occ = api.trace_any(ctx, nmh, rays_d)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "closest + any hit", "rays": int(args.rays), "triangles": N_TRIS,
+                      "hit_rate": float((hits_d[:, 3].view(torch.int32) != -1).float().mean().item()),
+                      "occluded": float((occ != -1).float().mean().item())}), flush=True)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    """Per-launch DRAM bytes of the closest-hit kernel from the committed ncu
+    summary, if present (a line 'traffic_bytes_per_launch: N')."""
+    p = os.path.join(ROOT, "profiles", "trace_closest_microbench.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return int(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(verts, perm, rays, sample, seed=7):
+    """The oracle's restatement of intersect() on a random sample of the rays,
+    all host threads."""
+    import oracle
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(rays.shape[0], size=min(sample, rays.shape[0]), replace=False))
+    sub = np.ascontiguousarray(rays[idx])
+    nth = os.cpu_count() or 1
+    oracle.trace_closest(verts, perm, sub[:1024], nthreads=nth)       # warm the library
+    t0 = time.perf_counter()
+    oracle.trace_closest(verts, perm, sub, nthreads=nth)
+    dt = time.perf_counter() - t0
+    return {"value": sub.shape[0] / dt / 1e6, "unit": "Mrays/s", "cores": nth, "kind": "port",
+            "sample": "%d rays drawn uniformly from the 2^24 (seed %d), closest hit, oracle C++ restatement of "
+                      "intersect(), %d host threads, %.1f s" % (sub.shape[0], seed, nth, dt)}
+
+
+def run_reference(args):
+    """--impl reference: the reference traversal restated in C++ (the oracle;
+    the reference's own sources do not travel to this machine) on the host
+    cores, on bounded samples of the same workload."""
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    from aurora_gb300 import scenes  # noqa: F401
+    V, rays = workload()
+    perm, _ = oracle.nmh_build(V)
+    verts = oracle.gather9(V, perm)
+    nth = os.cpu_count() or 1
+    rng = np.random.default_rng(11)
+    per_step = 1 << 17
+    times = []
+    for s in range(args.warmup + args.steps):
+        idx = rng.choice(rays.shape[0], size=per_step, replace=False)
+        sub = np.ascontiguousarray(rays[np.sort(idx)])
+        t0 = time.perf_counter()
+        oracle.trace_closest(verts, perm, sub, nthreads=nth)
+        if s >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    T = sum(times)
+    value = args.steps * per_step / T / 1e6
+    out = {"metric": METRIC, "value": value, "unit": "Mrays/s", "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "triangles": N_TRIS, "rays": N_RAYS,
+                                                    "step_sample_rays": per_step},
+           "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": nth, "kind": "port",
+                            "sample": "%d random rays of the 2^24 per step, oracle C++ restatement of intersect() "
+                                      "(the reference's traversal), %d host threads" % (per_step, nth)},
+           "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.profile:
+        return run_profile(args)
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from aurora_gb300 import api, build as abuild
+    abuild.build()
+    ctx = api.Context(local)
+    V, rays = workload()
+    Vd = torch.from_numpy(V.reshape(-1)).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    nmh = api.Nmh(ctx, Vd, count=V.shape[0])
+    build_ms = 1e3 * (time.perf_counter() - t0)
+    rays_d = api.rays_tensor(rays)
+    hits_d = torch.empty((N_RAYS, 4), dtype=torch.float32, device="cuda")
+    occ_d = torch.empty((N_RAYS,), dtype=torch.int32, device="cuda")
+    visits_closest, visits_any = api.count_visits(ctx, nmh, rays_d)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        api.trace_closest(ctx, nmh, rays_d, hits_d)
+    barrier()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(local) as clk:
+        ev[0].record(stream)
+        for s in range(args.steps):
+            api.trace_closest(ctx, nmh, rays_d, hits_d)
+            ev[s + 1].record(stream)
+        barrier()
+    launch_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[-1])
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * N_RAYS * args.steps / (total_ms * 1e-3) / 1e6
+
+    # any hit, same rays (reported beside the headline)
+    for _ in range(2):
+        api.trace_any(ctx, nmh, rays_d, occ_d)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        api.trace_any(ctx, nmh, rays_d, occ_d)
+    e1.record(stream)
+    barrier()
+    any_ms = e0.elapsed_time(e1) / args.steps
+
+    # end to end through the host-buffer C-ABI call
+    rays_h = torch.empty((N_RAYS, 8), dtype=torch.float32, pin_memory=True)
+    rays_h.numpy()[:] = rays.view(np.float32).reshape(-1, 8)
+    hits_h = torch.empty((N_RAYS, 4), dtype=torch.float32, pin_memory=True)
+    rh, hh = rays_h.numpy(), hits_h.numpy().view(np.uint8).view(
+        np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4")])).reshape(-1)
+    e2e_steps = max(3, min(args.steps, 10))
+    api.trace_closest_host(ctx, nmh, rh.view(np.uint8).view(rays.dtype).reshape(-1), hh)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        api.trace_closest_host(ctx, nmh, rh.view(np.uint8).view(rays.dtype).reshape(-1), hh)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_value = world * N_RAYS / e2e_s / 1e6
+    same = np.array_equal(hits_h.numpy().view(np.uint32), hits_d.cpu().numpy().view(np.uint32))
+
+    peak, peak_kind = load_peaks()
+    alg_bytes = N_RAYS * (RAY_IN_BYTES + HIT_OUT_BYTES) + NODE_BYTES * visits_closest
+    avg_launch_s = statistics.mean(launch_ms) * 1e-3
+    achieved = alg_bytes / avg_launch_s / 1e9
+    clocks = clk.summary()
+    out = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "triangles": N_TRIS, "rays": N_RAYS, "nmh_levels": nmh.info()[1],
+                   "l2": "inputs larger than L2: 512 MiB of rays streamed per step; the 40 MB of node records "
+                         "stay L2-resident as in any traversal",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": load_traffic(), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes_per_launch": alg_bytes, "node_fetches_per_ray": visits_closest / N_RAYS},
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 32,
+                "d2h_bytes_per_step": N_RAYS * 16, "matches_device_result": bool(same)},
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+        "any_hit": {"value": world * N_RAYS / (any_ms * 1e-3) / 1e6, "unit": "Mrays/s", "ms_per_step": any_ms,
+                    "node_fetches_per_ray": visits_any / N_RAYS},
+        "nmh_build_ms": build_ms,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        perm, verts = nmh.export()
+        out["cpu_baseline"] = cpu_baseline(verts, perm, rays, args.cpu_sample)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
