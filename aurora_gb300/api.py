@@ -39,6 +39,7 @@ SIGNATURES = {
     "aur_nmh_info": ([P, P, P], ctypes.c_int),
     "aur_nmh_export": ([P, P, P, P], ctypes.c_int),
     "aur_nmh_perm_device": ([P, P], ctypes.c_int),
+    "aur_nmh_build_noalloc": ([P, U32, P, P, P, P, P], ctypes.c_int),
     "aur_trace_closest": ([P, P, P, U32, P], ctypes.c_int),
     "aur_trace_any": ([P, P, P, U32, P], ctypes.c_int),
     "aur_trace_closest_host": ([P, P, P, U32, P], ctypes.c_int),

@@ -19,6 +19,7 @@
 //      (applyIndices, :217-245) and traversal node records are written.
 // Every ordering ties by the lower original prim id.
 #include <cstdio>
+#include <mutex>
 
 #include "aur_internal.h"
 #include "aur_math.cuh"
@@ -690,6 +691,178 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
     return AUR_OK;
 }
 
+
+// ------------------------------------------------ allocation-free variant
+//
+// aur_nmh_build_noalloc runs the same kernels as aur_nmh_build, but takes all
+// of its scratch from one file-scope device array sized for
+// kNoAllocMaxTriangles triangles, and writes into buffers the caller owns.
+// It exists for callers that cannot allocate device memory themselves: a
+// plug-in whose host application owns the GPU's memory budget and hands out
+// fixed buffers, or a render loop that must not pay for cudaMalloc/cudaFree
+// (which can synchronize the whole device). The array is part of the loaded
+// library, so every GPU that loads the library holds it until the process
+// exits.
+namespace {
+
+constexpr uint32_t kNoAllocMaxTriangles = 1u << 16;
+
+constexpr size_t na_round(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Byte offsets of the scratch regions for N (even) triangles; the same
+// regions as aur_nmh_build's stream-ordered scratch, plus the error flag word.
+struct NoAllocLayout {
+    size_t S, flags, mn, mx, keys, vals, k2, v2, nodeof, heap, pair0, best, ns, nl, nlb, tiles, hist, tot, end;
+};
+
+constexpr NoAllocLayout noalloc_layout(size_t N) {
+    NoAllocLayout L{};
+    const size_t n = N / 2;
+    const size_t nb = (N + kSortTile - 1) / kSortTile;
+    const size_t ntiles = (N + kTile - 1) / kTile;
+    L.S = (N + 63) & ~(size_t)63;
+    size_t off = 0;
+    L.flags = off; off += na_round(4);
+    L.mn = off; off += na_round(3 * L.S * 4);
+    L.mx = off; off += na_round(3 * L.S * 4);
+    L.keys = off; off += na_round(3 * L.S * 4);
+    L.vals = off; off += na_round(3 * L.S * 4);
+    L.k2 = off; off += na_round(3 * L.S * 4);
+    L.v2 = off; off += na_round(3 * L.S * 4);
+    L.nodeof = off; off += na_round(N * 4);
+    L.heap = off; off += na_round(N * 4);
+    L.pair0 = off; off += na_round(n * 4);
+    L.best = off; off += na_round(n * 8);
+    L.ns = off; off += na_round(n * 4);
+    L.nl = off; off += na_round(n * 4);
+    L.nlb = off; off += na_round(n * 4);
+    L.tiles = off; off += na_round(2 * ntiles * 8);
+    L.hist = off; off += na_round(3 * 256 * nb * 4);
+    L.tot = off; off += na_round(3 * 256 * 4);
+    L.end = off;
+    return L;
+}
+
+constexpr size_t kNoAllocScratchBytes = noalloc_layout(kNoAllocMaxTriangles).end;
+
+// Shared by every call on a device; see aur_nmh_build_noalloc.
+static __device__ __align__(256) unsigned char g_nmh_scratch[kNoAllocScratchBytes];
+
+// Device address of g_nmh_scratch per device, looked up once per device with
+// that device current (the host-side name of the array is not a device address).
+constexpr int kMaxDevices = 64;
+unsigned char* g_scratch_addr[kMaxDevices] = {};
+std::mutex g_scratch_mutex;
+
+aur_status noalloc_scratch(int device, unsigned char** out) {
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_addr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_nmh_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_nmh_scratch)", __FILE__, __LINE__);
+        g_scratch_addr[device] = static_cast<unsigned char*>(p);
+    }
+    *out = g_scratch_addr[device];
+    return AUR_OK;
+}
+
+}  // namespace
+
+aur_status nmh_build_noalloc_impl(const float* V, uint32_t count, cudaStream_t st, float4* recs, uint32_t* perm,
+                                  float* verts, uint32_t* levels_out) {
+    AUR_CHECK(count == 0 || (V && recs && perm && verts), AUR_ERR_INVALID,
+              "aur_nmh_build_noalloc: null vertex or output pointer for %u triangles", count);
+    AUR_CHECK(count <= kNoAllocMaxTriangles, AUR_ERR_INVALID,
+              "aur_nmh_build_noalloc: %u triangles exceed this entry point's fixed scratch for %u triangles; "
+              "use aur_nmh_build for larger soups", count, kNoAllocMaxTriangles);
+    AUR_CHECK(((uintptr_t)recs & 15) == 0, AUR_ERR_INVALID, "aur_nmh_build_noalloc: node_records must be 16-byte aligned");
+    const uint32_t N = count + (count & 1u);
+    const uint32_t n = N / 2;
+    const uint32_t levels = n ? log2i(n) + 1 : 0;
+    if (levels_out) *levels_out = levels;
+    if (N == 0) return AUR_OK;
+    int device = 0;
+    AUR_CUDA(cudaGetDevice(&device));
+    AUR_CHECK(device >= 0 && device < kMaxDevices, AUR_ERR_INVALID, "aur_nmh_build_noalloc: device %d", device);
+    unsigned char* base = nullptr;
+    aur_status stt = noalloc_scratch(device, &base);
+    if (stt != AUR_OK) return stt;
+
+    const NoAllocLayout L = noalloc_layout(N);
+    const size_t S = L.S;
+    uint32_t* flags = (uint32_t*)(base + L.flags);
+    float* mn = (float*)(base + L.mn);
+    float* mx = (float*)(base + L.mx);
+    uint32_t* keys = (uint32_t*)(base + L.keys);
+    uint32_t* vals = (uint32_t*)(base + L.vals);
+    uint32_t* k2 = (uint32_t*)(base + L.k2);
+    uint32_t* v2 = (uint32_t*)(base + L.v2);
+    uint32_t* node_of = (uint32_t*)(base + L.nodeof);
+    uint32_t* heap = (uint32_t*)(base + L.heap);
+    uint32_t* pair0 = (uint32_t*)(base + L.pair0);
+    unsigned long long* best = (unsigned long long*)(base + L.best);
+    uint32_t* ns = (uint32_t*)(base + L.ns);
+    uint32_t* nl = (uint32_t*)(base + L.nl);
+    uint32_t* nlb = (uint32_t*)(base + L.nlb);
+    uint2* tiles = (uint2*)(base + L.tiles);
+    uint32_t* hist = (uint32_t*)(base + L.hist);
+    uint32_t* tot = (uint32_t*)(base + L.tot);
+    const uint32_t nb = cdiv(N, kSortTile);
+
+    // The array keeps the previous call's contents: clear what must start at zero.
+    AUR_CUDA(cudaMemsetAsync(flags, 0, 4, st));
+    AUR_CUDA(cudaMemsetAsync(node_of, 0, (size_t)N * 4, st));
+    AUR_CUDA(cudaMemsetAsync(best, 0, (size_t)n * 8, st));
+    k_bounds<<<cdiv(N, 256), 256, 0, st>>>(V, N, S, count, mn, mx, keys, vals);
+    for (int pass = 0; pass < 4; ++pass) {
+        const int shift = pass * 8;
+        uint32_t* kin = (pass & 1) ? k2 : keys;
+        uint32_t* vin = (pass & 1) ? v2 : vals;
+        uint32_t* kout = (pass & 1) ? keys : k2;
+        uint32_t* vout = (pass & 1) ? vals : v2;
+        k_radix_hist<<<dim3(nb, 3), kThreads, 0, st>>>(kin, N, S, shift, hist, nb);
+        k_radix_scan_rows<<<dim3(256, 3), 1024, 0, st>>>(hist, nb, tot);
+        k_radix_scatter<<<dim3(nb, 3), kThreads, 0, st>>>(kin, vin, kout, vout, N, S, shift, hist, tot, nb, flags);
+    }
+    uint32_t* listA = vals;
+    uint32_t* listB = v2;
+    k_node_table<<<cdiv(n, 256), 256, 0, st>>>(n, ns, nl, nlb);
+    for (uint32_t lv = 0; lv < levels; ++lv) {
+        const uint32_t L0 = (1u << lv) - 1u;
+        const uint32_t L1 = ((2u << lv) - 1u) < n ? ((2u << lv) - 1u) : n;
+        const uint32_t M = N - 2u * L0;
+        const int a = (int)(lv % 3), b = (int)((lv + 1) % 3), c = (int)((lv + 2) % 3);
+        const uint32_t mt = cdiv(M, kTile);
+        k_select<<<mt, kThreads, 0, st>>>(listA + a * S, M, mx + a * S, node_of, ns, L0, best, pair0);
+        k_emit_pairs<<<cdiv(L1 - L0, 256), 256, 0, st>>>(L0, L1, best, pair0, heap, node_of);
+        if (lv + 1 == levels) break;
+        ListSet sb;
+        sb.in[0] = listA + b * S; sb.out[0] = listB + b * S;
+        sb.in[1] = nullptr; sb.out[1] = nullptr;
+        k_tile_count<false><<<dim3(mt, 1), kThreads, 0, st>>>(sb, M, node_of, tiles, mt);
+        k_tile_scan<<<1, 1024, 0, st>>>(tiles, mt);
+        k_split_next<<<mt, kThreads, 0, st>>>(sb, M, node_of, ns, nl, L0, tiles);
+        ListSet sac;
+        sac.in[0] = listA + a * S; sac.out[0] = listB + a * S;
+        sac.in[1] = listA + c * S; sac.out[1] = listB + c * S;
+        k_tile_count<true><<<dim3(mt, 2), kThreads, 0, st>>>(sac, M, node_of, tiles, mt);
+        k_tile_scan<<<2, 1024, 0, st>>>(tiles, mt);
+        k_partition<<<dim3(mt, 2), kThreads, 0, st>>>(sac, M, node_of, ns, nl, nlb, L0, tiles, mt, M - 2u * (L1 - L0),
+                                                      flags);
+        uint32_t* t = listA; listA = listB; listB = t;
+    }
+    const int al = (int)((levels - 1) % 3);
+    k_pair_order<<<cdiv(n, 256), 256, 0, st>>>(n, heap, mn + al * S, perm);
+    k_emit_nodes<<<cdiv(n, 128), 128, 0, st>>>(V, count, perm, n, verts, recs);
+    AUR_CUDA(cudaGetLastError());
+    uint32_t h_flags = 0;
+    AUR_CUDA(cudaMemcpyAsync(&h_flags, flags, 4, cudaMemcpyDeviceToHost, st));
+    AUR_CUDA(cudaStreamSynchronize(st));
+    AUR_CHECK(!(h_flags & 4u), AUR_ERR_CUDA, "aur_nmh_build_noalloc: internal partition check failed (flags 0x%x)",
+              h_flags);
+    return AUR_OK;
+}
+
 }  // namespace aur
 
 extern "C" {
@@ -704,6 +877,14 @@ aur_status aur_debug_nmh_layout(uint32_t n, uint32_t k, uint32_t out[3]) {
     out[1] = (2u * k + 1u < n) ? (uint32_t)(2 * aur::subtree_nodes(2u * k + 1u, n)) : 0u;
     out[2] = (uint32_t)aur::left_base(k, L0, n);
     return AUR_OK;
+}
+
+/* Allocation-free NMH build; see include/aurora_gb300.h. */
+aur_status aur_nmh_build_noalloc(const float* vertices, uint32_t count, void* cuda_stream, float* node_records,
+                                 uint32_t* perm, float* nmh_vertices, uint32_t* levels) {
+    aur::clear_error();
+    return aur::nmh_build_noalloc_impl(vertices, count, (cudaStream_t)cuda_stream,
+                                       reinterpret_cast<float4*>(node_records), perm, nmh_vertices, levels);
 }
 
 }  // extern "C"

@@ -194,6 +194,29 @@ aur_status aur_nmh_export(aur_ctx* ctx, const aur_nmh* nmh, uint32_t* perm, floa
 /* Device pointer to the perm array (count uint32) owned by the NMH. */
 aur_status aur_nmh_perm_device(const aur_nmh* nmh, const uint32_t** perm);
 
+/* NMH build that allocates no device memory. This entry point has no
+ * counterpart in the reference. It is for callers that cannot call
+ * cudaMalloc: a plug-in whose host application owns the GPU's memory budget
+ * and only hands out fixed buffers, or a render loop that must not pay for
+ * cudaMalloc / cudaFree, which can synchronize the whole device.
+ * Same result as aur_nmh_build, written into caller-owned device buffers:
+ *   node_records: ((count+1)/2) * 20 floats, 16-byte aligned (traversal records)
+ *   perm:         count + (count & 1) uint32 (NMH position -> original prim id)
+ *   nmh_vertices: (count + (count & 1)) * 9 floats (NMH-ordered soup)
+ *   levels:       host, nullable; receives log2i(count/2)+1
+ * Runs on `cuda_stream` (NULL = the legacy default stream) of the current
+ * device and returns after the build has finished on that stream.
+ * Limit: at most 65,536 triangles; larger counts return AUR_ERR_INVALID. The
+ * scratch is one fixed device array inside the library (about 6 MB), which
+ * every GPU that loads the library holds until the process exits. The first
+ * call on a device looks up that array's device address
+ * (cudaGetSymbolAddress) with the device current; make that first call before
+ * any stream capture. All calls share the array: calls whose work overlaps on
+ * the GPU (other streams, other host threads) race and must be serialized by
+ * the caller. */
+aur_status aur_nmh_build_noalloc(const float* vertices, uint32_t count, void* cuda_stream, float* node_records,
+                                 uint32_t* perm, float* nmh_vertices, uint32_t* levels);
+
 /* --------------------------------------------------------------- traversal */
 
 /* Closest hit for n rays (intersect(), kernels/lib/intersect.cuh:95-152).
