@@ -57,6 +57,12 @@ SIGNATURES = {
     "aur_draw_pixels": ([P, U32, U32, ctypes.c_float, P, P], ctypes.c_int),
     "aur_clear_pixels": ([P, U32, U32, P], ctypes.c_int),
     "aur_debug_nmh_layout": ([U32, U32, P], ctypes.c_int),
+    "aur_batch_create": ([P, P, P, P, U32, P, P], ctypes.c_int),
+    "aur_batch_render": ([P, P, P], ctypes.c_int),
+    "aur_batch_status": ([P, P, P], ctypes.c_int),
+    "aur_batch_tuning": ([P, P], ctypes.c_int),
+    "aur_batch_destroy": ([P], ctypes.c_int),
+    "aur_batch_autotune": ([P, P, P, P, U32, P, P], ctypes.c_int),
 }
 
 
@@ -293,3 +299,76 @@ def exported_symbols():
     hdr = os.path.join(os.path.dirname(LIB), "..", "..", "include", "aurora_gb300.h")
     text = open(hdr).read()
     return sorted(set(re.findall(r"^\s*(?:aur_status|const char\*)\s+(aur_\w+)\s*\(", text, re.M)))
+
+
+tuning_dtype = np.dtype([("paths_in_flight", "<u4"), ("samples_per_wave", "<u4"), ("block_size", "<u4"),
+                         ("blocks_per_sm", "<u4")])
+
+
+def make_tuning(paths_in_flight=0, samples_per_wave=0, block_size=0, blocks_per_sm=0):
+    t = np.zeros((), tuning_dtype)
+    t["paths_in_flight"], t["samples_per_wave"] = paths_in_flight, samples_per_wave
+    t["block_size"], t["blocks_per_sm"] = block_size, blocks_per_sm
+    return t
+
+
+def _batch_arrays(scenes, params, cameras=None):
+    n = len(scenes)
+    handles = (P * n)(*[s.handle for s in scenes])
+    cams = np.stack([np.asarray(s.data.camera if cameras is None else cameras[i], T.camera_dtype).reshape(())
+                     for i, s in enumerate(scenes)])
+    prm = np.stack([np.asarray(p, T.params_dtype).reshape(()) for p in params])
+    return handles, np.ascontiguousarray(cams), np.ascontiguousarray(prm)
+
+
+class Batch:
+    """aur_batch: a wavefront render of several scenes as one CUDA graph."""
+
+    def __init__(self, ctx, scenes, params, tuning=None, cameras=None):
+        self.ctx, self.scenes = ctx, list(scenes)
+        self._h, self._cams, self._prm = _batch_arrays(self.scenes, params, cameras)
+        t = None if tuning is None else np.asarray(tuning, tuning_dtype).reshape(())
+        h = P()
+        check(lib().aur_batch_create(ctx.handle, self._h, _ptr(self._cams), _ptr(self._prm), len(self.scenes),
+                                     _ptr(t) if t is not None else None, ctypes.byref(h)))
+        self.handle = h
+
+    def render(self, accums=None):
+        """Adds every scene's samples into its (H, W, 4) float32 device frame."""
+        torch = _torch()
+        if accums is None:
+            accums = [torch.zeros((int(p["height"]), int(p["width"]), 4), dtype=torch.float32, device="cuda")
+                      for p in self._prm]
+        ptrs = (P * len(accums))(*[a.data_ptr() for a in accums])
+        check(lib().aur_batch_render(self.ctx.handle, self.handle, ptrs))
+        return accums
+
+    def status(self):
+        it = U32()
+        check(lib().aur_batch_status(self.ctx.handle, self.handle, ctypes.byref(it)))
+        return it.value
+
+    def tuning(self):
+        t = np.zeros((), tuning_dtype)
+        check(lib().aur_batch_tuning(self.handle, _ptr(t)))
+        return t
+
+    def close(self):
+        if self.handle:
+            lib().aur_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def autotune(ctx, scenes, params, cameras=None):
+    """Runs the C-side autotuner; returns (tuning record, milliseconds of a 1-spp render)."""
+    h, cams, prm = _batch_arrays(list(scenes), params, cameras)
+    t = np.zeros((), tuning_dtype)
+    ms = ctypes.c_float()
+    check(lib().aur_batch_autotune(ctx.handle, h, _ptr(cams), _ptr(prm), len(scenes), _ptr(t), ctypes.byref(ms)))
+    return t, ms.value

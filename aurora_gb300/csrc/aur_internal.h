@@ -76,6 +76,7 @@ struct aur_scene {
 namespace aur {
 
 aur_status nmh_build_impl(aur_ctx* ctx, const float* vertices, uint32_t count, aur_nmh** out);
+aur_status check_params(const aur_render_params* p);
 aur_status launch_trace(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits,
                         uint32_t* occluder, unsigned long long* visit_counter, cudaStream_t stream);
 

@@ -1,0 +1,756 @@
+// wavefront.cu — batched wavefront path tracer: many scenes, one graph launch.
+//
+// Estimator: exactly the plain integrator's (aur_integrate.cuh, after
+// kernels/monteCarloRaytracer.cu:23-113) for non-specular materials — same
+// counter-RNG keys (seed, scene id) x (pixel, sample, ray index, slot), same
+// arithmetic in the same order — so every path sample has the same value as
+// in aur_render and the frames are identical.
+//
+// Structure (Laine, Karras, Aila, "Megakernels considered harmful", HPG'13):
+// a pool of paths in flight (SoA state) and index queues; each iteration runs
+//   generate  : refill free pool slots with new (scene, pixel, sample) items
+//   extend    : closest hit of every queued path          (persistent kernel)
+//   shade     : BSDF, light samples -> shadow-ray queue, bounce direction
+//   shadow    : any hit of every shadow ray                (persistent kernel)
+//   combine   : Li in the reference's light order, colour += Li * throughput,
+//               continue (next queue) or finish (write the sample, free slot)
+// Samples are processed in waves of `samples_per_wave` per pixel; a wave's
+// samples are added to each frame in sample order afterwards, as drawPixels
+// would. The whole render is one CUDA graph: an outer conditional while node
+// over waves and an inner one over iterations, both bounded by iteration
+// limits that stop the loop and raise an error instead of spinning.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "aur_integrate.cuh"
+#include "aur_internal.h"
+
+namespace aur {
+namespace {
+
+constexpr int kMaxLightSlots = 32;
+
+struct WfScene {
+    const float4* recs;
+    const uint32_t* perm;
+    const float* normals;
+    const uint16_t* sids;
+    const aur_shader* shaders;
+    const aur_light* lights;
+    uint32_t nodes;
+    uint32_t num_lights;
+    uint32_t width, height;
+    uint32_t pix_off;
+    uint32_t scene_id;
+    aur_camera cam;
+};
+
+struct WfCtl {
+    uint32_t wave, num_waves;
+    uint32_t s_begin, s_end, spw;
+    uint32_t s0, nb;
+    uint32_t items_total, items_issued;
+    uint32_t ext_count[2];
+    uint32_t shadow_count;
+    uint32_t free_count;
+    uint32_t iter, iter_limit;
+    uint32_t error;
+    uint32_t total_iters;
+};
+
+struct WfArgs {
+    WfCtl* ctl;
+    const WfScene* scenes;
+    const uint32_t* pix_off;      // num_scenes + 1
+    float4* const* accum;         // per scene frame
+    uint32_t num_scenes;
+    uint32_t P_tot;
+    uint32_t Q;                   // paths in flight
+    uint32_t M;                   // light-sample slots per path
+    uint32_t spp, max_depth, mode, seed;
+    int cap;                      // traversal stack entries
+    // path state, indexed by pool slot
+    float4* o;      // origin
+    float4* d;      // direction
+    float4* thr;    // throughput
+    float4* col;    // colour, w = any hit
+    float4* hit;    // t, u, v, tri
+    uint4* meta;    // item, depth, ray index, scene
+    float4* ndir;   // bounce direction, w = 1 if the path continues
+    float4* nthr;   // bounce throughput
+    float4* fsh;    // f = color1 / pi
+    float4* emi;    // emission
+    float4* cj;     // Q * M light-sample contributions, w = candidate
+    uint32_t* vis;  // visibility bits per slot
+    // queues
+    uint32_t* ext_q[2];
+    uint32_t* free_list;
+    float4* sh_o;   // shadow ray origin, w = tmax
+    float4* sh_d;   // shadow ray direction, w = (slot << 5 | light slot) bits
+    float4* out;    // per wave: nb * P_tot sample colours
+    cudaGraphConditionalHandle h_inner, h_outer;
+};
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
+
+// Warp-aggregated atomic increment.
+__device__ __forceinline__ uint32_t agg_inc(uint32_t* ctr) {
+    const uint32_t m = __activemask();
+    const int leader = __ffs(m) - 1;
+    uint32_t lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    uint32_t base = 0;
+    if ((int)lane_id() == leader) base = atomicAdd(ctr, (uint32_t)__popc(m));
+    base = __shfl_sync(m, base, leader);
+    return base + __popc(m & lt);
+}
+
+__device__ __forceinline__ StackRef wf_stack(uint32_t* smem, int cap) {
+    StackRef s;
+    s.idx = smem + threadIdx.x;
+    s.lo = reinterpret_cast<float*>(smem + cap * blockDim.x) + threadIdx.x;
+    s.hi = reinterpret_cast<float*>(smem + 2 * cap * blockDim.x) + threadIdx.x;
+    s.stride = blockDim.x;
+    s.cap = cap;
+    return s;
+}
+
+__device__ __forceinline__ uint32_t find_scene(const uint32_t* pix_off, uint32_t n, uint32_t gp) {
+    uint32_t lo = 0, hi = n;   // pix_off[lo] <= gp < pix_off[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (pix_off[mid] <= gp) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint32_t grid_threads() { return gridDim.x * blockDim.x; }
+__device__ __forceinline__ uint32_t global_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+
+__device__ __forceinline__ void finish_path(const WfArgs& a, uint32_t slot, uint32_t item, const float4& c) {
+    a.out[item] = c;
+    a.free_list[agg_inc(&a.ctl->free_count)] = slot;
+}
+
+// Wave set-up: sample range, counters, free list; (re)opens the inner loop.
+__global__ void k_wf_setup(WfArgs a) {
+    WfCtl* c = a.ctl;
+    const uint32_t Q = a.Q;
+    for (uint32_t i = global_tid(); i < Q; i += grid_threads()) a.free_list[i] = Q - 1 - i;
+    if (global_tid() == 0) {
+        const uint32_t s0 = c->s_begin + c->wave * c->spw;
+        const uint32_t nb = min(c->spw, c->s_end - s0);
+        c->s0 = s0;
+        c->nb = nb;
+        c->items_total = a.P_tot * nb;
+        c->items_issued = 0;
+        c->ext_count[0] = c->ext_count[1] = 0;
+        c->shadow_count = 0;
+        c->free_count = Q;
+        c->iter = 0;
+        cudaGraphSetConditional(a.h_inner, c->error ? 0u : 1u);
+    }
+}
+
+// Refill free slots with new camera samples, appended to the current queue.
+__global__ void k_wf_generate(WfArgs a) {
+    const WfCtl* c = a.ctl;
+    const uint32_t cur = c->iter & 1u;
+    const uint32_t remaining = c->items_total - c->items_issued;
+    const uint32_t n_new = min(c->free_count, remaining);
+    const uint32_t base = c->ext_count[cur];
+    for (uint32_t i = global_tid(); i < n_new; i += grid_threads()) {
+        const uint32_t slot = a.free_list[c->free_count - 1 - i];
+        const uint32_t item = c->items_issued + i;
+        const uint32_t b = item / a.P_tot, gp = item - b * a.P_tot;
+        const uint32_t s = find_scene(a.pix_off, a.num_scenes, gp);
+        const WfScene& sc = a.scenes[s];
+        const uint32_t lp = gp - sc.pix_off;
+        const PathRay r = camera_ray(sc.cam, sc.width, sc.height, lp % sc.width, lp / sc.width, c->s0 + b, a.spp);
+        a.o[slot] = make_float4(r.pos.x, r.pos.y, r.pos.z, 0.0f);
+        a.d[slot] = make_float4(r.dir.x, r.dir.y, r.dir.z, 0.0f);
+        a.thr[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        a.col[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        a.meta[slot] = make_uint4(item, 0u, 0u, s);
+        a.ext_q[cur][base + i] = slot;
+    }
+}
+
+__global__ void k_wf_generate_commit(WfArgs a) {
+    WfCtl* c = a.ctl;
+    const uint32_t cur = c->iter & 1u;
+    const uint32_t n_new = min(c->free_count, c->items_total - c->items_issued);
+    c->free_count -= n_new;
+    c->items_issued += n_new;
+    c->ext_count[cur] += n_new;
+}
+
+// Closest hit for every queued path.
+__global__ void k_wf_extend(WfArgs a) {
+    extern __shared__ uint32_t smem[];
+    const StackRef stk = wf_stack(smem, a.cap);
+    const WfCtl* c = a.ctl;
+    const uint32_t cur = c->iter & 1u;
+    const uint32_t n = c->ext_count[cur];
+    uint32_t visits = 0;
+    for (uint32_t i = global_tid(); i < n; i += grid_threads()) {
+        const uint32_t slot = a.ext_q[cur][i];
+        const uint32_t s = a.meta[slot].w;
+        const WfScene& sc = a.scenes[s];
+        const float4 o = a.o[slot], d = a.d[slot];
+        float t = kInfinity, u = 0.0f, v = 0.0f;
+        const uint32_t tri = traverse<false>(sc.recs, sc.nodes, sc.perm, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), t, u,
+                                             v, stk, visits, &a.ctl->error);
+        a.hit[slot] = make_float4(t, u, v, __uint_as_float(tri));
+    }
+}
+
+// Shading: misses finish; hits get their light samples (shadow rays queued)
+// and, in path mode, their bounce.
+__global__ void k_wf_shade(WfArgs a) {
+    WfCtl* c = a.ctl;
+    const uint32_t cur = c->iter & 1u;
+    const uint32_t n = c->ext_count[cur];
+    for (uint32_t i = global_tid(); i < n; i += grid_threads()) {
+        const uint32_t slot = a.ext_q[cur][i];
+        const uint4 m = a.meta[slot];
+        const float4 h = a.hit[slot];
+        const uint32_t tri = __float_as_uint(h.w);
+        if (tri == kNoPrim) {
+            finish_path(a, slot, m.x, a.col[slot]);
+            continue;
+        }
+        const WfScene& sc = a.scenes[m.w];
+        const uint32_t item = m.x;
+        const uint32_t b = item / a.P_tot, gp = item - b * a.P_tot;
+        const uint32_t pix = gp - sc.pix_off, sample = c->s0 + b, rix = m.z;
+        const float4 o4 = a.o[slot], d4 = a.d[slot];
+        const f3 pos = mk3(o4.x, o4.y, o4.z), dir = mk3(d4.x, d4.y, d4.z);
+        const f3 position = pos + (dir * h.x);
+        const f3 wo = -dir;
+        const uint32_t sid = sc.sids[tri];
+        const aur_shader* sh = sc.shaders + (sid > 0 ? sid - 1 : 0);
+        SceneView sv;
+        sv.normals = sc.normals;
+        const Bsdf bs = get_bsdf(sv, from(sh->diffuse_color), sh->diffuse, tri, h.y, h.z);
+        const f3 f = bsdf_f(bs);
+        a.fsh[slot] = make_float4(f.x, f.y, f.z, 0.0f);
+        a.emi[slot] = make_float4(sh->emission_color.x, sh->emission_color.y, sh->emission_color.z, 0.0f);
+        a.vis[slot] = 0u;
+        float4* cj = a.cj + (size_t)slot * a.M;
+        uint32_t q = 0;
+        for (uint32_t li = 0; li < sc.num_lights; ++li) {
+            const aur_light& L = sc.lights[li];
+            const uint32_t ns = L.type == AUR_LIGHT_AREA ? (uint32_t)L.samples : 1u;
+            for (uint32_t j = 0; j < ns; ++j, ++q) {
+                f3 wdir;
+                float wt, pdf;
+                const uint32_t lslot = L.type == AUR_LIGHT_AREA ? light_slot(li, j) : 0u;
+                const f3 Lr = sample_light(L, position, a.seed, sc.scene_id, pix, sample, rix, lslot, wdir, wt, pdf);
+                f3 wpos = position;
+                if (L.type == AUR_LIGHT_AREA) {
+                    wpos.x += kEpsilon * wdir.x;
+                    wpos.y += kEpsilon * wdir.y;
+                    wpos.z += kEpsilon * wdir.z;
+                    wt += kEpsilon;
+                }
+                const bool cand = pdf > 0.0f && !zero(Lr) && !zero(f);
+                const f3 cc = f * Lr * fmaxf(0.0f, dot(wdir, bs.N));
+                cj[q] = make_float4(cc.x, cc.y, cc.z, cand ? 1.0f : 0.0f);
+                if (cand) {
+                    const uint32_t e = agg_inc(&c->shadow_count);
+                    a.sh_o[e] = make_float4(wpos.x, wpos.y, wpos.z, wt);
+                    a.sh_d[e] = make_float4(wdir.x, wdir.y, wdir.z, __uint_as_float((slot << 5) | q));
+                }
+            }
+        }
+        // bounce (BSDF::samplef, bsdf.cuh:222-236)
+        float cont = 0.0f;
+        f3 wi = mk3(0.0f), nt = mk3(0.0f);
+        const uint32_t depth = m.y + 1u;
+        if (a.mode == AUR_MODE_PATH && depth <= a.max_depth) {
+            float u1, u2;
+            draw2(a.seed, sc.scene_id, pix, sample, rix, 0u, u1, u2);
+            const f3 lwo = world_to_local(wo, bs.N, bs.S, bs.T);
+            f3 lwi = sample_hemisphere_cosine(u1, u2);
+            if (lwo.z < 0.0f) lwi.z *= -1.0f;
+            const float bpdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
+            wi = local_to_world(lwi, bs.N, bs.S, bs.T);
+            if (bpdf > 0.0f && !zero(f)) {
+                const float4 t4 = a.thr[slot];
+                nt = mk3(t4.x, t4.y, t4.z) * (f * (fabsf(dot(wi, bs.N)) / bpdf));
+                cont = 1.0f;
+            }
+        }
+        a.ndir[slot] = make_float4(wi.x, wi.y, wi.z, cont);
+        a.nthr[slot] = make_float4(nt.x, nt.y, nt.z, 0.0f);
+        a.meta[slot].y = depth;
+    }
+}
+
+// Any hit for every queued shadow ray; unoccluded rays set their bit.
+__global__ void k_wf_shadow(WfArgs a) {
+    extern __shared__ uint32_t smem[];
+    const StackRef stk = wf_stack(smem, a.cap);
+    const uint32_t n = a.ctl->shadow_count;
+    uint32_t visits = 0;
+    for (uint32_t i = global_tid(); i < n; i += grid_threads()) {
+        const float4 o = a.sh_o[i], d = a.sh_d[i];
+        const uint32_t id = __float_as_uint(d.w);
+        const uint32_t slot = id >> 5;
+        const WfScene& sc = a.scenes[a.meta[slot].w];
+        float t = o.w, u = 0.0f, v = 0.0f;
+        const uint32_t occ = traverse<true>(sc.recs, sc.nodes, sc.perm, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), t, u, v,
+                                            stk, visits, &a.ctl->error);
+        if (occ == kNoPrim) atomicOr(&a.vis[slot], 1u << (id & 31u));
+    }
+}
+
+// Li in the reference's order (radiance.cuh:13-80, monteCarloRaytracer.cu:42-52),
+// colour update, then continue or finish.
+__global__ void k_wf_combine(WfArgs a) {
+    WfCtl* c = a.ctl;
+    const uint32_t cur = c->iter & 1u, nxt = cur ^ 1u;
+    const uint32_t n = c->ext_count[cur];
+    for (uint32_t i = global_tid(); i < n; i += grid_threads()) {
+        const uint32_t slot = a.ext_q[cur][i];
+        const float4 h = a.hit[slot];
+        if (__float_as_uint(h.w) == kNoPrim) continue;   // finished in shade
+        const uint4 m = a.meta[slot];
+        const WfScene& sc = a.scenes[m.w];
+        const float4 f4 = a.fsh[slot], e4 = a.emi[slot];
+        const f3 f = mk3(f4.x, f4.y, f4.z);
+        const uint32_t vis = a.vis[slot];
+        const float4* cj = a.cj + (size_t)slot * a.M;
+        f3 Li = mk3(e4.x, e4.y, e4.z);
+        uint32_t q = 0;
+        for (uint32_t li = 0; li < sc.num_lights; ++li) {
+            const aur_light& L = sc.lights[li];
+            if (L.type == AUR_LIGHT_AMBIENT) Li = Li + f * ((from(L.color) * L.intensity) * L.ambient);
+            if (L.type != AUR_LIGHT_AREA) {
+                const float4 v = cj[q];
+                if (v.w != 0.0f && ((vis >> q) & 1u)) Li = Li + mk3(v.x, v.y, v.z);
+                ++q;
+            } else {
+                f3 acc = mk3(0.0f);
+                for (int32_t j = 0; j < L.samples; ++j, ++q) {
+                    f3 Ls = mk3(0.0f);
+                    const float4 v = cj[q];
+                    if (v.w != 0.0f && ((vis >> q) & 1u)) Ls = Ls + mk3(v.x, v.y, v.z);
+                    acc = acc + Ls;
+                }
+                const float ns = (float)L.samples;
+                Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
+            }
+        }
+        const float4 t4 = a.thr[slot];
+        float4 col = a.col[slot];
+        const f3 cc = mk3(col.x, col.y, col.z) + Li * mk3(t4.x, t4.y, t4.z);
+        col = make_float4(cc.x, cc.y, cc.z, 1.0f);
+        const float4 nd = a.ndir[slot];
+        if (nd.w != 0.0f) {
+            const float4 o4 = a.o[slot], d4 = a.d[slot];
+            const f3 position = mk3(o4.x, o4.y, o4.z) + (mk3(d4.x, d4.y, d4.z) * h.x);
+            a.o[slot] = make_float4(position.x, position.y, position.z, 0.0f);
+            a.d[slot] = make_float4(nd.x, nd.y, nd.z, 0.0f);
+            a.thr[slot] = a.nthr[slot];
+            a.col[slot] = col;
+            a.meta[slot].z = m.z + 1u;
+            a.ext_q[nxt][agg_inc(&c->ext_count[nxt])] = slot;
+        } else {
+            finish_path(a, slot, m.x, col);
+        }
+    }
+}
+
+// End of an iteration: clear the consumed queue, decide whether to loop.
+__global__ void k_wf_end(WfArgs a) {
+    WfCtl* c = a.ctl;
+    const uint32_t cur = c->iter & 1u, nxt = cur ^ 1u;
+    c->ext_count[cur] = 0;
+    c->shadow_count = 0;
+    c->iter += 1;
+    c->total_iters += 1;
+    bool more = c->items_issued < c->items_total || c->ext_count[nxt] > 0;
+    if (c->iter > c->iter_limit) { c->error |= 1u; more = false; }
+    if (c->error) more = false;
+    cudaGraphSetConditional(a.h_inner, more ? 1u : 0u);
+}
+
+// drawPixels for the wave's samples, in sample order.
+__global__ void k_wf_accumulate(WfArgs a) {
+    const WfCtl* c = a.ctl;
+    const float weight = 1.0f / (float)a.spp;
+    const uint32_t nb = c->nb;
+    for (uint32_t gp = global_tid(); gp < a.P_tot; gp += grid_threads()) {
+        const uint32_t s = find_scene(a.pix_off, a.num_scenes, gp);
+        float4* acc = a.accum[s] + (gp - a.pix_off[s]);
+        float4 v = *acc;
+        for (uint32_t b = 0; b < nb; ++b) {
+            const float4 cv = a.out[(size_t)b * a.P_tot + gp];
+            if (cv.w != 0.0f) {
+                v.x += cv.x * weight;
+                v.y += cv.y * weight;
+                v.z += cv.z * weight;
+                v.w += weight;
+            }
+        }
+        *acc = v;
+    }
+}
+
+__global__ void k_wf_next_wave(WfArgs a) {
+    WfCtl* c = a.ctl;
+    c->wave += 1;
+    cudaGraphSetConditional(a.h_outer, (c->wave < c->num_waves && !c->error) ? 1u : 0u);
+}
+
+inline uint32_t cdiv(uint64_t x, uint64_t y) { return (uint32_t)((x + y - 1) / y); }
+
+}  // namespace
+}  // namespace aur
+
+using namespace aur;
+
+struct aur_batch {
+    int device = 0;
+    uint32_t num_scenes = 0;
+    aur_render_params params{};
+    aur_wavefront_tuning tuning{};
+    WfArgs args{};
+    void* mem = nullptr;             // one allocation for state, queues, tables
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cap_stream = nullptr;
+    uint32_t grid = 0, block = 0;
+    size_t smem = 0;
+    std::vector<float4*> accum_host;
+};
+
+namespace {
+
+aur_status make_graph(aur_batch* bt) {
+    WfArgs& a = bt->args;
+    AUR_CUDA(cudaGraphCreate(&bt->graph, 0));
+    AUR_CUDA(cudaGraphConditionalHandleCreate(&a.h_outer, bt->graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams outer = {};
+    outer.type = cudaGraphNodeTypeConditional;
+    outer.conditional.handle = a.h_outer;
+    outer.conditional.type = cudaGraphCondTypeWhile;
+    outer.conditional.size = 1;
+    cudaGraphNode_t outer_node;
+    AUR_CUDA(cudaGraphAddNode(&outer_node, bt->graph, nullptr, nullptr, 0, &outer));
+    cudaGraph_t wave_body = outer.conditional.phGraph_out[0];
+    // the inner handle belongs to the wave body; create it before capturing
+    AUR_CUDA(cudaGraphConditionalHandleCreate(&a.h_inner, wave_body, 1, cudaGraphCondAssignDefault));
+    const uint32_t g = bt->grid, bs = bt->block;
+    cudaStream_t s = bt->cap_stream;
+    // wave body part 1: set-up
+    AUR_CUDA(cudaStreamBeginCaptureToGraph(s, wave_body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    k_wf_setup<<<g, bs, 0, s>>>(a);
+    cudaGraph_t tmp;
+    AUR_CUDA(cudaStreamEndCapture(s, &tmp));
+    size_t nn = 0;
+    AUR_CUDA(cudaGraphGetNodes(wave_body, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    AUR_CUDA(cudaGraphGetNodes(wave_body, nodes.data(), &nn));
+    AUR_CHECK(nn == 1, AUR_ERR_CUDA, "wavefront graph: unexpected set-up node count %zu", nn);
+    cudaGraphNode_t setup_node = nodes[0];
+    // inner loop node
+    cudaGraphNodeParams inner = {};
+    inner.type = cudaGraphNodeTypeConditional;
+    inner.conditional.handle = a.h_inner;
+    inner.conditional.type = cudaGraphCondTypeWhile;
+    inner.conditional.size = 1;
+    cudaGraphNode_t inner_node;
+    AUR_CUDA(cudaGraphAddNode(&inner_node, wave_body, &setup_node, nullptr, 1, &inner));
+    cudaGraph_t iter_body = inner.conditional.phGraph_out[0];
+    AUR_CUDA(cudaStreamBeginCaptureToGraph(s, iter_body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    k_wf_generate<<<g, bs, 0, s>>>(a);
+    k_wf_generate_commit<<<1, 1, 0, s>>>(a);
+    k_wf_extend<<<g, bs, bt->smem, s>>>(a);
+    k_wf_shade<<<g, bs, 0, s>>>(a);
+    k_wf_shadow<<<g, bs, bt->smem, s>>>(a);
+    k_wf_combine<<<g, bs, 0, s>>>(a);
+    k_wf_end<<<1, 1, 0, s>>>(a);
+    AUR_CUDA(cudaStreamEndCapture(s, &tmp));
+    // wave body part 2: accumulate after the inner loop
+    AUR_CUDA(cudaStreamBeginCaptureToGraph(s, wave_body, &inner_node, nullptr, 1, cudaStreamCaptureModeThreadLocal));
+    k_wf_accumulate<<<g, bs, 0, s>>>(a);
+    k_wf_next_wave<<<1, 1, 0, s>>>(a);
+    AUR_CUDA(cudaStreamEndCapture(s, &tmp));
+    AUR_CUDA(cudaGraphInstantiate(&bt->exec, bt->graph, 0));
+    return AUR_OK;
+}
+
+void batch_free(aur_batch* bt) {
+    if (!bt) return;
+    cudaSetDevice(bt->device);
+    if (bt->exec) cudaGraphExecDestroy(bt->exec);
+    if (bt->graph) cudaGraphDestroy(bt->graph);
+    if (bt->cap_stream) cudaStreamDestroy(bt->cap_stream);
+    cudaFree(bt->mem);
+    delete bt;
+}
+
+}  // namespace
+
+extern "C" {
+
+aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const aur_camera* cameras,
+                            const aur_render_params* params, uint32_t num_scenes, const aur_wavefront_tuning* tuning,
+                            aur_batch** out) {
+    clear_error();
+    AUR_CHECK(ctx && scenes && cameras && params && out && num_scenes > 0, AUR_ERR_INVALID,
+              "aur_batch_create: null argument or no scenes");
+    const aur_render_params& p0 = params[0];
+    aur_status st = check_params(&p0);
+    if (st != AUR_OK) return st;
+    uint64_t P_tot = 0;
+    uint32_t M = 1, cap = 2;
+    std::vector<WfScene> table(num_scenes);
+    std::vector<uint32_t> pix_off(num_scenes + 1);
+    for (uint32_t i = 0; i < num_scenes; ++i) {
+        const aur_scene* sc = scenes[i];
+        const aur_render_params& p = params[i];
+        AUR_CHECK(sc, AUR_ERR_INVALID, "aur_batch_create: scene %u is null", i);
+        st = check_params(&p);
+        if (st != AUR_OK) return st;
+        AUR_CHECK(p.spp == p0.spp && p.max_depth == p0.max_depth && p.mode == p0.mode && p.seed == p0.seed &&
+                      p.sample_begin == p0.sample_begin && p.sample_end == p0.sample_end,
+                  AUR_ERR_INVALID, "aur_batch_create: scene %u differs in spp/depth/mode/seed/sample range", i);
+        AUR_CHECK(sc->nmh->device == ctx->device, AUR_ERR_INVALID, "aur_batch_create: scene %u on another device", i);
+        // specular materials need the per-sample ray stack of the plain path
+        std::vector<aur_shader> sh(sc->num_shaders);
+        AUR_CUDA(cudaMemcpy(sh.data(), sc->shaders, sizeof(aur_shader) * sc->num_shaders, cudaMemcpyDeviceToHost));
+        for (const aur_shader& s : sh)
+            AUR_CHECK(!(s.reflectivity > 0.0f) && !(s.translucence > 0.0f), AUR_ERR_UNSUPPORTED,
+                      "aur_batch_create: scene %u has a specular shader; use aur_render", i);
+        std::vector<aur_light> lt(sc->num_lights);
+        if (sc->num_lights)
+            AUR_CUDA(cudaMemcpy(lt.data(), sc->lights, sizeof(aur_light) * sc->num_lights, cudaMemcpyDeviceToHost));
+        uint32_t m = 0;
+        for (const aur_light& l : lt) m += l.type == AUR_LIGHT_AREA ? (uint32_t)l.samples : 1u;
+        AUR_CHECK(m <= (uint32_t)kMaxLightSlots, AUR_ERR_UNSUPPORTED,
+                  "aur_batch_create: scene %u needs %u light samples per hit (limit %d)", i, m, kMaxLightSlots);
+        M = std::max(M, m);
+        cap = std::max(cap, sc->nmh->levels + 1);
+        WfScene& w = table[i];
+        w.recs = sc->nmh->node_recs;
+        w.perm = sc->nmh->perm;
+        w.normals = sc->normals;
+        w.sids = sc->shader_ids;
+        w.shaders = sc->shaders;
+        w.lights = sc->lights;
+        w.nodes = sc->nmh->nodes;
+        w.num_lights = sc->num_lights;
+        w.width = p.width;
+        w.height = p.height;
+        w.pix_off = (uint32_t)P_tot;
+        w.scene_id = p.scene_id;
+        w.cam = cameras[i];
+        pix_off[i] = (uint32_t)P_tot;
+        P_tot += (uint64_t)p.width * p.height;
+        AUR_CHECK(P_tot < (1ull << 31), AUR_ERR_INVALID, "aur_batch_create: too many pixels in the batch");
+    }
+    pix_off[num_scenes] = (uint32_t)P_tot;
+    const uint32_t s_end = p0.sample_end ? p0.sample_end : p0.spp;
+    const uint32_t nsamp = s_end - p0.sample_begin;
+    AUR_CHECK(nsamp > 0, AUR_ERR_INVALID, "aur_batch_create: empty sample range");
+
+    aur_wavefront_tuning tn{};
+    if (tuning) tn = *tuning;
+    if (tn.paths_in_flight == 0) tn.paths_in_flight = 1u << 21;
+    if (tn.block_size == 0) tn.block_size = 128;
+    if (tn.blocks_per_sm == 0) tn.blocks_per_sm = 6;
+    if (tn.samples_per_wave == 0) {
+        // cap the wave's sample buffer at about 1 GiB
+        tn.samples_per_wave = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(nsamp, (1ull << 26) / P_tot));
+    }
+    tn.samples_per_wave = std::min(tn.samples_per_wave, nsamp);
+    AUR_CHECK(tn.block_size % 32 == 0 && tn.block_size >= 32 && tn.block_size <= 512, AUR_ERR_INVALID,
+              "aur_batch_create: block_size must be a multiple of 32 in [32, 512]");
+    AUR_CHECK(tn.paths_in_flight >= 1024 && tn.paths_in_flight <= (1u << 26), AUR_ERR_INVALID,
+              "aur_batch_create: paths_in_flight must be in [1024, 2^26]");
+    AUR_CHECK(tn.blocks_per_sm >= 1 && tn.blocks_per_sm <= 32, AUR_ERR_INVALID,
+              "aur_batch_create: blocks_per_sm must be in [1, 32]");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+
+    aur_batch* bt = new aur_batch();
+    bt->device = ctx->device;
+    bt->num_scenes = num_scenes;
+    bt->params = p0;
+    bt->tuning = tn;
+    bt->block = tn.block_size;
+    bt->grid = (uint32_t)ctx->sm_count * tn.blocks_per_sm;
+    bt->smem = (size_t)3 * cap * tn.block_size * sizeof(uint32_t);
+    bt->accum_host.assign(num_scenes, nullptr);
+    const uint64_t Q = tn.paths_in_flight;
+    const uint64_t out_items = P_tot * tn.samples_per_wave;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
+    const size_t o_ctl = take(sizeof(WfCtl)), o_tab = take(sizeof(WfScene) * num_scenes);
+    const size_t o_pix = take(4 * (num_scenes + 1)), o_acc = take(sizeof(float4*) * num_scenes);
+    const size_t o_o = take(16 * Q), o_d = take(16 * Q), o_thr = take(16 * Q), o_col = take(16 * Q);
+    const size_t o_hit = take(16 * Q), o_meta = take(16 * Q), o_ndir = take(16 * Q), o_nthr = take(16 * Q);
+    const size_t o_fsh = take(16 * Q), o_emi = take(16 * Q), o_cj = take(16 * Q * M), o_vis = take(4 * Q);
+    const size_t o_q0 = take(4 * Q), o_q1 = take(4 * Q), o_free = take(4 * Q);
+    const size_t o_sho = take(16 * Q * M), o_shd = take(16 * Q * M), o_out = take(16 * out_items);
+    if (cudaMalloc(&bt->mem, off) != cudaSuccess) {
+        cudaGetLastError();
+        batch_free(bt);
+        return fail(AUR_ERR_OOM, "aur_batch_create: out of device memory (%zu bytes)", off);
+    }
+    char* base = (char*)bt->mem;
+    WfArgs& a = bt->args;
+    a.ctl = (WfCtl*)(base + o_ctl);
+    a.scenes = (const WfScene*)(base + o_tab);
+    a.pix_off = (const uint32_t*)(base + o_pix);
+    a.accum = (float4* const*)(base + o_acc);
+    a.num_scenes = num_scenes;
+    a.P_tot = (uint32_t)P_tot;
+    a.Q = (uint32_t)Q;
+    a.M = M;
+    a.spp = p0.spp;
+    a.max_depth = p0.max_depth;
+    a.mode = p0.mode;
+    a.seed = p0.seed;
+    a.cap = (int)cap;
+    a.o = (float4*)(base + o_o); a.d = (float4*)(base + o_d); a.thr = (float4*)(base + o_thr);
+    a.col = (float4*)(base + o_col); a.hit = (float4*)(base + o_hit); a.meta = (uint4*)(base + o_meta);
+    a.ndir = (float4*)(base + o_ndir); a.nthr = (float4*)(base + o_nthr); a.fsh = (float4*)(base + o_fsh);
+    a.emi = (float4*)(base + o_emi); a.cj = (float4*)(base + o_cj); a.vis = (uint32_t*)(base + o_vis);
+    a.ext_q[0] = (uint32_t*)(base + o_q0); a.ext_q[1] = (uint32_t*)(base + o_q1);
+    a.free_list = (uint32_t*)(base + o_free);
+    a.sh_o = (float4*)(base + o_sho); a.sh_d = (float4*)(base + o_shd); a.out = (float4*)(base + o_out);
+    cudaMemcpy(base + o_tab, table.data(), sizeof(WfScene) * num_scenes, cudaMemcpyHostToDevice);
+    cudaMemcpy(base + o_pix, pix_off.data(), 4 * (num_scenes + 1), cudaMemcpyHostToDevice);
+    WfCtl ctl{};
+    ctl.s_begin = p0.sample_begin;
+    ctl.s_end = s_end;
+    ctl.spw = tn.samples_per_wave;
+    ctl.num_waves = cdiv(nsamp, tn.samples_per_wave);
+    // every iteration either starts new paths or advances live ones by a bounce
+    const uint64_t waves_of_pool = cdiv(P_tot * tn.samples_per_wave, Q) + 1;
+    ctl.iter_limit = (uint32_t)std::min<uint64_t>(0x7FFFFFFFull, 4 * waves_of_pool * (p0.max_depth + 2) + 64);
+    cudaMemcpy(a.ctl, &ctl, sizeof(ctl), cudaMemcpyHostToDevice);
+    if (cudaFuncSetAttribute(k_wf_extend, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k_wf_shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&bt->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        const cudaError_t e = cudaGetLastError();
+        batch_free(bt);
+        return cuda_fail(e, "aur_batch_create set-up", __FILE__, __LINE__);
+    }
+    st = make_graph(bt);
+    if (st != AUR_OK) {
+        cudaGetLastError();
+        batch_free(bt);
+        return st;
+    }
+    *out = bt;
+    return AUR_OK;
+}
+
+aur_status aur_batch_render(aur_ctx* ctx, aur_batch* bt, float* const* accum) {
+    clear_error();
+    AUR_CHECK(ctx && bt && accum, AUR_ERR_INVALID, "aur_batch_render: null argument");
+    AUR_CHECK(ctx->device == bt->device, AUR_ERR_INVALID, "aur_batch_render: batch lives on another device");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    for (uint32_t i = 0; i < bt->num_scenes; ++i) {
+        AUR_CHECK(accum[i], AUR_ERR_INVALID, "aur_batch_render: frame %u is null", i);
+        bt->accum_host[i] = (float4*)accum[i];
+    }
+    const WfArgs& a = bt->args;
+    AUR_CUDA(cudaMemcpyAsync((void*)a.accum, bt->accum_host.data(), sizeof(float4*) * bt->num_scenes,
+                             cudaMemcpyHostToDevice, ctx->stream));
+    // reset the per-launch part of the control block: wave, error, iteration count
+    AUR_CUDA(cudaMemsetAsync(&a.ctl->wave, 0, sizeof(uint32_t), ctx->stream));
+    AUR_CUDA(cudaMemsetAsync(&a.ctl->error, 0, sizeof(uint32_t) * 2, ctx->stream));
+    AUR_CUDA(cudaGraphLaunch(bt->exec, ctx->stream));
+    return AUR_OK;
+}
+
+aur_status aur_batch_status(aur_ctx* ctx, aur_batch* bt, uint32_t* iterations) {
+    AUR_CHECK(ctx && bt, AUR_ERR_INVALID, "aur_batch_status: null argument");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    WfCtl c;
+    AUR_CUDA(cudaMemcpyAsync(&c, bt->args.ctl, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (iterations) *iterations = c.total_iters;
+    AUR_CHECK(c.error == 0, AUR_ERR_TIMEOUT,
+              "wavefront render stopped: iteration limit %u reached or traversal stack overflow (flags 0x%x)",
+              c.iter_limit, c.error);
+    AUR_CHECK(c.wave == c.num_waves, AUR_ERR_TIMEOUT, "wavefront render ended after %u of %u waves", c.wave,
+              c.num_waves);
+    return AUR_OK;
+}
+
+aur_status aur_batch_tuning(const aur_batch* bt, aur_wavefront_tuning* out) {
+    AUR_CHECK(bt && out, AUR_ERR_INVALID, "aur_batch_tuning: null argument");
+    *out = bt->tuning;
+    return AUR_OK;
+}
+
+aur_status aur_batch_destroy(aur_batch* bt) {
+    batch_free(bt);
+    return AUR_OK;
+}
+
+aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, const aur_camera* cameras,
+                              const aur_render_params* params, uint32_t num_scenes, aur_wavefront_tuning* best,
+                              float* best_ms) {
+    clear_error();
+    AUR_CHECK(ctx && scenes && cameras && params && best && num_scenes > 0, AUR_ERR_INVALID,
+              "aur_batch_autotune: null argument");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    // one sample per pixel of the real batch, into scratch frames
+    std::vector<aur_render_params> p1(params, params + num_scenes);
+    for (auto& p : p1) { p.sample_end = p.sample_begin + 1; }
+    size_t pixels = 0;
+    for (uint32_t i = 0; i < num_scenes; ++i) pixels += (size_t)p1[i].width * p1[i].height;
+    float4* frames = nullptr;
+    AUR_CHECK(cudaMalloc(&frames, pixels * sizeof(float4)) == cudaSuccess, AUR_ERR_OOM, "aur_batch_autotune: out of memory");
+    std::vector<float*> acc(num_scenes);
+    for (uint32_t i = 0, o = 0; i < num_scenes; o += p1[i].width * p1[i].height, ++i) acc[i] = (float*)(frames + o);
+    const uint32_t pools[] = {1u << 20, 1u << 21, 1u << 22};
+    const uint32_t blocks[] = {64, 128, 256};
+    const uint32_t per_sm[] = {4, 8, 16};
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best_t = 1e30f;
+    aur_status st = AUR_OK;
+    for (uint32_t pool : pools)
+        for (uint32_t bs : blocks)
+            for (uint32_t bps : per_sm) {
+                if ((uint64_t)bs * bps > 2048) continue;
+                aur_wavefront_tuning t{pool, 1, bs, bps};
+                aur_batch* bt = nullptr;
+                if (aur_batch_create(ctx, scenes, cameras, p1.data(), num_scenes, &t, &bt) != AUR_OK) {
+                    clear_error();
+                    continue;
+                }
+                float ms = 0.0f;
+                for (int rep = 0; rep < 2; ++rep) {   // the first launch warms up
+                    cudaEventRecord(e0, ctx->stream);
+                    aur_batch_render(ctx, bt, acc.data());
+                    cudaEventRecord(e1, ctx->stream);
+                    cudaEventSynchronize(e1);
+                    cudaEventElapsedTime(&ms, e0, e1);
+                }
+                const aur_status s2 = aur_batch_status(ctx, bt, nullptr);
+                aur_batch_destroy(bt);
+                if (s2 != AUR_OK) { st = s2; continue; }
+                if (ms < best_t) { best_t = ms; *best = t; }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(frames);
+    if (best_t >= 1e30f) return st != AUR_OK ? st : fail(AUR_ERR_CUDA, "aur_batch_autotune: no candidate ran");
+    best->samples_per_wave = 0;   // chosen per batch from the frame size
+    if (best_ms) *best_ms = best_t;
+    return AUR_OK;
+}
+
+}  // extern "C"

@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=1 << 22)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-extras", action="store_true", help="headline traversal only")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling cases only)")
     ap.add_argument("--profile", action="store_true",
                     help="small profiling case: one warm-up, one closest-hit and one any-hit launch")
@@ -180,6 +181,95 @@ def cpu_baseline(verts, perm, rays, sample, seed=7):
     return {"value": sub.shape[0] / dt / 1e6, "unit": "Mrays/s", "cores": nth, "kind": "port",
             "sample": "%d rays drawn uniformly from the 2^24 (seed %d), closest hit, oracle C++ restatement of "
                       "intersect(), %d host threads, %.1f s" % (sub.shape[0], seed, nth, dt)}
+
+
+def bench_batched(ctx, n_scenes=64, size=512, spp=64, depth=6, samples=8):
+    """Batched workload: 64 sphere scenes (1k-500k triangles each), 512x512,
+    64 spp, depth 6, path mode; samples [0, 8) of the 64 are rendered by the
+    plain renderer (one aur_render per scene) and by the wavefront batch (one
+    graph launch), timed with CUDA events; the frames must be identical."""
+    import torch
+    from aurora_gb300 import api, scenes, types as T
+    sds = [scenes.sphere_scene(i) for i in range(n_scenes)]
+    scs = [api.Scene(ctx, sd) for sd in sds]
+    prm = [T.render_params(size, size, spp, depth, seed=0, mode=T.MODE_PATH, sample_end=samples, scene_id=i)
+           for i in range(n_scenes)]
+    n_samples = n_scenes * size * size * samples
+    stream = torch.cuda.current_stream()
+    frames = [torch.zeros((size, size, 4), dtype=torch.float32, device="cuda") for _ in range(n_scenes)]
+
+    def plain():
+        for sc, p, f in zip(scs, prm, frames):
+            sc.render(p, accum=f)
+
+    plain()                                   # warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for f in frames:
+        f.zero_()
+    e0.record(stream)
+    plain()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    plain_img = [f.clone() for f in frames]
+    t0 = time.perf_counter()
+    tuning, tune_ms = api.autotune(ctx, scs, prm)
+    tune_s = time.perf_counter() - t0
+    batch = api.Batch(ctx, scs, prm, tuning=tuning)
+    wf = [torch.zeros_like(f) for f in frames]
+    batch.render(wf)
+    batch.status()
+    for f in wf:
+        f.zero_()
+    e0.record(stream)
+    batch.render(wf)
+    e1.record(stream)
+    iters = batch.status()
+    wf_ms = e0.elapsed_time(e1)
+    same = all(torch.equal(a, b) for a, b in zip(wf, plain_img))
+    tris = [sd.count for sd in sds]
+    return {"workload": "%d sphere scenes (%d-%d triangles, %d total), %dx%d, %d spp, depth %d, path mode; "
+                        "samples [0, %d) timed" % (n_scenes, min(tris), max(tris), sum(tris), size, size, spp, depth,
+                                                   samples),
+            "plain_samples_per_s": n_samples / (plain_ms * 1e-3), "plain_ms": plain_ms,
+            "wavefront_samples_per_s": n_samples / (wf_ms * 1e-3), "wavefront_ms": wf_ms,
+            "speedup": plain_ms / wf_ms, "frames_identical": bool(same), "equal_rmse": bool(same),
+            "wavefront_graph_launches": 1, "wavefront_iterations": iters,
+            "tuning": {k: int(tuning[k]) for k in tuning.dtype.names}, "autotune_s": tune_s}
+
+
+def bench_cornell(ctx, cpu=True):
+    """Cornell workload: 34 triangles, 256x256, 16 spp, depth 4, seed 0, path
+    mode: plain GPU render vs the oracle on all host cores."""
+    import torch
+    from aurora_gb300 import api, scenes, types as T
+    sd = scenes.cornell()
+    sc = api.Scene(ctx, sd)
+    p = T.render_params(256, 256, 16, 4, seed=0, mode=T.MODE_PATH)
+    sc.render(p)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    e0.record(stream)
+    for _ in range(reps):
+        img = sc.render(p)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    out = {"workload": "Cornell box (34 triangles), 256x256, 16 spp, depth 4, path mode",
+           "gpu_samples_per_s": 256 * 256 * 16 / (ms * 1e-3), "gpu_ms": ms}
+    if cpu:
+        import oracle
+        ns = oracle.NmhScene(sd)
+        t0 = time.perf_counter()
+        ref, _ = oracle.render(ns, p, nthreads=os.cpu_count() or 1)
+        dt = time.perf_counter() - t0
+        out["cpu_samples_per_s"] = 256 * 256 * 16 / dt
+        out["cpu_cores"] = os.cpu_count()
+        out["matches_oracle"] = bool(np.array_equal(img.cpu().numpy(), ref))
+    return out
 
 
 def run_reference(args):
@@ -327,6 +417,10 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         perm, verts = nmh.export()
         out["cpu_baseline"] = cpu_baseline(verts, perm, rays, args.cpu_sample)
+    if not args.skip_extras:
+        del rays_d, hits_d, occ_d
+        out["cornell_plain"] = bench_cornell(ctx, cpu=rank == 0 and not args.no_cpu_baseline)
+        out["batched_wavefront"] = bench_batched(ctx)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

@@ -287,6 +287,42 @@ aur_status aur_draw_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float 
 /* Renderer::clearPixels (core/renderer.cpp:33-36). */
 aur_status aur_clear_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float* accum);
 
+/* ------------------------------------------------------ batched wavefront */
+
+/* Launch configuration of the wavefront integrator (0 = default). */
+typedef struct aur_wavefront_tuning {
+    uint32_t paths_in_flight;   /* path pool size (queue capacity) */
+    uint32_t samples_per_wave;  /* samples per pixel processed per wave */
+    uint32_t block_size;        /* threads per block of the stage kernels */
+    uint32_t blocks_per_sm;     /* persistent grid = SMs x blocks_per_sm */
+} aur_wavefront_tuning;
+
+typedef struct aur_batch aur_batch;
+
+/* Prepares a wavefront render of `num_scenes` scenes of uneven size as ONE
+ * CUDA graph (conditional while nodes over sample waves and integrator
+ * iterations). No counterpart in the reference, which renders one scene per
+ * frame with a host loop (render/monteCarloRaytracer.cpp:81-120); each scene's
+ * frame equals aur_render's with the same parameters (same estimator, same
+ * RNG streams keyed by params[i].scene_id). params[i] may differ in width,
+ * height and scene_id only. Materials must be non-specular. */
+aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const aur_camera* cameras,
+                            const aur_render_params* params, uint32_t num_scenes,
+                            const aur_wavefront_tuning* tuning, aur_batch** out);
+/* Adds every scene's samples into accum[i] (device float4 frames) with one
+ * graph launch on the context's stream. */
+aur_status aur_batch_render(aur_ctx* ctx, aur_batch* batch, float* const* accum);
+/* Waits for the batch and reports device-side failures (iteration limit or
+ * stack overflow: AUR_ERR_TIMEOUT). iterations: total integrator iterations. */
+aur_status aur_batch_status(aur_ctx* ctx, aur_batch* batch, uint32_t* iterations);
+aur_status aur_batch_tuning(const aur_batch* batch, aur_wavefront_tuning* out);
+aur_status aur_batch_destroy(aur_batch* batch);
+/* Autotuner: times one-sample renders of the batch for a set of candidate
+ * tunings (pool size, block size, blocks per SM) and returns the fastest. */
+aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, const aur_camera* cameras,
+                              const aur_render_params* params, uint32_t num_scenes,
+                              aur_wavefront_tuning* best, float* best_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,60 @@
+"""Batched wavefront integrator: every scene's frame equals the plain renderer's."""
+import numpy as np
+import pytest
+
+from aurora_gb300 import api, scenes, types as T
+
+pytestmark = pytest.mark.gpu
+
+
+def _scenes():
+    return [scenes.cornell(), scenes.cornell_sphere(seed=2), scenes.sphere_scene(5, max_tris=20000),
+            scenes.sphere_scene(9, max_tris=5000)]
+
+
+def _params(mode, sizes, spp=4, depth=3):
+    return [T.render_params(w, h, spp, depth, seed=7, mode=mode, scene_id=i) for i, (w, h) in enumerate(sizes)]
+
+
+@pytest.mark.parametrize("mode", [T.MODE_PATH, T.MODE_REFERENCE])
+@pytest.mark.parametrize("tuning", [dict(paths_in_flight=1024, samples_per_wave=1, block_size=64, blocks_per_sm=2),
+                                    dict()])
+def test_wavefront_equals_plain(ctx, mode, tuning):
+    sds = _scenes()
+    scs = [api.Scene(ctx, sd) for sd in sds]
+    sizes = [(40, 32), (24, 24), (33, 17), (16, 40)]
+    prm = _params(mode, sizes)
+    batch = api.Batch(ctx, scs, prm, tuning=api.make_tuning(**tuning) if tuning else None)
+    frames = batch.render()
+    iters = batch.status()
+    assert iters > 0
+    for sc, p, f in zip(scs, prm, frames):
+        plain = sc.render(p).cpu().numpy()
+        assert np.array_equal(f.cpu().numpy(), plain)
+    # a second launch of the same graph adds the same samples again
+    frames2 = batch.render(frames)
+    batch.status()
+    for sc, p, f in zip(scs, prm, frames2):
+        twice = sc.render(p, accum=sc.render(p))
+        assert np.array_equal(f.cpu().numpy(), twice.cpu().numpy())
+
+
+def test_wavefront_rejects_specular(ctx):
+    sd = scenes.cornell()
+    sd.shaders = sd.shaders.copy()
+    sd.shaders["reflectivity"][0] = 0.5
+    sc = api.Scene(ctx, sd)
+    with pytest.raises(api.AuroraError) as e:
+        api.Batch(ctx, [sc], _params(T.MODE_PATH, [(8, 8)]))
+    assert e.value.status == 6
+
+
+def test_autotune_returns_a_working_tuning(ctx):
+    scs = [api.Scene(ctx, sd) for sd in _scenes()[:2]]
+    prm = _params(T.MODE_PATH, [(64, 64), (32, 32)])
+    t, ms = api.autotune(ctx, scs, prm)
+    assert ms > 0 and int(t["paths_in_flight"]) >= 1024
+    b = api.Batch(ctx, scs, prm, tuning=t)
+    fr = b.render()
+    b.status()
+    assert np.array_equal(fr[0].cpu().numpy(), scs[0].render(prm[0]).cpu().numpy())
