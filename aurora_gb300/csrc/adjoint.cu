@@ -1,0 +1,245 @@
+// adjoint.cu — path-replay backpropagation through the integrator.
+//
+// Gradients of a loss L(image) with respect to every shader's diffuse colour
+// and every light's colour, given dL/dimage. No counterpart in the
+// reference. Method: path replay backpropagation (D. Vicini, S. Speierer,
+// W. Jakob, "Path Replay Backpropagation", ACM TOG 40(4), 2021). For each
+// camera sample the primal pass (aur_integrate.cuh, the same estimator as
+// aur_render) gives the sample's radiance C; the replay walks the same path
+// again with the same counter-RNG draws, keeps the radiance still to come
+// L_rem = C - sum of the contributions already passed, and at vertex k with
+// throughput T_k and Lambert colour c_k = diffuse_color * diffuse adds
+//   dL/dc_k  += g * (T_k * D_k / c_k + L_rem_after_k / c_k)
+//   dL/dcolor_l += g * T_k * dD_k/dcolor_l
+// where D_k is the direct light at k (ambient, delta and area terms,
+// radiance.cuh:13-80), g = dL/dpixel / spp, and c_k enters the bounce
+// throughput f*|cos|/pdf of every later vertex (BSDF::samplef, bsdf.cuh:222-236).
+// D_k / c_k is evaluated directly (f replaced by 1/pi), so the direct part
+// needs no division; the later-vertex part divides by c_k and is skipped for
+// colour channels that are exactly zero.
+#include <algorithm>
+#include <vector>
+
+#include "aur_integrate.cuh"
+#include "aur_internal.h"
+
+namespace aur {
+namespace {
+
+constexpr int kAdjThreads = 128;
+constexpr uint32_t kSharedLights = 64;
+
+// Per-unit-colour radiance of a light sample (Lr = color * s), light.cuh:228-259.
+__device__ __forceinline__ float light_scale(const aur_light& L, const f3& dir, float t) {
+    if (L.type == AUR_LIGHT_AMBIENT) return L.intensity * (1.0f - L.ambient);
+    if (L.type == AUR_LIGHT_POINT) return L.intensity / (t * t);
+    if (L.type == AUR_LIGHT_DIRECTIONAL) return L.intensity;
+    return L.intensity * fmaxf(0.0f, dot(from(L.direction), -dir));
+}
+
+// Replays one camera sample whose primal radiance is C and adds its
+// gradient contributions (scaled by g per colour channel).
+__device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, uint32_t seed, uint32_t scene,
+                       uint32_t pixel, uint32_t sample, PathRay ray, const StackRef& stk, const f3& C, const f3& g,
+                       float* __restrict__ d_diffuse, float* __restrict__ d_light, uint32_t& visits, uint32_t* err) {
+    f3 Lrem = C;
+    uint32_t depth = 0;
+    for (uint32_t rix = 0;; ++rix) {
+        float t = kInfinity, u = 0.0f, v = 0.0f;
+        const uint32_t tri = traverse<false>(sc.recs, sc.nodes, sc.perm, ray.pos, ray.dir, t, u, v, stk, visits, err);
+        if (tri == kNoPrim) return;
+        const f3 position = ray.pos + (ray.dir * t);
+        const f3 wo = -ray.dir;
+        const uint32_t sid = sc.sids[tri];
+        const uint32_t si = sid > 0 ? sid - 1 : 0;
+        const aur_shader* sh = sc.shaders + si;
+        const Bsdf b = get_bsdf(sc, from(sh->diffuse_color), sh->diffuse, tri, u, v);
+        const f3 f = bsdf_f(b);
+        const f3 thr = ray.thr;
+        f3 Li = from(sh->emission_color);
+        f3 Dp = mk3(0.0f);   // direct light per unit Lambert colour
+        for (uint32_t i = 0; i < sc.num_lights; ++i) {
+            const aur_light& L = sc.lights[i];
+            f3 dl = mk3(0.0f);   // d(direct)/d(light colour), per channel
+            if (L.type == AUR_LIGHT_AMBIENT) {
+                const f3 X = (from(L.color) * L.intensity) * L.ambient;
+                Li = Li + f * X;
+                Dp = Dp + X * kInvPi;
+                dl = dl + f * (L.intensity * L.ambient);
+            }
+            if (L.type != AUR_LIGHT_AREA) {
+                f3 wdir; float wt, pdf;
+                const f3 Ls = sample_light(L, position, seed, scene, pixel, sample, rix, 0u, wdir, wt, pdf);
+                if (pdf > 0.0f && !zero(Ls)) {
+                    float du = 0.0f, dv = 0.0f;
+                    if (!zero(f) &&
+                        traverse<true>(sc.recs, sc.nodes, sc.perm, position, wdir, wt, du, dv, stk, visits, err) == kNoPrim) {
+                        const float cs = fmaxf(0.0f, dot(wdir, b.N));
+                        Li = Li + f * Ls * cs;
+                        Dp = Dp + Ls * (kInvPi * cs);
+                        dl = dl + f * (light_scale(L, wdir, wt) * cs);
+                    }
+                }
+            } else {
+                f3 acc = mk3(0.0f), accp = mk3(0.0f), accl = mk3(0.0f);
+                for (int32_t j = 0; j < L.samples; ++j) {
+                    f3 wdir; float wt, lpdf;
+                    const f3 Lr = sample_light(L, position, seed, scene, pixel, sample, rix, light_slot(i, (uint32_t)j),
+                                               wdir, wt, lpdf);
+                    f3 wpos = position;
+                    wpos.x += kEpsilon * wdir.x;
+                    wpos.y += kEpsilon * wdir.y;
+                    wpos.z += kEpsilon * wdir.z;
+                    wt += kEpsilon;
+                    if (lpdf > 0.0f && !zero(Lr)) {
+                        float du = 0.0f, dv = 0.0f;
+                        if (!zero(f) &&
+                            traverse<true>(sc.recs, sc.nodes, sc.perm, wpos, wdir, wt, du, dv, stk, visits, err) == kNoPrim) {
+                            const float cs = fmaxf(0.0f, dot(wdir, b.N));
+                            acc = acc + f * Lr * cs;
+                            accp = accp + Lr * (kInvPi * cs);
+                            accl = accl + f * (light_scale(L, wdir, wt - kEpsilon) * cs);
+                        }
+                    }
+                }
+                const float ns = (float)L.samples;
+                Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
+                Dp = Dp + mk3(accp.x / ns, accp.y / ns, accp.z / ns);
+                dl = dl + mk3(accl.x / ns, accl.y / ns, accl.z / ns);
+            }
+            const f3 gl = g * thr * dl;
+            if (gl.x != 0.0f || gl.y != 0.0f || gl.z != 0.0f) {
+                atomicAdd(d_light + 3 * i + 0, gl.x);
+                atomicAdd(d_light + 3 * i + 1, gl.y);
+                atomicAdd(d_light + 3 * i + 2, gl.z);
+            }
+        }
+        Lrem = Lrem - Li * thr;
+        // bounce, as in the primal
+        bool cont = false;
+        PathRay nr;
+        if (mode == AUR_MODE_PATH) {
+            depth++;
+            if (depth <= max_depth) {
+                float u1, u2;
+                draw2(seed, scene, pixel, sample, rix, 0u, u1, u2);
+                const f3 lwo = world_to_local(wo, b.N, b.S, b.T);
+                f3 lwi = sample_hemisphere_cosine(u1, u2);
+                if (lwo.z < 0.0f) lwi.z *= -1.0f;
+                const float pdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
+                const f3 wi = local_to_world(lwi, b.N, b.S, b.T);
+                if (pdf > 0.0f && !zero(f)) {
+                    nr.pos = position;
+                    nr.dir = wi;
+                    nr.weight = 1.0f;
+                    nr.eta = ray.eta;
+                    nr.thr = thr * (f * (fabsf(dot(wi, b.N)) / pdf));
+                    cont = true;
+                }
+            }
+        }
+        const f3 c1 = b.color1;
+        f3 dc = thr * Dp;
+        if (cont) {
+            dc.x += c1.x != 0.0f ? Lrem.x / c1.x : 0.0f;
+            dc.y += c1.y != 0.0f ? Lrem.y / c1.y : 0.0f;
+            dc.z += c1.z != 0.0f ? Lrem.z / c1.z : 0.0f;
+        }
+        // color1 = diffuse_color * diffuse
+        const f3 gd = g * dc * sh->diffuse;
+        if (gd.x != 0.0f || gd.y != 0.0f || gd.z != 0.0f) {
+            atomicAdd(d_diffuse + 3 * si + 0, gd.x);
+            atomicAdd(d_diffuse + 3 * si + 1, gd.y);
+            atomicAdd(d_diffuse + 3 * si + 2, gd.z);
+        }
+        if (!cont) return;
+        ray = nr;
+    }
+}
+
+__global__ void __launch_bounds__(kAdjThreads) k_adjoint(SceneView sc, aur_camera cam, aur_render_params p, uint32_t s0,
+                                                         uint32_t nb, const float4* __restrict__ d_image,
+                                                         float* __restrict__ d_diffuse, float* __restrict__ d_light,
+                                                         uint32_t* __restrict__ err, int cap) {
+    extern __shared__ uint32_t smem[];
+    StackRef stk;
+    stk.idx = smem + threadIdx.x;
+    stk.lo = reinterpret_cast<float*>(smem + cap * kAdjThreads) + threadIdx.x;
+    stk.hi = reinterpret_cast<float*>(smem + 2 * cap * kAdjThreads) + threadIdx.x;
+    stk.stride = kAdjThreads;
+    stk.cap = cap;
+    // light gradients are reduced in shared memory first (one light is hit by every sample)
+    float* s_light = reinterpret_cast<float*>(smem + 3 * cap * kAdjThreads);
+    const bool shared_lights = sc.num_lights <= kSharedLights;
+    if (shared_lights)
+        for (uint32_t i = threadIdx.x; i < 3 * sc.num_lights; i += kAdjThreads) s_light[i] = 0.0f;
+    __syncthreads();
+    const uint64_t P = (uint64_t)p.width * p.height;
+    const uint64_t t = (uint64_t)blockIdx.x * kAdjThreads + threadIdx.x;
+    if (t < P * nb) {
+        const uint32_t pix = (uint32_t)(t % P);
+        const uint32_t s = s0 + (uint32_t)(t / P);
+        const PathRay r = camera_ray(cam, p.width, p.height, pix % p.width, pix / p.width, s, p.spp);
+        uint32_t visits = 0;
+        const SampleResult prim = integrate(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err);
+        if (prim.any_hit) {
+            const float4 di = d_image[pix];
+            const float w = 1.0f / (float)p.spp;
+            const f3 g = mk3(di.x * w, di.y * w, di.z * w);
+            replay(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, prim.color, g, d_diffuse,
+                   shared_lights ? s_light : d_light, visits, err);
+        }
+    }
+    __syncthreads();
+    if (shared_lights)
+        for (uint32_t i = threadIdx.x; i < 3 * sc.num_lights; i += kAdjThreads)
+            if (s_light[i] != 0.0f) atomicAdd(d_light + i, s_light[i]);
+}
+
+inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+}  // namespace
+
+SceneView scene_view(const aur_scene* sc);
+
+}  // namespace aur
+
+using namespace aur;
+
+extern "C" {
+
+aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_camera* camera,
+                              const aur_render_params* params, const float* d_image, float* d_diffuse,
+                              float* d_light_color) {
+    clear_error();
+    AUR_CHECK(ctx && scene && camera && d_image && d_diffuse && (d_light_color || scene->num_lights == 0),
+              AUR_ERR_INVALID, "aur_render_adjoint: null argument");
+    aur_status st = check_params(params);
+    if (st != AUR_OK) return st;
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    {
+        std::vector<aur_shader> sh(scene->num_shaders);
+        AUR_CUDA(cudaMemcpy(sh.data(), scene->shaders, sizeof(aur_shader) * sh.size(), cudaMemcpyDeviceToHost));
+        for (const aur_shader& s : sh)
+            AUR_CHECK(!(s.reflectivity > 0.0f) && !(s.translucence > 0.0f), AUR_ERR_UNSUPPORTED,
+                      "aur_render_adjoint: specular shaders are not differentiated");
+    }
+    const aur_render_params p = *params;
+    const uint32_t s0 = p.sample_begin, s1 = p.sample_end ? p.sample_end : p.spp;
+    if (s1 == s0) return AUR_OK;
+    const uint64_t P = (uint64_t)p.width * p.height;
+    const uint32_t batch = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(s1 - s0, (1ull << 24) / P));
+    const int cap = (int)scene->nmh->levels + 1;
+    const size_t smem = (size_t)3 * cap * kAdjThreads * sizeof(uint32_t) + 3 * kSharedLights * sizeof(float);
+    AUR_CUDA(cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const SceneView sv = scene_view(scene);
+    for (uint32_t s = s0; s < s1; s += batch) {
+        const uint32_t nb = std::min(batch, s1 - s);
+        k_adjoint<<<cdiv(P * nb, kAdjThreads), kAdjThreads, smem, ctx->stream>>>(
+            sv, *camera, p, s, nb, (const float4*)d_image, d_diffuse, d_light_color, ctx->d_flags, cap);
+    }
+    AUR_CUDA(cudaGetLastError());
+    return AUR_OK;
+}
+
+}  // extern "C"

@@ -272,6 +272,64 @@ def bench_cornell(ctx, cpu=True):
     return out
 
 
+def bench_adjoint(ctx, size=256, spp=64, depth=4):
+    """Differentiable workload: Cornell box + 4096-triangle sphere, one shader
+    per triangle (albedo U[0.2, 0.8]), 256x256, 64 spp, depth 4; L2 loss
+    against the frame rendered at albedo + N(0, 0.05). grad/fwd = adjoint
+    time / forward render time; two gradients are checked against central
+    differences (h = 1e-3, common random numbers)."""
+    import torch
+    from aurora_gb300 import api, scenes, types as T
+    sd = scenes.cornell_sphere(seed=0)
+    sc = api.Scene(ctx, sd)
+    p = T.render_params(size, size, spp, depth, seed=0, mode=T.MODE_PATH)
+    rng = np.random.default_rng(0)
+    tsh = sd.shaders.copy()
+    tsh["diffuse_color"] = np.clip(tsh["diffuse_color"] + rng.normal(0, 0.05, (sd.count, 3)), 0, 1)
+    sc.set_shaders(tsh)
+    target = sc.render(p)
+    sc.set_shaders(sd.shaders)
+    stream = torch.cuda.current_stream()
+    img = sc.render(p)
+    torch.cuda.synchronize()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0.record(stream)
+    img = sc.render(p)
+    e1.record(stream)
+    d_image = (2.0 * (img - target)).contiguous()
+    d_image[..., 3] = 0
+    gs, gl = sc.adjoint(p, d_image)
+    torch.cuda.synchronize()
+    gs.zero_(); gl.zero_()
+    e1.record(stream)
+    sc.adjoint(p, d_image, gs, gl)
+    e2.record(stream)
+    torch.cuda.synchronize()
+    fwd_ms, adj_ms = e0.elapsed_time(e1), e1.elapsed_time(e2)
+    g = gs.cpu().numpy()
+
+    def loss():
+        d = sc.render(p).double() - target.double()
+        return float((d[..., :3] ** 2).sum())
+
+    checks = []
+    for k in list(np.argsort(-np.abs(g).ravel())[:2]):
+        i, c = int(k // 3), int(k % 3)
+        vals = []
+        for sgn in (1, -1):
+            sh = sd.shaders.copy()
+            sh["diffuse_color"][i, c] += sgn * 1e-3
+            sc.set_shaders(sh)
+            vals.append(loss())
+        sc.set_shaders(sd.shaders)
+        fd = (vals[0] - vals[1]) / 2e-3
+        checks.append({"shader": i, "channel": c, "adjoint": float(g[i, c]), "fd": fd,
+                       "rel_err": abs(float(g[i, c]) - fd) / abs(fd)})
+    return {"workload": "Cornell box + 4096-triangle sphere (4130 per-triangle shaders), %dx%d, %d spp, depth %d, "
+                        "path mode, L2 loss" % (size, size, spp, depth),
+            "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "grad_over_fwd": adj_ms / fwd_ms, "fd_checks": checks}
+
+
 def run_reference(args):
     """--impl reference: the reference traversal restated in C++ (the oracle;
     the reference's own sources do not travel to this machine) on the host
@@ -421,6 +479,7 @@ def main():
         del rays_d, hits_d, occ_d
         out["cornell_plain"] = bench_cornell(ctx, cpu=rank == 0 and not args.no_cpu_baseline)
         out["batched_wavefront"] = bench_batched(ctx)
+        out["adjoint"] = bench_adjoint(ctx)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

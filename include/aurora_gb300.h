@@ -287,6 +287,19 @@ aur_status aur_draw_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float 
 /* Renderer::clearPixels (core/renderer.cpp:33-36). */
 aur_status aur_clear_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float* accum);
 
+/* ----------------------------------------------------------------- adjoint */
+
+/* Gradients of a loss with respect to every shader's diffuse_color and every
+ * light's color, by path replay backpropagation. No counterpart in the
+ * reference. d_image: device, width*height float4 = dLoss/d(accum) of
+ * aur_render with the same parameters (alpha ignored). d_diffuse
+ * (num_shaders*3) and d_light_color (num_lights*3), device: gradients are
+ * ADDED. Same estimator and RNG streams as aur_render; materials must be
+ * non-specular (AUR_ERR_UNSUPPORTED otherwise). */
+aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_camera* camera,
+                              const aur_render_params* params, const float* d_image, float* d_diffuse,
+                              float* d_light_color);
+
 /* ------------------------------------------------------ batched wavefront */
 
 /* Launch configuration of the wavefront integrator (0 = default). */

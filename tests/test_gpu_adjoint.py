@@ -1,0 +1,95 @@
+"""Path-replay adjoint: gradients against central finite differences of the
+plain renderer with common random numbers, and through a torch.autograd
+wrapper (the wrapper lives only here, in the test harness)."""
+import numpy as np
+import pytest
+
+from aurora_gb300 import api, scenes, types as T
+
+pytestmark = pytest.mark.gpu
+
+H = 1e-3
+
+
+def _loss(img, target):
+    d = img.double() - target.double()
+    return float((d[..., :3] ** 2).sum())
+
+
+def _setup(ctx, mode, W=48, spp=8, depth=4):
+    sd = scenes.cornell_sphere(seed=3)
+    sc = api.Scene(ctx, sd)
+    p = T.render_params(W, W, spp, depth, seed=5, mode=mode)
+    rng = np.random.default_rng(1)
+    target_sh = sd.shaders.copy()
+    target_sh["diffuse_color"] = np.clip(target_sh["diffuse_color"] + rng.normal(0, 0.05, (sd.count, 3)), 0, 1)
+    sc.set_shaders(target_sh)
+    target = sc.render(p)
+    sc.set_shaders(sd.shaders)
+    return sd, sc, p, target
+
+
+def _fd(sc, sd, p, target, kind, idx, ch):
+    vals = []
+    for sgn in (+1, -1):
+        sh, lt = sd.shaders.copy(), sd.lights.copy()
+        if kind == "shader":
+            sh["diffuse_color"][idx, ch] += sgn * H
+        else:
+            lt["color"][idx, ch] += sgn * H
+        sc.set_shaders(sh)
+        sc.set_lights(lt)
+        vals.append(_loss(sc.render(p), target))
+    sc.set_shaders(sd.shaders)
+    sc.set_lights(sd.lights)
+    return (vals[0] - vals[1]) / (2 * H)
+
+
+@pytest.mark.parametrize("mode", [T.MODE_PATH, T.MODE_REFERENCE])
+def test_adjoint_matches_finite_differences(ctx, mode):
+    sd, sc, p, target = _setup(ctx, mode)
+    img = sc.render(p)
+    d_image = (2.0 * (img - target)).contiguous()
+    d_image[..., 3] = 0.0
+    g_sh, g_lt = sc.adjoint(p, d_image)
+    g_sh, g_lt = g_sh.cpu().numpy(), g_lt.cpu().numpy()
+    # the largest shader gradients (wall, box and sphere triangles) and the light colour
+    order = np.argsort(-np.abs(g_sh).ravel())[:6]
+    checks = [("shader", int(k // 3), int(k % 3), g_sh.ravel()[k]) for k in order]
+    checks += [("light", 0, c, g_lt[0, c]) for c in range(3)]
+    for kind, idx, ch, g in checks:
+        fd = _fd(sc, sd, p, target, kind, idx, ch)
+        assert abs(g - fd) <= 1e-3 * abs(fd) + 1e-6, (kind, idx, ch, g, fd)
+
+
+def test_adjoint_through_torch_autograd(ctx):
+    import torch
+    sd, sc, p, target = _setup(ctx, T.MODE_PATH, W=32, spp=4)
+
+    class Render(torch.autograd.Function):
+        @staticmethod
+        def forward(fctx, albedo, light_color):
+            sh, lt = sd.shaders.copy(), sd.lights.copy()
+            sh["diffuse_color"] = albedo.detach().cpu().numpy()
+            lt["color"] = light_color.detach().cpu().numpy()
+            sc.set_shaders(sh)
+            sc.set_lights(lt)
+            return sc.render(p)
+
+        @staticmethod
+        def backward(fctx, grad_img):
+            g = grad_img.contiguous().clone()
+            g[..., 3] = 0.0
+            d_sh, d_lt = sc.adjoint(p, g)
+            return d_sh.cpu().double(), d_lt[: sd.lights.shape[0]].cpu().double()
+
+    albedo = torch.tensor(sd.shaders["diffuse_color"], dtype=torch.float64, requires_grad=True)
+    light = torch.tensor(sd.lights["color"], dtype=torch.float64, requires_grad=True)
+    img = Render.apply(albedo, light)
+    loss = ((img.double() - target.double())[..., :3] ** 2).sum()
+    loss.backward()
+    k = int(torch.argmax(albedo.grad.abs()))
+    fd = _fd(sc, sd, p, target, "shader", k // 3, k % 3)
+    assert abs(float(albedo.grad.view(-1)[k]) - fd) <= 1e-3 * abs(fd) + 1e-6
+    fdl = _fd(sc, sd, p, target, "light", 0, 1)
+    assert abs(float(light.grad[0, 1]) - fdl) <= 1e-3 * abs(fdl) + 1e-6
