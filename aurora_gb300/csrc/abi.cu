@@ -277,6 +277,8 @@ aur_status aur_scene_create(aur_ctx* ctx, const float* vertices, const float* no
     }
     sc->num_shaders = num_shaders;
     sc->num_lights = num_lights;
+    for (uint32_t i = 0; i < num_shaders; ++i)
+        sc->has_specular |= shaders[i].reflectivity > 0.0f || shaders[i].translucence > 0.0f;
     cudaMemcpyAsync(sc->shaders, shaders, sizeof(aur_shader) * num_shaders, cudaMemcpyHostToDevice, s);
     if (num_lights) cudaMemcpyAsync(sc->lights, lights, sizeof(aur_light) * num_lights, cudaMemcpyHostToDevice, s);
     const cudaError_t e = cudaStreamSynchronize(s);
@@ -312,6 +314,9 @@ aur_status aur_scene_set_shaders(aur_ctx* ctx, aur_scene* sc, const aur_shader* 
     AUR_CUDA(cudaSetDevice(ctx->device));
     AUR_CUDA(cudaMemcpyAsync(sc->shaders, shaders, sizeof(aur_shader) * n, cudaMemcpyHostToDevice, ctx->stream));
     AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    sc->has_specular = false;
+    for (uint32_t i = 0; i < n; ++i)
+        sc->has_specular |= shaders[i].reflectivity > 0.0f || shaders[i].translucence > 0.0f;
     return AUR_OK;
 }
 

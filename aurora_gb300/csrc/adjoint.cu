@@ -39,9 +39,12 @@ __device__ __forceinline__ float light_scale(const aur_light& L, const f3& dir, 
 
 // Replays one camera sample whose primal radiance is C and adds its
 // gradient contributions (scaled by g per colour channel).
+// Gradients of light 0 are summed in `gl0` (reduced once per block by the
+// caller); those of further lights go to d_light with atomics.
 __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, uint32_t seed, uint32_t scene,
                        uint32_t pixel, uint32_t sample, PathRay ray, const StackRef& stk, const f3& C, const f3& g,
-                       float* __restrict__ d_diffuse, float* __restrict__ d_light, uint32_t& visits, uint32_t* err) {
+                       float* __restrict__ d_diffuse, float* __restrict__ d_light, f3& gl0, uint32_t& visits,
+                       uint32_t* err) {
     f3 Lrem = C;
     uint32_t depth = 0;
     for (uint32_t rix = 0;; ++rix) {
@@ -108,7 +111,9 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
                 dl = dl + mk3(accl.x / ns, accl.y / ns, accl.z / ns);
             }
             const f3 gl = g * thr * dl;
-            if (gl.x != 0.0f || gl.y != 0.0f || gl.z != 0.0f) {
+            if (i == 0) {
+                gl0 = gl0 + gl;
+            } else if (gl.x != 0.0f || gl.y != 0.0f || gl.z != 0.0f) {
                 atomicAdd(d_light + 3 * i + 0, gl.x);
                 atomicAdd(d_light + 3 * i + 1, gl.y);
                 atomicAdd(d_light + 3 * i + 2, gl.z);
@@ -176,19 +181,34 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(SceneView sc, aur_camer
     __syncthreads();
     const uint64_t P = (uint64_t)p.width * p.height;
     const uint64_t t = (uint64_t)blockIdx.x * kAdjThreads + threadIdx.x;
+    f3 gl0 = mk3(0.0f);
     if (t < P * nb) {
         const uint32_t pix = (uint32_t)(t % P);
         const uint32_t s = s0 + (uint32_t)(t / P);
         const PathRay r = camera_ray(cam, p.width, p.height, pix % p.width, pix / p.width, s, p.spp);
         uint32_t visits = 0;
-        const SampleResult prim = integrate(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err);
+        const SampleResult prim =
+            integrate_diffuse(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err);
         if (prim.any_hit) {
             const float4 di = d_image[pix];
             const float w = 1.0f / (float)p.spp;
             const f3 g = mk3(di.x * w, di.y * w, di.z * w);
             replay(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, prim.color, g, d_diffuse,
-                   shared_lights ? s_light : d_light, visits, err);
+                   shared_lights ? s_light : d_light, gl0, visits, err);
         }
+    }
+    // light 0: warp sum, then one shared atomic per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        gl0.x += __shfl_down_sync(0xffffffffu, gl0.x, o);
+        gl0.y += __shfl_down_sync(0xffffffffu, gl0.y, o);
+        gl0.z += __shfl_down_sync(0xffffffffu, gl0.z, o);
+    }
+    if ((threadIdx.x & 31) == 0 && sc.num_lights > 0) {
+        float* dst = shared_lights ? s_light : d_light;
+        atomicAdd(dst + 0, gl0.x);
+        atomicAdd(dst + 1, gl0.y);
+        atomicAdd(dst + 2, gl0.z);
     }
     __syncthreads();
     if (shared_lights)

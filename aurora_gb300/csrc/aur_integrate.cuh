@@ -99,6 +99,76 @@ struct SampleResult {
     f3 last_pos, last_wo;
 };
 
+// Li at a hit: emission + ambient + direct light of every light, in the
+// reference's order (monteCarloRaytracer.cu:42-52, radiance.cuh:13-80).
+__device__ __forceinline__ f3 direct_light(const SceneView& sc, const aur_shader* sh, const Bsdf& b, const f3& position,
+                                           uint32_t seed, uint32_t scene, uint32_t pixel, uint32_t sample,
+                                           uint32_t rix, const StackRef& stk, uint32_t& visits, uint32_t* err) {
+    f3 Li = from(sh->emission_color);
+    for (uint32_t i = 0; i < sc.num_lights; ++i) {
+        const aur_light& L = sc.lights[i];
+        if (L.type == AUR_LIGHT_AMBIENT) Li = Li + bsdf_f(b) * ((from(L.color) * L.intensity) * L.ambient);
+        if (L.type != AUR_LIGHT_AREA) {
+            // estimateDirectRadianceDelta (radiance.cuh:18-33): no offset
+            f3 wdir; float wt, pdf;
+            const f3 Ls = sample_light(L, position, seed, scene, pixel, sample, rix, 0u, wdir, wt, pdf);
+            if (pdf > 0.0f && !zero(Ls)) {
+                const f3 f = bsdf_f(b);
+                float du = 0.0f, dv = 0.0f;
+                if (!zero(f) &&
+                    traverse<true>(sc.recs, sc.nodes, sc.perm, position, wdir, wt, du, dv, stk, visits, err) == kNoPrim)
+                    Li = Li + f * Ls * fmaxf(0.0f, dot(wdir, b.N));
+            }
+        } else {
+            // estimateDirectRadiance (radiance.cuh:35-80), light-sampling half
+            f3 acc = mk3(0.0f);
+            for (int32_t j = 0; j < L.samples; ++j) {
+                f3 Ls = mk3(0.0f);
+                f3 wdir; float wt, lpdf;
+                const f3 Lr = sample_light(L, position, seed, scene, pixel, sample, rix, light_slot(i, (uint32_t)j),
+                                           wdir, wt, lpdf);
+                // Ray::offset(Epsilon) (ray.cuh:184-191)
+                f3 wpos = position;
+                wpos.x += kEpsilon * wdir.x;
+                wpos.y += kEpsilon * wdir.y;
+                wpos.z += kEpsilon * wdir.z;
+                wt += kEpsilon;
+                if (lpdf > 0.0f && !zero(Lr)) {
+                    const f3 f = bsdf_f(b);
+                    float du = 0.0f, dv = 0.0f;
+                    if (!zero(f) &&
+                        traverse<true>(sc.recs, sc.nodes, sc.perm, wpos, wdir, wt, du, dv, stk, visits, err) == kNoPrim)
+                        Ls = Ls + f * Lr * fmaxf(0.0f, dot(wdir, b.N));
+                }
+                acc = acc + Ls;
+            }
+            const float ns = (float)L.samples;
+            Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
+        }
+    }
+    return Li;
+}
+
+// Diffuse bounce of path mode: BSDF::samplef (bsdf.cuh:222-236) with
+// throughput f * |wi.N| / pdf. Returns false when the path ends here.
+__device__ __forceinline__ bool diffuse_bounce(const Bsdf& b, const f3& wo, const f3& thr, uint32_t seed,
+                                               uint32_t scene, uint32_t pixel, uint32_t sample, uint32_t rix, f3& wi,
+                                               f3& nthr) {
+    float u1, u2;
+    draw2(seed, scene, pixel, sample, rix, 0u, u1, u2);
+    const f3 lwo = world_to_local(wo, b.N, b.S, b.T);
+    f3 lwi = sample_hemisphere_cosine(u1, u2);
+    if (lwo.z < 0.0f) lwi.z *= -1.0f;
+    const float pdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
+    const f3 f = bsdf_f(b);
+    wi = local_to_world(lwi, b.N, b.S, b.T);
+    if (pdf > 0.0f && !zero(f)) {
+        nthr = thr * (f * (fabsf(dot(wi, b.N)) / pdf));
+        return true;
+    }
+    return false;
+}
+
 // Integrates one camera ray. RNG key: (seed, scene_id) x (pixel, sample,
 // ray index within the sample, slot).
 __device__ __forceinline__ SampleResult integrate(const SceneView& sc, uint32_t max_depth, uint32_t mode,
@@ -131,48 +201,7 @@ __device__ __forceinline__ SampleResult integrate(const SceneView& sc, uint32_t 
         const aur_shader* sh = sc.shaders + (sid > 0 ? sid - 1 : 0);   // getSafeID (util/array.h:16-17)
         const float refl = sh->reflectivity, trans = sh->translucence;
         const Bsdf b = get_bsdf(sc, from(sh->diffuse_color), sh->diffuse, tri, u, v);
-        f3 Li = from(sh->emission_color);
-        for (uint32_t i = 0; i < sc.num_lights; ++i) {
-            const aur_light& L = sc.lights[i];
-            if (L.type == AUR_LIGHT_AMBIENT) Li = Li + bsdf_f(b) * ((from(L.color) * L.intensity) * L.ambient);
-            if (L.type != AUR_LIGHT_AREA) {
-                // estimateDirectRadianceDelta (radiance.cuh:18-33): no offset
-                f3 wdir; float wt, pdf;
-                const f3 Ls = sample_light(L, position, seed, scene, pixel, sample, rix, 0u, wdir, wt, pdf);
-                if (pdf > 0.0f && !zero(Ls)) {
-                    const f3 f = bsdf_f(b);
-                    float du = 0.0f, dv = 0.0f;
-                    if (!zero(f) &&
-                        traverse<true>(sc.recs, sc.nodes, sc.perm, position, wdir, wt, du, dv, stk, visits, err) == kNoPrim)
-                        Li = Li + f * Ls * fmaxf(0.0f, dot(wdir, b.N));
-                }
-            } else {
-                // estimateDirectRadiance (radiance.cuh:35-80), light-sampling half
-                f3 acc = mk3(0.0f);
-                for (int32_t j = 0; j < L.samples; ++j) {
-                    f3 Ls = mk3(0.0f);
-                    f3 wdir; float wt, lpdf;
-                    const f3 Lr = sample_light(L, position, seed, scene, pixel, sample, rix, light_slot(i, (uint32_t)j),
-                                               wdir, wt, lpdf);
-                    // Ray::offset(Epsilon) (ray.cuh:184-191)
-                    f3 wpos = position;
-                    wpos.x += kEpsilon * wdir.x;
-                    wpos.y += kEpsilon * wdir.y;
-                    wpos.z += kEpsilon * wdir.z;
-                    wt += kEpsilon;
-                    if (lpdf > 0.0f && !zero(Lr)) {
-                        const f3 f = bsdf_f(b);
-                        float du = 0.0f, dv = 0.0f;
-                        if (!zero(f) &&
-                            traverse<true>(sc.recs, sc.nodes, sc.perm, wpos, wdir, wt, du, dv, stk, visits, err) == kNoPrim)
-                            Ls = Ls + f * Lr * fmaxf(0.0f, dot(wdir, b.N));
-                    }
-                    acc = acc + Ls;
-                }
-                const float ns = (float)L.samples;
-                Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
-            }
-        }
+        const f3 Li = direct_light(sc, sh, b, position, seed, scene, pixel, sample, rix, stk, visits, err);
         const bool specular = refl > 0.0f || trans > 0.0f;
         if (specular) depth++;
         if (depth <= maxd && refl > 0.0f) {
@@ -206,26 +235,55 @@ __device__ __forceinline__ SampleResult integrate(const SceneView& sc, uint32_t 
         if (mode == AUR_MODE_PATH && !specular) {
             depth++;
             if (depth <= maxd) {
-                float u1, u2;
-                draw2(seed, scene, pixel, sample, rix, 0u, u1, u2);
-                const f3 lwo = world_to_local(wo, b.N, b.S, b.T);
-                f3 lwi = sample_hemisphere_cosine(u1, u2);
-                if (lwo.z < 0.0f) lwi.z *= -1.0f;
-                const float pdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
-                const f3 f = bsdf_f(b);
-                const f3 wi = local_to_world(lwi, b.N, b.S, b.T);
-                if (pdf > 0.0f && !zero(f)) {
-                    PathRay nr;
-                    nr.pos = position;
-                    nr.dir = wi;
-                    nr.weight = 1.0f;
-                    nr.eta = ray.eta;
-                    nr.thr = ray.thr * (f * (fabsf(dot(wi, b.N)) / pdf));
+                PathRay nr;
+                nr.pos = position;
+                nr.weight = 1.0f;
+                nr.eta = ray.eta;
+                if (diffuse_bounce(b, wo, ray.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr)) {
                     if (sp < AUR_MAX_DEPTH + 2) stack[sp++] = nr; else atomicOr(err, 2u);
                 }
             }
         }
         res.color = res.color + Li * ray.thr;
+    }
+    return res;
+}
+
+// The same estimator for scenes without specular shaders: one ray in flight
+// per sample, no ray stack (a Lambert hit spawns at most the diffuse bounce).
+// Same operations in the same order as integrate().
+__device__ __forceinline__ SampleResult integrate_diffuse(const SceneView& sc, uint32_t max_depth, uint32_t mode,
+                                                          uint32_t seed, uint32_t scene, uint32_t pixel,
+                                                          uint32_t sample, const PathRay& primary, const StackRef& stk,
+                                                          uint32_t& visits, uint32_t* err) {
+    SampleResult res;
+    res.color = mk3(0.0f);
+    res.any_hit = false;
+    res.last_tri = kNoPrim;
+    res.last_u = res.last_v = 0.0f;
+    res.last_pos = res.last_wo = mk3(0.0f);
+    f3 pos = primary.pos, dir = primary.dir, thr = primary.thr;
+    uint32_t depth = 0;
+    for (uint32_t rix = 0;; ++rix) {
+        float t = kInfinity, u = 0.0f, v = 0.0f;
+        const uint32_t tri = traverse<false>(sc.recs, sc.nodes, sc.perm, pos, dir, t, u, v, stk, visits, err);
+        if (tri == kNoPrim) break;
+        res.any_hit = true;
+        const f3 position = pos + (dir * t);
+        const f3 wo = -dir;
+        res.last_tri = tri; res.last_u = u; res.last_v = v; res.last_pos = position; res.last_wo = wo;
+        const uint32_t sid = sc.sids[tri];
+        const aur_shader* sh = sc.shaders + (sid > 0 ? sid - 1 : 0);
+        const Bsdf b = get_bsdf(sc, from(sh->diffuse_color), sh->diffuse, tri, u, v);
+        const f3 Li = direct_light(sc, sh, b, position, seed, scene, pixel, sample, rix, stk, visits, err);
+        res.color = res.color + Li * thr;
+        if (mode != AUR_MODE_PATH) break;
+        if (++depth > max_depth) break;
+        f3 wi, nthr;
+        if (!diffuse_bounce(b, wo, thr, seed, scene, pixel, sample, rix, wi, nthr)) break;
+        pos = position;
+        dir = wi;
+        thr = nthr;
     }
     return res;
 }

@@ -71,6 +71,7 @@ struct aur_scene {
     uint32_t num_shaders = 0;
     aur_light* lights = nullptr;
     uint32_t num_lights = 0;
+    bool has_specular = false;        // any shader with reflectivity or translucence > 0
 };
 
 namespace aur {

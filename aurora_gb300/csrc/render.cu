@@ -29,7 +29,9 @@ __device__ __forceinline__ StackRef stack_ref(uint32_t* smem, int cap) {
     return s;
 }
 
-// colors[b * P + p] = (rgb, hit) of sample s0 + b at pixel p.
+// colors[b * P + p] = (rgb, hit) of sample s0 + b at pixel p. kGeneric
+// selects the integrator with the specular ray stack.
+template <bool kGeneric>
 __global__ void __launch_bounds__(kRenderThreads) k_render_samples(SceneView sc, aur_camera cam, aur_render_params p,
                                                                    uint32_t s0, uint32_t nb, float4* __restrict__ colors,
                                                                    uint32_t* __restrict__ err, int cap) {
@@ -42,7 +44,9 @@ __global__ void __launch_bounds__(kRenderThreads) k_render_samples(SceneView sc,
     const uint32_t s = s0 + (uint32_t)(t / P);
     const PathRay r = camera_ray(cam, p.width, p.height, pix % p.width, pix / p.width, s, p.spp);
     uint32_t visits = 0;
-    const SampleResult res = integrate(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err);
+    const SampleResult res =
+        kGeneric ? integrate(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err)
+                 : integrate_diffuse(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err);
     colors[t] = make_float4(res.color.x, res.color.y, res.color.z, res.any_hit ? 1.0f : 0.0f);
 }
 
@@ -82,6 +86,7 @@ __global__ void k_generate_rays(uint32_t W, uint32_t H, uint32_t sample, uint32_
 }
 
 // cudaRaytraceKernel (monteCarloRaytracer.cu:90-113) on caller-provided rays.
+template <bool kGeneric>
 __global__ void __launch_bounds__(kRenderThreads) k_raytrace_mc(SceneView sc, aur_render_params p, uint32_t sample,
                                                                 uint32_t offset, uint32_t num,
                                                                 const aur_path_ray* __restrict__ rays,
@@ -100,7 +105,9 @@ __global__ void __launch_bounds__(kRenderThreads) k_raytrace_mc(SceneView sc, au
     r.eta = in.eta;
     r.thr = mk3(in.weight);
     uint32_t visits = 0;
-    const SampleResult res = integrate(sc, p.max_depth, p.mode, p.seed, p.scene_id, id, sample, r, stk, visits, err);
+    const SampleResult res =
+        kGeneric ? integrate(sc, p.max_depth, p.mode, p.seed, p.scene_id, id, sample, r, stk, visits, err)
+                 : integrate_diffuse(sc, p.max_depth, p.mode, p.seed, p.scene_id, id, sample, r, stk, visits, err);
     aur_hitpoint h = hits[id];
     h.color = to(from(h.color) + res.color);
     if (res.any_hit) {
@@ -187,8 +194,12 @@ aur_status aur_render(aur_ctx* ctx, const aur_scene* scene, const aur_camera* ca
     const float weight = 1.0f / (float)p.spp;
     for (uint32_t s = s0; s < s1; s += batch) {
         const uint32_t nb = std::min(batch, s1 - s);
-        k_render_samples<<<cdiv(P * nb, kRenderThreads), kRenderThreads, smem, ctx->stream>>>(
-            sv, *camera, p, s, nb, colors, ctx->d_flags, cap);
+        if (scene->has_specular)
+            k_render_samples<true><<<cdiv(P * nb, kRenderThreads), kRenderThreads, smem, ctx->stream>>>(
+                sv, *camera, p, s, nb, colors, ctx->d_flags, cap);
+        else
+            k_render_samples<false><<<cdiv(P * nb, kRenderThreads), kRenderThreads, smem, ctx->stream>>>(
+                sv, *camera, p, s, nb, colors, ctx->d_flags, cap);
         k_accumulate<<<cdiv(P, 256), 256, 0, ctx->stream>>>(colors, (uint32_t)P, nb, weight, (float4*)accum);
     }
     cudaFreeAsync(colors, ctx->stream);
@@ -218,8 +229,12 @@ aur_status aur_raytrace_monte_carlo(aur_ctx* ctx, const aur_scene* scene, const 
     if (num_rays == 0) return AUR_OK;
     const int cap = stack_cap(scene);
     const size_t smem = (size_t)3 * cap * kRenderThreads * sizeof(uint32_t);
-    k_raytrace_mc<<<cdiv(num_rays, kRenderThreads), kRenderThreads, smem, ctx->stream>>>(
-        scene_view(scene), *params, sample_id, offset, num_rays, rays, hits, ctx->d_flags, cap);
+    if (scene->has_specular)
+        k_raytrace_mc<true><<<cdiv(num_rays, kRenderThreads), kRenderThreads, smem, ctx->stream>>>(
+            scene_view(scene), *params, sample_id, offset, num_rays, rays, hits, ctx->d_flags, cap);
+    else
+        k_raytrace_mc<false><<<cdiv(num_rays, kRenderThreads), kRenderThreads, smem, ctx->stream>>>(
+            scene_view(scene), *params, sample_id, offset, num_rays, rays, hits, ctx->d_flags, cap);
     AUR_CUDA(cudaGetLastError());
     return AUR_OK;
 }

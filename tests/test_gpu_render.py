@@ -86,3 +86,23 @@ def test_invalid_arguments_raise(ctx):
     with pytest.raises(api.AuroraError) as e:
         sc.set_shaders(bad)
     assert e.value.status == 6
+
+
+@pytest.mark.parametrize("mode", [T.MODE_REFERENCE, T.MODE_PATH])
+def test_specular_render_matches_oracle(ctx, mode):
+    """Reflective and refractive shaders exercise the reference's ray stack
+    (monteCarloRaytracer.cu:54-85)."""
+    sd = scenes.cornell()
+    sh = np.concatenate([sd.shaders, np.stack([T.lambert((0.9, 0.9, 0.9)), T.lambert((0.8, 0.9, 1.0))])])
+    sh["reflectivity"][3] = 0.6
+    sh["translucence"][4] = 0.7
+    sh["refractive_index"][4] = 1.5
+    sids = sd.shader_ids.copy()
+    sids[10:22] = 4          # short block: mirror-like
+    sids[22:34] = 5          # tall block: glass-like
+    sd2 = scenes.SceneData("cornell_specular", sd.vertices, sd.normals, sids, sh, sd.lights, sd.camera)
+    sc = api.Scene(ctx, sd2)
+    p = T.render_params(48, 48, 4, 5, seed=11, mode=mode)
+    img = sc.render(p).cpu().numpy()
+    ref, _ = oracle.render(oracle.NmhScene(sd2), p)
+    assert np.array_equal(img, ref)
