@@ -20,6 +20,9 @@
 #include <algorithm>
 #include <vector>
 
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
+
 #include "aur_integrate.cuh"
 #include "aur_internal.h"
 
@@ -150,31 +153,65 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
             dc.y += c1.y != 0.0f ? Lrem.y / c1.y : 0.0f;
             dc.z += c1.z != 0.0f ? Lrem.z / c1.z : 0.0f;
         }
-        // color1 = diffuse_color * diffuse
+        // color1 = diffuse_color * diffuse. Lanes that hit the same shader
+        // (large triangles are hit by most of a warp) are summed first, so a
+        // warp issues one atomic per shader instead of one per lane.
         const f3 gd = g * dc * sh->diffuse;
-        if (gd.x != 0.0f || gd.y != 0.0f || gd.z != 0.0f) {
-            atomicAdd(d_diffuse + 3 * si + 0, gd.x);
-            atomicAdd(d_diffuse + 3 * si + 1, gd.y);
-            atomicAdd(d_diffuse + 3 * si + 2, gd.z);
+        {
+            namespace cg = cooperative_groups;
+            const cg::coalesced_group active = cg::coalesced_threads();
+            const cg::coalesced_group same = cg::labeled_partition(active, si);
+            const float sx = cg::reduce(same, gd.x, cg::plus<float>());
+            const float sy = cg::reduce(same, gd.y, cg::plus<float>());
+            const float sz = cg::reduce(same, gd.z, cg::plus<float>());
+            if (same.thread_rank() == 0 && (sx != 0.0f || sy != 0.0f || sz != 0.0f)) {
+                atomicAdd(d_diffuse + 3 * si + 0, sx);
+                atomicAdd(d_diffuse + 3 * si + 1, sy);
+                atomicAdd(d_diffuse + 3 * si + 2, sz);
+            }
         }
         if (!cont) return;
         ray = nr;
     }
 }
 
-__global__ void __launch_bounds__(kAdjThreads) k_adjoint(SceneView sc, aur_camera cam, aur_render_params p, uint32_t s0,
-                                                         uint32_t nb, const float4* __restrict__ d_image,
-                                                         float* __restrict__ d_diffuse, float* __restrict__ d_light,
-                                                         uint32_t* __restrict__ err, int cap) {
-    extern __shared__ uint32_t smem[];
+__device__ __forceinline__ StackRef adj_stack(uint32_t* smem, int cap) {
     StackRef stk;
-    stk.idx = smem + threadIdx.x;
-    stk.lo = reinterpret_cast<float*>(smem + cap * kAdjThreads) + threadIdx.x;
-    stk.hi = reinterpret_cast<float*>(smem + 2 * cap * kAdjThreads) + threadIdx.x;
+    stk.lo = reinterpret_cast<float*>(smem) + threadIdx.x;
+    stk.hi = reinterpret_cast<float*>(smem + cap * kAdjThreads) + threadIdx.x;
     stk.stride = kAdjThreads;
     stk.cap = cap;
+    return stk;
+}
+
+// Primal pass: the radiance C of every camera sample (the estimator of
+// aur_render), w = 1 when the sample hit something.
+__global__ void __launch_bounds__(kAdjThreads) k_adj_primal(SceneView sc, aur_camera cam, aur_render_params p, uint32_t s0,
+                                                            uint32_t nb, float4* __restrict__ prim,
+                                                            uint32_t* __restrict__ err, int cap) {
+    extern __shared__ uint32_t smem[];
+    const StackRef stk = adj_stack(smem, cap);
+    const uint64_t P = (uint64_t)p.width * p.height;
+    const uint64_t t = (uint64_t)blockIdx.x * kAdjThreads + threadIdx.x;
+    if (t >= P * nb) return;
+    const uint32_t pix = (uint32_t)(t % P);
+    const uint32_t s = s0 + (uint32_t)(t / P);
+    const PathRay r = camera_ray(cam, p.width, p.height, pix % p.width, pix / p.width, s, p.spp);
+    uint32_t visits = 0;
+    const SampleResult res = integrate_diffuse(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err);
+    prim[t] = make_float4(res.color.x, res.color.y, res.color.z, res.any_hit ? 1.0f : 0.0f);
+}
+
+// Replay pass.
+__global__ void __launch_bounds__(kAdjThreads) k_adj_replay(SceneView sc, aur_camera cam, aur_render_params p, uint32_t s0,
+                                                            uint32_t nb, const float4* __restrict__ prim,
+                                                            const float4* __restrict__ d_image,
+                                                            float* __restrict__ d_diffuse, float* __restrict__ d_light,
+                                                            uint32_t* __restrict__ err, int cap) {
+    extern __shared__ uint32_t smem[];
+    const StackRef stk = adj_stack(smem, cap);
     // light gradients are reduced in shared memory first (one light is hit by every sample)
-    float* s_light = reinterpret_cast<float*>(smem + 3 * cap * kAdjThreads);
+    float* s_light = reinterpret_cast<float*>(smem + 2 * cap * kAdjThreads);
     const bool shared_lights = sc.num_lights <= kSharedLights;
     if (shared_lights)
         for (uint32_t i = threadIdx.x; i < 3 * sc.num_lights; i += kAdjThreads) s_light[i] = 0.0f;
@@ -183,17 +220,16 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint(SceneView sc, aur_camer
     const uint64_t t = (uint64_t)blockIdx.x * kAdjThreads + threadIdx.x;
     f3 gl0 = mk3(0.0f);
     if (t < P * nb) {
-        const uint32_t pix = (uint32_t)(t % P);
-        const uint32_t s = s0 + (uint32_t)(t / P);
-        const PathRay r = camera_ray(cam, p.width, p.height, pix % p.width, pix / p.width, s, p.spp);
-        uint32_t visits = 0;
-        const SampleResult prim =
-            integrate_diffuse(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err);
-        if (prim.any_hit) {
+        const float4 c = prim[t];
+        if (c.w != 0.0f) {
+            const uint32_t pix = (uint32_t)(t % P);
+            const uint32_t s = s0 + (uint32_t)(t / P);
+            const PathRay r = camera_ray(cam, p.width, p.height, pix % p.width, pix / p.width, s, p.spp);
             const float4 di = d_image[pix];
             const float w = 1.0f / (float)p.spp;
             const f3 g = mk3(di.x * w, di.y * w, di.z * w);
-            replay(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, prim.color, g, d_diffuse,
+            uint32_t visits = 0;
+            replay(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, mk3(c.x, c.y, c.z), g, d_diffuse,
                    shared_lights ? s_light : d_light, gl0, visits, err);
         }
     }
@@ -250,14 +286,21 @@ aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_ca
     const uint64_t P = (uint64_t)p.width * p.height;
     const uint32_t batch = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(s1 - s0, (1ull << 24) / P));
     const int cap = (int)scene->nmh->levels + 1;
-    const size_t smem = (size_t)3 * cap * kAdjThreads * sizeof(uint32_t) + 3 * kSharedLights * sizeof(float);
-    AUR_CUDA(cudaFuncSetAttribute(k_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem_p = (size_t)2 * cap * kAdjThreads * sizeof(uint32_t);
+    const size_t smem_r = smem_p + 3 * kSharedLights * sizeof(float);
+    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
+    float4* prim = nullptr;
+    AUR_CHECK(cudaMallocAsync(&prim, P * batch * sizeof(float4), ctx->stream) == cudaSuccess, AUR_ERR_OOM,
+              "aur_render_adjoint: out of device memory");
     const SceneView sv = scene_view(scene);
     for (uint32_t s = s0; s < s1; s += batch) {
         const uint32_t nb = std::min(batch, s1 - s);
-        k_adjoint<<<cdiv(P * nb, kAdjThreads), kAdjThreads, smem, ctx->stream>>>(
-            sv, *camera, p, s, nb, (const float4*)d_image, d_diffuse, d_light_color, ctx->d_flags, cap);
+        const uint32_t grid = cdiv(P * nb, kAdjThreads);
+        k_adj_primal<<<grid, kAdjThreads, smem_p, ctx->stream>>>(sv, *camera, p, s, nb, prim, ctx->d_flags, cap);
+        k_adj_replay<<<grid, kAdjThreads, smem_r, ctx->stream>>>(sv, *camera, p, s, nb, prim, (const float4*)d_image,
+                                                                d_diffuse, d_light_color, ctx->d_flags, cap);
     }
+    cudaFreeAsync(prim, ctx->stream);
     AUR_CUDA(cudaGetLastError());
     return AUR_OK;
 }

@@ -21,9 +21,8 @@ inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b
 
 __device__ __forceinline__ StackRef stack_ref(uint32_t* smem, int cap) {
     StackRef s;
-    s.idx = smem + threadIdx.x;
-    s.lo = reinterpret_cast<float*>(smem + cap * blockDim.x) + threadIdx.x;
-    s.hi = reinterpret_cast<float*>(smem + 2 * cap * blockDim.x) + threadIdx.x;
+    s.lo = reinterpret_cast<float*>(smem) + threadIdx.x;
+    s.hi = reinterpret_cast<float*>(smem + cap * blockDim.x) + threadIdx.x;
     s.stride = blockDim.x;
     s.cap = cap;
     return s;
@@ -189,7 +188,7 @@ aur_status aur_render(aur_ctx* ctx, const aur_scene* scene, const aur_camera* ca
     AUR_CHECK(cudaMallocAsync(&colors, P * batch * sizeof(float4), ctx->stream) == cudaSuccess, AUR_ERR_OOM,
               "aur_render: out of device memory");
     const int cap = stack_cap(scene);
-    const size_t smem = (size_t)3 * cap * kRenderThreads * sizeof(uint32_t);
+    const size_t smem = (size_t)2 * cap * kRenderThreads * sizeof(uint32_t);
     const SceneView sv = scene_view(scene);
     const float weight = 1.0f / (float)p.spp;
     for (uint32_t s = s0; s < s1; s += batch) {
@@ -228,7 +227,7 @@ aur_status aur_raytrace_monte_carlo(aur_ctx* ctx, const aur_scene* scene, const 
     AUR_CUDA(cudaSetDevice(ctx->device));
     if (num_rays == 0) return AUR_OK;
     const int cap = stack_cap(scene);
-    const size_t smem = (size_t)3 * cap * kRenderThreads * sizeof(uint32_t);
+    const size_t smem = (size_t)2 * cap * kRenderThreads * sizeof(uint32_t);
     if (scene->has_specular)
         k_raytrace_mc<true><<<cdiv(num_rays, kRenderThreads), kRenderThreads, smem, ctx->stream>>>(
             scene_view(scene), *params, sample_id, offset, num_rays, rays, hits, ctx->d_flags, cap);

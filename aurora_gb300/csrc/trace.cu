@@ -10,6 +10,8 @@
 // when the slab is hit. The traversal stack lives in shared memory: the
 // near child is visited next, only the far child is pushed, so the stack
 // never holds more entries than the heap has levels.
+#include <algorithm>
+
 #include "aur_internal.h"
 #include "aur_math.cuh"
 #include "aur_traverse.cuh"
@@ -18,79 +20,114 @@ namespace aur {
 namespace {
 
 constexpr int kTraceThreads = 128;
+constexpr uint32_t kNoRay = 0xFFFFFFFFu;
 
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Persistent traversal kernel with dynamic ray fetch: a lane whose ray is
+// done takes the next unprocessed ray at once (one atomic per warp for all
+// lanes asking together), so warps stay full until the ray pool is drained
+// (Aila & Laine, "Understanding the efficiency of ray traversal on GPUs",
+// HPG'09). Every ray is traversed exactly as intersect()/intersectAny().
 template <bool kAny, bool kCount>
 __global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restrict__ recs, uint32_t nodes,
                                                          const uint32_t* __restrict__ perm,
                                                          const float4* __restrict__ rays, uint32_t n,
                                                          float4* __restrict__ hits, uint32_t* __restrict__ occ,
                                                          unsigned long long* __restrict__ visit_counter,
-                                                         uint32_t* __restrict__ err, int cap) {
+                                                         uint32_t* __restrict__ ray_counter, int cap) {
     extern __shared__ uint32_t smem[];
     const int tid = threadIdx.x;
     StackRef stk;
-    stk.idx = smem + tid;
-    stk.lo = reinterpret_cast<float*>(smem + cap * kTraceThreads) + tid;
-    stk.hi = reinterpret_cast<float*>(smem + 2 * cap * kTraceThreads) + tid;
+    stk.lo = reinterpret_cast<float*>(smem) + tid;
+    stk.hi = reinterpret_cast<float*>(smem + cap * kTraceThreads) + tid;
     stk.stride = kTraceThreads;
     stk.cap = cap;
-    const uint32_t i = blockIdx.x * kTraceThreads + tid;
     uint32_t visits = 0;
-    if (i < n) {
-        const float4 r0 = rays[2 * (size_t)i];
-        const float4 r1 = rays[2 * (size_t)i + 1];
-        const f3 pos = mk3(r0.x, r0.y, r0.z);
-        const f3 dir = mk3(r1.x, r1.y, r1.z);
-        float best_t = r0.w, bu = 0.0f, bv = 0.0f;
-        const uint32_t best = traverse<kAny>(recs, nodes, perm, pos, dir, best_t, bu, bv, stk, visits, err);
-        if (kAny) {
-            occ[i] = best == kNoPrim ? AUR_NO_HIT : perm[best];
+    uint32_t i = kNoRay;
+    f3 pos = mk3(0.0f), dir = mk3(0.0f);
+    float tmax = 0.0f, best_t = 0.0f, bu = 0.0f, bv = 0.0f;
+    uint32_t best = kNoPrim;
+    TravState s;
+    trav_init(s);
+    for (;;) {
+        if (i == kNoRay) {
+            const uint32_t m = __activemask();
+            const int leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if ((tid & 31) == leader) base = atomicAdd(ray_counter, (uint32_t)__popc(m));
+            base = __shfl_sync(m, base, leader);
+            i = base + __popc(m & lanemask_lt());
+            if (i >= n) break;
+            const float4 r0 = rays[2 * (size_t)i];
+            const float4 r1 = rays[2 * (size_t)i + 1];
+            pos = mk3(r0.x, r0.y, r0.z);
+            dir = mk3(r1.x, r1.y, r1.z);
+            tmax = best_t = r0.w;
+            bu = bv = 0.0f;
+            best = kNoPrim;
+            trav_init(s);
+        }
+        float4 q0;
+        float nlo, nhi;
+        bool done;
+        if (trav_next(s, recs, nodes, pos, dir, best_t, stk, q0, nlo, nhi, visits)) {
+            done = node_triangles<kAny>(recs, s.k, q0, perm, pos, dir, best_t, bu, bv, best);
+            if (!done) trav_descend(s, dir, nodes, stk, nlo, nhi);
         } else {
-            float4 h;
-            h.x = best == kNoPrim ? r0.w : best_t;
-            h.y = best == kNoPrim ? 0.0f : bu;
-            h.z = best == kNoPrim ? 0.0f : bv;
-            h.w = __uint_as_float(best == kNoPrim ? AUR_NO_HIT : perm[best]);
-            hits[i] = h;
+            done = true;
+        }
+        if (done) {
+            if (kAny) {
+                occ[i] = best == kNoPrim ? AUR_NO_HIT : perm[best];
+            } else {
+                float4 h;
+                h.x = best == kNoPrim ? tmax : best_t;
+                h.y = best == kNoPrim ? 0.0f : bu;
+                h.z = best == kNoPrim ? 0.0f : bv;
+                h.w = __uint_as_float(best == kNoPrim ? AUR_NO_HIT : perm[best]);
+                hits[i] = h;
+            }
+            i = kNoRay;
         }
     }
-    if (kCount) {
-        unsigned long long v = visits;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if ((tid & 31) == 0 && v) atomicAdd(visit_counter, v);
-    }
+    if (kCount && visits) atomicAdd(visit_counter, (unsigned long long)visits);
 }
 
 inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
 }  // namespace
 
+template <bool kAny, bool kCount>
+aur_status launch_one(aur_ctx* ctx, const aur_nmh* nmh, const float4* r, uint32_t n, float4* h, uint32_t* occ,
+                      unsigned long long* visit_counter, cudaStream_t stream) {
+    const int cap = (int)nmh->levels + 1;
+    const size_t smem = (size_t)2 * cap * kTraceThreads * sizeof(uint32_t);
+    int per_sm = 0;
+    AUR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<kAny, kCount>, kTraceThreads, smem));
+    const uint32_t grid = std::max(1u, std::min<uint32_t>(cdiv(n, kTraceThreads), (uint32_t)(ctx->sm_count * per_sm)));
+    uint32_t* ray_counter = ctx->d_flags + 8;
+    AUR_CUDA(cudaMemsetAsync(ray_counter, 0, sizeof(uint32_t), stream));
+    k_trace<kAny, kCount><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r, n, h, occ,
+                                                                visit_counter, ray_counter, cap);
+    AUR_CUDA(cudaGetLastError());
+    return AUR_OK;
+}
+
 aur_status launch_trace(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits,
                         uint32_t* occluder, unsigned long long* visit_counter, cudaStream_t stream) {
     if (n == 0) return AUR_OK;
-    const int cap = (int)nmh->levels + 1;
-    const size_t smem = (size_t)3 * cap * kTraceThreads * sizeof(uint32_t);
-    const dim3 grid(cdiv(n, kTraceThreads));
     const float4* r = reinterpret_cast<const float4*>(rays);
     float4* h = reinterpret_cast<float4*>(hits);
-    uint32_t* err = ctx->d_flags;
-    if (visit_counter) {
-        if (occluder)
-            k_trace<true, true><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r, n,
-                                                                      nullptr, occluder, visit_counter, err, cap);
-        else
-            k_trace<false, true><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r, n,
-                                                                       h, nullptr, visit_counter, err, cap);
-    } else if (occluder) {
-        k_trace<true, false><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r, n,
-                                                                   nullptr, occluder, nullptr, err, cap);
-    } else {
-        k_trace<false, false><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r, n, h,
-                                                                    nullptr, nullptr, err, cap);
-    }
-    AUR_CUDA(cudaGetLastError());
-    return AUR_OK;
+    if (visit_counter)
+        return occluder ? launch_one<true, true>(ctx, nmh, r, n, nullptr, occluder, visit_counter, stream)
+                        : launch_one<false, true>(ctx, nmh, r, n, h, nullptr, visit_counter, stream);
+    return occluder ? launch_one<true, false>(ctx, nmh, r, n, nullptr, occluder, nullptr, stream)
+                    : launch_one<false, false>(ctx, nmh, r, n, h, nullptr, nullptr, stream);
 }
 
 }  // namespace aur

@@ -108,9 +108,8 @@ __device__ __forceinline__ uint32_t agg_inc(uint32_t* ctr) {
 
 __device__ __forceinline__ StackRef wf_stack(uint32_t* smem, int cap) {
     StackRef s;
-    s.idx = smem + threadIdx.x;
-    s.lo = reinterpret_cast<float*>(smem + cap * blockDim.x) + threadIdx.x;
-    s.hi = reinterpret_cast<float*>(smem + 2 * cap * blockDim.x) + threadIdx.x;
+    s.lo = reinterpret_cast<float*>(smem) + threadIdx.x;
+    s.hi = reinterpret_cast<float*>(smem + cap * blockDim.x) + threadIdx.x;
     s.stride = blockDim.x;
     s.cap = cap;
     return s;
@@ -584,7 +583,7 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     bt->tuning = tn;
     bt->block = tn.block_size;
     bt->grid = (uint32_t)ctx->sm_count * tn.blocks_per_sm;
-    bt->smem = (size_t)3 * cap * tn.block_size * sizeof(uint32_t);
+    bt->smem = (size_t)2 * cap * tn.block_size * sizeof(uint32_t);
     bt->accum_host.assign(num_scenes, nullptr);
     const uint64_t Q = tn.paths_in_flight;
     const uint64_t out_items = P_tot * tn.samples_per_wave;
