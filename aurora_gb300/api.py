@@ -64,6 +64,7 @@ SIGNATURES = {
     "aur_batch_destroy": ([P], ctypes.c_int),
     "aur_batch_autotune": ([P, P, P, P, U32, P, P], ctypes.c_int),
     "aur_render_adjoint": ([P, P, P, P, P, P, P], ctypes.c_int),
+    "aur_batch_profile": ([P, P, P, P], ctypes.c_int),
 }
 
 
@@ -356,6 +357,14 @@ class Batch:
         ptrs = (P * len(accums))(*[a.data_ptr() for a in accums])
         check(lib().aur_batch_render(self.ctx.handle, self.handle, ptrs))
         return accums
+
+    def profile(self, accums):
+        """Stepped render without the graph; returns per-stage milliseconds."""
+        ptrs = (P * len(accums))(*[a.data_ptr() for a in accums])
+        ms = np.zeros(7, np.float32)
+        check(lib().aur_batch_profile(self.ctx.handle, self.handle, ptrs, _ptr(ms)))
+        return dict(zip(["setup", "generate", "extend", "shade", "shadow", "combine", "accumulate"],
+                        [float(x) for x in ms]))
 
     def status(self):
         it = U32()

@@ -696,6 +696,72 @@ aur_status aur_batch_destroy(aur_batch* bt) {
     return AUR_OK;
 }
 
+// Runs the batch's stage kernels one by one from the host, without the
+// graph, and accumulates the time of each stage with CUDA events:
+// stage_ms[0..6] = set-up, generate (+commit), extend, shade, shadow,
+// combine (+end), accumulate (+next wave). Same kernels, same results; for
+// profiling only (one host round trip per iteration).
+aur_status aur_batch_profile(aur_ctx* ctx, aur_batch* bt, float* const* accum, float stage_ms[7]) {
+    clear_error();
+    AUR_CHECK(ctx && bt && accum && stage_ms, AUR_ERR_INVALID, "aur_batch_profile: null argument");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    for (uint32_t i = 0; i < bt->num_scenes; ++i) bt->accum_host[i] = (float4*)accum[i];
+    const WfArgs& a = bt->args;
+    cudaStream_t st = ctx->stream;
+    AUR_CUDA(cudaMemcpyAsync((void*)a.accum, bt->accum_host.data(), sizeof(float4*) * bt->num_scenes,
+                             cudaMemcpyHostToDevice, st));
+    AUR_CUDA(cudaMemsetAsync(&a.ctl->wave, 0, sizeof(uint32_t), st));
+    AUR_CUDA(cudaMemsetAsync(&a.ctl->error, 0, sizeof(uint32_t) * 2, st));
+    cudaEvent_t ev[8];
+    for (auto& e : ev) cudaEventCreate(&e);
+    for (int i = 0; i < 7; ++i) stage_ms[i] = 0.0f;
+    auto lap = [&](int stage, int e0, int e1) {
+        float ms = 0.0f;
+        cudaEventSynchronize(ev[e1]);
+        cudaEventElapsedTime(&ms, ev[e0], ev[e1]);
+        stage_ms[stage] += ms;
+    };
+    const uint32_t g = bt->grid, bs = bt->block;
+    WfCtl c;
+    AUR_CUDA(cudaMemcpyAsync(&c, a.ctl, sizeof(c), cudaMemcpyDeviceToHost, st));
+    AUR_CUDA(cudaStreamSynchronize(st));
+    for (uint32_t w = 0; w < c.num_waves; ++w) {
+        cudaEventRecord(ev[0], st);
+        k_wf_setup<<<g, bs, 0, st>>>(a);
+        cudaEventRecord(ev[1], st);
+        lap(0, 0, 1);
+        for (uint32_t it = 0;; ++it) {
+            cudaEventRecord(ev[0], st);
+            k_wf_generate<<<g, bs, 0, st>>>(a);
+            k_wf_generate_commit<<<1, 1, 0, st>>>(a);
+            cudaEventRecord(ev[1], st);
+            k_wf_extend<<<g, bs, bt->smem, st>>>(a);
+            cudaEventRecord(ev[2], st);
+            k_wf_shade<<<g, bs, 0, st>>>(a);
+            cudaEventRecord(ev[3], st);
+            k_wf_shadow<<<g, bs, bt->smem, st>>>(a);
+            cudaEventRecord(ev[4], st);
+            k_wf_combine<<<g, bs, 0, st>>>(a);
+            k_wf_end<<<1, 1, 0, st>>>(a);
+            cudaEventRecord(ev[5], st);
+            AUR_CUDA(cudaMemcpyAsync(&c, a.ctl, sizeof(c), cudaMemcpyDeviceToHost, st));
+            AUR_CUDA(cudaStreamSynchronize(st));
+            lap(1, 0, 1); lap(2, 1, 2); lap(3, 2, 3); lap(4, 3, 4); lap(5, 4, 5);
+            const uint32_t nxt = c.iter & 1u;
+            const bool more = (c.items_issued < c.items_total || c.ext_count[nxt] > 0) && !c.error;
+            if (!more || it > c.iter_limit) break;
+        }
+        cudaEventRecord(ev[0], st);
+        k_wf_accumulate<<<g, bs, 0, st>>>(a);
+        k_wf_next_wave<<<1, 1, 0, st>>>(a);
+        cudaEventRecord(ev[1], st);
+        lap(6, 0, 1);
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    AUR_CUDA(cudaGetLastError());
+    return aur_batch_status(ctx, bt, nullptr);
+}
+
 aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, const aur_camera* cameras,
                               const aur_render_params* params, uint32_t num_scenes, aur_wavefront_tuning* best,
                               float* best_ms) {

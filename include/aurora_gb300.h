@@ -329,6 +329,10 @@ aur_status aur_batch_render(aur_ctx* ctx, aur_batch* batch, float* const* accum)
  * stack overflow: AUR_ERR_TIMEOUT). iterations: total integrator iterations. */
 aur_status aur_batch_status(aur_ctx* ctx, aur_batch* batch, uint32_t* iterations);
 aur_status aur_batch_tuning(const aur_batch* batch, aur_wavefront_tuning* out);
+/* Profiling form of aur_batch_render: the same kernels launched one by one
+ * without the graph, with per-stage CUDA-event times (ms) in stage_ms:
+ * set-up, generate, extend, shade, shadow, combine, accumulate. */
+aur_status aur_batch_profile(aur_ctx* ctx, aur_batch* batch, float* const* accum, float stage_ms[7]);
 aur_status aur_batch_destroy(aur_batch* batch);
 /* Autotuner: times one-sample renders of the batch for a set of candidate
  * tunings (pool size, block size, blocks per SM) and returns the fastest. */
