@@ -90,6 +90,7 @@ struct WfArgs {
     float4* sh_d;   // shadow ray direction, w = (slot << 5 | light slot) bits
     float4* out;    // per wave: nb * P_tot sample colours
     cudaGraphConditionalHandle h_inner, h_outer;
+    uint32_t in_graph;   // 1 when launched by the graph: only then may kernels set its conditionals
 };
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
@@ -148,7 +149,7 @@ __global__ void k_wf_setup(WfArgs a) {
         c->shadow_count = 0;
         c->free_count = Q;
         c->iter = 0;
-        cudaGraphSetConditional(a.h_inner, c->error ? 0u : 1u);
+        if (a.in_graph) cudaGraphSetConditional(a.h_inner, c->error ? 0u : 1u);
     }
 }
 
@@ -374,7 +375,7 @@ __global__ void k_wf_end(WfArgs a) {
     bool more = c->items_issued < c->items_total || c->ext_count[nxt] > 0;
     if (c->iter > c->iter_limit) { c->error |= 1u; more = false; }
     if (c->error) more = false;
-    cudaGraphSetConditional(a.h_inner, more ? 1u : 0u);
+    if (a.in_graph) cudaGraphSetConditional(a.h_inner, more ? 1u : 0u);
 }
 
 // drawPixels for the wave's samples, in sample order.
@@ -402,7 +403,7 @@ __global__ void k_wf_accumulate(WfArgs a) {
 __global__ void k_wf_next_wave(WfArgs a) {
     WfCtl* c = a.ctl;
     c->wave += 1;
-    cudaGraphSetConditional(a.h_outer, (c->wave < c->num_waves && !c->error) ? 1u : 0u);
+    if (a.in_graph) cudaGraphSetConditional(a.h_outer, (c->wave < c->num_waves && !c->error) ? 1u : 0u);
 }
 
 inline uint32_t cdiv(uint64_t x, uint64_t y) { return (uint32_t)((x + y - 1) / y); }
@@ -431,6 +432,7 @@ namespace {
 
 aur_status make_graph(aur_batch* bt) {
     WfArgs& a = bt->args;
+    a.in_graph = 1;
     AUR_CUDA(cudaGraphCreate(&bt->graph, 0));
     AUR_CUDA(cudaGraphConditionalHandleCreate(&a.h_outer, bt->graph, 1, cudaGraphCondAssignDefault));
     cudaGraphNodeParams outer = {};
@@ -480,6 +482,7 @@ aur_status make_graph(aur_batch* bt) {
     k_wf_next_wave<<<1, 1, 0, s>>>(a);
     AUR_CUDA(cudaStreamEndCapture(s, &tmp));
     AUR_CUDA(cudaGraphInstantiate(&bt->exec, bt->graph, 0));
+    a.in_graph = 0;   // the host-launched (profiling) form must not touch the conditionals
     return AUR_OK;
 }
 
