@@ -57,6 +57,7 @@ struct WfCtl {
     uint32_t iter, iter_limit;
     uint32_t error;
     uint32_t total_iters;
+    uint32_t ext_fetch, shadow_fetch;   // dynamic-fetch cursors of the extend / shadow kernels
 };
 
 struct WfArgs {
@@ -184,25 +185,53 @@ __global__ void k_wf_generate_commit(WfArgs a) {
     c->free_count -= n_new;
     c->items_issued += n_new;
     c->ext_count[cur] += n_new;
+    c->ext_fetch = 0;
+    c->shadow_fetch = 0;
 }
 
-// Closest hit for every queued path.
+// Next queue position for a lane that needs work (one atomic per warp).
+__device__ __forceinline__ uint32_t fetch_next(uint32_t* cursor) { return agg_inc(cursor); }
+
+// Closest hit for every queued path: persistent lanes fetch queue entries
+// dynamically, so a lane whose ray finished takes the next one at once.
 __global__ void k_wf_extend(WfArgs a) {
     extern __shared__ uint32_t smem[];
     const StackRef stk = wf_stack(smem, a.cap);
-    const WfCtl* c = a.ctl;
+    WfCtl* c = a.ctl;
     const uint32_t cur = c->iter & 1u;
     const uint32_t n = c->ext_count[cur];
     uint32_t visits = 0;
-    for (uint32_t i = global_tid(); i < n; i += grid_threads()) {
-        const uint32_t slot = a.ext_q[cur][i];
-        const uint32_t s = a.meta[slot].w;
-        const WfScene& sc = a.scenes[s];
-        const float4 o = a.o[slot], d = a.d[slot];
-        float t = kInfinity, u = 0.0f, v = 0.0f;
-        const uint32_t tri = traverse<false>(sc.recs, sc.nodes, sc.perm, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), t, u,
-                                             v, stk, visits, &a.ctl->error);
-        a.hit[slot] = make_float4(t, u, v, __uint_as_float(tri));
+    uint32_t slot = 0xFFFFFFFFu;
+    const float4* recs = nullptr;
+    const uint32_t* perm = nullptr;
+    uint32_t nodes = 0;
+    f3 pos = mk3(0.0f), dir = mk3(0.0f);
+    float best_t = 0.0f, bu = 0.0f, bv = 0.0f;
+    uint32_t best = kNoPrim;
+    TravState s;
+    trav_init(s);
+    for (;;) {
+        if (slot == 0xFFFFFFFFu) {
+            const uint32_t i = fetch_next(&c->ext_fetch);
+            if (i >= n) break;
+            slot = a.ext_q[cur][i];
+            const WfScene& sc = a.scenes[a.meta[slot].w];
+            recs = sc.recs; perm = sc.perm; nodes = sc.nodes;
+            const float4 o = a.o[slot], d = a.d[slot];
+            pos = mk3(o.x, o.y, o.z);
+            dir = mk3(d.x, d.y, d.z);
+            best_t = kInfinity; bu = bv = 0.0f; best = kNoPrim;
+            trav_init(s);
+        }
+        float4 q0;
+        float nlo, nhi;
+        if (trav_next(s, recs, nodes, pos, dir, best_t, stk, q0, nlo, nhi, visits)) {
+            node_triangles<false>(recs, s.k, q0, perm, pos, dir, best_t, bu, bv, best);
+            trav_descend(s, dir, nodes, stk, nlo, nhi);
+        } else {
+            a.hit[slot] = make_float4(best_t, bu, bv, __uint_as_float(best));
+            slot = 0xFFFFFFFFu;
+        }
     }
 }
 
@@ -290,20 +319,49 @@ __global__ void k_wf_shade(WfArgs a) {
 }
 
 // Any hit for every queued shadow ray; unoccluded rays set their bit.
+// Persistent lanes with dynamic fetch, as in k_wf_extend.
 __global__ void k_wf_shadow(WfArgs a) {
     extern __shared__ uint32_t smem[];
     const StackRef stk = wf_stack(smem, a.cap);
-    const uint32_t n = a.ctl->shadow_count;
+    WfCtl* c = a.ctl;
+    const uint32_t n = c->shadow_count;
     uint32_t visits = 0;
-    for (uint32_t i = global_tid(); i < n; i += grid_threads()) {
-        const float4 o = a.sh_o[i], d = a.sh_d[i];
-        const uint32_t id = __float_as_uint(d.w);
-        const uint32_t slot = id >> 5;
-        const WfScene& sc = a.scenes[a.meta[slot].w];
-        float t = o.w, u = 0.0f, v = 0.0f;
-        const uint32_t occ = traverse<true>(sc.recs, sc.nodes, sc.perm, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), t, u, v,
-                                            stk, visits, &a.ctl->error);
-        if (occ == kNoPrim) atomicOr(&a.vis[slot], 1u << (id & 31u));
+    uint32_t id = 0xFFFFFFFFu;
+    const float4* recs = nullptr;
+    const uint32_t* perm = nullptr;
+    uint32_t nodes = 0;
+    f3 pos = mk3(0.0f), dir = mk3(0.0f);
+    float tmax = 0.0f, bu = 0.0f, bv = 0.0f;
+    uint32_t best = kNoPrim;
+    TravState s;
+    trav_init(s);
+    for (;;) {
+        if (id == 0xFFFFFFFFu) {
+            const uint32_t i = fetch_next(&c->shadow_fetch);
+            if (i >= n) break;
+            const float4 o = a.sh_o[i], d = a.sh_d[i];
+            id = __float_as_uint(d.w);
+            const WfScene& sc = a.scenes[a.meta[id >> 5].w];
+            recs = sc.recs; perm = sc.perm; nodes = sc.nodes;
+            pos = mk3(o.x, o.y, o.z);
+            dir = mk3(d.x, d.y, d.z);
+            tmax = o.w;
+            best = kNoPrim;
+            trav_init(s);
+        }
+        float4 q0;
+        float nlo, nhi;
+        bool done;
+        if (trav_next(s, recs, nodes, pos, dir, tmax, stk, q0, nlo, nhi, visits)) {
+            done = node_triangles<true>(recs, s.k, q0, perm, pos, dir, tmax, bu, bv, best);
+            if (!done) trav_descend(s, dir, nodes, stk, nlo, nhi);
+        } else {
+            done = true;
+        }
+        if (done) {
+            if (best == kNoPrim) atomicOr(&a.vis[id >> 5], 1u << (id & 31u));
+            id = 0xFFFFFFFFu;
+        }
     }
 }
 
