@@ -51,8 +51,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-extras", action="store_true", help="headline traversal only")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling cases only)")
-    ap.add_argument("--profile", action="store_true",
-                    help="small profiling case: one warm-up, one closest-hit and one any-hit launch")
+    ap.add_argument("--profile", nargs="?", const="trace", default=None,
+                    choices=["trace", "render", "wavefront", "adjoint", "build"],
+                    help="small profiling case: trace = one closest-hit and one any-hit launch; render = Cornell "
+                         "+ sphere frames; wavefront = stepped 8-scene batch; adjoint = one adjoint; "
+                         "build = NMH build of the 1M-triangle soup")
     return ap.parse_args()
 
 
@@ -71,11 +74,44 @@ def workload(n_rays=N_RAYS):
 
 
 def run_profile(args):
-    """One warm-up, then exactly one closest-hit and one any-hit launch."""
+    """Small cases for ncu captures (see --profile)."""
     import torch
-    from aurora_gb300 import api, build as abuild
+    from aurora_gb300 import api, build as abuild, scenes, types as T
     abuild.build()
     ctx = api.Context(0)
+    if args.profile == "render":
+        for sd, p in ((scenes.cornell(), T.render_params(256, 256, 16, 4, mode=T.MODE_PATH)),
+                      (scenes.cornell_sphere(seed=0), T.render_params(256, 256, 16, 4, mode=T.MODE_PATH))):
+            sc = api.Scene(ctx, sd)
+            sc.render(p)
+            torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "render"}))
+        return
+    if args.profile == "wavefront":
+        sds = [scenes.sphere_scene(i) for i in range(8)]
+        scs = [api.Scene(ctx, sd) for sd in sds]
+        prm = [T.render_params(256, 256, 64, 6, mode=T.MODE_PATH, sample_end=2, scene_id=i) for i in range(8)]
+        b = api.Batch(ctx, scs, prm, tuning=api.make_tuning(1 << 20, 0, 128, 8))
+        st = b.profile([torch.zeros((256, 256, 4), device="cuda") for _ in range(8)])
+        print(json.dumps({"profile_case": "wavefront", "stage_ms": st}))
+        return
+    if args.profile == "adjoint":
+        sd = scenes.cornell_sphere(seed=0)
+        sc = api.Scene(ctx, sd)
+        p = T.render_params(128, 128, 16, 4, mode=T.MODE_PATH)
+        img = sc.render(p)
+        sc.adjoint(p, img.contiguous())
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "adjoint"}))
+        return
+    if args.profile == "build":
+        V, _ = workload(16)
+        Vd = torch.from_numpy(V.reshape(-1)).cuda()
+        for _ in range(2):
+            api.Nmh(ctx, Vd, count=V.shape[0])
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "build"}))
+        return
     V, rays = workload(args.rays)
     nmh = api.Nmh(ctx, torch.from_numpy(V.reshape(-1)).cuda(), count=V.shape[0])
     rays_d = api.rays_tensor(rays)
