@@ -136,7 +136,7 @@ def load_peaks():
 def load_traffic():
     """Per-launch DRAM bytes of the closest-hit kernel from the committed ncu
     summary, if present (a line 'traffic_bytes_per_launch: N')."""
-    p = os.path.join(ROOT, "profiles", "trace_closest_microbench.md")
+    p = os.path.join(ROOT, "profiles", "k_trace_microbench_full.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
