@@ -65,6 +65,7 @@ SIGNATURES = {
     "aur_batch_autotune": ([P, P, P, P, U32, P, P], ctypes.c_int),
     "aur_render_adjoint": ([P, P, P, P, P, P, P], ctypes.c_int),
     "aur_batch_profile": ([P, P, P, P], ctypes.c_int),
+    "aur_batch_counters": ([P, P, P], ctypes.c_int),
 }
 
 
@@ -317,13 +318,14 @@ def exported_symbols():
 
 
 tuning_dtype = np.dtype([("paths_in_flight", "<u4"), ("samples_per_wave", "<u4"), ("block_size", "<u4"),
-                         ("blocks_per_sm", "<u4")])
+                         ("blocks_per_sm", "<u4"), ("max_iterations", "<u4")])
 
 
-def make_tuning(paths_in_flight=0, samples_per_wave=0, block_size=0, blocks_per_sm=0):
+def make_tuning(paths_in_flight=0, samples_per_wave=0, block_size=0, blocks_per_sm=0, max_iterations=0):
     t = np.zeros((), tuning_dtype)
     t["paths_in_flight"], t["samples_per_wave"] = paths_in_flight, samples_per_wave
     t["block_size"], t["blocks_per_sm"] = block_size, blocks_per_sm
+    t["max_iterations"] = max_iterations
     return t
 
 
@@ -370,6 +372,12 @@ class Batch:
         it = U32()
         check(lib().aur_batch_status(self.ctx.handle, self.handle, ctypes.byref(it)))
         return it.value
+
+    def counters(self):
+        """(closest-hit rays, shadow rays, iterations) of the last render."""
+        out = (ctypes.c_ulonglong * 3)()
+        check(lib().aur_batch_counters(self.ctx.handle, self.handle, out))
+        return int(out[0]), int(out[1]), int(out[2])
 
     def tuning(self):
         t = np.zeros((), tuning_dtype)

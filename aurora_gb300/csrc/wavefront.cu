@@ -20,6 +20,7 @@
 // over waves and an inner one over iterations, both bounded by iteration
 // limits that stop the loop and raise an error instead of spinning.
 #include <algorithm>
+#include <cstddef>
 #include <cstring>
 #include <vector>
 
@@ -47,6 +48,9 @@ struct WfScene {
 };
 
 struct WfCtl {
+    unsigned long long total_ext, total_shadow;   // work counters (reset per render)
+    uint32_t error;
+    uint32_t total_iters;
     uint32_t wave, num_waves;
     uint32_t s_begin, s_end, spw;
     uint32_t s0, nb;
@@ -55,8 +59,6 @@ struct WfCtl {
     uint32_t shadow_count;
     uint32_t free_count;
     uint32_t iter, iter_limit;
-    uint32_t error;
-    uint32_t total_iters;
     uint32_t ext_fetch, shadow_fetch;   // dynamic-fetch cursors of the extend / shadow kernels
 };
 
@@ -426,6 +428,8 @@ __global__ void k_wf_combine(WfArgs a) {
 __global__ void k_wf_end(WfArgs a) {
     WfCtl* c = a.ctl;
     const uint32_t cur = c->iter & 1u, nxt = cur ^ 1u;
+    c->total_ext += c->ext_count[cur];
+    c->total_shadow += c->shadow_count;
     c->ext_count[cur] = 0;
     c->shadow_count = 0;
     c->iter += 1;
@@ -694,6 +698,7 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     // every iteration either starts new paths or advances live ones by a bounce
     const uint64_t waves_of_pool = cdiv(P_tot * tn.samples_per_wave, Q) + 1;
     ctl.iter_limit = (uint32_t)std::min<uint64_t>(0x7FFFFFFFull, 4 * waves_of_pool * (p0.max_depth + 2) + 64);
+    if (tn.max_iterations) ctl.iter_limit = tn.max_iterations;
     cudaMemcpy(a.ctl, &ctl, sizeof(ctl), cudaMemcpyHostToDevice);
     if (cudaFuncSetAttribute(k_wf_extend, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem) != cudaSuccess ||
         cudaFuncSetAttribute(k_wf_shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem) != cudaSuccess ||
@@ -725,8 +730,8 @@ aur_status aur_batch_render(aur_ctx* ctx, aur_batch* bt, float* const* accum) {
     AUR_CUDA(cudaMemcpyAsync((void*)a.accum, bt->accum_host.data(), sizeof(float4*) * bt->num_scenes,
                              cudaMemcpyHostToDevice, ctx->stream));
     // reset the per-launch part of the control block: wave, error, iteration count
-    AUR_CUDA(cudaMemsetAsync(&a.ctl->wave, 0, sizeof(uint32_t), ctx->stream));
-    AUR_CUDA(cudaMemsetAsync(&a.ctl->error, 0, sizeof(uint32_t) * 2, ctx->stream));
+    // counters, error and iteration total sit at the front of the control block
+    AUR_CUDA(cudaMemsetAsync(a.ctl, 0, offsetof(WfCtl, num_waves), ctx->stream));
     AUR_CUDA(cudaGraphLaunch(bt->exec, ctx->stream));
     return AUR_OK;
 }
@@ -743,6 +748,18 @@ aur_status aur_batch_status(aur_ctx* ctx, aur_batch* bt, uint32_t* iterations) {
               c.iter_limit, c.error);
     AUR_CHECK(c.wave == c.num_waves, AUR_ERR_TIMEOUT, "wavefront render ended after %u of %u waves", c.wave,
               c.num_waves);
+    return AUR_OK;
+}
+
+aur_status aur_batch_counters(aur_ctx* ctx, aur_batch* bt, unsigned long long counters[3]) {
+    AUR_CHECK(ctx && bt && counters, AUR_ERR_INVALID, "aur_batch_counters: null argument");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    WfCtl c;
+    AUR_CUDA(cudaMemcpyAsync(&c, bt->args.ctl, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    counters[0] = c.total_ext;
+    counters[1] = c.total_shadow;
+    counters[2] = c.total_iters;
     return AUR_OK;
 }
 
@@ -771,8 +788,7 @@ aur_status aur_batch_profile(aur_ctx* ctx, aur_batch* bt, float* const* accum, f
     cudaStream_t st = ctx->stream;
     AUR_CUDA(cudaMemcpyAsync((void*)a.accum, bt->accum_host.data(), sizeof(float4*) * bt->num_scenes,
                              cudaMemcpyHostToDevice, st));
-    AUR_CUDA(cudaMemsetAsync(&a.ctl->wave, 0, sizeof(uint32_t), st));
-    AUR_CUDA(cudaMemsetAsync(&a.ctl->error, 0, sizeof(uint32_t) * 2, st));
+    AUR_CUDA(cudaMemsetAsync(a.ctl, 0, offsetof(WfCtl, num_waves), st));
     cudaEvent_t ev[8];
     for (auto& e : ev) cudaEventCreate(&e);
     for (int i = 0; i < 7; ++i) stage_ms[i] = 0.0f;
@@ -851,7 +867,7 @@ aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, cons
         for (uint32_t bs : blocks)
             for (uint32_t bps : per_sm) {
                 if ((uint64_t)bs * bps > 2048) continue;
-                aur_wavefront_tuning t{pool, 1, bs, bps};
+                aur_wavefront_tuning t{pool, 1, bs, bps, 0};
                 aur_batch* bt = nullptr;
                 if (aur_batch_create(ctx, scenes, cameras, p1.data(), num_scenes, &t, &bt) != AUR_OK) {
                     clear_error();

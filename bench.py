@@ -66,6 +66,22 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value, world, device="cpu"):
+    """Maximum of a per-rank time over all ranks (replicas time the slowest)."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, world, seconds):
+    """Whole-job throughput of `world` independent replicas timed together."""
+    return world * units_per_rank / seconds
+
+
 def workload(n_rays=N_RAYS):
     from aurora_gb300 import scenes
     V = scenes.random_soup(N_TRIS, seed=0)
@@ -447,13 +463,9 @@ def main():
             ev[s + 1].record(stream)
         barrier()
     launch_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
-    total_ms = ev[0].elapsed_time(ev[-1])
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(ev[0].elapsed_time(ev[-1]), world, "cuda")
     ms_per_step = total_ms / args.steps
-    value = world * N_RAYS * args.steps / (total_ms * 1e-3) / 1e6
+    value = replica_throughput(N_RAYS * args.steps, world, total_ms * 1e-3) / 1e6
 
     # any hit, same rays (reported beside the headline)
     for _ in range(2):

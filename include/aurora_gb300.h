@@ -308,6 +308,7 @@ typedef struct aur_wavefront_tuning {
     uint32_t samples_per_wave;  /* samples per pixel processed per wave */
     uint32_t block_size;        /* threads per block of the stage kernels */
     uint32_t blocks_per_sm;     /* persistent grid = SMs x blocks_per_sm */
+    uint32_t max_iterations;    /* device-side loop limit per wave (0 = derived from the work) */
 } aur_wavefront_tuning;
 
 typedef struct aur_batch aur_batch;
@@ -329,6 +330,9 @@ aur_status aur_batch_render(aur_ctx* ctx, aur_batch* batch, float* const* accum)
  * stack overflow: AUR_ERR_TIMEOUT). iterations: total integrator iterations. */
 aur_status aur_batch_status(aur_ctx* ctx, aur_batch* batch, uint32_t* iterations);
 aur_status aur_batch_tuning(const aur_batch* batch, aur_wavefront_tuning* out);
+/* Work counters of the last render: counters[0] = closest-hit rays (path
+ * segments), counters[1] = shadow rays, counters[2] = integrator iterations. */
+aur_status aur_batch_counters(aur_ctx* ctx, aur_batch* batch, unsigned long long counters[3]);
 /* Profiling form of aur_batch_render: the same kernels launched one by one
  * without the graph, with per-stage CUDA-event times (ms) in stage_ms:
  * set-up, generate, extend, shade, shadow, combine, accumulate. */

@@ -58,3 +58,22 @@ def test_autotune_returns_a_working_tuning(ctx):
     fr = b.render()
     b.status()
     assert np.array_equal(fr[0].cpu().numpy(), scs[0].render(prm[0]).cpu().numpy())
+
+
+def test_iteration_limit_reports_timeout_and_context_survives(ctx):
+    """The device-side integrator loop is bounded: with a limit of one
+    iteration it stops, the render reports AUR_ERR_TIMEOUT, and the context
+    keeps working."""
+    scs = [api.Scene(ctx, sd) for sd in _scenes()[:2]]
+    prm = _params(T.MODE_PATH, [(32, 32), (16, 16)])
+    b = api.Batch(ctx, scs, prm, tuning=api.make_tuning(paths_in_flight=1024, max_iterations=1))
+    b.render()
+    with pytest.raises(api.AuroraError) as e:
+        b.status()
+    assert e.value.status == 4
+    ok = api.Batch(ctx, scs, prm)
+    fr = ok.render()
+    ok.status()
+    assert np.array_equal(fr[0].cpu().numpy(), scs[0].render(prm[0]).cpu().numpy())
+    ext, shadow, iters = ok.counters()
+    assert ext > 0 and shadow > 0 and iters > 0
