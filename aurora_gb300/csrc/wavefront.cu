@@ -629,8 +629,8 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     if (tn.block_size == 0) tn.block_size = 128;
     if (tn.blocks_per_sm == 0) tn.blocks_per_sm = 6;
     if (tn.samples_per_wave == 0) {
-        // cap the wave's sample buffer at about 1 GiB
-        tn.samples_per_wave = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(nsamp, (1ull << 26) / P_tot));
+        // cap the wave's sample buffer at about 4 GiB (16 B per sample)
+        tn.samples_per_wave = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(nsamp, (1ull << 28) / P_tot));
     }
     tn.samples_per_wave = std::min(tn.samples_per_wave, nsamp);
     AUR_CHECK(tn.block_size % 32 == 0 && tn.block_size >= 32 && tn.block_size <= 512, AUR_ERR_INVALID,
@@ -855,8 +855,8 @@ aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, cons
     AUR_CHECK(cudaMalloc(&frames, pixels * sizeof(float4)) == cudaSuccess, AUR_ERR_OOM, "aur_batch_autotune: out of memory");
     std::vector<float*> acc(num_scenes);
     for (uint32_t i = 0, o = 0; i < num_scenes; o += p1[i].width * p1[i].height, ++i) acc[i] = (float*)(frames + o);
-    const uint32_t pools[] = {1u << 20, 1u << 21, 1u << 22};
-    const uint32_t blocks[] = {64, 128, 256};
+    const uint32_t pools[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23};
+    const uint32_t blocks[] = {128, 256};
     const uint32_t per_sm[] = {4, 8, 16};
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);

@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=1 << 22)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-extras", action="store_true", help="headline traversal only")
+    ap.add_argument("--terrain", action="store_true",
+                    help="only the large terrain workload (plain vs wavefront, RMSE against 16384 spp)")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling cases only)")
     ap.add_argument("--profile", nargs="?", const="trace", default=None,
                     choices=["trace", "render", "wavefront", "adjoint", "build"],
@@ -279,6 +281,7 @@ def bench_batched(ctx, n_scenes=64, size=512, spp=64, depth=6, samples=8):
     e1.record(stream)
     iters = batch.status()
     wf_ms = e0.elapsed_time(e1)
+    ext, shadow, _ = batch.counters()
     same = all(torch.equal(a, b) for a, b in zip(wf, plain_img))
     tris = [sd.count for sd in sds]
     return {"workload": "%d sphere scenes (%d-%d triangles, %d total), %dx%d, %d spp, depth %d, path mode; "
@@ -288,6 +291,8 @@ def bench_batched(ctx, n_scenes=64, size=512, spp=64, depth=6, samples=8):
             "wavefront_samples_per_s": n_samples / (wf_ms * 1e-3), "wavefront_ms": wf_ms,
             "speedup": plain_ms / wf_ms, "frames_identical": bool(same), "equal_rmse": bool(same),
             "wavefront_graph_launches": 1, "wavefront_iterations": iters,
+            "wavefront_rays": {"closest": ext, "shadow": shadow,
+                               "mrays_per_s": (ext + shadow) / (wf_ms * 1e-3) / 1e6},
             "tuning": {k: int(tuning[k]) for k in tuning.dtype.names}, "autotune_s": tune_s}
 
 
@@ -382,6 +387,80 @@ def bench_adjoint(ctx, size=256, spp=64, depth=4):
             "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "grad_over_fwd": adj_ms / fwd_ms, "fd_checks": checks}
 
 
+def bench_terrain(ctx, res=2048, samples=1, ref_spp=16384, small=(64, 36), small_spp=64):
+    """Large workload: 2048x2048-vertex fBm heightfield (8,380,418 triangles),
+    16 area lights, 1920x1080, 256 spp, depth 8, path mode. Times the NMH
+    build, then plain vs wavefront on samples [0, `samples`) of the 256 (the
+    frames must be identical). RMSE: both forms render a small (64x36) crop
+    of the same camera at 64 spp and are compared with a 16384-spp render of
+    that crop."""
+    import torch
+    from aurora_gb300 import api, scenes, types as T
+    t0 = time.perf_counter()
+    sd = scenes.terrain(res=res, seed=0)
+    gen_s = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sc = api.Scene(ctx, sd)
+    torch.cuda.synchronize()
+    scene_s = time.perf_counter() - t0
+    Vd = torch.from_numpy(sd.vertices.reshape(-1)).cuda()
+    api.Nmh(ctx, Vd, count=sd.count)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    api.Nmh(ctx, Vd, count=sd.count)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    build_ms = e0.elapsed_time(e1)
+    del Vd
+    W, H = 1920, 1080
+    p = T.render_params(W, H, 256, 8, seed=0, mode=T.MODE_PATH, sample_end=samples)
+    sc.render(T.render_params(W, H, 256, 8, seed=0, mode=T.MODE_PATH, sample_end=1))     # warm-up
+    torch.cuda.synchronize()
+    e0.record(stream)
+    plain = sc.render(p)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    batch = api.Batch(ctx, [sc], [p])
+    batch.render()
+    batch.status()
+    e0.record(stream)
+    wf = batch.render()[0]
+    e1.record(stream)
+    batch.status()
+    wf_ms = e0.elapsed_time(e1)
+    ext, shadow, iters = batch.counters()
+    same = bool(torch.equal(wf, plain))
+    batch.close()
+    # RMSE at equal spp against a 16384-spp reference of a small frame
+    sw, sh = small
+    cam = sd.camera
+    ref = sc.render(T.render_params(sw, sh, ref_spp, 8, seed=1, mode=T.MODE_PATH), camera=cam)
+    ps = T.render_params(sw, sh, small_spp, 8, seed=0, mode=T.MODE_PATH)
+    pl = sc.render(ps, camera=cam)
+    b2 = api.Batch(ctx, [sc], [ps], cameras=[cam])
+    wfs = b2.render()[0]
+    b2.status()
+
+    def rmse(a):
+        return float(torch.sqrt(((a[..., :3].double() - ref[..., :3].double()) ** 2).mean()))
+
+    n_samples = W * H * samples
+    return {"workload": "fBm terrain %dx%d vertices (%d triangles), 16 area lights, %dx%d, 256 spp, depth 8, path mode; "
+                        "samples [0, %d) timed" % (res, res, sd.count, W, H, samples),
+            "generate_s": gen_s, "scene_upload_and_build_s": scene_s, "nmh_build_ms": build_ms,
+            "plain_samples_per_s": n_samples / (plain_ms * 1e-3), "plain_ms": plain_ms,
+            "wavefront_samples_per_s": n_samples / (wf_ms * 1e-3), "wavefront_ms": wf_ms,
+            "speedup": plain_ms / wf_ms, "frames_identical": same,
+            "wavefront_rays": {"closest": ext, "shadow": shadow, "iterations": iters,
+                               "mrays_per_s": (ext + shadow) / (wf_ms * 1e-3) / 1e6},
+            "rmse": {"reference": "%dx%d at %d spp (seed 1)" % (sw, sh, ref_spp), "spp": small_spp,
+                     "plain": rmse(pl), "wavefront": rmse(wfs)}}
+
+
 def run_reference(args):
     """--impl reference: the reference traversal restated in C++ (the oracle;
     the reference's own sources do not travel to this machine) on the host
@@ -425,6 +504,11 @@ def main():
         return run_reference(args)
     if args.profile:
         return run_profile(args)
+    if args.terrain:
+        from aurora_gb300 import api, build as abuild
+        abuild.build()
+        print(json.dumps({"terrain": bench_terrain(api.Context(0))}), flush=True)
+        return
     import torch
     rank, world, local = dist_env()
     if world > 1:
