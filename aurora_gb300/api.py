@@ -66,6 +66,8 @@ SIGNATURES = {
     "aur_render_adjoint": ([P, P, P, P, P, P, P], ctypes.c_int),
     "aur_batch_profile": ([P, P, P, P], ctypes.c_int),
     "aur_batch_counters": ([P, P, P], ctypes.c_int),
+    "aur_transform": ([P, P, P, U32, P, U32, P, P], ctypes.c_int),
+    "aur_generate_tb": ([P, P, U32, P, P], ctypes.c_int),
 }
 
 
@@ -403,3 +405,14 @@ def autotune(ctx, scenes, params, cameras=None):
     ms = ctypes.c_float()
     check(lib().aur_batch_autotune(ctx.handle, h, _ptr(cams), _ptr(prm), len(scenes), _ptr(t), ctypes.byref(ms)))
     return t, ms.value
+
+
+def transform(ctx, src_vertices, src_normals, transforms, dst_vertices, dst_normals):
+    """aur_transform on device tensors (count*9 floats each); transforms: host records."""
+    xf = np.ascontiguousarray(transforms, T.object_transform_dtype)
+    check(lib().aur_transform(ctx.handle, _ptr(src_vertices), _ptr(src_normals), src_vertices.numel() // 9,
+                              _ptr(xf), xf.shape[0], _ptr(dst_vertices), _ptr(dst_normals)))
+
+
+def generate_tb(ctx, normals, tangents, bitangents):
+    check(lib().aur_generate_tb(ctx.handle, _ptr(normals), normals.numel() // 9, _ptr(tangents), _ptr(bitangents)))

@@ -217,6 +217,32 @@ aur_status aur_nmh_perm_device(const aur_nmh* nmh, const uint32_t** perm);
 aur_status aur_nmh_build_noalloc(const float* vertices, uint32_t count, void* cuda_stream, float* node_records,
                                  uint32_t* perm, float* nmh_vertices, uint32_t* levels);
 
+/* ------------------------------------------------------------- scene prep */
+
+/* Object-to-world transform of one object (util/transform.h:12-26):
+ * triangles [offset, offset + size) use row-vector matrices,
+ * p' = p * world_matrix, n' = n * normal_matrix (the inverse transpose). */
+typedef struct aur_object_transform {
+    uint32_t offset;
+    uint32_t size;
+    float world_matrix[4][4];
+    float normal_matrix[4][4];
+} aur_object_transform;
+
+/* cudaTransform (kernels/utility.cu:96-134): writes world-space vertices and
+ * normals of `count` triangles. Triangle i uses the last object whose offset
+ * is <= i (offsets must be non-decreasing); triangles before the first
+ * object are left untouched. src_*, dst_*: device, count*9 floats;
+ * transforms: host array of num_objects. */
+aur_status aur_transform(aur_ctx* ctx, const float* src_vertices, const float* src_normals, uint32_t count,
+                         const aur_object_transform* transforms, uint32_t num_objects, float* dst_vertices,
+                         float* dst_normals);
+/* cudaGenerateTB (kernels/utility.cu:136-180): per-vertex tangents
+ * n x (0,1,0) (n x (0,0,1) when shorter than Epsilon) and bitangents
+ * n x tangent. normals, tangents, bitangents: device, count*9 floats. The
+ * renderers compute the same frames at shading time and need no stored ones. */
+aur_status aur_generate_tb(aur_ctx* ctx, const float* normals, uint32_t count, float* tangents, float* bitangents);
+
 /* --------------------------------------------------------------- traversal */
 
 /* Closest hit for n rays (intersect(), kernels/lib/intersect.cuh:95-152).

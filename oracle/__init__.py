@@ -47,6 +47,8 @@ def lib():
         L.orc_generate_rays.argtypes = [P, U32, U32, U32, U32, P]
         L.orc_render.argtypes = [P, P, P, P, U32, P, U32, P, U32, P, P, P, ctypes.c_int]
         L.orc_render.restype = ctypes.c_uint64
+        L.orc_transform.argtypes = [P, P, U32, P, U32, P, P]
+        L.orc_generate_tb.argtypes = [P, U32, P, P]
         _lib = L
     return _lib
 
@@ -200,3 +202,21 @@ def ref_trace_any(V_nmh, rays):
     ids = np.zeros(rays.shape[0], np.int32)
     L.ref_trace_any(_ptr(V), V.shape[0], _ptr(rays), rays.shape[0], _ptr(ids))
     return ids
+
+
+def transform(vertices, normals, transforms, dst_vertices=None, dst_normals=None):
+    """cudaTransform restated: returns world-space (vertices, normals)."""
+    V = np.ascontiguousarray(vertices, np.float32).reshape(-1, 9)
+    N = np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
+    xf = np.ascontiguousarray(transforms, T.object_transform_dtype)
+    dv = np.zeros_like(V) if dst_vertices is None else np.array(dst_vertices, np.float32)
+    dn = np.zeros_like(N) if dst_normals is None else np.array(dst_normals, np.float32)
+    lib().orc_transform(_ptr(V), _ptr(N), V.shape[0], _ptr(xf), xf.shape[0], _ptr(dv), _ptr(dn))
+    return dv, dn
+
+
+def generate_tb(normals):
+    N = np.ascontiguousarray(normals, np.float32).reshape(-1, 9)
+    t = np.zeros_like(N); b = np.zeros_like(N)
+    lib().orc_generate_tb(_ptr(N), N.shape[0], _ptr(t), _ptr(b))
+    return t, b

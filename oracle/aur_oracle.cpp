@@ -839,3 +839,43 @@ uint64_t orc_render(const float* V, const float* N, const uint16_t* S, const uin
 }
 
 }  // extern "C"
+
+extern "C" {
+
+/* cudaTransformKernel (kernels/utility.cu:96-124) with Transform::getPoint /
+ * getNormal (kernels/lib/transform.cuh:8-24): triangle i uses the LAST object
+ * in array order whose offset <= i (a linear scan, as the reference does);
+ * triangles before every object are left untouched. */
+void orc_transform(const float* sv, const float* sn, uint32_t count, const aur_object_transform* xf, uint32_t nobj,
+                   float* dv, float* dn) {
+    for (uint32_t i = 0; i < count; ++i) {
+        const aur_object_transform* t = nullptr;
+        for (uint32_t k = 0; k < nobj; ++k)
+            if (xf[k].offset <= i) t = &xf[k];
+        if (!t) continue;
+        const float(*m)[4] = t->world_matrix;
+        const float(*q)[4] = t->normal_matrix;
+        for (int c = 0; c < 3; ++c) {
+            const float px = sv[(size_t)i * 9 + c], py = sv[(size_t)i * 9 + 3 + c], pz = sv[(size_t)i * 9 + 6 + c];
+            dv[(size_t)i * 9 + c] = m[0][0] * px + m[1][0] * py + m[2][0] * pz + m[3][0];
+            dv[(size_t)i * 9 + 3 + c] = m[0][1] * px + m[1][1] * py + m[2][1] * pz + m[3][1];
+            dv[(size_t)i * 9 + 6 + c] = m[0][2] * px + m[1][2] * py + m[2][2] * pz + m[3][2];
+            const float nx = sn[(size_t)i * 9 + 3 * c], ny = sn[(size_t)i * 9 + 3 * c + 1], nz = sn[(size_t)i * 9 + 3 * c + 2];
+            dn[(size_t)i * 9 + 3 * c] = q[0][0] * nx + q[1][0] * ny + q[2][0] * nz;
+            dn[(size_t)i * 9 + 3 * c + 1] = q[0][1] * nx + q[1][1] * ny + q[2][1] * nz;
+            dn[(size_t)i * 9 + 3 * c + 2] = q[0][2] * nx + q[1][2] * ny + q[2][2] * nz;
+        }
+    }
+}
+
+/* cudaGenerateTBKernel (kernels/utility.cu:136-167). */
+void orc_generate_tb(const float* nrm, uint32_t count, float* tan, float* bit) {
+    for (uint32_t i = 0; i < (size_t)count * 3; ++i) {
+        F3 t, b;
+        vertexTB(mk3(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]), t, b);
+        tan[3 * i] = t.x; tan[3 * i + 1] = t.y; tan[3 * i + 2] = t.z;
+        bit[3 * i] = b.x; bit[3 * i + 1] = b.y; bit[3 * i + 2] = b.z;
+    }
+}
+
+}  // extern "C"
