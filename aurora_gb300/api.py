@@ -40,6 +40,12 @@ SIGNATURES = {
     "aur_nmh_export": ([P, P, P, P], ctypes.c_int),
     "aur_nmh_perm_device": ([P, P], ctypes.c_int),
     "aur_nmh_build_noalloc": ([P, U32, P, P, P, P, P], ctypes.c_int),
+    "aur_nmh_apply": ([P, P, P, U32, P], ctypes.c_int),
+    "aur_malloc": ([P, ctypes.c_size_t, ctypes.c_int, P], ctypes.c_int),
+    "aur_free": ([P, P, ctypes.c_int], ctypes.c_int),
+    "aur_memzero": ([P, P, ctypes.c_size_t, ctypes.c_int], ctypes.c_int),
+    "aur_memupload": ([P, P, P, ctypes.c_size_t, ctypes.c_int], ctypes.c_int),
+    "aur_memdownload": ([P, P, P, ctypes.c_size_t], ctypes.c_int),
     "aur_trace_closest": ([P, P, P, U32, P], ctypes.c_int),
     "aur_trace_any": ([P, P, P, U32, P], ctypes.c_int),
     "aur_trace_closest_host": ([P, P, P, U32, P], ctypes.c_int),

@@ -64,5 +64,26 @@ def build(verbose=False, ptxas_info=False):
     return LIB
 
 
+HOST = os.path.join(HERE, "host")
+DRIVER = os.path.join(BUILD, "aurora_render")
+
+
+def build_host(verbose=False):
+    """Builds the C++ host layer and the standalone driver aurora_render
+    against libaurora_gb300.so (g++, no CUDA headers needed)."""
+    lib = build(verbose)
+    srcs = [os.path.join(HOST, "aurora.cpp"), os.path.join(HOST, "aurora_render.cpp")]
+    deps = srcs + [os.path.join(HOST, "aurora.h"), os.path.join(INCLUDE, "aurora_gb300.h"), lib, __file__]
+    if os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= max(os.path.getmtime(p) for p in deps):
+        return DRIVER
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + INCLUDE, "-I" + HOST, *srcs, "-L" + BUILD,
+           "-laurora_gb300", "-Wl,-rpath,$ORIGIN", "-o", DRIVER]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("host build failed:\n%s%s" % (r.stdout, r.stderr))
+    return DRIVER
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv, ptxas_info="--ptxas" in sys.argv))
+    print(build_host())

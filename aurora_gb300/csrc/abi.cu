@@ -2,6 +2,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -46,6 +47,16 @@ __global__ void k_permute_attrs(const uint32_t* __restrict__ perm, uint32_t N, u
 #pragma unroll
     for (int q = 0; q < 9; ++q) nout[(size_t)i * 9 + q] = nin[(size_t)src * 9 + q];
     sout[i] = sin[src];
+}
+
+// applyIndices for an attribute of `words` 16-bit words per triangle.
+__global__ void k_apply(const uint32_t* __restrict__ perm, uint32_t N, uint32_t count_in,
+                        const uint16_t* __restrict__ src, uint32_t words, uint16_t* __restrict__ dst) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    uint32_t p = perm[i];
+    if (p >= count_in) p = count_in - 1;
+    for (uint32_t w = 0; w < words; ++w) dst[(size_t)i * words + w] = src[(size_t)p * words + w];
 }
 
 }  // namespace
@@ -177,6 +188,86 @@ aur_status aur_nmh_export(aur_ctx* ctx, const aur_nmh* nmh, uint32_t* perm, floa
         AUR_CUDA(cudaMemcpyAsync(perm, nmh->perm, (size_t)nmh->count * 4, cudaMemcpyDeviceToHost, ctx->stream));
     if (vertices)
         AUR_CUDA(cudaMemcpyAsync(vertices, nmh->verts, (size_t)nmh->count * 36, cudaMemcpyDeviceToHost, ctx->stream));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    return AUR_OK;
+}
+
+aur_status aur_nmh_apply(aur_ctx* ctx, const aur_nmh* nmh, const void* src, uint32_t bytes_per_triangle, void* dst) {
+    clear_error();
+    AUR_CHECK(ctx && nmh, AUR_ERR_INVALID, "aur_nmh_apply: null context or NMH");
+    AUR_CHECK(bytes_per_triangle > 0 && bytes_per_triangle % 2 == 0, AUR_ERR_INVALID,
+              "aur_nmh_apply: bytes_per_triangle must be a positive multiple of 2");
+    if (nmh->count == 0) return AUR_OK;
+    AUR_CHECK(src && dst, AUR_ERR_INVALID, "aur_nmh_apply: null buffer");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    k_apply<<<(nmh->count + 255) / 256, 256, 0, ctx->stream>>>(nmh->perm, nmh->count, nmh->input_count,
+                                                              (const uint16_t*)src, bytes_per_triangle / 2,
+                                                              (uint16_t*)dst);
+    AUR_CUDA(cudaGetLastError());
+    return AUR_OK;
+}
+
+// --------------------------------------------------------------- memory
+
+aur_status aur_malloc(aur_ctx* ctx, size_t bytes, int policy, void** out) {
+    clear_error();
+    AUR_CHECK(ctx && out, AUR_ERR_INVALID, "aur_malloc: null argument");
+    *out = nullptr;
+    if (bytes == 0) return AUR_OK;
+    if (policy == AUR_HOST_MEMORY) {
+        *out = std::malloc(bytes);
+        AUR_CHECK(*out, AUR_ERR_OOM, "aur_malloc: out of host memory (%zu bytes)", bytes);
+        return AUR_OK;
+    }
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    cudaError_t e;
+    if (policy == AUR_DEVICE_MEMORY) e = cudaMalloc(out, bytes);
+    else if (policy == AUR_PINNED_MEMORY) e = cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+    else return fail(AUR_ERR_INVALID, "aur_malloc: unknown memory policy %d", policy);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return fail(AUR_ERR_OOM, "aur_malloc: %zu bytes: %s", bytes, cudaGetErrorString(e));
+    }
+    return AUR_OK;
+}
+
+aur_status aur_free(aur_ctx* ctx, void* ptr, int policy) {
+    AUR_CHECK(ctx, AUR_ERR_INVALID, "aur_free: null context");
+    if (!ptr) return AUR_OK;
+    if (policy == AUR_HOST_MEMORY) { std::free(ptr); return AUR_OK; }
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    if (policy == AUR_DEVICE_MEMORY) AUR_CUDA(cudaFree(ptr));
+    else if (policy == AUR_PINNED_MEMORY) AUR_CUDA(cudaFreeHost(ptr));
+    else return fail(AUR_ERR_INVALID, "aur_free: unknown memory policy %d", policy);
+    return AUR_OK;
+}
+
+aur_status aur_memzero(aur_ctx* ctx, void* ptr, size_t bytes, int policy) {
+    AUR_CHECK(ctx && (ptr || bytes == 0), AUR_ERR_INVALID, "aur_memzero: null argument");
+    if (bytes == 0) return AUR_OK;
+    if (policy != AUR_DEVICE_MEMORY) { std::memset(ptr, 0, bytes); return AUR_OK; }
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    AUR_CUDA(cudaMemsetAsync(ptr, 0, bytes, ctx->stream));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    return AUR_OK;
+}
+
+aur_status aur_memupload(aur_ctx* ctx, void* dst, const void* src, size_t bytes, int policy) {
+    AUR_CHECK(ctx && ((dst && src) || bytes == 0), AUR_ERR_INVALID, "aur_memupload: null argument");
+    if (bytes == 0) return AUR_OK;
+    if (policy != AUR_DEVICE_MEMORY) { std::memcpy(dst, src, bytes); return AUR_OK; }
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    AUR_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    return AUR_OK;
+}
+
+aur_status aur_memdownload(aur_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    AUR_CHECK(ctx && ((dst && src) || bytes == 0), AUR_ERR_INVALID, "aur_memdownload: null argument");
+    if (bytes == 0) return AUR_OK;
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    AUR_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     AUR_CUDA(cudaStreamSynchronize(ctx->stream));
     return AUR_OK;
 }

@@ -39,6 +39,42 @@ class SceneData:
         return self.vertices.shape[0]
 
 
+SCENE_MAGIC = b"AURSCN1\0"
+
+
+def write_scene_file(sd, path):
+    """Writes sd in the binary scene format read by the C++ host layer's
+    loadSceneFile: magic "AURSCN1\\0", uint32 counts (triangles, shaders,
+    lights, 0), the aur_camera record, 4 pad bytes, vertices and normals
+    (36 B per triangle each), shader ids (uint16, padded to an even count),
+    shaders (80 B each), lights (80 B each); all little-endian."""
+    n = sd.count
+    ids = sd.shader_ids
+    if n % 2:
+        ids = np.concatenate([ids, np.zeros(1, np.uint16)])
+    with open(path, "wb") as f:
+        f.write(SCENE_MAGIC)
+        f.write(np.array([n, sd.shaders.shape[0], sd.lights.shape[0], 0], "<u4").tobytes())
+        f.write(sd.camera.reshape(1).tobytes())
+        f.write(bytes(4))
+        f.write(sd.vertices.astype("<f4").tobytes())
+        f.write(sd.normals.astype("<f4").tobytes())
+        f.write(ids.astype("<u2").tobytes())
+        f.write(sd.shaders.tobytes())
+        f.write(sd.lights.tobytes())
+
+
+def read_pfm(path):
+    """Reads an RGB PFM (bottom row first) into an (H, W, 3) float32 array
+    with row 0 at the bottom, the layout of the accumulation buffers."""
+    with open(path, "rb") as f:
+        assert f.readline().strip() == b"PF"
+        w, h = (int(x) for x in f.readline().split())
+        scale = float(f.readline())
+        data = np.frombuffer(f.read(), "<f4" if scale < 0 else ">f4")
+    return data.reshape(h, w, 3).astype(np.float32)
+
+
 # ----------------------------------------------------------------- helpers
 
 def _f(x):

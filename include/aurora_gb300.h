@@ -172,6 +172,23 @@ aur_status aur_ctx_synchronize(aur_ctx* ctx);
 /* Number of SMs of the context's device. */
 aur_status aur_ctx_sm_count(aur_ctx* ctx, int* sm_count);
 
+/* ------------------------------------------------------------------ memory */
+
+/* Memory policies of core/memory.h (HostMemory, DeviceMemory) plus pinned
+ * host memory (the mapped staging buffers of Geometry::resizeStaging,
+ * data/geometry.cpp:50-73). */
+enum { AUR_HOST_MEMORY = 0, AUR_DEVICE_MEMORY = 1, AUR_PINNED_MEMORY = 2 };
+
+/* Aurora::malloc / memzero / memupload / free (core/memory.cpp). memupload
+ * copies `bytes` from host memory to `dst` of the given policy; memdownload
+ * copies device memory to host memory. Device operations run on the context's
+ * stream and are complete when the call returns. */
+aur_status aur_malloc(aur_ctx* ctx, size_t bytes, int policy, void** out);
+aur_status aur_free(aur_ctx* ctx, void* ptr, int policy);
+aur_status aur_memzero(aur_ctx* ctx, void* ptr, size_t bytes, int policy);
+aur_status aur_memupload(aur_ctx* ctx, void* dst, const void* src, size_t bytes, int policy);
+aur_status aur_memdownload(aur_ctx* ctx, void* dst, const void* src, size_t bytes);
+
 /* --------------------------------------------------------------------- NMH */
 
 typedef struct aur_nmh aur_nmh;
@@ -191,6 +208,11 @@ aur_status aur_nmh_info(const aur_nmh* nmh, uint32_t* count, uint32_t* levels);
  * position i (count entries); vertices (nullable) = count*9 floats of the
  * permuted soup in the reference layout (applyIndices, rebuilder.cu:217-245). */
 aur_status aur_nmh_export(aur_ctx* ctx, const aur_nmh* nmh, uint32_t* perm, float* vertices);
+/* applyIndices (kernels/rebuilder.cu:217-245) for any per-triangle
+ * attribute: dst[i] = src[perm[i]] for the `count` NMH positions, each
+ * `bytes_per_triangle` bytes (a multiple of 2); the padding triangle of an odd
+ * soup reads the last input triangle. src, dst: device. */
+aur_status aur_nmh_apply(aur_ctx* ctx, const aur_nmh* nmh, const void* src, uint32_t bytes_per_triangle, void* dst);
 /* Device pointer to the perm array (count uint32) owned by the NMH. */
 aur_status aur_nmh_perm_device(const aur_nmh* nmh, const uint32_t** perm);
 
