@@ -51,6 +51,7 @@ SIGNATURES = {
     "aur_trace_closest_host": ([P, P, P, U32, P], ctypes.c_int),
     "aur_trace_any_host": ([P, P, P, U32, P], ctypes.c_int),
     "aur_trace_count_visits": ([P, P, P, U32, P], ctypes.c_int),
+    "aur_trace_stats": ([P, P, P, U32, P, P], ctypes.c_int),
     "aur_scene_create": ([P, P, P, P, U32, P, U32, P, U32, P], ctypes.c_int),
     "aur_scene_destroy": ([P], ctypes.c_int),
     "aur_scene_nmh": ([P, P], ctypes.c_int),
@@ -231,6 +232,16 @@ def count_visits(ctx, nmh, rays_dev):
     out = (ctypes.c_ulonglong * 2)()
     check(lib().aur_trace_count_visits(ctx.handle, nmh.handle, _ptr(rays_dev), rays_dev.shape[0], out))
     return int(out[0]), int(out[1])
+
+
+def trace_stats(ctx, nmh, rays_dev):
+    """Work of the shipped (box-pruned) traversal: per kind ("closest",
+    "any") the node fetches, slab crossings and child-box loads."""
+    c = (ctypes.c_ulonglong * 3)()
+    a = (ctypes.c_ulonglong * 3)()
+    check(lib().aur_trace_stats(ctx.handle, nmh.handle, _ptr(rays_dev), rays_dev.shape[0], c, a))
+    keys = ("node_fetches", "slab_crossings", "box_loads")
+    return {"closest": dict(zip(keys, map(int, c))), "any": dict(zip(keys, map(int, a)))}
 
 
 class Scene:

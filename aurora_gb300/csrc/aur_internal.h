@@ -58,7 +58,7 @@ struct aur_nmh {
     uint32_t input_count = 0; // triangles as given
     uint32_t levels = 0;
     uint32_t nodes = 0;       // count / 2
-    float4* node_recs = nullptr;  // nodes * 5 float4 (slab, 2 x (v1, e1, e2))
+    float4* node_recs = nullptr;  // nodes * 8 float4 (slab, 2 x (v1, e1, e2), children's boxes)
     uint32_t* perm = nullptr;     // NMH position -> original prim id
     float* verts = nullptr;       // count * 9, NMH order, reference layout
 };
@@ -79,6 +79,6 @@ namespace aur {
 aur_status nmh_build_impl(aur_ctx* ctx, const float* vertices, uint32_t count, aur_nmh** out);
 aur_status check_params(const aur_render_params* p);
 aur_status launch_trace(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits,
-                        uint32_t* occluder, unsigned long long* visit_counter, cudaStream_t stream);
+                        uint32_t* occluder, unsigned long long* counters, cudaStream_t stream, bool pruned);
 
 }  // namespace aur

@@ -6,10 +6,22 @@
 // axis, range clipped cumulatively by each node's slab (ray.cuh:225-237),
 // Moller-Trumbore with culling (ray.cuh:198-223), hits need
 // Epsilon < t < best. Closest-hit ties in t go to the lower original prim id.
-// Node k occupies recs[5k .. 5k+4]: (slab_lo, slab_hi, tri0.v1.xy),
-// (tri0.v1.z, tri0.e1), (tri0.e2, tri1.v1.x), (tri1.v1.yz, tri1.e1.xy),
-// (tri1.e1.z, tri1.e2). Children of node k are 2k+1, 2k+2; the axis of a node
-// is its level mod 3.
+//
+// Node k occupies the 128-byte record recs[8k .. 8k+7]:
+//   [0] (slab_lo, slab_hi, tri0.v1.xy)   [1] (tri0.v1.z, tri0.e1)
+//   [2] (tri0.e2, tri1.v1.x)             [3] (tri1.v1.yz, tri1.e1.xy)
+//   [4] (tri1.e1.z, tri1.e2)
+//   [5..7] padded subtree boxes of the children 2k+1 and 2k+2:
+//          (c1.lo.xyz, c1.hi.x), (c1.hi.yz, c2.lo.xy), (c2.lo.z, c2.hi.xyz)
+// The axis of a node is its level mod 3.
+//
+// Subtree-box pruning: before descending, each child's box is tested against
+// the ray over (0, best t]; a child whose box the ray misses is neither
+// fetched nor pushed. The boxes are padded (relative 1e-5 in space, 1e-4 in
+// t) well beyond float rounding of both the box test and the triangle test,
+// so a pruned subtree holds no triangle the unpruned traversal would accept:
+// visit order, slab arithmetic and every accepted hit stay those of
+// intersect(), only subtrees without an acceptable hit are skipped.
 #pragma once
 
 #include "aur_math.cuh"
@@ -17,6 +29,29 @@
 namespace aur {
 
 constexpr uint32_t kNoPrim = 0xFFFFFFFFu;
+constexpr uint32_t kRecStride = 8;          // float4 per node record
+// Set on TravState::k when the current node was pruned by its box: the node
+// is not fetched, but its heap position still locates the pending far nodes.
+constexpr uint32_t kSkipBit = 0x80000000u;
+constexpr float kBoxNear = 0.9999f, kBoxFar = 1.0001f;
+
+// Reciprocal direction for box tests; zero components become +-1e-30 so that
+// no 0 * inf product (NaN) can occur.
+__device__ __forceinline__ f3 box_inv(const f3& d) {
+    return mk3(1.0f / copysignf(fmaxf(fabsf(d.x), 1e-30f), d.x), 1.0f / copysignf(fmaxf(fabsf(d.y), 1e-30f), d.y),
+               1.0f / copysignf(fmaxf(fabsf(d.z), 1e-30f), d.z));
+}
+
+// Conservative ray/box overlap over (0, tlimit].
+__device__ __forceinline__ bool box_hit(float lx, float ly, float lz, float hx, float hy, float hz, const f3& pos,
+                                        const f3& inv, float tlimit) {
+    const float x0 = (lx - pos.x) * inv.x, x1 = (hx - pos.x) * inv.x;
+    const float y0 = (ly - pos.y) * inv.y, y1 = (hy - pos.y) * inv.y;
+    const float z0 = (lz - pos.z) * inv.z, z1 = (hz - pos.z) * inv.z;
+    const float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), 0.0f));
+    const float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tlimit));
+    return tn * kBoxNear <= tf * kBoxFar;
+}
 
 // Per-thread storage of pending far-child ranges, one (lo, hi) pair per heap
 // level, in shared memory: level L of thread t lives at [L * stride] of the
@@ -56,7 +91,7 @@ __device__ __forceinline__ bool trav_next(TravState& s, const float4* __restrict
     for (;;) {
         if (s.k < nodes) {
             ++visits;
-            q0 = __ldg(recs + (size_t)s.k * 5);
+            q0 = __ldg(recs + (size_t)s.k * kRecStride);
             const float p = sel3(s.a, pos.x, pos.y, pos.z);
             const float d = sel3(s.a, dir.x, dir.y, dir.z);
             const float d0 = (q0.x - p) / d;
@@ -68,7 +103,7 @@ __device__ __forceinline__ bool trav_next(TravState& s, const float4* __restrict
         if (s.trail == 0) return false;
         const uint32_t L = 31u - (uint32_t)__clz(s.trail);
         s.trail &= ~(1u << L);
-        s.k = (((s.k + 1u) >> (s.lvl - L)) ^ 1u) - 1u;
+        s.k = ((((s.k & ~kSkipBit) + 1u) >> (s.lvl - L)) ^ 1u) - 1u;
         s.lvl = L;
         s.a = L % 3u;
         s.lo = stk.lo[L * stk.stride];
@@ -77,20 +112,34 @@ __device__ __forceinline__ bool trav_next(TravState& s, const float4* __restrict
 }
 
 // Descends from the current node (whose slab was crossed) to its near child,
-// leaving the far child pending on the child level.
-__device__ __forceinline__ void trav_descend(TravState& s, const f3& dir, uint32_t nodes, const StackRef& stk, float nlo,
-                                             float nhi) {
+// leaving the far child pending on the child level. With kBoxes, children
+// whose subtree box the ray misses within (0, tlimit] are dropped.
+template <bool kBoxes = true>
+__device__ __forceinline__ void trav_descend(TravState& s, const float4* __restrict__ recs, const f3& pos,
+                                             const f3& dir, const f3& inv, float tlimit, uint32_t nodes,
+                                             const StackRef& stk, float nlo, float nhi) {
     const uint32_t na = s.a == 2 ? 0 : s.a + 1;
     const bool neg = sel3(na, dir.x, dir.y, dir.z) < 0.0f;
-    const uint32_t near = neg ? 2 * s.k + 2 : 2 * s.k + 1;
-    const uint32_t far = neg ? 2 * s.k + 1 : 2 * s.k + 2;
+    const uint32_t c1 = 2 * s.k + 1;
+    bool h1 = c1 < nodes, h2 = c1 + 1 < nodes;
+    if (kBoxes && h1) {
+        const float4* r = recs + (size_t)s.k * kRecStride + 5;
+        const float4 b0 = __ldg(r), b1 = __ldg(r + 1);
+        h1 = box_hit(b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, pos, inv, tlimit);
+        if (h2) {
+            const float4 b2 = __ldg(r + 2);
+            h2 = box_hit(b1.z, b1.w, b2.x, b2.y, b2.z, b2.w, pos, inv, tlimit);
+        }
+    }
+    const bool near_ok = neg ? h2 : h1;
+    const bool far_ok = neg ? h1 : h2;
     const uint32_t L = s.lvl + 1;
-    if (far < nodes) {
+    if (far_ok) {
         stk.lo[L * stk.stride] = nlo;
         stk.hi[L * stk.stride] = nhi;
         s.trail |= 1u << L;
     }
-    s.k = near;
+    s.k = (neg ? c1 + 1 : c1) | (near_ok ? 0u : kSkipBit);
     s.lvl = L;
     s.a = na;
     s.lo = nlo;
@@ -104,10 +153,10 @@ template <bool kAny>
 __device__ __forceinline__ bool node_triangles(const float4* __restrict__ recs, uint32_t k, const float4& q0,
                                                const uint32_t* __restrict__ perm, const f3& pos, const f3& dir,
                                                float& best_t, float& bu, float& bv, uint32_t& best) {
-    const float4 q1 = __ldg(recs + (size_t)k * 5 + 1);
-    const float4 q2 = __ldg(recs + (size_t)k * 5 + 2);
-    const float4 q3 = __ldg(recs + (size_t)k * 5 + 3);
-    const float4 q4 = __ldg(recs + (size_t)k * 5 + 4);
+    const float4 q1 = __ldg(recs + (size_t)k * kRecStride + 1);
+    const float4 q2 = __ldg(recs + (size_t)k * kRecStride + 2);
+    const float4 q3 = __ldg(recs + (size_t)k * kRecStride + 3);
+    const float4 q4 = __ldg(recs + (size_t)k * kRecStride + 4);
     float u, v, t;
     if (intersect_tri(pos, dir, mk3(q0.z, q0.w, q1.x), mk3(q1.y, q1.z, q1.w), mk3(q2.x, q2.y, q2.z), u, v, t) &&
         t > kEpsilon) {
@@ -142,13 +191,14 @@ __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ recs, ui
                                              uint32_t& visits, uint32_t* __restrict__ err) {
     (void)err;
     uint32_t best = kNoPrim;
+    const f3 inv = box_inv(dir);
     TravState s;
     trav_init(s);
     float4 q0;
     float nlo, nhi;
     while (trav_next(s, recs, nodes, pos, dir, best_t, stk, q0, nlo, nhi, visits)) {
         if (node_triangles<kAny>(recs, s.k, q0, perm, pos, dir, best_t, bu, bv, best)) return best;
-        trav_descend(s, dir, nodes, stk, nlo, nhi);
+        trav_descend(s, recs, pos, dir, inv, best_t, nodes, stk, nlo, nhi);
     }
     return best;
 }

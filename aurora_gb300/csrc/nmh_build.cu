@@ -23,6 +23,7 @@
 
 #include "aur_internal.h"
 #include "aur_math.cuh"
+#include "aur_traverse.cuh"
 
 namespace aur {
 namespace {
@@ -511,9 +512,11 @@ __global__ void k_pair_order(uint32_t n, const uint32_t* __restrict__ heap, cons
 
 // applyIndices (rebuilder.cu:217-245) for the vertices, plus the traversal
 // record of each node: slab of the pair on the node's axis
-// (intersect.cuh:106-111) and both triangles as (v1, e1, e2).
+// (intersect.cuh:106-111) and both triangles as (v1, e1, e2). The bounding
+// box of the pair goes to box[6k..6k+5] (lo.xyz, hi.xyz) for k_node_boxes.
 __global__ void k_emit_nodes(const float* __restrict__ V, uint32_t count_in, const uint32_t* __restrict__ perm,
-                             uint32_t n, float* __restrict__ verts, float4* __restrict__ recs) {
+                             uint32_t n, float* __restrict__ verts, float4* __restrict__ recs,
+                             float* __restrict__ box) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int a = (int)(level_of(k) % 3u);
@@ -527,13 +530,19 @@ __global__ void k_emit_nodes(const float* __restrict__ V, uint32_t count_in, con
 #pragma unroll
         for (int q = 0; q < 9; ++q) { c[t][q] = v[q]; o[q] = c[t][q]; }
     }
-    const float lo = fminf(fminf(fminf(c[0][3 * a], c[0][3 * a + 1]), c[0][3 * a + 2]),
-                           fminf(fminf(c[1][3 * a], c[1][3 * a + 1]), c[1][3 * a + 2]));
-    const float hi = fmaxf(fmaxf(fmaxf(c[0][3 * a], c[0][3 * a + 1]), c[0][3 * a + 2]),
-                           fmaxf(fmaxf(c[1][3 * a], c[1][3 * a + 1]), c[1][3 * a + 2]));
+    float blo[3], bhi[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        blo[ax] = fminf(fminf(fminf(c[0][3 * ax], c[0][3 * ax + 1]), c[0][3 * ax + 2]),
+                        fminf(fminf(c[1][3 * ax], c[1][3 * ax + 1]), c[1][3 * ax + 2]));
+        bhi[ax] = fmaxf(fmaxf(fmaxf(c[0][3 * ax], c[0][3 * ax + 1]), c[0][3 * ax + 2]),
+                        fmaxf(fmaxf(c[1][3 * ax], c[1][3 * ax + 1]), c[1][3 * ax + 2]));
+        box[6 * (size_t)k + ax] = blo[ax];
+        box[6 * (size_t)k + 3 + ax] = bhi[ax];
+    }
     float r[20];
-    r[0] = lo;
-    r[1] = hi;
+    r[0] = a == 0 ? blo[0] : (a == 1 ? blo[1] : blo[2]);
+    r[1] = a == 0 ? bhi[0] : (a == 1 ? bhi[1] : bhi[2]);
 #pragma unroll
     for (int t = 0; t < 2; ++t) {
         // layout [x1 x2 x3 y1 y2 y3 z1 z2 z3]: v1 = (c0, c3, c6), v2 = (c1, c4, c7), v3 = (c2, c5, c8)
@@ -542,9 +551,53 @@ __global__ void k_emit_nodes(const float* __restrict__ V, uint32_t count_in, con
         o[3] = c[t][1] - c[t][0]; o[4] = c[t][4] - c[t][3]; o[5] = c[t][7] - c[t][6];
         o[6] = c[t][2] - c[t][0]; o[7] = c[t][5] - c[t][3]; o[8] = c[t][8] - c[t][6];
     }
-    float4* rec = recs + (size_t)k * 5;
+    float4* rec = recs + (size_t)k * kRecStride;
 #pragma unroll
     for (int q = 0; q < 5; ++q) rec[q] = make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
+}
+
+// Box padding: relative 1e-5 of the coordinates' magnitude, far above the
+// rounding of the triangle test and of the box test.
+__device__ __forceinline__ void pad_interval(float lo, float hi, float& plo, float& phi) {
+    const float p = 1e-5f * (fabsf(lo) + fabsf(hi)) + 1e-30f;
+    plo = lo - p;
+    phi = hi + p;
+}
+
+// One heap level, bottom-up: box[k] becomes the bounding box of node k's
+// subtree (its pair and its children's subtrees, computed one launch
+// earlier), and the padded subtree boxes of the children go into record
+// words 5..7 of node k (an empty box where a child does not exist).
+__global__ void k_node_boxes(uint32_t L0, uint32_t L1, uint32_t n, float* __restrict__ box,
+                             float4* __restrict__ recs) {
+    const uint32_t k = L0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= L1) return;
+    float b[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) b[q] = box[6 * (size_t)k + q];
+    float cb[2][6];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const uint32_t c = 2 * k + 1 + j;
+        if (c < n) {
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                const float lo = box[6 * (size_t)c + ax], hi = box[6 * (size_t)c + 3 + ax];
+                b[ax] = fminf(b[ax], lo);
+                b[3 + ax] = fmaxf(b[3 + ax], hi);
+                pad_interval(lo, hi, cb[j][ax], cb[j][3 + ax]);
+            }
+        } else {
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) { cb[j][ax] = 1.0f; cb[j][3 + ax] = -1.0f; }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 6; ++q) box[6 * (size_t)k + q] = b[q];
+    float4* rec = recs + (size_t)k * kRecStride + 5;
+    rec[0] = make_float4(cb[0][0], cb[0][1], cb[0][2], cb[0][3]);
+    rec[1] = make_float4(cb[0][4], cb[0][5], cb[1][0], cb[1][1]);
+    rec[2] = make_float4(cb[1][2], cb[1][3], cb[1][4], cb[1][5]);
 }
 
 inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
@@ -553,6 +606,18 @@ uint32_t log2i(uint32_t x) {
     uint32_t r = (uint32_t)(-1);
     while (x) { x >>= 1; r++; }
     return r;
+}
+
+// Node records: pairs and slabs, then the children's subtree boxes level by
+// level from the bottom. box: 6 floats per node of scratch.
+void emit_records(const float* V, uint32_t count, const uint32_t* perm, uint32_t n, uint32_t levels, float* verts,
+                  float4* recs, float* box, cudaStream_t st) {
+    k_emit_nodes<<<cdiv(n, 128), 128, 0, st>>>(V, count, perm, n, verts, recs, box);
+    for (int lv = (int)levels - 1; lv >= 0; --lv) {
+        const uint32_t L0 = (1u << lv) - 1u;
+        const uint32_t L1 = ((2u << lv) - 1u) < n ? ((2u << lv) - 1u) : n;
+        k_node_boxes<<<cdiv(L1 - L0, 256), 256, 0, st>>>(L0, L1, n, box, recs);
+    }
 }
 
 }  // namespace
@@ -579,7 +644,7 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
         cudaFree(nmh->verts);
         delete nmh;
     };
-    if (cudaMalloc(&nmh->node_recs, (size_t)n * 5 * sizeof(float4)) != cudaSuccess ||
+    if (cudaMalloc(&nmh->node_recs, (size_t)n * kRecStride * sizeof(float4)) != cudaSuccess ||
         cudaMalloc(&nmh->perm, (size_t)N * sizeof(uint32_t)) != cudaSuccess ||
         cudaMalloc(&nmh->verts, (size_t)N * 9 * sizeof(float)) != cudaSuccess) {
         cudaGetLastError();
@@ -672,7 +737,8 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
     }
     const int al = (int)((nmh->levels - 1) % 3);
     k_pair_order<<<cdiv(n, 256), 256, 0, st>>>(n, heap, mn + al * S, nmh->perm);
-    k_emit_nodes<<<cdiv(n, 128), 128, 0, st>>>(V, count, nmh->perm, n, nmh->verts, nmh->node_recs);
+    // mx is free once the levels are placed: 3*S >= 6*n floats for the boxes
+    emit_records(V, count, nmh->perm, n, nmh->levels, nmh->verts, nmh->node_recs, mx, st);
     cudaFreeAsync(base, st);
     cudaError_t e = cudaGetLastError();
     uint32_t flags = 0;
@@ -853,7 +919,7 @@ aur_status nmh_build_noalloc_impl(const float* V, uint32_t count, cudaStream_t s
     }
     const int al = (int)((levels - 1) % 3);
     k_pair_order<<<cdiv(n, 256), 256, 0, st>>>(n, heap, mn + al * S, perm);
-    k_emit_nodes<<<cdiv(n, 128), 128, 0, st>>>(V, count, perm, n, verts, recs);
+    emit_records(V, count, perm, n, levels, verts, recs, mx, st);
     AUR_CUDA(cudaGetLastError());
     uint32_t h_flags = 0;
     AUR_CUDA(cudaMemcpyAsync(&h_flags, flags, 4, cudaMemcpyDeviceToHost, st));

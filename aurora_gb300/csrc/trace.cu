@@ -5,11 +5,12 @@
 // sign of the ray direction on the child's axis, range clipped cumulatively
 // by each node's slab (ray.cuh:225-237), Moller-Trumbore with culling
 // (ray.cuh:198-223). The node of the reference is 72 scattered bytes read
-// with 24 scalar loads; here it is an 80-byte record (slab + two triangles as
-// v1, e1, e2) read as one 16-byte load for the slab test and four more only
-// when the slab is hit. The traversal stack lives in shared memory: the
-// near child is visited next, only the far child is pushed, so the stack
-// never holds more entries than the heap has levels.
+// with 24 scalar loads; here it is a 128-byte record (slab, two triangles as
+// v1, e1, e2, and the subtree boxes of both children) read as one 16-byte
+// load for the slab test, four more only when the slab is hit and three more
+// for the children's boxes before descending. The traversal stack lives in
+// shared memory: the near child is visited next, only the far child is
+// pushed, so the stack never holds more entries than the heap has levels.
 #include <algorithm>
 
 #include "aur_internal.h"
@@ -32,13 +33,16 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // done takes the next unprocessed ray at once (one atomic per warp for all
 // lanes asking together), so warps stay full until the ray pool is drained
 // (Aila & Laine, "Understanding the efficiency of ray traversal on GPUs",
-// HPG'09). Every ray is traversed exactly as intersect()/intersectAny().
-template <bool kAny, bool kCount>
+// HPG'09). Every ray is traversed as intersect()/intersectAny(); kBoxes adds
+// the subtree-box pruning (off only to count the reference's own node visits).
+// kCount adds up node fetches, slab crossings (triangle tests) and crossings
+// of nodes with children (box loads) into counters[0..2].
+template <bool kAny, bool kCount, bool kBoxes>
 __global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restrict__ recs, uint32_t nodes,
                                                          const uint32_t* __restrict__ perm,
                                                          const float4* __restrict__ rays, uint32_t n,
                                                          float4* __restrict__ hits, uint32_t* __restrict__ occ,
-                                                         unsigned long long* __restrict__ visit_counter,
+                                                         unsigned long long* __restrict__ counters,
                                                          uint32_t* __restrict__ ray_counter, int cap) {
     extern __shared__ uint32_t smem[];
     const int tid = threadIdx.x;
@@ -47,9 +51,9 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restric
     stk.hi = reinterpret_cast<float*>(smem + cap * kTraceThreads) + tid;
     stk.stride = kTraceThreads;
     stk.cap = cap;
-    uint32_t visits = 0;
+    uint32_t visits = 0, crossings = 0, inner = 0;
     uint32_t i = kNoRay;
-    f3 pos = mk3(0.0f), dir = mk3(0.0f);
+    f3 pos = mk3(0.0f), dir = mk3(0.0f), inv = mk3(0.0f);
     float tmax = 0.0f, best_t = 0.0f, bu = 0.0f, bv = 0.0f;
     uint32_t best = kNoPrim;
     TravState s;
@@ -67,6 +71,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restric
             const float4 r1 = rays[2 * (size_t)i + 1];
             pos = mk3(r0.x, r0.y, r0.z);
             dir = mk3(r1.x, r1.y, r1.z);
+            inv = box_inv(dir);
             tmax = best_t = r0.w;
             bu = bv = 0.0f;
             best = kNoPrim;
@@ -76,8 +81,12 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restric
         float nlo, nhi;
         bool done;
         if (trav_next(s, recs, nodes, pos, dir, best_t, stk, q0, nlo, nhi, visits)) {
+            if (kCount) {
+                ++crossings;
+                inner += 2 * s.k + 1 < nodes;
+            }
             done = node_triangles<kAny>(recs, s.k, q0, perm, pos, dir, best_t, bu, bv, best);
-            if (!done) trav_descend(s, dir, nodes, stk, nlo, nhi);
+            if (!done) trav_descend<kBoxes>(s, recs, pos, dir, inv, best_t, nodes, stk, nlo, nhi);
         } else {
             done = true;
         }
@@ -95,37 +104,45 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restric
             i = kNoRay;
         }
     }
-    if (kCount && visits) atomicAdd(visit_counter, (unsigned long long)visits);
+    if (kCount) {
+        atomicAdd(counters, (unsigned long long)visits);
+        atomicAdd(counters + 1, (unsigned long long)crossings);
+        atomicAdd(counters + 2, (unsigned long long)inner);
+    }
 }
 
 inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
 }  // namespace
 
-template <bool kAny, bool kCount>
+template <bool kAny, bool kCount, bool kBoxes = true>
 aur_status launch_one(aur_ctx* ctx, const aur_nmh* nmh, const float4* r, uint32_t n, float4* h, uint32_t* occ,
-                      unsigned long long* visit_counter, cudaStream_t stream) {
+                      unsigned long long* counters, cudaStream_t stream) {
     const int cap = (int)nmh->levels + 1;
     const size_t smem = (size_t)2 * cap * kTraceThreads * sizeof(uint32_t);
     int per_sm = 0;
-    AUR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<kAny, kCount>, kTraceThreads, smem));
+    AUR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<kAny, kCount, kBoxes>, kTraceThreads,
+                                                           smem));
     const uint32_t grid = std::max(1u, std::min<uint32_t>(cdiv(n, kTraceThreads), (uint32_t)(ctx->sm_count * per_sm)));
     uint32_t* ray_counter = ctx->d_flags + 8;
     AUR_CUDA(cudaMemsetAsync(ray_counter, 0, sizeof(uint32_t), stream));
-    k_trace<kAny, kCount><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r, n, h, occ,
-                                                                visit_counter, ray_counter, cap);
+    k_trace<kAny, kCount, kBoxes><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r,
+                                                                        n, h, occ, counters, ray_counter, cap);
     AUR_CUDA(cudaGetLastError());
     return AUR_OK;
 }
 
 aur_status launch_trace(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits,
-                        uint32_t* occluder, unsigned long long* visit_counter, cudaStream_t stream) {
+                        uint32_t* occluder, unsigned long long* counters, cudaStream_t stream, bool pruned) {
     if (n == 0) return AUR_OK;
     const float4* r = reinterpret_cast<const float4*>(rays);
     float4* h = reinterpret_cast<float4*>(hits);
-    if (visit_counter)
-        return occluder ? launch_one<true, true>(ctx, nmh, r, n, nullptr, occluder, visit_counter, stream)
-                        : launch_one<false, true>(ctx, nmh, r, n, h, nullptr, visit_counter, stream);
+    if (counters && !pruned)
+        return occluder ? launch_one<true, true, false>(ctx, nmh, r, n, nullptr, occluder, counters, stream)
+                        : launch_one<false, true, false>(ctx, nmh, r, n, h, nullptr, counters, stream);
+    if (counters)
+        return occluder ? launch_one<true, true>(ctx, nmh, r, n, nullptr, occluder, counters, stream)
+                        : launch_one<false, true>(ctx, nmh, r, n, h, nullptr, counters, stream);
     return occluder ? launch_one<true, false>(ctx, nmh, r, n, nullptr, occluder, nullptr, stream)
                     : launch_one<false, false>(ctx, nmh, r, n, h, nullptr, nullptr, stream);
 }
@@ -186,7 +203,7 @@ aur_status trace_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uin
         AUR_CUDA(cudaEventRecord(in_done[s], ctx->copy_in));
         AUR_CUDA(cudaStreamWaitEvent(ctx->stream, in_done[s], 0));
         st = launch_trace(ctx, nmh, (const aur_ray*)ctx->pipe[s].ptr, m, any ? nullptr : (aur_hit*)ctx->out[s].ptr,
-                          any ? (uint32_t*)ctx->out[s].ptr : nullptr, nullptr, ctx->stream);
+                          any ? (uint32_t*)ctx->out[s].ptr : nullptr, nullptr, ctx->stream, true);
         if (st != AUR_OK) return st;
         AUR_CUDA(cudaEventRecord(comp_done[s], ctx->stream));
         AUR_CUDA(cudaStreamWaitEvent(ctx->copy_out, comp_done[s], 0));
@@ -208,14 +225,14 @@ aur_status aur_trace_closest(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* ra
     aur_status st = check_trace_args(ctx, nmh, rays, n, hits);
     if (st != AUR_OK) return st;
     AUR_CUDA(cudaSetDevice(ctx->device));
-    return launch_trace(ctx, nmh, rays, n, hits, nullptr, nullptr, ctx->stream);
+    return launch_trace(ctx, nmh, rays, n, hits, nullptr, nullptr, ctx->stream, true);
 }
 
 aur_status aur_trace_any(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, uint32_t* occluder) {
     aur_status st = check_trace_args(ctx, nmh, rays, n, occluder);
     if (st != AUR_OK) return st;
     AUR_CUDA(cudaSetDevice(ctx->device));
-    return launch_trace(ctx, nmh, rays, n, nullptr, occluder, nullptr, ctx->stream);
+    return launch_trace(ctx, nmh, rays, n, nullptr, occluder, nullptr, ctx->stream, true);
 }
 
 aur_status aur_trace_closest_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits) {
@@ -226,31 +243,62 @@ aur_status aur_trace_any_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* r
     return trace_host(ctx, nmh, rays, n, occluder, true);
 }
 
+namespace {
+
+// Runs closest hit and any hit over n device rays with the counting kernels;
+// out[0..2] closest (fetches, crossings, inner crossings), out[3..5] any hit.
+aur_status count_work(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, bool pruned,
+                      unsigned long long out[6]) {
+    for (int q = 0; q < 6; ++q) out[q] = 0;
+    if (n == 0) return AUR_OK;
+    void* scratch = nullptr;
+    const size_t bytes = 256 + (size_t)n * sizeof(aur_hit);
+    AUR_CHECK(cudaMallocAsync(&scratch, bytes, ctx->stream) == cudaSuccess, AUR_ERR_OOM,
+              "trace counters: out of memory");
+    unsigned long long* cnt = (unsigned long long*)scratch;
+    aur_hit* hits = (aur_hit*)((char*)scratch + 256);
+    cudaMemsetAsync(cnt, 0, 48, ctx->stream);
+    aur_status st = launch_trace(ctx, nmh, rays, n, hits, nullptr, cnt, ctx->stream, pruned);
+    if (st == AUR_OK) st = launch_trace(ctx, nmh, rays, n, nullptr, (uint32_t*)hits, cnt + 3, ctx->stream, pruned);
+    unsigned long long host[6] = {0, 0, 0, 0, 0, 0};
+    cudaMemcpyAsync(host, cnt, 48, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaFreeAsync(scratch, ctx->stream);
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (st != AUR_OK) return st;
+    for (int q = 0; q < 6; ++q) out[q] = host[q];
+    return AUR_OK;
+}
+
+}  // namespace
+
 aur_status aur_trace_count_visits(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n,
                                   unsigned long long node_visits[2]) {
     AUR_CHECK(node_visits, AUR_ERR_INVALID, "aur_trace_count_visits: null output");
     aur_status st = check_trace_args(ctx, nmh, rays, n, rays);
     if (st != AUR_OK) return st;
     AUR_CUDA(cudaSetDevice(ctx->device));
-    node_visits[0] = node_visits[1] = 0;
-    if (n == 0) return AUR_OK;
-    void* scratch = nullptr;
-    const size_t bytes = 256 + (size_t)n * sizeof(aur_hit);
-    AUR_CHECK(cudaMallocAsync(&scratch, bytes, ctx->stream) == cudaSuccess, AUR_ERR_OOM,
-              "aur_trace_count_visits: out of memory");
-    unsigned long long* cnt = (unsigned long long*)scratch;
-    aur_hit* hits = (aur_hit*)((char*)scratch + 256);
-    cudaMemsetAsync(cnt, 0, 16, ctx->stream);
-    st = launch_trace(ctx, nmh, rays, n, hits, nullptr, cnt, ctx->stream);
-    if (st == AUR_OK) st = launch_trace(ctx, nmh, rays, n, nullptr, (uint32_t*)hits, cnt + 1, ctx->stream);
-    unsigned long long host[2] = {0, 0};
-    cudaMemcpyAsync(host, cnt, 16, cudaMemcpyDeviceToHost, ctx->stream);
-    cudaFreeAsync(scratch, ctx->stream);
-    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    unsigned long long c[6];
+    st = count_work(ctx, nmh, rays, n, false, c);
+    node_visits[0] = c[0];
+    node_visits[1] = c[3];
+    return st;
+}
+
+aur_status aur_trace_stats(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n,
+                           aur_trace_work* closest, aur_trace_work* any) {
+    AUR_CHECK(closest && any, AUR_ERR_INVALID, "aur_trace_stats: null output");
+    aur_status st = check_trace_args(ctx, nmh, rays, n, rays);
     if (st != AUR_OK) return st;
-    node_visits[0] = host[0];
-    node_visits[1] = host[1];
-    return AUR_OK;
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    unsigned long long c[6];
+    st = count_work(ctx, nmh, rays, n, true, c);
+    closest->node_fetches = c[0];
+    closest->slab_crossings = c[1];
+    closest->box_loads = c[2];
+    any->node_fetches = c[3];
+    any->slab_crossings = c[4];
+    any->box_loads = c[5];
+    return st;
 }
 
 }  // extern "C"

@@ -207,7 +207,7 @@ __global__ void k_wf_extend(WfArgs a) {
     const float4* recs = nullptr;
     const uint32_t* perm = nullptr;
     uint32_t nodes = 0;
-    f3 pos = mk3(0.0f), dir = mk3(0.0f);
+    f3 pos = mk3(0.0f), dir = mk3(0.0f), inv = mk3(0.0f);
     float best_t = 0.0f, bu = 0.0f, bv = 0.0f;
     uint32_t best = kNoPrim;
     TravState s;
@@ -222,6 +222,7 @@ __global__ void k_wf_extend(WfArgs a) {
             const float4 o = a.o[slot], d = a.d[slot];
             pos = mk3(o.x, o.y, o.z);
             dir = mk3(d.x, d.y, d.z);
+            inv = box_inv(dir);
             best_t = kInfinity; bu = bv = 0.0f; best = kNoPrim;
             trav_init(s);
         }
@@ -229,7 +230,7 @@ __global__ void k_wf_extend(WfArgs a) {
         float nlo, nhi;
         if (trav_next(s, recs, nodes, pos, dir, best_t, stk, q0, nlo, nhi, visits)) {
             node_triangles<false>(recs, s.k, q0, perm, pos, dir, best_t, bu, bv, best);
-            trav_descend(s, dir, nodes, stk, nlo, nhi);
+            trav_descend(s, recs, pos, dir, inv, best_t, nodes, stk, nlo, nhi);
         } else {
             a.hit[slot] = make_float4(best_t, bu, bv, __uint_as_float(best));
             slot = 0xFFFFFFFFu;
@@ -332,7 +333,7 @@ __global__ void k_wf_shadow(WfArgs a) {
     const float4* recs = nullptr;
     const uint32_t* perm = nullptr;
     uint32_t nodes = 0;
-    f3 pos = mk3(0.0f), dir = mk3(0.0f);
+    f3 pos = mk3(0.0f), dir = mk3(0.0f), inv = mk3(0.0f);
     float tmax = 0.0f, bu = 0.0f, bv = 0.0f;
     uint32_t best = kNoPrim;
     TravState s;
@@ -347,6 +348,7 @@ __global__ void k_wf_shadow(WfArgs a) {
             recs = sc.recs; perm = sc.perm; nodes = sc.nodes;
             pos = mk3(o.x, o.y, o.z);
             dir = mk3(d.x, d.y, d.z);
+            inv = box_inv(dir);
             tmax = o.w;
             best = kNoPrim;
             trav_init(s);
@@ -356,7 +358,7 @@ __global__ void k_wf_shadow(WfArgs a) {
         bool done;
         if (trav_next(s, recs, nodes, pos, dir, tmax, stk, q0, nlo, nhi, visits)) {
             done = node_triangles<true>(recs, s.k, q0, perm, pos, dir, tmax, bu, bv, best);
-            if (!done) trav_descend(s, dir, nodes, stk, nlo, nhi);
+            if (!done) trav_descend(s, recs, pos, dir, inv, tmax, nodes, stk, nlo, nhi);
         } else {
             done = true;
         }

@@ -11,8 +11,12 @@ the metric is Mrays/s closest-hit. Inputs are seeded synthetic data.
 Prints one JSON line. `e2e` measures the same metric through the C ABI's
 host-buffer call (aur_trace_closest_host: rays copied in from pinned host
 memory and hits copied back inside the timed region). `roofline` divides the
-algorithmic bytes of a launch (28 B ray in + 16 B hit out + 72 B per node
-fetched, the reference's per-node read) by the kernel's CUDA-event duration.
+algorithmic bytes of a launch by the kernel's CUDA-event duration: 28 B ray
+in + 16 B hit out + per node record fetched 16 B (slab), per slab crossed
+64 B (two triangles) and per crossing of a node with children 48 B (the
+children's subtree boxes), the reads of this traversal as counted by
+aur_trace_stats. The reference algorithm's own figure (72 B per node it
+visits, counted by the unpruned traversal) is reported beside it.
 `cpu_baseline` times the oracle's C++ restatement of the reference traversal
 on a sample of the same rays on all host cores. With --gpus N > 1 (under
 torchrun) every rank runs an independent replica of the workload.
@@ -36,6 +40,9 @@ N_RAYS = 1 << 24
 RAY_IN_BYTES = 28      # origin, direction, tmax
 HIT_OUT_BYTES = 16     # t, u, v, prim
 NODE_BYTES = 72        # two triangles, as the reference fetches per visited node
+SLAB_BYTES = 16        # first word of a node record: slab lo/hi (+ 8 B of triangle)
+TRI_BYTES = 64         # rest of the two triangles, read when the slab is crossed
+BOX_BYTES = 48         # children's subtree boxes, read before descending
 METRIC = "Mrays/s closest-hit"
 WORKLOAD = ("traversal microbench: 1M triangles (centroid U[0,1]^3, edges LogNormal(-4,0.5)), 2^24 rays "
             "(half coherent pinhole 4096x4096 even rows, half random origin/direction), closest hit")
@@ -528,6 +535,7 @@ def main():
     hits_d = torch.empty((N_RAYS, 4), dtype=torch.float32, device="cuda")
     occ_d = torch.empty((N_RAYS,), dtype=torch.int32, device="cuda")
     visits_closest, visits_any = api.count_visits(ctx, nmh, rays_d)
+    work = api.trace_stats(ctx, nmh, rays_d)
     stream = torch.cuda.current_stream()
 
     def barrier():
@@ -581,7 +589,10 @@ def main():
     same = np.array_equal(hits_h.numpy().view(np.uint32), hits_d.cpu().numpy().view(np.uint32))
 
     peak, peak_kind = load_peaks()
-    alg_bytes = N_RAYS * (RAY_IN_BYTES + HIT_OUT_BYTES) + NODE_BYTES * visits_closest
+    wc = work["closest"]
+    alg_bytes = (N_RAYS * (RAY_IN_BYTES + HIT_OUT_BYTES) + SLAB_BYTES * wc["node_fetches"] +
+                 TRI_BYTES * wc["slab_crossings"] + BOX_BYTES * wc["box_loads"])
+    ref_bytes = N_RAYS * (RAY_IN_BYTES + HIT_OUT_BYTES) + NODE_BYTES * visits_closest
     avg_launch_s = statistics.mean(launch_ms) * 1e-3
     achieved = alg_bytes / avg_launch_s / 1e9
     clocks = clk.summary()
@@ -595,13 +606,19 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": load_traffic(), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                     "algorithmic_bytes_per_launch": alg_bytes, "node_fetches_per_ray": visits_closest / N_RAYS},
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "node_fetches_per_ray": wc["node_fetches"] / N_RAYS,
+                     "slab_crossings_per_ray": wc["slab_crossings"] / N_RAYS,
+                     "reference_node_visits_per_ray": visits_closest / N_RAYS,
+                     "reference_algorithm_bytes_per_launch": ref_bytes,
+                     "reference_algorithm_GBps": ref_bytes / avg_launch_s / 1e9},
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 32,
                 "d2h_bytes_per_step": N_RAYS * 16, "matches_device_result": bool(same)},
         "gpu_launches": args.steps,
         "clocks": clocks,
         "any_hit": {"value": world * N_RAYS / (any_ms * 1e-3) / 1e6, "unit": "Mrays/s", "ms_per_step": any_ms,
-                    "node_fetches_per_ray": visits_any / N_RAYS},
+                    "node_fetches_per_ray": work["any"]["node_fetches"] / N_RAYS,
+                    "reference_node_visits_per_ray": visits_any / N_RAYS},
         "nmh_build_ms": build_ms,
     }
     if rank == 0 and not args.no_cpu_baseline:

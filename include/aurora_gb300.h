@@ -222,7 +222,7 @@ aur_status aur_nmh_perm_device(const aur_nmh* nmh, const uint32_t** perm);
  * and only hands out fixed buffers, or a render loop that must not pay for
  * cudaMalloc / cudaFree, which can synchronize the whole device.
  * Same result as aur_nmh_build, written into caller-owned device buffers:
- *   node_records: ((count+1)/2) * 20 floats, 16-byte aligned (traversal records)
+ *   node_records: ((count+1)/2) * 32 floats, 16-byte aligned (traversal records)
  *   perm:         count + (count & 1) uint32 (NMH position -> original prim id)
  *   nmh_vertices: (count + (count & 1)) * 9 floats (NMH-ordered soup)
  *   levels:       host, nullable; receives log2i(count/2)+1
@@ -278,11 +278,24 @@ aur_status aur_trace_any(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, 
  * traversal on the context's stream plus two internal copy streams. */
 aur_status aur_trace_closest_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits);
 aur_status aur_trace_any_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, uint32_t* occluder);
-/* Counts traversal work for n device rays: node_visits[0] = nodes fetched by
- * closest hit, node_visits[1] = by any hit (a node is fetched when popped with
- * index < count, intersect.cuh:103-111). Used for roofline accounting. */
+/* Counts the reference algorithm's traversal work for n device rays:
+ * node_visits[0] = nodes fetched by closest hit, node_visits[1] = by any hit
+ * (a node is fetched when popped with index < count, intersect.cuh:103-111),
+ * counted by running the traversal without subtree-box pruning. */
 aur_status aur_trace_count_visits(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n,
                                   unsigned long long node_visits[2]);
+
+/* Work of this library's traversal (with subtree-box pruning) over n rays:
+ * node records fetched (16-byte slab load), slabs crossed (two triangles,
+ * 64 bytes, tested) and children's boxes loaded (48 bytes). No reference
+ * counterpart; used for roofline accounting. */
+typedef struct aur_trace_work {
+    unsigned long long node_fetches;
+    unsigned long long slab_crossings;
+    unsigned long long box_loads;
+} aur_trace_work;
+aur_status aur_trace_stats(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_trace_work* closest,
+                           aur_trace_work* any);
 
 /* ------------------------------------------------------------------- scene */
 

@@ -32,31 +32,45 @@ def _noalloc_build(V):
     count = V.shape[0]
     N = count + (count & 1)
     Vd = torch.from_numpy(np.ascontiguousarray(V, np.float32).reshape(-1)).cuda()
-    recs = torch.full((max(N // 2, 1) * 20,), float("nan"), dtype=torch.float32, device="cuda")
+    recs = torch.full((max(N // 2, 1) * 32,), float("nan"), dtype=torch.float32, device="cuda")
     perm = torch.full((max(N, 1),), -1, dtype=torch.int32, device="cuda")
     verts = torch.full((max(N, 1) * 9,), float("nan"), dtype=torch.float32, device="cuda")
     levels = ctypes.c_uint32(0)
     api.check(api.lib().aur_nmh_build_noalloc(api._ptr(Vd), count, _stream_arg(), api._ptr(recs), api._ptr(perm),
                                               api._ptr(verts), ctypes.byref(levels)))
-    return (recs.cpu().numpy()[:N // 2 * 20].reshape(-1, 20), perm.cpu().numpy()[:N].view(np.uint32),
+    return (recs.cpu().numpy()[:N // 2 * 32].reshape(-1, 32), perm.cpu().numpy()[:N].view(np.uint32),
             verts.cpu().numpy()[:N * 9].reshape(-1, 9), levels.value)
 
 
 def _expected_records(verts):
     """Node records from the NMH-ordered soup: slab of the pair on the node's
-    axis, then each triangle as v1, v2 - v1, v3 - v1 (float32)."""
+    axis, each triangle as v1, v2 - v1, v3 - v1, then the padded subtree boxes
+    of the two children (empty box (1, -1) where a child does not exist)."""
     n = verts.shape[0] // 2
-    recs = np.zeros((n, 20), np.float32)
+    recs = np.zeros((n, 32), np.float32)
+    box = np.zeros((n, 6), np.float32)
     for k in range(n):
         a = ((k + 1).bit_length() - 1) % 3
         t0, t1 = verts[2 * k], verts[2 * k + 1]
-        recs[k, 0] = min(t0[3 * a:3 * a + 3].min(), t1[3 * a:3 * a + 3].min())
-        recs[k, 1] = max(t0[3 * a:3 * a + 3].max(), t1[3 * a:3 * a + 3].max())
+        for ax in range(3):
+            box[k, ax] = min(t0[3 * ax:3 * ax + 3].min(), t1[3 * ax:3 * ax + 3].min())
+            box[k, 3 + ax] = max(t0[3 * ax:3 * ax + 3].max(), t1[3 * ax:3 * ax + 3].max())
+        recs[k, 0] = box[k, a]
+        recs[k, 1] = box[k, 3 + a]
         for i, t in enumerate((t0, t1)):
             v1 = np.array([t[0], t[3], t[6]], np.float32)
             v2 = np.array([t[1], t[4], t[7]], np.float32)
             v3 = np.array([t[2], t[5], t[8]], np.float32)
             recs[k, 2 + 9 * i:11 + 9 * i] = np.concatenate([v1, v2 - v1, v3 - v1])
+    for k in range(n - 1, -1, -1):              # children have higher indices: bottom-up
+        for j, c in enumerate((2 * k + 1, 2 * k + 2)):
+            cb = np.array([1, 1, 1, -1, -1, -1], np.float32)
+            if c < n:
+                box[k, :3] = np.minimum(box[k, :3], box[c, :3])
+                box[k, 3:] = np.maximum(box[k, 3:], box[c, 3:])
+                pad = np.float32(1e-5) * (np.abs(box[c, :3]) + np.abs(box[c, 3:])) + np.float32(1e-30)
+                cb = np.concatenate([box[c, :3] - pad, box[c, 3:] + pad]).astype(np.float32)
+            recs[k, 20 + 6 * j:26 + 6 * j] = cb
     return recs
 
 
