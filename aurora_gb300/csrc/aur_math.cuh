@@ -174,12 +174,21 @@ __device__ __forceinline__ bool intersect_tri(const f3& pos, const f3& dir, cons
     const f3 P = cross(dir, e2);
     const float det = dot(e1, P);
     if (det < kEpsilon) return false;
-    const float invdet = 1.0f / det;
     const f3 T = pos - v1;
-    u = dot(T, P) * invdet;
-    if (u < 0.0f || u > 1.0f) return false;
+    const float du = dot(T, P);
+    // Early rejects, taken only where the test below rejects too, so that the
+    // division is paid only by likely hits: du < -1e-30 det makes
+    // u = du * (1/det) <= -1e-30 (negative, no underflow to -0 since
+    // det >= Epsilon); du > 1.000001 det makes u > 1 after both roundings;
+    // likewise for v < 0 and u + v > 1 (margin 1e-5 covers three roundings).
+    if (du < -1e-30f * det || du > 1.000001f * det) return false;
     const f3 Q = cross(T, e1);
-    v = dot(dir, Q) * invdet;
+    const float dv = dot(dir, Q);
+    if (dv < -1e-30f * det || du + dv > 1.00001f * det) return false;
+    const float invdet = 1.0f / det;
+    u = du * invdet;
+    if (u < 0.0f || u > 1.0f) return false;
+    v = dv * invdet;
     if (v < 0.0f || u + v > 1.0f) return false;
     t = dot(e2, Q) * invdet;
     return true;

@@ -65,6 +65,21 @@ struct StackRef {
 
 __device__ __forceinline__ float sel3(uint32_t a, float x, float y, float z) { return a == 0 ? x : (a == 1 ? y : z); }
 
+// One 32-byte sector of a node record, read by a single 256-bit load
+// (ld.global.nc.v8.f32; records are 128-byte aligned): half as many L1
+// accesses per node as 16-byte loads, and the L1 data pipe is what bounds the
+// traversal.
+struct Sector {
+    float4 a, b;
+};
+__device__ __forceinline__ Sector ld_sector(const float4* __restrict__ p) {
+    Sector s;
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(s.a.x), "=f"(s.a.y), "=f"(s.a.z), "=f"(s.a.w), "=f"(s.b.x), "=f"(s.b.y), "=f"(s.b.z), "=f"(s.b.w)
+        : "l"(p));
+    return s;
+}
+
 // Traversal state of one ray. The heap is implicit, so a pending far child
 // needs no stored index: it is the sibling of the current node's ancestor on
 // the far child's level, ((k+1) >> (lvl - L) ^ 1) - 1 in 0-based heap
@@ -83,15 +98,16 @@ __device__ __forceinline__ void trav_init(TravState& s) {
 
 // Advances to the next node whose slab the ray crosses (slab test of
 // ray.cuh:225-237 with the cumulative range). Returns false when the
-// traversal is exhausted; otherwise q0 holds the node's first record word and
-// nlo/nhi its clipped range.
+// traversal is exhausted; otherwise s0 holds the node's first record sector
+// (words 0 and 1) and nlo/nhi its clipped range.
 __device__ __forceinline__ bool trav_next(TravState& s, const float4* __restrict__ recs, uint32_t nodes, const f3& pos,
-                                          const f3& dir, float best_t, const StackRef& stk, float4& q0, float& nlo,
+                                          const f3& dir, float best_t, const StackRef& stk, Sector& s0, float& nlo,
                                           float& nhi, uint32_t& visits) {
     for (;;) {
         if (s.k < nodes) {
             ++visits;
-            q0 = __ldg(recs + (size_t)s.k * kRecStride);
+            s0 = ld_sector(recs + (size_t)s.k * kRecStride);
+            const float4& q0 = s0.a;
             const float p = sel3(s.a, pos.x, pos.y, pos.z);
             const float d = sel3(s.a, dir.x, dir.y, dir.z);
             const float d0 = (q0.x - p) / d;
@@ -114,22 +130,22 @@ __device__ __forceinline__ bool trav_next(TravState& s, const float4* __restrict
 // Descends from the current node (whose slab was crossed) to its near child,
 // leaving the far child pending on the child level. With kBoxes, children
 // whose subtree box the ray misses within (0, tlimit] are dropped.
+// q5 is record word 5 (first child's box lo.xyz, hi.x), already read with
+// the triangles; words 6 and 7 are read here.
 template <bool kBoxes = true>
-__device__ __forceinline__ void trav_descend(TravState& s, const float4* __restrict__ recs, const f3& pos,
-                                             const f3& dir, const f3& inv, float tlimit, uint32_t nodes,
-                                             const StackRef& stk, float nlo, float nhi) {
+__device__ __forceinline__ void trav_descend(TravState& s, const float4* __restrict__ recs, const float4& q5,
+                                             const f3& pos, const f3& dir, const f3& inv, float tlimit,
+                                             uint32_t nodes, const StackRef& stk, float nlo, float nhi) {
     const uint32_t na = s.a == 2 ? 0 : s.a + 1;
     const bool neg = sel3(na, dir.x, dir.y, dir.z) < 0.0f;
     const uint32_t c1 = 2 * s.k + 1;
     bool h1 = c1 < nodes, h2 = c1 + 1 < nodes;
     if (kBoxes && h1) {
-        const float4* r = recs + (size_t)s.k * kRecStride + 5;
-        const float4 b0 = __ldg(r), b1 = __ldg(r + 1);
-        h1 = box_hit(b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, pos, inv, tlimit);
-        if (h2) {
-            const float4 b2 = __ldg(r + 2);
-            h2 = box_hit(b1.z, b1.w, b2.x, b2.y, b2.z, b2.w, pos, inv, tlimit);
-        }
+        const Sector s3 = ld_sector(recs + (size_t)s.k * kRecStride + 6);
+        const float4& b1 = s3.a;
+        const float4& b2 = s3.b;
+        h1 = box_hit(q5.x, q5.y, q5.z, q5.w, b1.x, b1.y, pos, inv, tlimit);
+        if (h2) h2 = box_hit(b1.z, b1.w, b2.x, b2.y, b2.z, b2.w, pos, inv, tlimit);
     }
     const bool near_ok = neg ? h2 : h1;
     const bool far_ok = neg ? h1 : h2;
@@ -149,14 +165,20 @@ __device__ __forceinline__ void trav_descend(TravState& s, const float4* __restr
 // Tests the two triangles of node k (Moller-Trumbore with culling,
 // ray.cuh:198-223) in order. Closest hit: ties in t go to the lower original
 // prim id. Any hit: returns true on the first hit with Epsilon < t < best_t.
+// s0: record sector 0 (from trav_next); sectors 1 and 2 are read here, and
+// word 5 (the tail of sector 2) is handed back in q5 for trav_descend.
 template <bool kAny>
-__device__ __forceinline__ bool node_triangles(const float4* __restrict__ recs, uint32_t k, const float4& q0,
+__device__ __forceinline__ bool node_triangles(const float4* __restrict__ recs, uint32_t k, const Sector& s0,
                                                const uint32_t* __restrict__ perm, const f3& pos, const f3& dir,
-                                               float& best_t, float& bu, float& bv, uint32_t& best) {
-    const float4 q1 = __ldg(recs + (size_t)k * kRecStride + 1);
-    const float4 q2 = __ldg(recs + (size_t)k * kRecStride + 2);
-    const float4 q3 = __ldg(recs + (size_t)k * kRecStride + 3);
-    const float4 q4 = __ldg(recs + (size_t)k * kRecStride + 4);
+                                               float& best_t, float& bu, float& bv, uint32_t& best, float4& q5) {
+    const Sector s1 = ld_sector(recs + (size_t)k * kRecStride + 2);
+    const Sector s2 = ld_sector(recs + (size_t)k * kRecStride + 4);
+    const float4& q0 = s0.a;
+    const float4& q1 = s0.b;
+    const float4& q2 = s1.a;
+    const float4& q3 = s1.b;
+    const float4& q4 = s2.a;
+    q5 = s2.b;
     float u, v, t;
     if (intersect_tri(pos, dir, mk3(q0.z, q0.w, q1.x), mk3(q1.y, q1.z, q1.w), mk3(q2.x, q2.y, q2.z), u, v, t) &&
         t > kEpsilon) {
@@ -194,11 +216,12 @@ __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ recs, ui
     const f3 inv = box_inv(dir);
     TravState s;
     trav_init(s);
-    float4 q0;
+    Sector s0;
+    float4 q5;
     float nlo, nhi;
-    while (trav_next(s, recs, nodes, pos, dir, best_t, stk, q0, nlo, nhi, visits)) {
-        if (node_triangles<kAny>(recs, s.k, q0, perm, pos, dir, best_t, bu, bv, best)) return best;
-        trav_descend(s, recs, pos, dir, inv, best_t, nodes, stk, nlo, nhi);
+    while (trav_next(s, recs, nodes, pos, dir, best_t, stk, s0, nlo, nhi, visits)) {
+        if (node_triangles<kAny>(recs, s.k, s0, perm, pos, dir, best_t, bu, bv, best, q5)) return best;
+        trav_descend(s, recs, q5, pos, dir, inv, best_t, nodes, stk, nlo, nhi);
     }
     return best;
 }

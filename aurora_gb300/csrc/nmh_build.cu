@@ -841,7 +841,7 @@ aur_status nmh_build_noalloc_impl(const float* V, uint32_t count, cudaStream_t s
     AUR_CHECK(count <= kNoAllocMaxTriangles, AUR_ERR_INVALID,
               "aur_nmh_build_noalloc: %u triangles exceed this entry point's fixed scratch for %u triangles; "
               "use aur_nmh_build for larger soups", count, kNoAllocMaxTriangles);
-    AUR_CHECK(((uintptr_t)recs & 15) == 0, AUR_ERR_INVALID, "aur_nmh_build_noalloc: node_records must be 16-byte aligned");
+    AUR_CHECK(((uintptr_t)recs & 31) == 0, AUR_ERR_INVALID, "aur_nmh_build_noalloc: node_records must be 32-byte aligned");
     const uint32_t N = count + (count & 1u);
     const uint32_t n = N / 2;
     const uint32_t levels = n ? log2i(n) + 1 : 0;

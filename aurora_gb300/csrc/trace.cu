@@ -77,16 +77,17 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restric
             best = kNoPrim;
             trav_init(s);
         }
-        float4 q0;
+        Sector s0;
+        float4 q5;
         float nlo, nhi;
         bool done;
-        if (trav_next(s, recs, nodes, pos, dir, best_t, stk, q0, nlo, nhi, visits)) {
+        if (trav_next(s, recs, nodes, pos, dir, best_t, stk, s0, nlo, nhi, visits)) {
             if (kCount) {
                 ++crossings;
                 inner += 2 * s.k + 1 < nodes;
             }
-            done = node_triangles<kAny>(recs, s.k, q0, perm, pos, dir, best_t, bu, bv, best);
-            if (!done) trav_descend<kBoxes>(s, recs, pos, dir, inv, best_t, nodes, stk, nlo, nhi);
+            done = node_triangles<kAny>(recs, s.k, s0, perm, pos, dir, best_t, bu, bv, best, q5);
+            if (!done) trav_descend<kBoxes>(s, recs, q5, pos, dir, inv, best_t, nodes, stk, nlo, nhi);
         } else {
             done = true;
         }

@@ -226,11 +226,12 @@ __global__ void k_wf_extend(WfArgs a) {
             best_t = kInfinity; bu = bv = 0.0f; best = kNoPrim;
             trav_init(s);
         }
-        float4 q0;
+        Sector s0;
+        float4 q5;
         float nlo, nhi;
-        if (trav_next(s, recs, nodes, pos, dir, best_t, stk, q0, nlo, nhi, visits)) {
-            node_triangles<false>(recs, s.k, q0, perm, pos, dir, best_t, bu, bv, best);
-            trav_descend(s, recs, pos, dir, inv, best_t, nodes, stk, nlo, nhi);
+        if (trav_next(s, recs, nodes, pos, dir, best_t, stk, s0, nlo, nhi, visits)) {
+            node_triangles<false>(recs, s.k, s0, perm, pos, dir, best_t, bu, bv, best, q5);
+            trav_descend(s, recs, q5, pos, dir, inv, best_t, nodes, stk, nlo, nhi);
         } else {
             a.hit[slot] = make_float4(best_t, bu, bv, __uint_as_float(best));
             slot = 0xFFFFFFFFu;
@@ -353,12 +354,13 @@ __global__ void k_wf_shadow(WfArgs a) {
             best = kNoPrim;
             trav_init(s);
         }
-        float4 q0;
+        Sector s0;
+        float4 q5;
         float nlo, nhi;
         bool done;
-        if (trav_next(s, recs, nodes, pos, dir, tmax, stk, q0, nlo, nhi, visits)) {
-            done = node_triangles<true>(recs, s.k, q0, perm, pos, dir, tmax, bu, bv, best);
-            if (!done) trav_descend(s, recs, pos, dir, inv, tmax, nodes, stk, nlo, nhi);
+        if (trav_next(s, recs, nodes, pos, dir, tmax, stk, s0, nlo, nhi, visits)) {
+            done = node_triangles<true>(recs, s.k, s0, perm, pos, dir, tmax, bu, bv, best, q5);
+            if (!done) trav_descend(s, recs, q5, pos, dir, inv, tmax, nodes, stk, nlo, nhi);
         } else {
             done = true;
         }

@@ -246,9 +246,14 @@ def cpu_baseline(verts, perm, rays, sample, seed=7):
 
 def bench_batched(ctx, n_scenes=64, size=512, spp=64, depth=6, samples=8):
     """Batched workload: 64 sphere scenes (1k-500k triangles each), 512x512,
-    64 spp, depth 6, path mode; samples [0, 8) of the 64 are rendered by the
-    plain renderer (one aur_render per scene) and by the wavefront batch (one
-    graph launch), timed with CUDA events; the frames must be identical."""
+    64 spp, depth 6, path mode; samples [0, 8) of the 64 are rendered three
+    ways, timed with CUDA events, and the frames must be identical:
+      * the plain path as the reference structures it
+        (render/monteCarloRaytracer.cpp:81-120): per scene and sample,
+        generate rays, the megakernel over 65,536-ray tiles, draw pixels;
+      * this library's fused plain renderer (one aur_render per scene, all
+        samples of a scene in one launch);
+      * the wavefront batch (one graph launch for all scenes)."""
     import torch
     from aurora_gb300 import api, scenes, types as T
     sds = [scenes.sphere_scene(i) for i in range(n_scenes)]
@@ -274,6 +279,30 @@ def bench_batched(ctx, n_scenes=64, size=512, spp=64, depth=6, samples=8):
     torch.cuda.synchronize()
     plain_ms = e0.elapsed_time(e1)
     plain_img = [f.clone() for f in frames]
+
+    tile = 65536
+    rays_b = torch.empty((size * size * 9,), dtype=torch.float32, device="cuda")     # aur_path_ray, 36 B
+    hits_b = torch.empty((size * size * 12,), dtype=torch.float32, device="cuda")    # aur_hitpoint, 48 B
+
+    def plain_tiles(k):
+        for sc, p, f in zip(scs[:k], prm[:k], frames[:k]):
+            for smp in range(samples):
+                api.generate_rays(ctx, size, size, smp, spp, sc.data.camera, rays_b, hits_b)
+                for off in range(0, size * size, tile):
+                    api.raytrace_monte_carlo(ctx, sc, p, smp, off, min(tile, size * size - off), rays_b, hits_b)
+                api.draw_pixels(ctx, size, size, 1.0 / spp, hits_b, f)
+
+    plain_tiles(1)                            # warm-up
+    torch.cuda.synchronize()
+    for f in frames:
+        f.zero_()
+    e0.record(stream)
+    plain_tiles(n_scenes)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    tiles_ms = e0.elapsed_time(e1)
+    tiles_same = all(torch.equal(a, b) for a, b in zip(frames, plain_img))
+    del rays_b, hits_b
     t0 = time.perf_counter()
     tuning, tune_ms = api.autotune(ctx, scs, prm)
     tune_s = time.perf_counter() - t0
@@ -294,9 +323,12 @@ def bench_batched(ctx, n_scenes=64, size=512, spp=64, depth=6, samples=8):
     return {"workload": "%d sphere scenes (%d-%d triangles, %d total), %dx%d, %d spp, depth %d, path mode; "
                         "samples [0, %d) timed" % (n_scenes, min(tris), max(tris), sum(tris), size, size, spp, depth,
                                                    samples),
+            "plain_reference_loop_samples_per_s": n_samples / (tiles_ms * 1e-3), "plain_reference_loop_ms": tiles_ms,
+            "plain_reference_loop_launches": n_scenes * samples * (2 + (size * size + tile - 1) // tile),
             "plain_samples_per_s": n_samples / (plain_ms * 1e-3), "plain_ms": plain_ms,
             "wavefront_samples_per_s": n_samples / (wf_ms * 1e-3), "wavefront_ms": wf_ms,
-            "speedup": plain_ms / wf_ms, "frames_identical": bool(same), "equal_rmse": bool(same),
+            "speedup_vs_reference_loop": tiles_ms / wf_ms, "speedup": plain_ms / wf_ms,
+            "frames_identical": bool(same and tiles_same), "equal_rmse": bool(same and tiles_same),
             "wavefront_graph_launches": 1, "wavefront_iterations": iters,
             "wavefront_rays": {"closest": ext, "shadow": shadow,
                                "mrays_per_s": (ext + shadow) / (wf_ms * 1e-3) / 1e6},

@@ -222,7 +222,8 @@ aur_status aur_nmh_perm_device(const aur_nmh* nmh, const uint32_t** perm);
  * and only hands out fixed buffers, or a render loop that must not pay for
  * cudaMalloc / cudaFree, which can synchronize the whole device.
  * Same result as aur_nmh_build, written into caller-owned device buffers:
- *   node_records: ((count+1)/2) * 32 floats, 16-byte aligned (traversal records)
+ *   node_records: ((count+1)/2) * 32 floats, 32-byte aligned (traversal records,
+ *                 read with 256-bit loads)
  *   perm:         count + (count & 1) uint32 (NMH position -> original prim id)
  *   nmh_vertices: (count + (count & 1)) * 9 floats (NMH-ordered soup)
  *   levels:       host, nullable; receives log2i(count/2)+1
