@@ -91,7 +91,7 @@ struct WfArgs {
     uint32_t* free_list;
     float4* sh_o;   // shadow ray origin, w = tmax
     float4* sh_d;   // shadow ray direction, w = (slot << 5 | light slot) bits
-    float4* out;    // per wave: nb * P_tot sample colours
+    float4* out;    // per wave: nb * P_tot sample colours, indexed by item
     cudaGraphConditionalHandle h_inner, h_outer;
     uint32_t in_graph;   // 1 when launched by the graph: only then may kernels set its conditionals
 };
@@ -131,6 +131,23 @@ __device__ __forceinline__ uint32_t find_scene(const uint32_t* pix_off, uint32_t
 __device__ __forceinline__ uint32_t grid_threads() { return gridDim.x * blockDim.x; }
 __device__ __forceinline__ uint32_t global_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
 
+// Work items of a wave are numbered scene-major: scene s owns items
+// [nb * pix_off[s], nb * pix_off[s + 1]), sample b of its local pixel lp is
+// item nb * pix_off[s] + b * (width * height) + lp. The paths in flight then
+// come from a few scenes at a time, whose node records stay in L2, instead of
+// the same sample of every scene.
+struct ItemRef {
+    uint32_t b, lp;
+};
+__device__ __forceinline__ ItemRef decode_item(uint32_t item, uint32_t nb, const WfScene& sc) {
+    const uint32_t local = item - nb * sc.pix_off;
+    const uint32_t npix = sc.width * sc.height;
+    ItemRef r;
+    r.b = local / npix;
+    r.lp = local - r.b * npix;
+    return r;
+}
+
 __device__ __forceinline__ void finish_path(const WfArgs& a, uint32_t slot, uint32_t item, const float4& c) {
     a.out[item] = c;
     a.free_list[agg_inc(&a.ctl->free_count)] = slot;
@@ -166,11 +183,11 @@ __global__ void k_wf_generate(WfArgs a) {
     for (uint32_t i = global_tid(); i < n_new; i += grid_threads()) {
         const uint32_t slot = a.free_list[c->free_count - 1 - i];
         const uint32_t item = c->items_issued + i;
-        const uint32_t b = item / a.P_tot, gp = item - b * a.P_tot;
-        const uint32_t s = find_scene(a.pix_off, a.num_scenes, gp);
+        const uint32_t s = find_scene(a.pix_off, a.num_scenes, item / c->nb);
         const WfScene& sc = a.scenes[s];
-        const uint32_t lp = gp - sc.pix_off;
-        const PathRay r = camera_ray(sc.cam, sc.width, sc.height, lp % sc.width, lp / sc.width, c->s0 + b, a.spp);
+        const ItemRef ir = decode_item(item, c->nb, sc);
+        const uint32_t lp = ir.lp;
+        const PathRay r = camera_ray(sc.cam, sc.width, sc.height, lp % sc.width, lp / sc.width, c->s0 + ir.b, a.spp);
         a.o[slot] = make_float4(r.pos.x, r.pos.y, r.pos.z, 0.0f);
         a.d[slot] = make_float4(r.dir.x, r.dir.y, r.dir.z, 0.0f);
         a.thr[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
@@ -255,9 +272,8 @@ __global__ void k_wf_shade(WfArgs a) {
             continue;
         }
         const WfScene& sc = a.scenes[m.w];
-        const uint32_t item = m.x;
-        const uint32_t b = item / a.P_tot, gp = item - b * a.P_tot;
-        const uint32_t pix = gp - sc.pix_off, sample = c->s0 + b, rix = m.z;
+        const ItemRef ir = decode_item(m.x, c->nb, sc);
+        const uint32_t pix = ir.lp, sample = c->s0 + ir.b, rix = m.z;
         const float4 o4 = a.o[slot], d4 = a.d[slot];
         const f3 pos = mk3(o4.x, o4.y, o4.z), dir = mk3(d4.x, d4.y, d4.z);
         const f3 position = pos + (dir * h.x);
@@ -451,10 +467,13 @@ __global__ void k_wf_accumulate(WfArgs a) {
     const uint32_t nb = c->nb;
     for (uint32_t gp = global_tid(); gp < a.P_tot; gp += grid_threads()) {
         const uint32_t s = find_scene(a.pix_off, a.num_scenes, gp);
-        float4* acc = a.accum[s] + (gp - a.pix_off[s]);
+        const uint32_t lp = gp - a.pix_off[s];
+        const uint32_t npix = a.pix_off[s + 1] - a.pix_off[s];
+        const float4* out = a.out + (size_t)nb * a.pix_off[s] + lp;
+        float4* acc = a.accum[s] + lp;
         float4 v = *acc;
         for (uint32_t b = 0; b < nb; ++b) {
-            const float4 cv = a.out[(size_t)b * a.P_tot + gp];
+            const float4 cv = out[(size_t)b * npix];
             if (cv.w != 0.0f) {
                 v.x += cv.x * weight;
                 v.y += cv.y * weight;
