@@ -57,6 +57,8 @@ SIGNATURES = {
     "aur_scene_nmh": ([P, P], ctypes.c_int),
     "aur_scene_set_shaders": ([P, P, P, U32], ctypes.c_int),
     "aur_scene_set_lights": ([P, P, P, U32], ctypes.c_int),
+    "aur_scene_set_textures": ([P, P, P, P, U32], ctypes.c_int),
+    "aur_scene_texfetch": ([P, P, U32, P, U32, P], ctypes.c_int),
     "aur_camera_make": None,  # struct-by-value arguments; not bound
     "aur_render": ([P, P, P, P, P], ctypes.c_int),
     "aur_generate_rays": ([P, U32, U32, U32, U32, P, P, P], ctypes.c_int),
@@ -262,6 +264,27 @@ class Scene:
     def set_shaders(self, shaders):
         shaders = np.ascontiguousarray(shaders, T.shader_dtype)
         check(lib().aur_scene_set_shaders(self.ctx.handle, self.handle, _ptr(shaders), shaders.shape[0]))
+
+    def set_textures(self, texcoords, textures):
+        """texcoords: (count, 6) float32 in the original triangle order;
+        textures: list of (height, width, 4) uint8 RGBA images."""
+        tc = np.ascontiguousarray(texcoords, np.float32).reshape(-1, 6)
+        imgs = [np.ascontiguousarray(t, np.uint8) for t in textures]
+        table = (T.texture_ctype * max(1, len(imgs)))()
+        for i, im in enumerate(imgs):
+            table[i].width, table[i].height = im.shape[1], im.shape[0]
+            table[i].rgba = im.ctypes.data
+        check(lib().aur_scene_set_textures(self.ctx.handle, self.handle, _ptr(tc), P(ctypes.addressof(table)),
+                                           len(imgs)))
+        self._textures = imgs
+
+    def texfetch(self, texture, uv_dev):
+        """RGB of texture `texture` (1-based) at n device (u, v) pairs."""
+        import torch
+        out = torch.empty((uv_dev.shape[0], 3), dtype=torch.float32, device="cuda")
+        check(lib().aur_scene_texfetch(self.ctx.handle, self.handle, texture, _ptr(uv_dev.contiguous()),
+                                       uv_dev.shape[0], _ptr(out)))
+        return out
 
     def set_lights(self, lights):
         lights = np.ascontiguousarray(lights, T.light_dtype)

@@ -6,6 +6,7 @@
 #include <cstring>
 #include <vector>
 
+#include "aur_integrate.cuh"
 #include "aur_internal.h"
 #include "aur_math.cuh"
 
@@ -57,6 +58,26 @@ __global__ void k_apply(const uint32_t* __restrict__ perm, uint32_t N, uint32_t 
     uint32_t p = perm[i];
     if (p >= count_in) p = count_in - 1;
     for (uint32_t w = 0; w < words; ++w) dst[(size_t)i * words + w] = src[(size_t)p * words + w];
+}
+
+void free_textures(aur_scene* sc) {
+    cudaFree(sc->texels);
+    cudaFree(sc->tex_info);
+    cudaFree(sc->texcoords);
+    sc->texels = nullptr;
+    sc->tex_info = nullptr;
+    sc->texcoords = nullptr;
+    sc->num_textures = 0;
+}
+
+__global__ void k_texfetch(SceneView sv, uint32_t texture, const float* __restrict__ uv, uint32_t n,
+                           float* __restrict__ rgb) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const f3 c = texfetch(sv, texture - 1, uv[2 * i], uv[2 * i + 1]);
+    rgb[3 * i] = c.x;
+    rgb[3 * i + 1] = c.y;
+    rgb[3 * i + 2] = c.z;
 }
 
 }  // namespace
@@ -284,8 +305,6 @@ static aur_status validate_materials(const aur_shader* shaders, uint32_t ns, con
     AUR_CHECK(ns >= 1 && shaders, AUR_ERR_INVALID, "scene: at least one shader is required (id 0 selects shader 0)");
     AUR_CHECK(nl == 0 || lights, AUR_ERR_INVALID, "scene: null light table");
     for (uint32_t i = 0; i < ns; ++i) {
-        AUR_CHECK(shaders[i].texture == 0, AUR_ERR_UNSUPPORTED, "scene: shader %u uses a texture; textures are out of scope",
-                  i);
         AUR_CHECK(shaders[i].type == AUR_SHADER_LAMBERT || shaders[i].type == AUR_SHADER_PHONG, AUR_ERR_INVALID,
                   "scene: shader %u has unknown type %d", i, shaders[i].type);
     }
@@ -296,6 +315,13 @@ static aur_status validate_materials(const aur_shader* shaders, uint32_t ns, con
                   "scene: area light %u needs samples >= 1", i);
     }
     return AUR_OK;
+}
+
+static uint32_t max_texture_id(const aur_shader* shaders, uint32_t n) {
+    uint32_t m = 0;
+    for (uint32_t i = 0; i < n; ++i)
+        if (shaders[i].texture <= AUR_MAX_TEXTURES && shaders[i].texture > m) m = shaders[i].texture;
+    return m;
 }
 
 aur_status aur_scene_create(aur_ctx* ctx, const float* vertices, const float* normals, const uint16_t* shader_ids,
@@ -368,6 +394,7 @@ aur_status aur_scene_create(aur_ctx* ctx, const float* vertices, const float* no
     }
     sc->num_shaders = num_shaders;
     sc->num_lights = num_lights;
+    sc->max_texture = max_texture_id(shaders, num_shaders);
     for (uint32_t i = 0; i < num_shaders; ++i)
         sc->has_specular |= shaders[i].reflectivity > 0.0f || shaders[i].translucence > 0.0f;
     cudaMemcpyAsync(sc->shaders, shaders, sizeof(aur_shader) * num_shaders, cudaMemcpyHostToDevice, s);
@@ -385,6 +412,7 @@ aur_status aur_scene_destroy(aur_scene* sc) {
     cudaFree(sc->shader_ids);
     cudaFree(sc->shaders);
     cudaFree(sc->lights);
+    free_textures(sc);
     aur_nmh_destroy(sc->nmh);
     delete sc;
     return AUR_OK;
@@ -408,6 +436,80 @@ aur_status aur_scene_set_shaders(aur_ctx* ctx, aur_scene* sc, const aur_shader* 
     sc->has_specular = false;
     for (uint32_t i = 0; i < n; ++i)
         sc->has_specular |= shaders[i].reflectivity > 0.0f || shaders[i].translucence > 0.0f;
+    sc->max_texture = max_texture_id(shaders, n);
+    return AUR_OK;
+}
+
+aur_status aur_scene_set_textures(aur_ctx* ctx, aur_scene* sc, const float* texcoords, const aur_texture* textures,
+                                  uint32_t n) {
+    clear_error();
+    AUR_CHECK(ctx && sc, AUR_ERR_INVALID, "aur_scene_set_textures: null argument");
+    AUR_CHECK(n <= AUR_MAX_TEXTURES, AUR_ERR_INVALID, "aur_scene_set_textures: %u textures, at most %d", n,
+              AUR_MAX_TEXTURES);
+    AUR_CHECK(n == 0 || textures, AUR_ERR_INVALID, "aur_scene_set_textures: null texture table");
+    const uint32_t count = sc->nmh->input_count;
+    AUR_CHECK(count == 0 || texcoords, AUR_ERR_INVALID, "aur_scene_set_textures: null texcoords");
+    for (uint32_t i = 0; i < n; ++i)
+        AUR_CHECK(textures[i].width >= 1 && textures[i].height >= 1 && textures[i].rgba, AUR_ERR_INVALID,
+                  "aur_scene_set_textures: texture %u is empty", i);
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    free_textures(sc);
+    cudaStream_t s = ctx->stream;
+    const uint32_t N = sc->nmh->count;
+    if (N) {
+        float* staged = nullptr;
+        if (cudaMalloc(&sc->texcoords, (size_t)N * 24) != cudaSuccess ||
+            cudaMallocAsync(&staged, (size_t)count * 24, s) != cudaSuccess) {
+            cudaGetLastError();
+            free_textures(sc);
+            return fail(AUR_ERR_OOM, "aur_scene_set_textures: out of device memory");
+        }
+        cudaMemcpyAsync(staged, texcoords, (size_t)count * 24, cudaMemcpyHostToDevice, s);
+        // applyIndices for the texcoords (rebuilder.cu:217-245)
+        k_apply<<<(N + 255) / 256, 256, 0, s>>>(sc->nmh->perm, N, count, (const uint16_t*)staged, 12,
+                                               (uint16_t*)sc->texcoords);
+        cudaFreeAsync(staged, s);
+    }
+    // every texture's texels in one buffer; tex_info[t] = (first texel, width, height)
+    uint4 info[AUR_MAX_TEXTURES];
+    std::memset(info, 0, sizeof(info));
+    size_t texels = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        info[i] = make_uint4((uint32_t)texels, textures[i].width, textures[i].height, 0u);
+        texels += (size_t)textures[i].width * textures[i].height;
+        AUR_CHECK(texels < (1ull << 32), AUR_ERR_INVALID, "aur_scene_set_textures: more than 2^32 texels");
+    }
+    if (cudaMalloc(&sc->tex_info, sizeof(info)) != cudaSuccess ||
+        (texels && cudaMalloc(&sc->texels, texels * sizeof(uchar4)) != cudaSuccess)) {
+        cudaGetLastError();
+        free_textures(sc);
+        return fail(AUR_ERR_OOM, "aur_scene_set_textures: out of device memory");
+    }
+    cudaMemcpyAsync(sc->tex_info, info, sizeof(info), cudaMemcpyHostToDevice, s);
+    for (uint32_t i = 0; i < n; ++i)
+        cudaMemcpyAsync(sc->texels + info[i].x, textures[i].rgba,
+                        (size_t)textures[i].width * textures[i].height * sizeof(uchar4), cudaMemcpyHostToDevice, s);
+    sc->num_textures = n;
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        free_textures(sc);
+        return cuda_fail(e, "aur_scene_set_textures", __FILE__, __LINE__);
+    }
+    return AUR_OK;
+}
+
+aur_status aur_scene_texfetch(aur_ctx* ctx, const aur_scene* sc, uint32_t texture, const float* uv, uint32_t n,
+                              float* rgb) {
+    clear_error();
+    AUR_CHECK(ctx && sc, AUR_ERR_INVALID, "aur_scene_texfetch: null argument");
+    AUR_CHECK(n == 0 || (uv && rgb), AUR_ERR_INVALID, "aur_scene_texfetch: null buffer");
+    AUR_CHECK(texture >= 1 && (texture > AUR_MAX_TEXTURES || texture <= sc->num_textures), AUR_ERR_INVALID,
+              "aur_scene_texfetch: texture %u, scene has %u", texture, sc->num_textures);
+    if (n == 0) return AUR_OK;
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    k_texfetch<<<(n + 255) / 256, 256, 0, ctx->stream>>>(scene_view(sc), texture, uv, n, rgb);
+    AUR_CUDA(cudaGetLastError());
     return AUR_OK;
 }
 

@@ -59,7 +59,7 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
         const uint32_t sid = sc.sids[tri];
         const uint32_t si = sid > 0 ? sid - 1 : 0;
         const aur_shader* sh = sc.shaders + si;
-        const Bsdf b = get_bsdf(sc, from(sh->diffuse_color), sh->diffuse, tri, u, v);
+        const Bsdf b = get_bsdf(sc, sh, tri, u, v);
         const f3 f = bsdf_f(b);
         const f3 thr = ray.thr;
         f3 Li = from(sh->emission_color);
@@ -156,7 +156,7 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
         // color1 = diffuse_color * diffuse. Lanes that hit the same shader
         // (large triangles are hit by most of a warp) are summed first, so a
         // warp issues one atomic per shader instead of one per lane.
-        const f3 gd = g * dc * sh->diffuse;
+        const f3 gd = sh->texture > 0 ? mk3(0.0f) : g * dc * sh->diffuse;   // textured: colour is not diffuse_color
         {
             namespace cg = cooperative_groups;
             const cg::coalesced_group active = cg::coalesced_threads();
@@ -256,7 +256,6 @@ inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b
 
 }  // namespace
 
-SceneView scene_view(const aur_scene* sc);
 
 }  // namespace aur
 
@@ -271,6 +270,7 @@ aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_ca
     AUR_CHECK(ctx && scene && camera && d_image && d_diffuse && (d_light_color || scene->num_lights == 0),
               AUR_ERR_INVALID, "aur_render_adjoint: null argument");
     aur_status st = check_params(params);
+    if (st == AUR_OK) st = check_scene_textures(scene);
     if (st != AUR_OK) return st;
     AUR_CUDA(cudaSetDevice(ctx->device));
     {

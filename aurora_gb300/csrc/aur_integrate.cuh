@@ -23,7 +23,51 @@ struct SceneView {
     const aur_shader* shaders;
     const aur_light* lights;
     uint32_t num_lights;
+    const float* texcoords;    // NMH order, 6 floats per triangle (null without textures)
+    const uchar4* texels;      // RGBA8 texels of all textures
+    const uint4* tex_info;     // per texture: first texel, width, height
 };
+
+SceneView scene_view(const aur_scene* sc);
+
+// Texture units of the reference (texunit.cuh:11-18): normalised
+// coordinates, wrap addressing, linear filtering, RGBA8 read as byte / 255.
+// Filtered here in software, by the formula the CUDA C++ Programming Guide
+// gives for tex2D linear filtering (appendix "Texture Fetching"): wrap
+// replaces u by frac(u); xB = frac(u) * width - 0.5; texels floor(xB) and
+// floor(xB) + 1 (wrapped); weight alpha = frac(xB) rounded to 8 fractional
+// bits (to nearest, as a probe of the hardware shows); result
+// (1-a)(1-b) T00 + a(1-b) T10 + (1-a) b T01 + a b T11 in float. The hardware
+// blends at a precision the guide leaves open (within 1.3e-3 of this on
+// GB300); the software form is exact and the same on every GPU and the CPU.
+__device__ __forceinline__ float tex_weight(float f) { return floorf(f * 256.0f + 0.5f) * (1.0f / 256.0f); }
+
+__device__ __forceinline__ f3 texel(const uchar4* __restrict__ t, uint32_t w, uint32_t i, uint32_t j) {
+    const uchar4 q = __ldg(t + (size_t)j * w + i);
+    return mk3((float)q.x / 255.0f, (float)q.y / 255.0f, (float)q.z / 255.0f);
+}
+
+// texfetch (kernels/lib/texunit.cuh:54-94); units past the 32 the reference
+// binds return white.
+__device__ __forceinline__ f3 texfetch(const SceneView& sc, uint32_t id, float u, float v) {
+    if (id >= (uint32_t)AUR_MAX_TEXTURES) return mk3(1.0f, 1.0f, 1.0f);
+    const uint4 ti = __ldg(sc.tex_info + id);
+    const uchar4* t = sc.texels + ti.x;
+    const uint32_t W = ti.y, H = ti.z;
+    if (W == 0 || H == 0) return mk3(1.0f, 1.0f, 1.0f);   // no such texture (render entry points reject this)
+    float xu = u - floorf(u), xv = v - floorf(v);
+    if (!(xu >= 0.0f && xu <= 1.0f)) xu = 0.0f;   // NaN / inf coordinates
+    if (!(xv >= 0.0f && xv <= 1.0f)) xv = 0.0f;
+    const float xb = xu * (float)W - 0.5f, yb = xv * (float)H - 0.5f;
+    const float fi = floorf(xb), fj = floorf(yb);
+    const float a = tex_weight(xb - fi), b = tex_weight(yb - fj);
+    const uint32_t i0 = fi < 0.0f ? W - 1 : min((uint32_t)fi, W - 1);
+    const uint32_t j0 = fj < 0.0f ? H - 1 : min((uint32_t)fj, H - 1);
+    const uint32_t i1 = i0 + 1 == W ? 0 : i0 + 1, j1 = j0 + 1 == H ? 0 : j0 + 1;
+    const f3 t00 = texel(t, W, i0, j0), t10 = texel(t, W, i1, j0), t01 = texel(t, W, i0, j1),
+             t11 = texel(t, W, i1, j1);
+    return t00 * ((1.0f - a) * (1.0f - b)) + t10 * (a * (1.0f - b)) + t01 * ((1.0f - a) * b) + t11 * (a * b);
+}
 
 struct PathRay {
     f3 pos, dir;
@@ -43,8 +87,10 @@ __device__ __forceinline__ void vertex_tb(const f3& n, f3& t, f3& b) {
 }
 
 // getBasisVectors + Shader::getBSDF (common.cuh:314-327, shader.cuh:243-262)
-__device__ __forceinline__ Bsdf get_bsdf(const SceneView& sc, const f3& diffuse_color, float diffuse, uint32_t tri,
-                                         float u, float v) {
+// Shader::getBSDF (kernels/lib/shader.cuh) with the texture branch of
+// raytrace() (monteCarloRaytracer.cu:37-40): a textured shader's colour is
+// texfetch(texture - 1, uv) * diffuse, uv from getTexCoord (common.cuh:45-51).
+__device__ __forceinline__ Bsdf get_bsdf(const SceneView& sc, const aur_shader* sh, uint32_t tri, float u, float v) {
     const float* nv = sc.normals + (size_t)tri * 9;
     const f3 n1 = mk3(nv[0], nv[1], nv[2]), n2 = mk3(nv[3], nv[4], nv[5]), n3 = mk3(nv[6], nv[7], nv[8]);
     f3 t1, t2, t3, b1, b2, b3;
@@ -55,7 +101,19 @@ __device__ __forceinline__ Bsdf get_bsdf(const SceneView& sc, const f3& diffuse_
     b.N = normalize(bclerp(n1, n2, n3, u, v));
     b.S = normalize(bclerp(t1, t2, t3, u, v));
     b.T = normalize(bclerp(b1, b2, b3, u, v));
-    b.color1 = diffuse_color * diffuse;
+    if (sh->texture > 0) {
+        f3 c = mk3(1.0f, 1.0f, 1.0f);   // units past the 32 bound fetch white
+        if (sh->texture <= (uint32_t)AUR_MAX_TEXTURES) {
+            const float* tc = sc.texcoords + (size_t)tri * 6;
+            const float w = 1.0f - u - v;
+            const float tu = w * tc[0] + u * tc[2] + v * tc[4];
+            const float tv = w * tc[1] + u * tc[3] + v * tc[5];
+            c = texfetch(sc, sh->texture - 1, tu, tv);
+        }
+        b.color1 = c * sh->diffuse;
+    } else {
+        b.color1 = from(sh->diffuse_color) * sh->diffuse;
+    }
     return b;
 }
 
@@ -200,7 +258,7 @@ __device__ __forceinline__ SampleResult integrate(const SceneView& sc, uint32_t 
         const uint32_t sid = sc.sids[tri];
         const aur_shader* sh = sc.shaders + (sid > 0 ? sid - 1 : 0);   // getSafeID (util/array.h:16-17)
         const float refl = sh->reflectivity, trans = sh->translucence;
-        const Bsdf b = get_bsdf(sc, from(sh->diffuse_color), sh->diffuse, tri, u, v);
+        const Bsdf b = get_bsdf(sc, sh, tri, u, v);
         const f3 Li = direct_light(sc, sh, b, position, seed, scene, pixel, sample, rix, stk, visits, err);
         const bool specular = refl > 0.0f || trans > 0.0f;
         if (specular) depth++;
@@ -274,7 +332,7 @@ __device__ __forceinline__ SampleResult integrate_diffuse(const SceneView& sc, u
         res.last_tri = tri; res.last_u = u; res.last_v = v; res.last_pos = position; res.last_wo = wo;
         const uint32_t sid = sc.sids[tri];
         const aur_shader* sh = sc.shaders + (sid > 0 ? sid - 1 : 0);
-        const Bsdf b = get_bsdf(sc, from(sh->diffuse_color), sh->diffuse, tri, u, v);
+        const Bsdf b = get_bsdf(sc, sh, tri, u, v);
         const f3 Li = direct_light(sc, sh, b, position, seed, scene, pixel, sample, rix, stk, visits, err);
         res.color = res.color + Li * thr;
         if (mode != AUR_MODE_PATH) break;

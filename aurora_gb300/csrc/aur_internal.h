@@ -72,12 +72,19 @@ struct aur_scene {
     aur_light* lights = nullptr;
     uint32_t num_lights = 0;
     bool has_specular = false;        // any shader with reflectivity or translucence > 0
+    uint32_t max_texture = 0;         // largest texture id (<= 32) any shader names
+    float* texcoords = nullptr;       // count * 6, NMH order
+    uint32_t num_textures = 0;
+    uchar4* texels = nullptr;         // all textures' RGBA8 texels, row-major, one after another
+    uint4* tex_info = nullptr;        // per texture: first texel, width, height
 };
 
 namespace aur {
 
 aur_status nmh_build_impl(aur_ctx* ctx, const float* vertices, uint32_t count, aur_nmh** out);
 aur_status check_params(const aur_render_params* p);
+// Every texture the scene's shaders name exists (and texcoords were given).
+aur_status check_scene_textures(const aur_scene* sc);
 aur_status launch_trace(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits,
                         uint32_t* occluder, unsigned long long* counters, cudaStream_t stream, bool pruned);
 

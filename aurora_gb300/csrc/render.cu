@@ -146,7 +146,17 @@ SceneView scene_view(const aur_scene* sc) {
     v.shaders = sc->shaders;
     v.lights = sc->lights;
     v.num_lights = sc->num_lights;
+    v.texcoords = sc->texcoords;
+    v.texels = sc->texels;
+    v.tex_info = sc->tex_info;
     return v;
+}
+
+aur_status check_scene_textures(const aur_scene* sc) {
+    AUR_CHECK(sc->max_texture <= sc->num_textures, AUR_ERR_INVALID,
+              "render: a shader uses texture %u but the scene has %u textures (aur_scene_set_textures)",
+              sc->max_texture, sc->num_textures);
+    return AUR_OK;
 }
 
 aur_status check_params(const aur_render_params* p) {
@@ -177,6 +187,7 @@ aur_status aur_render(aur_ctx* ctx, const aur_scene* scene, const aur_camera* ca
     clear_error();
     AUR_CHECK(ctx && scene && camera && accum, AUR_ERR_INVALID, "aur_render: null argument");
     aur_status st = check_params(params);
+    if (st == AUR_OK) st = check_scene_textures(scene);
     if (st != AUR_OK) return st;
     AUR_CUDA(cudaSetDevice(ctx->device));
     const aur_render_params p = *params;
@@ -224,6 +235,8 @@ aur_status aur_raytrace_monte_carlo(aur_ctx* ctx, const aur_scene* scene, const 
     AUR_CHECK(ctx && scene && params && rays && hits, AUR_ERR_INVALID, "aur_raytrace_monte_carlo: null argument");
     AUR_CHECK(params->max_depth <= AUR_MAX_DEPTH && params->mode <= AUR_MODE_PATH, AUR_ERR_INVALID,
               "aur_raytrace_monte_carlo: bad parameters");
+    const aur_status st = check_scene_textures(scene);
+    if (st != AUR_OK) return st;
     AUR_CUDA(cudaSetDevice(ctx->device));
     if (num_rays == 0) return AUR_OK;
     const int cap = stack_cap(scene);

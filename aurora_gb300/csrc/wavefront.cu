@@ -39,6 +39,9 @@ struct WfScene {
     const uint16_t* sids;
     const aur_shader* shaders;
     const aur_light* lights;
+    const float* texcoords;
+    const uchar4* texels;
+    const uint4* tex_info;
     uint32_t nodes;
     uint32_t num_lights;
     uint32_t width, height;
@@ -282,7 +285,10 @@ __global__ void k_wf_shade(WfArgs a) {
         const aur_shader* sh = sc.shaders + (sid > 0 ? sid - 1 : 0);
         SceneView sv;
         sv.normals = sc.normals;
-        const Bsdf bs = get_bsdf(sv, from(sh->diffuse_color), sh->diffuse, tri, h.y, h.z);
+        sv.texcoords = sc.texcoords;
+        sv.texels = sc.texels;
+        sv.tex_info = sc.tex_info;
+        const Bsdf bs = get_bsdf(sv, sh, tri, h.y, h.z);
         const f3 f = bsdf_f(bs);
         a.fsh[slot] = make_float4(f.x, f.y, f.z, 0.0f);
         a.emi[slot] = make_float4(sh->emission_color.x, sh->emission_color.y, sh->emission_color.z, 0.0f);
@@ -603,6 +609,7 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
         const aur_render_params& p = params[i];
         AUR_CHECK(sc, AUR_ERR_INVALID, "aur_batch_create: scene %u is null", i);
         st = check_params(&p);
+        if (st == AUR_OK) st = check_scene_textures(sc);
         if (st != AUR_OK) return st;
         AUR_CHECK(p.spp == p0.spp && p.max_depth == p0.max_depth && p.mode == p0.mode && p.seed == p0.seed &&
                       p.sample_begin == p0.sample_begin && p.sample_end == p0.sample_end,
@@ -630,6 +637,9 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
         w.sids = sc->shader_ids;
         w.shaders = sc->shaders;
         w.lights = sc->lights;
+        w.texcoords = sc->texcoords;
+        w.texels = sc->texels;
+        w.tex_info = sc->tex_info;
         w.nodes = sc->nmh->nodes;
         w.num_lights = sc->num_lights;
         w.width = p.width;

@@ -220,6 +220,52 @@ def cornell():
                      np.stack([cornell_light()]), cornell_camera())
 
 
+def planar_texcoords(vertices, scale=1.0):
+    """Per-triangle texcoords (n, 6) = (u1 v1 u2 v2 u3 v3): each triangle's
+    corners projected onto the two axes orthogonal to its dominant normal
+    axis, times `scale` (values above 1 exercise the wrapping)."""
+    V = np.asarray(vertices, np.float32).reshape(-1, 9)
+    P = np.stack([V[:, 0::3], V[:, 1::3], V[:, 2::3]], -1)         # (n, corner, xyz)
+    n = np.abs(np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0]))
+    dom = np.argmax(n, axis=1)
+    a1 = np.where(dom == 0, 2, 0)
+    a2 = np.where(dom == 1, 2, 1)
+    idx = np.arange(V.shape[0])
+    tc = np.empty((V.shape[0], 6), np.float32)
+    for k in range(3):
+        tc[:, 2 * k] = P[idx, k, a1] * scale
+        tc[:, 2 * k + 1] = P[idx, k, a2] * scale
+    return tc
+
+
+def cornell_textured(seed=0):
+    """The Cornell workload with textures: the floor and back wall use
+    shaders with textures 1 and 2 (random RGBA8 images of odd size, mapped
+    with wrapping), the short box a shader naming texture 40 (beyond the 32
+    units the reference binds: white)."""
+    rng = np.random.default_rng(seed)
+    sd = cornell()
+    tex = [rng.integers(0, 256, size=(9, 13, 4), dtype=np.uint8),
+           rng.integers(0, 256, size=(32, 17, 4), dtype=np.uint8)]
+    sh = np.concatenate([sd.shaders, np.stack([T.lambert((1.0, 1.0, 1.0), diffuse=0.8),
+                                               T.lambert((1.0, 1.0, 1.0), diffuse=0.7),
+                                               T.lambert((1.0, 1.0, 1.0), diffuse=0.6)])])
+    sh["texture"][3], sh["texture"][4], sh["texture"][5] = 1, 2, 40
+    sids = sd.shader_ids.copy()
+    V = sd.vertices
+    ys = V[:, 3:6]
+    zs = V[:, 6:9]
+    floor = np.all(ys == 0.0, axis=1)
+    back = np.all(zs == 0.0, axis=1)
+    sids[floor] = 4
+    sids[back] = 5
+    sids[10:22] = 6                                                    # the short box
+    out = SceneData("cornell_textured", V, sd.normals, sids, sh, sd.lights, sd.camera)
+    out.texcoords = planar_texcoords(V, scale=2.5)
+    out.textures = tex
+    return out
+
+
 def cornell_sphere(seed=0, slices=64, stacks=32):
     """Cornell box + UV sphere; one shader per triangle, albedo U[0.2, 0.8]."""
     rng = np.random.default_rng(seed)

@@ -41,6 +41,14 @@ assert shader_dtype.itemsize == 80 and light_dtype.itemsize == 80
 assert camera_dtype.itemsize == 60 and params_dtype.itemsize == 36
 assert path_ray_dtype.itemsize == 36 and hitpoint_dtype.itemsize == 48
 
+import ctypes  # noqa: E402
+
+
+class texture_ctype(ctypes.Structure):
+    """aur_texture: width, height, host RGBA8 pointer."""
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("rgba", ctypes.c_void_p)]
+
+
 NO_HIT = 0xFFFFFFFF
 MODE_REFERENCE, MODE_PATH = 0, 1
 SHADER_LAMBERT, SHADER_PHONG = 0, 1

@@ -315,6 +315,36 @@ aur_status aur_scene_nmh(const aur_scene* scene, const aur_nmh** nmh);
 aur_status aur_scene_set_shaders(aur_ctx* ctx, aur_scene* scene, const aur_shader* shaders, uint32_t num_shaders);
 aur_status aur_scene_set_lights(aur_ctx* ctx, aur_scene* scene, const aur_light* lights, uint32_t num_lights);
 
+/* An RGBA8 image in host memory: width * height texels of 4 bytes, row-major,
+ * row 0 first (Texture::load, data/texture.cpp:15-26). */
+typedef struct aur_texture {
+    uint32_t width, height;
+    const uint8_t* rgba;
+} aur_texture;
+#define AUR_MAX_TEXTURES 32
+/* Textures of a scene (Scene::updateTextures, core/scene.cpp:298-327) and the
+ * per-triangle texture coordinates of Geometry::texcoords: `texcoords` holds
+ * 6 floats per triangle (u1 v1 u2 v2 u3 v3, Primitive2::readValues,
+ * kernels/lib/primitive.cuh:14-19) in the scene's original triangle order,
+ * host memory. A shader with texture = t (1-based, shader.h:37) then shades
+ * with texel(t - 1, uv) * diffuse instead of diffuse_color * diffuse, where
+ * uv interpolates the texcoords barycentrically and texel() is a bilinear,
+ * wrapping fetch of normalised RGBA8 (monteCarloRaytracer.cu:37-40,
+ * texunit.cuh:11-18, 54-94), computed by the formula the CUDA Programming
+ * Guide documents for the texture unit (weights with 8 fractional bits); the
+ * texture unit itself blends at a precision the guide leaves open (within
+ * 1.3e-3 of this formula on GB300). t > 32 fetches white, as the reference's
+ * texfetch does. At most AUR_MAX_TEXTURES textures. Replaces earlier ones.
+ * Every render entry point checks that each texture a shader names exists.
+ * Frees the scene's previous textures: not while a batch built from the scene
+ * (aur_batch_create) or a render on another stream may still read them. */
+aur_status aur_scene_set_textures(aur_ctx* ctx, aur_scene* scene, const float* texcoords, const aur_texture* textures,
+                                  uint32_t num_textures);
+/* texel(texture - 1, uv) for n device (u, v) pairs into n device RGB triples
+ * (the fetch the integrators use; no reference counterpart). */
+aur_status aur_scene_texfetch(aur_ctx* ctx, const aur_scene* scene, uint32_t texture, const float* uv, uint32_t n,
+                              float* rgb);
+
 /* --------------------------------------------------------------- rendering */
 
 /* Camera::Camera (util/camera.h:15-28): forward = normalize(direction),

@@ -49,6 +49,9 @@ def lib():
         L.orc_render.restype = ctypes.c_uint64
         L.orc_transform.argtypes = [P, P, U32, P, U32, P, P]
         L.orc_generate_tb.argtypes = [P, U32, P, P]
+        L.orc_render_textured.argtypes = [P, P, P, P, U32, P, U32, P, U32, P, P, P, ctypes.c_int, P, P, U32]
+        L.orc_render_textured.restype = ctypes.c_uint64
+        L.orc_texfetch.argtypes = [P, P, U32, P]
         _lib = L
     return _lib
 
@@ -152,6 +155,23 @@ def generate_rays(camera, W, H, sample, samples):
     return rays
 
 
+def _texture_table(textures):
+    imgs = [np.ascontiguousarray(t, np.uint8) for t in textures]
+    table = (T.texture_ctype * max(1, len(imgs)))()
+    for i, im in enumerate(imgs):
+        table[i].width, table[i].height, table[i].rgba = im.shape[1], im.shape[0], im.ctypes.data
+    return table, imgs
+
+
+def texfetch(texture, uv):
+    """Bilinear, wrapping fetch of an (H, W, 4) uint8 texture at (n, 2) uv."""
+    table, keep = _texture_table([texture])
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    rgb = np.zeros((uv.shape[0], 3), np.float32)
+    lib().orc_texfetch(ctypes.c_void_p(ctypes.addressof(table)), _ptr(uv), uv.shape[0], _ptr(rgb))
+    return rgb
+
+
 class NmhScene:
     """A scene reordered into NMH order, as the renderer consumes it."""
 
@@ -170,6 +190,14 @@ class NmhScene:
         self.shaders = np.ascontiguousarray(scene.shaders, T.shader_dtype)
         self.lights = np.ascontiguousarray(scene.lights, T.light_dtype)
         self.camera = np.asarray(scene.camera, T.camera_dtype).reshape(())
+        self.textures = list(getattr(scene, "textures", None) or [])
+        tc = getattr(scene, "texcoords", None)
+        self.TC = None
+        if tc is not None:
+            tc = np.ascontiguousarray(tc, np.float32).reshape(-1, 6)
+            if tc.shape[0] % 2:
+                tc = np.concatenate([tc, tc[-1:]])
+            self.TC = np.ascontiguousarray(tc[self.perm])
 
 
 def render(nscene, params, camera=None, accum=None, nthreads=None):
@@ -180,6 +208,14 @@ def render(nscene, params, camera=None, accum=None, nthreads=None):
     if accum is None:
         accum = np.zeros((H, W, 4), np.float32)
     cam = np.asarray(nscene.camera if camera is None else camera, T.camera_dtype).reshape(())
+    if nscene.TC is not None:
+        table, keep = _texture_table(nscene.textures)
+        tot = lib().orc_render_textured(_ptr(nscene.V), _ptr(nscene.N), _ptr(nscene.S), _ptr(nscene.perm),
+                                        nscene.V.shape[0], _ptr(nscene.shaders), nscene.shaders.shape[0],
+                                        _ptr(nscene.lights), nscene.lights.shape[0], _ptr(cam), _ptr(p), _ptr(accum),
+                                        nthreads or nthreads_default(), _ptr(nscene.TC),
+                                        ctypes.c_void_p(ctypes.addressof(table)), len(keep))
+        return accum, int(tot)
     tot = lib().orc_render(_ptr(nscene.V), _ptr(nscene.N), _ptr(nscene.S), _ptr(nscene.perm),
                            nscene.V.shape[0], _ptr(nscene.shaders), nscene.shaders.shape[0],
                            _ptr(nscene.lights), nscene.lights.shape[0], _ptr(cam), _ptr(p), _ptr(accum),

@@ -535,7 +535,44 @@ struct Scene {
     uint32_t nshaders;
     const aur_light* lights;
     uint32_t nlights;
+    const float* TC = nullptr;          // NMH-ordered texcoords, count*6
+    const aur_texture* tex = nullptr;
+    uint32_t ntex = 0;
 };
+
+// ------------------------------------------------------------ textures
+// tex2D with normalised coordinates, wrap addressing, linear filtering and
+// cudaReadModeNormalizedFloat on RGBA8 (the reference's texture units,
+// texunit.cuh:11-18), restated from the CUDA C++ Programming Guide appendix
+// "Texture Fetching": wrap replaces the coordinate by its fractional part;
+// xB = frac(u) * width - 0.5, texels floor(xB) and floor(xB) + 1 (wrapped),
+// alpha = frac(xB) in fixed point with 8 fractional bits, rounded to nearest;
+// result = (1-a)(1-b) T[i,j] + a(1-b) T[i+1,j] + (1-a) b T[i,j+1] + a b T[i+1,j+1]
+// in float, with T = byte / 255.
+inline float texWeight(float f) { return floorf(f * 256.0f + 0.5f) * (1.0f / 256.0f); }
+inline F3 texel(const aur_texture& t, uint32_t i, uint32_t j) {
+    const unsigned char* q = t.rgba + ((size_t)j * t.width + i) * 4;
+    return mk3((float)q[0] / 255.0f, (float)q[1] / 255.0f, (float)q[2] / 255.0f);
+}
+inline F3 texFetch(const aur_texture& t, float u, float v) {
+    const uint32_t W = t.width, H = t.height;
+    float xu = u - floorf(u), xv = v - floorf(v);
+    if (!(xu >= 0.0f && xu <= 1.0f)) xu = 0.0f;   // NaN / inf coordinates
+    if (!(xv >= 0.0f && xv <= 1.0f)) xv = 0.0f;
+    const float xb = xu * (float)W - 0.5f, yb = xv * (float)H - 0.5f;
+    const float fi = floorf(xb), fj = floorf(yb);
+    const float a = texWeight(xb - fi), b = texWeight(yb - fj);
+    const uint32_t i0 = fi < 0.0f ? W - 1 : std::min((uint32_t)fi, W - 1);
+    const uint32_t j0 = fj < 0.0f ? H - 1 : std::min((uint32_t)fj, H - 1);
+    const uint32_t i1 = i0 + 1 == W ? 0 : i0 + 1, j1 = j0 + 1 == H ? 0 : j0 + 1;
+    const F3 t00 = texel(t, i0, j0), t10 = texel(t, i1, j0), t01 = texel(t, i0, j1), t11 = texel(t, i1, j1);
+    return t00 * ((1.0f - a) * (1.0f - b)) + t10 * (a * (1.0f - b)) + t01 * ((1.0f - a) * b) + t11 * (a * b);
+}
+// texfetch (texunit.cuh:54-94): units past the 32 bound return white.
+inline F3 texFetchUnit(const Scene& sc, uint32_t id, float u, float v) {
+    if (id >= 32u) return mk3(1.0f, 1.0f, 1.0f);
+    return texFetch(sc.tex[id], u, v);
+}
 
 struct BSDF { F3 N, S, T, color1; };
 
@@ -560,7 +597,20 @@ inline BSDF getBSDF(const Scene& sc, const aur_shader& sh, uint32_t idx, float u
     bs.N = normalize(bclerp(n1, n2, n3, u, v));
     bs.S = normalize(bclerp(t1, t2, t3, u, v));
     bs.T = normalize(bclerp(b1, b2, b3, u, v));
-    bs.color1 = from(sh.diffuse_color) * sh.diffuse;
+    if (sh.texture > 0) {
+        // raytrace() texture branch (monteCarloRaytracer.cu:37-40), getTexCoord (common.cuh:45-51)
+        F3 c = mk3(1.0f, 1.0f, 1.0f);
+        if (sh.texture <= 32u) {
+            const float* tc = sc.TC + (size_t)idx * 6;
+            const float w = 1.0f - u - v;
+            const float tu = w * tc[0] + u * tc[2] + v * tc[4];
+            const float tv = w * tc[1] + u * tc[3] + v * tc[5];
+            c = texFetchUnit(sc, sh.texture - 1, tu, tv);
+        }
+        bs.color1 = c * sh.diffuse;
+    } else {
+        bs.color1 = from(sh.diffuse_color) * sh.diffuse;
+    }
     return bs;
 }
 
@@ -806,12 +856,43 @@ void orc_generate_rays(const aur_camera* cam, uint32_t W, uint32_t H, uint32_t s
  * Scene arrays are NMH-ordered (perm: NMH position -> original id).
  * Returns the number of node fetches (closest + any).
  */
+static uint64_t render_scene(const Scene& sc, const aur_camera* cam, const aur_render_params* p, float* accum,
+                             int nthreads);
+
 uint64_t orc_render(const float* V, const float* N, const uint16_t* S, const uint32_t* perm, uint32_t count,
                     const aur_shader* shaders, uint32_t nshaders, const aur_light* lights, uint32_t nlights,
                     const aur_camera* cam, const aur_render_params* p, float* accum, int nthreads) {
     Scene sc;
     sc.V = V; sc.N = N; sc.S = S; sc.perm = perm; sc.count = count;
     sc.shaders = shaders; sc.nshaders = nshaders; sc.lights = lights; sc.nlights = nlights;
+    return render_scene(sc, cam, p, accum, nthreads);
+}
+
+/* orc_render with textures: TC = NMH-ordered texcoords (count*6), tex = the
+ * scene's textures. */
+uint64_t orc_render_textured(const float* V, const float* N, const uint16_t* S, const uint32_t* perm, uint32_t count,
+                             const aur_shader* shaders, uint32_t nshaders, const aur_light* lights, uint32_t nlights,
+                             const aur_camera* cam, const aur_render_params* p, float* accum, int nthreads,
+                             const float* TC, const aur_texture* tex, uint32_t ntex) {
+    Scene sc;
+    sc.V = V; sc.N = N; sc.S = S; sc.perm = perm; sc.count = count;
+    sc.shaders = shaders; sc.nshaders = nshaders; sc.lights = lights; sc.nlights = nlights;
+    sc.TC = TC; sc.tex = tex; sc.ntex = ntex;
+    return render_scene(sc, cam, p, accum, nthreads);
+}
+
+/* The texture fetch alone: rgb[3i..] = texFetch(t, uv[2i], uv[2i+1]). */
+void orc_texfetch(const aur_texture* t, const float* uv, uint32_t n, float* rgb) {
+    for (uint32_t i = 0; i < n; ++i) {
+        const F3 c = texFetch(*t, uv[2 * i], uv[2 * i + 1]);
+        rgb[3 * i] = c.x; rgb[3 * i + 1] = c.y; rgb[3 * i + 2] = c.z;
+    }
+}
+
+}  // extern "C"
+
+static uint64_t render_scene(const Scene& sc, const aur_camera* cam, const aur_render_params* p, float* accum,
+                             int nthreads) {
     const uint32_t W = p->width, H = p->height;
     const uint32_t s0 = p->sample_begin, s1 = p->sample_end ? p->sample_end : p->spp;
     const float weight = 1.0f / (float)p->spp;
@@ -837,8 +918,6 @@ uint64_t orc_render(const float* V, const float* N, const uint16_t* S, const uin
     for (uint64_t x : tot) s += x;
     return s;
 }
-
-}  // extern "C"
 
 extern "C" {
 

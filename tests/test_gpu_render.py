@@ -82,10 +82,14 @@ def test_invalid_arguments_raise(ctx):
     with pytest.raises(api.AuroraError):
         sc.render(T.render_params(8, 8, 4, 99))
     bad = sd.shaders.copy()
-    bad["texture"][0] = 1
+    bad["texture"][0] = 1               # names texture 1, but the scene has none
+    sc.set_shaders(bad)
     with pytest.raises(api.AuroraError) as e:
+        sc.render(T.render_params(8, 8, 1, 4))
+    assert e.value.status == 1 and "texture" in str(e.value)
+    bad["type"][0] = 7
+    with pytest.raises(api.AuroraError):
         sc.set_shaders(bad)
-    assert e.value.status == 6
 
 
 @pytest.mark.parametrize("mode", [T.MODE_REFERENCE, T.MODE_PATH])
