@@ -191,6 +191,22 @@ Status loadSceneFile(const std::string& path, SceneData& out) {
                std::fread(out.shaders.data(), sizeof(aur_shader), counts[1], f) == counts[1] &&
                std::fread(out.lights.data(), sizeof(aur_light), counts[2], f) == counts[2];
         out.shaderIds.resize(tri);
+        // optional: counts[3] textures, after the per-triangle texcoords
+        if (good && counts[3]) {
+            out.texcoords.resize(tri * 6);
+            good = std::fread(out.texcoords.data(), 24, tri, f) == tri;
+            out.textures.resize(counts[3]);
+            for (uint32_t i = 0; good && i < counts[3]; ++i) {
+                uint32_t wh[2];
+                good = std::fread(wh, 4, 2, f) == 2 && wh[0] && wh[1] && (uint64_t)wh[0] * wh[1] < (1ull << 30);
+                if (!good) break;
+                TextureData& t = out.textures[i];
+                t.width = wh[0];
+                t.height = wh[1];
+                t.rgba.resize((size_t)wh[0] * wh[1] * 4);
+                good = std::fread(t.rgba.data(), 1, t.rgba.size(), f) == t.rgba.size();
+            }
+        }
     }
     std::fclose(f);
     if (!good) {
@@ -215,6 +231,26 @@ Status Scene::update(const SceneData& d) {
                                                 d.shaders.data(), (uint32_t)d.shaders.size(), d.lights.data(),
                                                 (uint32_t)d.lights.size(), &m_scene));
     if (s != Status::Success) return s;
+    // Scene::updateTextures (core/scene.cpp:298-327)
+    if (!d.textures.empty()) {
+        if (d.texcoords.size() != (size_t)n * 6) {
+            g_message = "Scene::update: textures need 6 texcoords per triangle";
+            free();
+            return Status::InvalidParameter;
+        }
+        std::vector<aur_texture> table(d.textures.size());
+        for (size_t i = 0; i < table.size(); ++i) {
+            table[i].width = d.textures[i].width;
+            table[i].height = d.textures[i].height;
+            table[i].rgba = d.textures[i].rgba.data();
+        }
+        const Status ts = status_of(aur_scene_set_textures(c, m_scene, d.texcoords.data(), table.data(),
+                                                           (uint32_t)table.size()));
+        if (ts != Status::Success) {
+            free();
+            return ts;
+        }
+    }
     m_shaders = d.shaders;
     m_lights = d.lights;
     m_count = n;

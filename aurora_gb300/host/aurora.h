@@ -76,6 +76,12 @@ public:
     static const size_t TriangleUVs = 6;
 };
 
+// An RGBA8 image (Texture, data/texture.h): width * height * 4 bytes, row 0 first.
+struct TextureData {
+    unsigned int width = 0, height = 0;
+    std::vector<uint8_t> rgba;
+};
+
 // A scene in host memory: what Scene::update reads instead of Maya nodes.
 struct SceneData {
     std::vector<float> vertices;        // count * 9, reference layout
@@ -83,6 +89,8 @@ struct SceneData {
     std::vector<uint16_t> shaderIds;    // count, 1-based
     std::vector<aur_shader> shaders;
     std::vector<aur_light> lights;
+    std::vector<float> texcoords;       // count * 6 (u1 v1 u2 v2 u3 v3), with textures
+    std::vector<TextureData> textures;  // shader.texture t selects textures[t - 1]
     aur_camera camera{};
     unsigned int count() const { return (unsigned int)(vertices.size() / 9); }
 };

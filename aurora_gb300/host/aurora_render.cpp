@@ -58,8 +58,9 @@ int main(int argc, char** argv) {
     SceneData data;
     if (loadSceneFile(scenePath, data) != Status::Success) return fail("loading the scene");
     if (dry) {
-        std::printf("{\"triangles\": %u, \"shaders\": %zu, \"lights\": %zu, \"vertex_checksum\": %llu}\n",
-                    data.count(), data.shaders.size(), data.lights.size(),
+        std::printf("{\"triangles\": %u, \"shaders\": %zu, \"lights\": %zu, \"textures\": %zu, "
+                    "\"vertex_checksum\": %llu}\n",
+                    data.count(), data.shaders.size(), data.lights.size(), data.textures.size(),
                     (unsigned long long)fnv1a(data.vertices.data(), data.vertices.size() * sizeof(float)));
         return 0;
     }

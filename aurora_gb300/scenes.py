@@ -45,16 +45,19 @@ SCENE_MAGIC = b"AURSCN1\0"
 def write_scene_file(sd, path):
     """Writes sd in the binary scene format read by the C++ host layer's
     loadSceneFile: magic "AURSCN1\\0", uint32 counts (triangles, shaders,
-    lights, 0), the aur_camera record, 4 pad bytes, vertices and normals
-    (36 B per triangle each), shader ids (uint16, padded to an even count),
-    shaders (80 B each), lights (80 B each); all little-endian."""
+    lights, textures), the aur_camera record, 4 pad bytes, vertices and
+    normals (36 B per triangle each), shader ids (uint16, padded to an even
+    count), shaders (80 B each), lights (80 B each); with textures, then the
+    texcoords (24 B per triangle) and per texture uint32 width, height and its
+    RGBA8 texels; all little-endian."""
     n = sd.count
     ids = sd.shader_ids
     if n % 2:
         ids = np.concatenate([ids, np.zeros(1, np.uint16)])
     with open(path, "wb") as f:
         f.write(SCENE_MAGIC)
-        f.write(np.array([n, sd.shaders.shape[0], sd.lights.shape[0], 0], "<u4").tobytes())
+        textures = list(getattr(sd, "textures", None) or [])
+        f.write(np.array([n, sd.shaders.shape[0], sd.lights.shape[0], len(textures)], "<u4").tobytes())
         f.write(sd.camera.reshape(1).tobytes())
         f.write(bytes(4))
         f.write(sd.vertices.astype("<f4").tobytes())
@@ -62,6 +65,12 @@ def write_scene_file(sd, path):
         f.write(ids.astype("<u2").tobytes())
         f.write(sd.shaders.tobytes())
         f.write(sd.lights.tobytes())
+        if textures:
+            f.write(np.ascontiguousarray(sd.texcoords, "<f4").reshape(n, 6).tobytes())
+            for t in textures:
+                t = np.ascontiguousarray(t, np.uint8)
+                f.write(np.array([t.shape[1], t.shape[0]], "<u4").tobytes())
+                f.write(t.tobytes())
 
 
 def read_pfm(path):

@@ -37,6 +37,10 @@ def test_scene_file_round_trip(driver, tmp_path):
     assert out["triangles"] == sd.count
     assert out["shaders"] == sd.shaders.shape[0] and out["lights"] == sd.lights.shape[0]
     assert out["vertex_checksum"] == _fnv1a(sd.vertices.tobytes())
+    tsd = scenes.cornell_textured()
+    scenes.write_scene_file(tsd, str(path))
+    out = _run([driver, str(path), "--dry-run"])
+    assert out["textures"] == 2 and out["triangles"] == tsd.count
 
 
 def test_malformed_scene_file_fails(driver, tmp_path):
@@ -47,11 +51,11 @@ def test_malformed_scene_file_fails(driver, tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", ["path", "reference"])
-def test_driver_render_matches_api(driver, ctx, tmp_path, mode):
+@pytest.mark.parametrize("mode,textured", [("path", False), ("reference", False), ("path", True)])
+def test_driver_render_matches_api(driver, ctx, tmp_path, mode, textured):
     """MonteCarloRaytracer::render (per-sample, 65,536-ray tiles) gives the
     image of the fused renderer bit for bit."""
-    sd = scenes.cornell_sphere(seed=3, slices=24, stacks=12)
+    sd = scenes.cornell_textured(seed=4) if textured else scenes.cornell_sphere(seed=3, slices=24, stacks=12)
     path = tmp_path / "scene.bin"
     out = tmp_path / "out.pfm"
     scenes.write_scene_file(sd, str(path))
@@ -60,7 +64,10 @@ def test_driver_render_matches_api(driver, ctx, tmp_path, mode):
           "--depth", str(depth), "--seed", str(seed), "--mode", mode])
     img = scenes.read_pfm(str(out))
     m = T.MODE_PATH if mode == "path" else T.MODE_REFERENCE
-    ref = api.Scene(ctx, sd).render(T.render_params(W, H, spp, depth, seed=seed, mode=m)).cpu().numpy()
+    sc = api.Scene(ctx, sd)
+    if textured:
+        sc.set_textures(sd.texcoords, sd.textures)
+    ref = sc.render(T.render_params(W, H, spp, depth, seed=seed, mode=m)).cpu().numpy()
     assert np.array_equal(img, ref[..., :3])
 
 
