@@ -907,14 +907,15 @@ aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, cons
                     continue;
                 }
                 float ms = 0.0f;
-                for (int rep = 0; rep < 2; ++rep) {   // the first launch warms up
+                aur_status s2 = AUR_OK;
+                for (int rep = 0; rep < 2 && s2 == AUR_OK; ++rep) {   // the first launch warms up
                     cudaEventRecord(e0, ctx->stream);
-                    aur_batch_render(ctx, bt, acc.data());
+                    s2 = aur_batch_render(ctx, bt, acc.data());
                     cudaEventRecord(e1, ctx->stream);
                     cudaEventSynchronize(e1);
                     cudaEventElapsedTime(&ms, e0, e1);
                 }
-                const aur_status s2 = aur_batch_status(ctx, bt, nullptr);
+                if (s2 == AUR_OK) s2 = aur_batch_status(ctx, bt, nullptr);
                 aur_batch_destroy(bt);
                 if (s2 != AUR_OK) { st = s2; continue; }
                 if (ms < best_t) { best_t = ms; *best = t; }

@@ -470,7 +470,25 @@ def bench_terrain(ctx, res=2048, samples=1, ref_spp=16384, small=(64, 36), small
     e1.record(stream)
     torch.cuda.synchronize()
     plain_ms = e0.elapsed_time(e1)
-    batch = api.Batch(ctx, [sc], [p])
+    # the plain path as the reference structures it: generate, 65,536-ray
+    # megakernel tiles, draw (render/monteCarloRaytracer.cpp:81-120)
+    tile = 65536
+    rays_b = torch.empty((W * H * 9,), dtype=torch.float32, device="cuda")
+    hits_b = torch.empty((W * H * 12,), dtype=torch.float32, device="cuda")
+    loop_img = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    e0.record(stream)
+    for smp in range(samples):
+        api.generate_rays(ctx, W, H, smp, 256, sd.camera, rays_b, hits_b)
+        for off in range(0, W * H, tile):
+            api.raytrace_monte_carlo(ctx, sc, p, smp, off, min(tile, W * H - off), rays_b, hits_b)
+        api.draw_pixels(ctx, W, H, 1.0 / 256, hits_b, loop_img)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    loop_ms = e0.elapsed_time(e1)
+    loop_same = bool(torch.equal(loop_img, plain))
+    del rays_b, hits_b, loop_img
+    tuning, _ = api.autotune(ctx, [sc], [p])
+    batch = api.Batch(ctx, [sc], [p], tuning=tuning)
     batch.render()
     batch.status()
     e0.record(stream)
@@ -498,9 +516,12 @@ def bench_terrain(ctx, res=2048, samples=1, ref_spp=16384, small=(64, 36), small
     return {"workload": "fBm terrain %dx%d vertices (%d triangles), 16 area lights, %dx%d, 256 spp, depth 8, path mode; "
                         "samples [0, %d) timed" % (res, res, sd.count, W, H, samples),
             "generate_s": gen_s, "scene_upload_and_build_s": scene_s, "nmh_build_ms": build_ms,
+            "plain_reference_loop_samples_per_s": n_samples / (loop_ms * 1e-3), "plain_reference_loop_ms": loop_ms,
             "plain_samples_per_s": n_samples / (plain_ms * 1e-3), "plain_ms": plain_ms,
             "wavefront_samples_per_s": n_samples / (wf_ms * 1e-3), "wavefront_ms": wf_ms,
-            "speedup": plain_ms / wf_ms, "frames_identical": same,
+            "speedup_vs_reference_loop": loop_ms / wf_ms, "speedup": plain_ms / wf_ms,
+            "frames_identical": same and loop_same,
+            "tuning": {k: int(tuning[k]) for k in tuning.dtype.names},
             "wavefront_rays": {"closest": ext, "shadow": shadow, "iterations": iters,
                                "mrays_per_s": (ext + shadow) / (wf_ms * 1e-3) / 1e6},
             "rmse": {"reference": "%dx%d at %d spp (seed 1)" % (sw, sh, ref_spp), "spp": small_spp,
