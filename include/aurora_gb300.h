@@ -398,7 +398,7 @@ aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_ca
 typedef struct aur_wavefront_tuning {
     uint32_t paths_in_flight;   /* path pool size (queue capacity) */
     uint32_t samples_per_wave;  /* samples per pixel processed per wave */
-    uint32_t block_size;        /* threads per block of the stage kernels */
+    uint32_t block_size;        /* threads per block of the stage kernels: multiple of 32, at most 256 */
     uint32_t blocks_per_sm;     /* persistent grid = SMs x blocks_per_sm */
     uint32_t max_iterations;    /* device-side loop limit per wave (0 = derived from the work) */
 } aur_wavefront_tuning;

@@ -77,3 +77,13 @@ def test_iteration_limit_reports_timeout_and_context_survives(ctx):
     assert np.array_equal(fr[0].cpu().numpy(), scs[0].render(prm[0]).cpu().numpy())
     ext, shadow, iters = ok.counters()
     assert ext > 0 and shadow > 0 and iters > 0
+
+
+def test_tuning_is_validated(ctx):
+    sd = scenes.cornell()
+    sc = api.Scene(ctx, sd)
+    p = [T.render_params(16, 16, 2, 2, mode=T.MODE_PATH)]
+    for bad in (dict(block_size=512), dict(block_size=100), dict(paths_in_flight=10), dict(blocks_per_sm=64)):
+        with pytest.raises(api.AuroraError):
+            api.Batch(ctx, [sc], p, tuning=api.make_tuning(**bad))
+    api.Batch(ctx, [sc], p, tuning=api.make_tuning(block_size=256)).close()
