@@ -65,6 +65,7 @@ SIGNATURES = {
     "aur_raytrace_monte_carlo": ([P, P, P, U32, U32, U32, P, P], ctypes.c_int),
     "aur_draw_pixels": ([P, U32, U32, ctypes.c_float, P, P], ctypes.c_int),
     "aur_clear_pixels": ([P, U32, U32, P], ctypes.c_int),
+    "aur_filter_pixels": ([P, U32, U32, P, P, P], ctypes.c_int),
     "aur_debug_nmh_layout": ([U32, U32, P], ctypes.c_int),
     "aur_batch_create": ([P, P, P, P, U32, P, P], ctypes.c_int),
     "aur_batch_render": ([P, P, P], ctypes.c_int),
@@ -339,6 +340,12 @@ def raytrace_monte_carlo(ctx, scene, params, sample, offset, num, rays_dev, hits
 
 def draw_pixels(ctx, W, H, weight, hits_dev, accum_dev):
     check(lib().aur_draw_pixels(ctx.handle, W, H, weight, _ptr(hits_dev), _ptr(accum_dev)))
+
+
+def filter_pixels(ctx, W, H, in_dev, out_dev, region=None):
+    """aur_filter_pixels: region = (left, right, bottom, top) inclusive or None."""
+    r = None if region is None else np.array(region, np.uint32)
+    check(lib().aur_filter_pixels(ctx.handle, W, H, _ptr(r), _ptr(in_dev), _ptr(out_dev)))
 
 
 def clear_pixels(ctx, W, H, accum_dev):

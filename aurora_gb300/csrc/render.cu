@@ -134,6 +134,31 @@ __global__ void k_draw_pixels(uint32_t P, float weight, const aur_hitpoint* __re
     }
 }
 
+// cudaFilterPixelsKernel (kernels/utility.cu:231-252): one thread per pixel
+// of the region, nine taps clamped to the region (the row below clamped to
+// region.top), summed in the reference's order.
+__global__ void k_filter_pixels(uint32_t width, aur_rect r, const float4* __restrict__ in, float4* __restrict__ out) {
+    const uint32_t x = r.left + blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t y = r.bottom + blockIdx.y * blockDim.y + threadIdx.y;
+    if (x > r.right || y > r.top) return;
+    const uint32_t xl = x > r.left ? x - 1 : r.left, xr = x < r.right ? x + 1 : r.right;
+    const uint32_t yb = y > r.bottom ? y - 1 : r.bottom, yt = y < r.top ? y + 1 : r.top;
+    const size_t row0 = (size_t)width * yb, row1 = (size_t)width * y, row2 = (size_t)width * yt;
+    const float4 p00 = __ldg(in + row0 + xl), p01 = __ldg(in + row0 + x), p02 = __ldg(in + row0 + xr);
+    const float4 p10 = __ldg(in + row1 + xl), p11 = __ldg(in + row1 + x), p12 = __ldg(in + row1 + xr);
+    const float4 p20 = __ldg(in + row2 + xl), p21 = __ldg(in + row2 + x), p22 = __ldg(in + row2 + xr);
+    float4 v;
+#define AUR_TAPS(c)                                                                                              \
+    v.c = p00.c * 0.0625f + p01.c * 0.125f + p02.c * 0.0625f + p10.c * 0.125f + p11.c * 0.25f + p12.c * 0.125f + \
+          p20.c * 0.0625f + p21.c * 0.125f + p22.c * 0.0625f
+    AUR_TAPS(x);
+    AUR_TAPS(y);
+    AUR_TAPS(z);
+    AUR_TAPS(w);
+#undef AUR_TAPS
+    out[row1 + x] = v;
+}
+
 }  // namespace
 
 SceneView scene_view(const aur_scene* sc) {
@@ -258,6 +283,28 @@ aur_status aur_draw_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float 
     const uint32_t P = width * height;
     if (P == 0) return AUR_OK;
     k_draw_pixels<<<cdiv(P, 256), 256, 0, ctx->stream>>>(P, weight, hits, (float4*)accum);
+    AUR_CUDA(cudaGetLastError());
+    return AUR_OK;
+}
+
+aur_status aur_filter_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, const aur_rect* region, const float* in,
+                             float* out) {
+    clear_error();
+    AUR_CHECK(ctx && in && out, AUR_ERR_INVALID, "aur_filter_pixels: null argument");
+    AUR_CHECK(in != out, AUR_ERR_INVALID, "aur_filter_pixels: in and out must be distinct buffers");
+    AUR_CHECK(width && height && (uint64_t)width * height < (1ull << 31), AUR_ERR_INVALID,
+              "aur_filter_pixels: bad frame size %ux%u", width, height);
+    const aur_rect r = region ? *region : aur_rect{0u, width - 1, 0u, height - 1};
+    AUR_CHECK(r.left <= r.right && r.right < width && r.bottom <= r.top && r.top < height, AUR_ERR_INVALID,
+              "aur_filter_pixels: region [%u, %u] x [%u, %u] outside %ux%u", r.left, r.right, r.bottom, r.top, width,
+              height);
+    AUR_CHECK(r.top - r.bottom < 65535u * 8u, AUR_ERR_INVALID, "aur_filter_pixels: region taller than %u rows",
+              65535u * 8u);
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    const dim3 block(32, 8);
+    const dim3 grid(cdiv(r.right - r.left + 1, block.x), cdiv(r.top - r.bottom + 1, block.y));
+    k_filter_pixels<<<grid, block, 0, ctx->stream>>>(width, r, reinterpret_cast<const float4*>(in),
+                                                    reinterpret_cast<float4*>(out));
     AUR_CUDA(cudaGetLastError());
     return AUR_OK;
 }

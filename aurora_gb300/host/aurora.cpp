@@ -343,7 +343,6 @@ Status MonteCarloRaytracer::setRegion(const Rect& region) {
 }
 
 Status MonteCarloRaytracer::render(bool ipr) {
-    (void)ipr;
     if (!m_pixels || !m_scene) return Status::Failure;
     const float weight = 1.0f / m_size.depth;
     const unsigned int numRays = m_size.width * m_size.height;
@@ -355,10 +354,14 @@ Status MonteCarloRaytracer::render(bool ipr) {
     p.max_depth = m_maxDepth;
     p.seed = m_seed;
     p.mode = m_mode;
-    Status s = clearPixels(m_size, m_pixels);
-    if (s != Status::Success) return s;
-    for (unsigned short i = 0; i < m_size.depth; i++) {
-        if ((s = generateRays(m_camera, m_size, i, m_rays, m_hit)) != Status::Success) return s;
+    Status s;
+    if (!ipr || m_done == 0 || m_done >= m_size.depth) {
+        if ((s = clearPixels(m_size, m_pixels)) != Status::Success) return s;
+        m_done = 0;
+    }
+    const unsigned int first = ipr ? m_done : 0u, last = ipr ? m_done + 1 : (unsigned int)m_size.depth;
+    for (unsigned int i = first; i < last; i++) {
+        if ((s = generateRays(m_camera, m_size, (unsigned short)i, m_rays, m_hit)) != Status::Success) return s;
         for (unsigned int j = 0; j < numTiles; j++) {
             const unsigned int offset = j * TileSize;
             const unsigned int numTileRays = std::min(numRays - offset, TileSize);
@@ -368,6 +371,9 @@ Status MonteCarloRaytracer::render(bool ipr) {
         }
         if ((s = drawPixels(m_size, m_hit, weight, m_pixels)) != Status::Success) return s;
     }
+    m_done = last;
+    if (m_filter && m_done == m_size.depth)
+        if ((s = filterPixels(m_size, m_region, &m_pixels)) != Status::Success) return s;
     return status_of(aur_ctx_synchronize(context()));
 }
 
@@ -375,7 +381,31 @@ const float* MonteCarloRaytracer::framebuffer() {
     if (!m_pixels) return nullptr;
     if (!ok(aur_memdownload(context(), m_framebuffer.data(), m_pixels, m_framebuffer.size() * sizeof(float))))
         return nullptr;
+    if (m_done > 0 && m_done < m_size.depth) {   // progressive: normalise by the samples done
+        const float scale = (float)m_size.depth / (float)m_done;
+        for (float& v : m_framebuffer) v *= scale;
+    }
     return m_framebuffer.data();
+}
+
+Status Renderer::filterPixels(const Dim& size, const Rect& region, float** pixels) {
+    aur_ctx* c = context();
+    const size_t bytes = (size_t)size.width * size.height * 4 * sizeof(float);
+    float* out = nullptr;
+    if (!ok(aur_malloc(c, bytes, AUR_DEVICE_MEMORY, (void**)&out))) return Status::InsufficientMemory;
+    const aur_rect r{region.left, region.right, region.bottom, region.top};
+    if (!ok(aur_memzero(c, out, bytes, AUR_DEVICE_MEMORY)) ||
+        !ok(aur_filter_pixels(c, size.width, size.height, &r, *pixels, out))) {
+        aur_free(c, out, AUR_DEVICE_MEMORY);
+        return Status::Failure;
+    }
+    if (!ok(aur_ctx_synchronize(c))) {
+        aur_free(c, out, AUR_DEVICE_MEMORY);
+        return Status::Failure;
+    }
+    aur_free(c, *pixels, AUR_DEVICE_MEMORY);
+    *pixels = out;
+    return Status::Success;
 }
 
 }  // namespace Aurora

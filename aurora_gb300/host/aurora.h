@@ -139,10 +139,18 @@ protected:
                                aur_path_ray* rays, aur_hitpoint* hit);
     static Status clearPixels(const Dim& size, void* pixels);
     static Status drawPixels(const Dim& size, const aur_hitpoint* hit, const float weight, void* pixels);
+    // Renderer::filterPixels (core/renderer.cpp): filters `region` of *pixels
+    // into a new buffer (other pixels zero), frees the old one and swaps.
+    static Status filterPixels(const Dim& size, const Rect& region, float** pixels);
 };
 
 // render/monteCarloRaytracer.h:14-39 with the render loop of
 // render/monteCarloRaytracer.cpp:81-120 (65,536-ray tiles per sample).
+// render(false) clears and renders every sample of the frame. render(true),
+// the interactive (IPR) call, adds the next single sample pass to the frame
+// without clearing (starting over once all samples are in), and framebuffer()
+// then returns the frame normalised by the samples done: a progressive image
+// that after `samples` calls equals render(false)'s bit for bit.
 class MonteCarloRaytracer : public Renderer {
 public:
     MonteCarloRaytracer();
@@ -158,6 +166,11 @@ public:
     // Integrator settings the reference fixes at compile time (MAX_DEPTH) or
     // seeds from GetTickCount(); AUR_MODE_REFERENCE reproduces it.
     void setIntegrator(unsigned int maxDepth, unsigned int seed, unsigned int mode);
+    // Applies filterPixels after each complete render (the reference's call
+    // is commented out, monteCarloRaytracer.cpp:117).
+    void setFilter(bool on) { m_filter = on; }
+    // Samples accumulated so far in the frame (progressive rendering).
+    unsigned int samplesDone() const { return m_done; }
 
     static const unsigned int TileSize = 256 * 256;
 
@@ -171,6 +184,8 @@ protected:
     Rect m_region;
     Dim m_size;
     unsigned int m_maxDepth, m_seed, m_mode;
+    unsigned int m_done = 0;
+    bool m_filter = false;
 };
 
 }  // namespace Aurora

@@ -3,6 +3,7 @@
 //
 //   aurora_render SCENE.bin OUT.pfm [--width W] [--height H] [--spp S]
 //                 [--depth D] [--seed N] [--mode reference|path] [--device K]
+//                 [--filter] [--progressive]
 //   aurora_render SCENE.bin --dry-run          parse the scene file only
 //   aurora_render SCENE.bin --geometry-check   Geometry upload + rebuild + TB
 //
@@ -39,7 +40,7 @@ int main(int argc, char** argv) {
     std::string scenePath = argv[1], outPath;
     unsigned width = 256, height = 256, spp = 16, depth = 4, seed = 0, mode = AUR_MODE_PATH;
     int device = 0;
-    bool dry = false, geomCheck = false;
+    bool dry = false, geomCheck = false, filter = false, progressive = false;
     for (int i = 2; i < argc; ++i) {
         const std::string a = argv[i];
         auto next = [&]() { return (i + 1 < argc) ? std::strtoul(argv[++i], nullptr, 10) : 0ul; };
@@ -52,6 +53,8 @@ int main(int argc, char** argv) {
         else if (a == "--mode") mode = (i + 1 < argc && std::string(argv[++i]) == "reference") ? AUR_MODE_REFERENCE : AUR_MODE_PATH;
         else if (a == "--dry-run") dry = true;
         else if (a == "--geometry-check") geomCheck = true;
+        else if (a == "--filter") filter = true;
+        else if (a == "--progressive") progressive = true;
         else if (outPath.empty()) outPath = a;
         else { std::fprintf(stderr, "aurora_render: unknown argument %s\n", a.c_str()); return 2; }
     }
@@ -101,10 +104,16 @@ int main(int argc, char** argv) {
     if (scene.update(data) != Status::Success) return fail("updating the scene");
     MonteCarloRaytracer renderer;
     renderer.setIntegrator(depth, seed, mode);
+    renderer.setFilter(filter);
     if (renderer.createFrame(width, height, (unsigned short)spp, &scene, data.camera) != Status::Success)
         return fail("creating the frame");
     const auto t0 = std::chrono::steady_clock::now();
-    if (renderer.render(false) != Status::Success) return fail("rendering");
+    if (progressive) {   // the interactive loop: one sample pass per call
+        for (unsigned int k = 0; k < spp; ++k)
+            if (renderer.render(true) != Status::Success) return fail("rendering");
+    } else if (renderer.render(false) != Status::Success) {
+        return fail("rendering");
+    }
     const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     const float* fb = renderer.framebuffer();
     if (!fb) return fail("reading the framebuffer");

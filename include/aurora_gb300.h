@@ -379,6 +379,20 @@ aur_status aur_draw_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float 
 /* Renderer::clearPixels (core/renderer.cpp:33-36). */
 aur_status aur_clear_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float* accum);
 
+/* A pixel rectangle, bounds inclusive (Rect, util/math.h:283-313). */
+typedef struct aur_rect {
+    uint32_t left, right, bottom, top;
+} aur_rect;
+/* cudaFilterPixels (kernels/utility.cu:231-268): 3x3 binomial filter
+ * (1 2 1 / 2 4 2 / 1 2 1) / 16 of the float4 pixels of `region` (NULL = the
+ * whole frame) from `in` into `out`, taps clamped to the region; pixels of
+ * `out` outside the region are left as they are. The reference clamps the
+ * row below to region.bottom instead of region.top (utility.cu:241-243); here
+ * it is clamped to region.top. in and out: device, width*height float4 each,
+ * distinct. */
+aur_status aur_filter_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, const aur_rect* region, const float* in,
+                             float* out);
+
 /* ----------------------------------------------------------------- adjoint */
 
 /* Gradients of a loss with respect to every shader's diffuse_color and every

@@ -52,6 +52,7 @@ def lib():
         L.orc_render_textured.argtypes = [P, P, P, P, U32, P, U32, P, U32, P, P, P, ctypes.c_int, P, P, U32]
         L.orc_render_textured.restype = ctypes.c_uint64
         L.orc_texfetch.argtypes = [P, P, U32, P]
+        L.orc_filter_pixels.argtypes = [U32, P, P, P]
         _lib = L
     return _lib
 
@@ -170,6 +171,18 @@ def texfetch(texture, uv):
     rgb = np.zeros((uv.shape[0], 3), np.float32)
     lib().orc_texfetch(ctypes.c_void_p(ctypes.addressof(table)), _ptr(uv), uv.shape[0], _ptr(rgb))
     return rgb
+
+
+def filter_pixels(img, region=None):
+    """cudaFilterPixels with the row-below clamp fixed: img (H, W, 4) float32;
+    region (left, right, bottom, top) inclusive, default the whole frame.
+    Returns a copy of img with the region filtered."""
+    img = np.ascontiguousarray(img, np.float32)
+    H, W = img.shape[:2]
+    reg = np.array(region if region is not None else (0, W - 1, 0, H - 1), np.uint32)
+    out = img.copy()
+    lib().orc_filter_pixels(W, _ptr(reg), _ptr(img), _ptr(out))
+    return out
 
 
 class NmhScene:

@@ -881,6 +881,27 @@ uint64_t orc_render_textured(const float* V, const float* N, const uint16_t* S, 
     return render_scene(sc, cam, p, accum, nthreads);
 }
 
+/* cudaFilterPixelsKernel (kernels/utility.cu:231-252) over the inclusive
+ * region (left, right, bottom, top), with the row below clamped to top
+ * (the reference clamps it to bottom). in/out: width*height float4. */
+void orc_filter_pixels(uint32_t width, const uint32_t* region, const float* in, float* out) {
+    const uint32_t L = region[0], R = region[1], B = region[2], T = region[3];
+    for (uint32_t y = B; y <= T; ++y)
+        for (uint32_t x = L; x <= R; ++x) {
+            const uint32_t xl = x > L ? x - 1 : L, xr = x < R ? x + 1 : R;
+            const uint32_t yb = y > B ? y - 1 : B, yt = y < T ? y + 1 : T;
+            const float* p00 = in + ((size_t)width * yb + xl) * 4; const float* p01 = in + ((size_t)width * yb + x) * 4;
+            const float* p02 = in + ((size_t)width * yb + xr) * 4; const float* p10 = in + ((size_t)width * y + xl) * 4;
+            const float* p11 = in + ((size_t)width * y + x) * 4;   const float* p12 = in + ((size_t)width * y + xr) * 4;
+            const float* p20 = in + ((size_t)width * yt + xl) * 4; const float* p21 = in + ((size_t)width * yt + x) * 4;
+            const float* p22 = in + ((size_t)width * yt + xr) * 4;
+            float* o = out + ((size_t)width * y + x) * 4;
+            for (int c = 0; c < 4; ++c)
+                o[c] = p00[c] * 0.0625f + p01[c] * 0.125f + p02[c] * 0.0625f + p10[c] * 0.125f + p11[c] * 0.25f +
+                       p12[c] * 0.125f + p20[c] * 0.0625f + p21[c] * 0.125f + p22[c] * 0.0625f;
+        }
+}
+
 /* The texture fetch alone: rgb[3i..] = texFetch(t, uv[2i], uv[2i+1]). */
 void orc_texfetch(const aur_texture* t, const float* uv, uint32_t n, float* rgb) {
     for (uint32_t i = 0; i < n; ++i) {

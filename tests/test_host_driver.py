@@ -89,3 +89,20 @@ def test_geometry_rebuild_matches_oracle(driver, tmp_path):
     assert out["perm_checksum"] == _fnv1a(perm.tobytes())
     assert out["vertex_checksum"] == _fnv1a(V.tobytes())
     assert out["tangent_checksum"] == _fnv1a(tb.tobytes())
+
+
+@pytest.mark.gpu
+def test_driver_progressive_and_filter(driver, ctx, tmp_path):
+    """render(true) called spp times (one sample pass each, no clearing) ends
+    on render(false)'s image; --filter applies cudaFilterPixels (row-below
+    clamp fixed) to the finished frame."""
+    sd = scenes.cornell()
+    path = tmp_path / "c.bin"
+    scenes.write_scene_file(sd, str(path))
+    W, H, spp = 70, 50, 5
+    args = ["--width", str(W), "--height", str(H), "--spp", str(spp), "--depth", "3", "--seed", "2"]
+    _run([driver, str(path), str(tmp_path / "prog.pfm"), "--progressive", *args])
+    _run([driver, str(path), str(tmp_path / "filt.pfm"), "--filter", *args])
+    full = api.Scene(ctx, sd).render(T.render_params(W, H, spp, 3, seed=2, mode=T.MODE_PATH)).cpu().numpy()
+    assert np.array_equal(scenes.read_pfm(str(tmp_path / "prog.pfm")), full[..., :3])
+    assert np.array_equal(scenes.read_pfm(str(tmp_path / "filt.pfm")), oracle.filter_pixels(full)[..., :3])
