@@ -143,15 +143,34 @@ __device__ __forceinline__ uint32_t global_tid() { return blockIdx.x * blockDim.
 // item nb * pix_off[s] + b * (width * height) + lp. The paths in flight then
 // come from a few scenes at a time, whose node records stay in L2, instead of
 // the same sample of every scene.
+// Within a sample, consecutive items walk the frame in 8x4-pixel tiles
+// (bands of 4 rows, blocks of 8 columns; narrower blocks at the right and top
+// edges), so that the 32 primary rays a warp generates share a compact
+// footprint. `tile_pixel` maps the item's position in that walk to the
+// row-major pixel index; it is a bijection on [0, width * height).
+constexpr uint32_t kTileW = 8, kTileH = 4;
+
+__device__ __forceinline__ uint32_t tile_pixel(uint32_t q, uint32_t w, uint32_t h) {
+    const uint32_t band = q / (w * kTileH);
+    const uint32_t hb = min(kTileH, h - band * kTileH);
+    const uint32_t idx = q - band * w * kTileH;
+    const uint32_t cb = idx / (kTileW * hb);
+    const uint32_t wb = min(kTileW, w - cb * kTileW);
+    const uint32_t i = idx - cb * kTileW * hb;
+    const uint32_t x = cb * kTileW + i % wb, y = band * kTileH + i / wb;
+    return y * w + x;
+}
+
 struct ItemRef {
-    uint32_t b, lp;
+    uint32_t b, q, pix;   // sample within the wave, position in the tile walk, row-major pixel
 };
 __device__ __forceinline__ ItemRef decode_item(uint32_t item, uint32_t nb, const WfScene& sc) {
     const uint32_t local = item - nb * sc.pix_off;
     const uint32_t npix = sc.width * sc.height;
     ItemRef r;
     r.b = local / npix;
-    r.lp = local - r.b * npix;
+    r.q = local - r.b * npix;
+    r.pix = tile_pixel(r.q, sc.width, sc.height);
     return r;
 }
 
@@ -193,7 +212,7 @@ __global__ void k_wf_generate(WfArgs a) {
         const uint32_t s = find_scene(a.pix_off, a.num_scenes, item / c->nb);
         const WfScene& sc = a.scenes[s];
         const ItemRef ir = decode_item(item, c->nb, sc);
-        const uint32_t lp = ir.lp;
+        const uint32_t lp = ir.pix;
         const PathRay r = camera_ray(sc.cam, sc.width, sc.height, lp % sc.width, lp / sc.width, c->s0 + ir.b, a.spp);
         a.o[slot] = make_float4(r.pos.x, r.pos.y, r.pos.z, 0.0f);
         a.d[slot] = make_float4(r.dir.x, r.dir.y, r.dir.z, 0.0f);
@@ -280,7 +299,7 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
         }
         const WfScene& sc = a.scenes[m.w];
         const ItemRef ir = decode_item(m.x, c->nb, sc);
-        const uint32_t pix = ir.lp, sample = c->s0 + ir.b, rix = m.z;
+        const uint32_t pix = ir.pix, sample = c->s0 + ir.b, rix = m.z;
         const float4 o4 = a.o[slot], d4 = a.d[slot];
         const f3 pos = mk3(o4.x, o4.y, o4.z), dir = mk3(d4.x, d4.y, d4.z);
         const f3 position = pos + (dir * h.x);
@@ -477,10 +496,10 @@ __global__ void k_wf_accumulate(WfArgs a) {
     const uint32_t nb = c->nb;
     for (uint32_t gp = global_tid(); gp < a.P_tot; gp += grid_threads()) {
         const uint32_t s = find_scene(a.pix_off, a.num_scenes, gp);
-        const uint32_t lp = gp - a.pix_off[s];
+        const uint32_t q = gp - a.pix_off[s];   // position in the tile walk
         const uint32_t npix = a.pix_off[s + 1] - a.pix_off[s];
-        const float4* out = a.out + (size_t)nb * a.pix_off[s] + lp;
-        float4* acc = a.accum[s] + lp;
+        const float4* out = a.out + (size_t)nb * a.pix_off[s] + q;
+        float4* acc = a.accum[s] + tile_pixel(q, a.scenes[s].width, a.scenes[s].height);
         float4 v = *acc;
         for (uint32_t b = 0; b < nb; ++b) {
             const float4 cv = out[(size_t)b * npix];
