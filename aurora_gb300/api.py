@@ -59,6 +59,7 @@ SIGNATURES = {
     "aur_scene_set_lights": ([P, P, P, U32], ctypes.c_int),
     "aur_scene_set_textures": ([P, P, P, P, U32], ctypes.c_int),
     "aur_scene_texfetch": ([P, P, U32, P, U32, P], ctypes.c_int),
+    "aur_scene_emitters": ([P, P, P, P], ctypes.c_int),
     "aur_camera_make": None,  # struct-by-value arguments; not bound
     "aur_render": ([P, P, P, P, P], ctypes.c_int),
     "aur_generate_rays": ([P, U32, U32, U32, U32, P, P, P], ctypes.c_int),
@@ -278,6 +279,15 @@ class Scene:
         check(lib().aur_scene_set_textures(self.ctx.handle, self.handle, _ptr(tc), P(ctypes.addressof(table)),
                                            len(imgs)))
         self._textures = imgs
+
+    def emitters(self):
+        """The scene's emissive-triangle table (numpy, emitter_dtype)."""
+        import torch
+        n = self.nmh.info()[0]
+        buf = torch.empty((max(1, n) * T.emitter_dtype.itemsize,), dtype=torch.uint8, device="cuda")
+        m = ctypes.c_uint32(0)
+        check(lib().aur_scene_emitters(self.ctx.handle, self.handle, _ptr(buf), ctypes.byref(m)))
+        return buf[:m.value * T.emitter_dtype.itemsize].cpu().numpy().view(T.emitter_dtype)
 
     def texfetch(self, texture, uv_dev):
         """RGB of texture `texture` (1-based) at n device (u, v) pairs."""

@@ -32,11 +32,13 @@ path_ray_dtype = np.dtype([("pos",) + F3, ("dir",) + F3, ("t", "<f4"), ("weight"
 hitpoint_dtype = np.dtype([("color",) + F3, ("position",) + F3, ("wo",) + F3, ("u", "<f4"), ("v", "<f4"),
                            ("triangle_id", "<i4")])
 
+emitter_dtype = np.dtype([("area", "<f4"), ("pdf", "<f4"), ("cdf", "<f4"), ("power",) + F3, ("triangle_id", "<u4")])
+
 object_transform_dtype = np.dtype([("offset", "<u4"), ("size", "<u4"), ("world_matrix", "<f4", (4, 4)),
                                    ("normal_matrix", "<f4", (4, 4))])
 
 assert ray_dtype.itemsize == 32 and hit_dtype.itemsize == 16
-assert object_transform_dtype.itemsize == 136
+assert object_transform_dtype.itemsize == 136 and emitter_dtype.itemsize == 28
 assert shader_dtype.itemsize == 80 and light_dtype.itemsize == 80
 assert camera_dtype.itemsize == 60 and params_dtype.itemsize == 36
 assert path_ray_dtype.itemsize == 36 and hitpoint_dtype.itemsize == 48

@@ -340,6 +340,21 @@ typedef struct aur_texture {
  * (aur_batch_create) or a render on another stream may still read them. */
 aur_status aur_scene_set_textures(aur_ctx* ctx, aur_scene* scene, const float* texcoords, const aur_texture* textures,
                                   uint32_t num_textures);
+/* An emissive triangle (Emitter, util/emitter.h:10-21): triangle_id is its
+ * NMH position, as the reference's ids after the rebuild are. */
+typedef struct aur_emitter {
+    float area, pdf, cdf;
+    aur_float3 power;
+    uint32_t triangle_id;
+} aur_emitter;
+/* cudaCreateEmitters (kernels/emitter.cu:39-119): the triangles (NMH order,
+ * the even-padding copy included, as in the reference) whose shader has
+ * emission > 0, with area (Primitive3::area), pdf = 1 / area, power = the
+ * shader's emission colour and the inclusive CDF of the emission weights
+ * normalised to 1 (summed in double; the reference sums in float in Thrust's
+ * scan order). `emitters`: device, room for one record per triangle;
+ * *num_emitters (host) receives the count. */
+aur_status aur_scene_emitters(aur_ctx* ctx, const aur_scene* scene, aur_emitter* emitters, uint32_t* num_emitters);
 /* texel(texture - 1, uv) for n device (u, v) pairs into n device RGB triples
  * (the fetch the integrators use; no reference counterpart). */
 aur_status aur_scene_texfetch(aur_ctx* ctx, const aur_scene* scene, uint32_t texture, const float* uv, uint32_t n,

@@ -53,6 +53,8 @@ def lib():
         L.orc_render_textured.restype = ctypes.c_uint64
         L.orc_texfetch.argtypes = [P, P, U32, P]
         L.orc_filter_pixels.argtypes = [U32, P, P, P]
+        L.orc_emitters.argtypes = [P, P, U32, P, P]
+        L.orc_emitters.restype = U32
         _lib = L
     return _lib
 
@@ -171,6 +173,13 @@ def texfetch(texture, uv):
     rgb = np.zeros((uv.shape[0], 3), np.float32)
     lib().orc_texfetch(ctypes.c_void_p(ctypes.addressof(table)), _ptr(uv), uv.shape[0], _ptr(rgb))
     return rgb
+
+
+def emitters(nscene):
+    """cudaCreateEmitters over an NmhScene: the emitter records (emitter_dtype)."""
+    out = np.zeros(nscene.V.shape[0], T.emitter_dtype)
+    m = lib().orc_emitters(_ptr(nscene.V), _ptr(nscene.S), nscene.V.shape[0], _ptr(nscene.shaders), _ptr(out))
+    return out[:m]
 
 
 def filter_pixels(img, region=None):

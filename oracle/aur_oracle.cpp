@@ -902,6 +902,41 @@ void orc_filter_pixels(uint32_t width, const uint32_t* region, const float* in, 
         }
 }
 
+/* cudaCreateEmitters (kernels/emitter.cu:39-119) restated sequentially:
+ * triangles of the NMH-ordered soup (V: count*9, S: 1-based shader ids)
+ * whose shader has emission > 0, in order; area by Primitive3::area
+ * (primitive.cuh:74-85), pdf = 1/area, power = emission colour; the CDF of
+ * the emission weights summed in double and normalised, rounded to float.
+ * Returns the number of emitters written to out. */
+uint32_t orc_emitters(const float* V, const uint16_t* S, uint32_t count, const aur_shader* shaders, aur_emitter* out) {
+    uint32_t m = 0;
+    std::vector<double> w;
+    for (uint32_t i = 0; i < count; ++i) {
+        const aur_shader& sh = shaders[S[i] > 0 ? S[i] - 1 : 0];
+        if (!(sh.emission > 0.0f)) continue;
+        const float* v = V + (size_t)i * 9;
+        const F3 v1 = mk3(v[0], v[3], v[6]), v2 = mk3(v[1], v[4], v[7]), v3 = mk3(v[2], v[5], v[8]);
+        const F3 va = v1 - v2, vb = v1 - v3, vc = v2 - v3;
+        const float a = dot(va, va), b = dot(vb, vb), c = dot(vc, vc);
+        aur_emitter e;
+        e.area = sqrtf((2 * a * b + 2 * b * c + 2 * c * a - a * a - b * b - c * c) / 16.0f);
+        e.pdf = 1.0f / e.area;
+        e.cdf = 0.0f;
+        e.power = sh.emission_color;
+        e.triangle_id = i;
+        out[m++] = e;
+        w.push_back((double)sh.emission);
+    }
+    double total = 0.0;
+    for (double x : w) total += x;
+    double run = 0.0;
+    for (uint32_t j = 0; j < m; ++j) {
+        run += w[j];
+        out[j].cdf = (float)(run / total);
+    }
+    return m;
+}
+
 /* The texture fetch alone: rgb[3i..] = texFetch(t, uv[2i], uv[2i+1]). */
 void orc_texfetch(const aur_texture* t, const float* uv, uint32_t n, float* rgb) {
     for (uint32_t i = 0; i < n; ++i) {
