@@ -16,6 +16,12 @@ namespace aur {
 namespace {
 
 constexpr int kRenderThreads = 128;
+// The fused sample kernel is compiled for 10 resident blocks per SM (at most
+// 51 registers, a few hundred bytes of spills served by L1): measured 19 %
+// faster than its free 128 registers, which allowed 4 blocks. The per-tile
+// kernel (k_raytrace_mc) runs grids of one 65,536-ray tile, too small for
+// occupancy to matter, and is left unconstrained (a cap made it slower).
+constexpr int kRenderBlocksPerSm = 10;
 
 inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
@@ -31,7 +37,7 @@ __device__ __forceinline__ StackRef stack_ref(uint32_t* smem, int cap) {
 // colors[b * P + p] = (rgb, hit) of sample s0 + b at pixel p. kGeneric
 // selects the integrator with the specular ray stack.
 template <bool kGeneric>
-__global__ void __launch_bounds__(kRenderThreads) k_render_samples(SceneView sc, aur_camera cam, aur_render_params p,
+__global__ void __launch_bounds__(kRenderThreads, kRenderBlocksPerSm) k_render_samples(SceneView sc, aur_camera cam, aur_render_params p,
                                                                    uint32_t s0, uint32_t nb, float4* __restrict__ colors,
                                                                    uint32_t* __restrict__ err, int cap) {
     extern __shared__ uint32_t smem[];
