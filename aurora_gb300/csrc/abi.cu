@@ -113,6 +113,7 @@ aur_status aur_ctx_create(int device, aur_ctx** out) {
     if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->compute2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&c->d_flags, 256) != cudaSuccess || cudaMemset(c->d_flags, 0, 256) != cudaSuccess) {
         e = cudaGetLastError();
         aur_ctx_destroy(c);
@@ -141,6 +142,7 @@ aur_status aur_ctx_destroy(aur_ctx* ctx) {
     cudaFree(ctx->d_flags);
     if (ctx->copy_in) cudaStreamDestroy(ctx->copy_in);
     if (ctx->copy_out) cudaStreamDestroy(ctx->copy_out);
+    if (ctx->compute2) cudaStreamDestroy(ctx->compute2);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
     return AUR_OK;

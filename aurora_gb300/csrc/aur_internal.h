@@ -46,6 +46,7 @@ struct aur_ctx {
     cudaStream_t stream = nullptr;       // launch stream (own or caller's)
     cudaStream_t copy_in = nullptr;      // host-buffer pipelines
     cudaStream_t copy_out = nullptr;
+    cudaStream_t compute2 = nullptr;     // second launch stream of the host-buffer pipelines
     uint32_t* d_flags = nullptr;         // small device scratch: counters, error flags
     aur::Scratch pipe[2];                // double-buffered device chunks for *_host calls
     aur::Scratch out[2];
@@ -85,7 +86,10 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* vertices, uint32_t count, a
 aur_status check_params(const aur_render_params* p);
 // Every texture the scene's shaders name exists (and texcoords were given).
 aur_status check_scene_textures(const aur_scene* sc);
+// ray_counter: the persistent kernel's work counter (default d_flags[8]);
+// launches that may run concurrently need distinct counters.
 aur_status launch_trace(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits,
-                        uint32_t* occluder, unsigned long long* counters, cudaStream_t stream, bool pruned);
+                        uint32_t* occluder, unsigned long long* counters, cudaStream_t stream, bool pruned,
+                        uint32_t* ray_counter = nullptr);
 
 }  // namespace aur

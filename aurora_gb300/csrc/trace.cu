@@ -118,14 +118,13 @@ inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b
 
 template <bool kAny, bool kCount, bool kBoxes = true>
 aur_status launch_one(aur_ctx* ctx, const aur_nmh* nmh, const float4* r, uint32_t n, float4* h, uint32_t* occ,
-                      unsigned long long* counters, cudaStream_t stream) {
+                      unsigned long long* counters, cudaStream_t stream, uint32_t* ray_counter) {
     const int cap = (int)nmh->levels + 1;
     const size_t smem = (size_t)2 * cap * kTraceThreads * sizeof(uint32_t);
     int per_sm = 0;
     AUR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<kAny, kCount, kBoxes>, kTraceThreads,
                                                            smem));
     const uint32_t grid = std::max(1u, std::min<uint32_t>(cdiv(n, kTraceThreads), (uint32_t)(ctx->sm_count * per_sm)));
-    uint32_t* ray_counter = ctx->d_flags + 8;
     AUR_CUDA(cudaMemsetAsync(ray_counter, 0, sizeof(uint32_t), stream));
     k_trace<kAny, kCount, kBoxes><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r,
                                                                         n, h, occ, counters, ray_counter, cap);
@@ -134,18 +133,20 @@ aur_status launch_one(aur_ctx* ctx, const aur_nmh* nmh, const float4* r, uint32_
 }
 
 aur_status launch_trace(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits,
-                        uint32_t* occluder, unsigned long long* counters, cudaStream_t stream, bool pruned) {
+                        uint32_t* occluder, unsigned long long* counters, cudaStream_t stream, bool pruned,
+                        uint32_t* rc) {
     if (n == 0) return AUR_OK;
+    if (!rc) rc = ctx->d_flags + 8;
     const float4* r = reinterpret_cast<const float4*>(rays);
     float4* h = reinterpret_cast<float4*>(hits);
     if (counters && !pruned)
-        return occluder ? launch_one<true, true, false>(ctx, nmh, r, n, nullptr, occluder, counters, stream)
-                        : launch_one<false, true, false>(ctx, nmh, r, n, h, nullptr, counters, stream);
+        return occluder ? launch_one<true, true, false>(ctx, nmh, r, n, nullptr, occluder, counters, stream, rc)
+                        : launch_one<false, true, false>(ctx, nmh, r, n, h, nullptr, counters, stream, rc);
     if (counters)
-        return occluder ? launch_one<true, true>(ctx, nmh, r, n, nullptr, occluder, counters, stream)
-                        : launch_one<false, true>(ctx, nmh, r, n, h, nullptr, counters, stream);
-    return occluder ? launch_one<true, false>(ctx, nmh, r, n, nullptr, occluder, nullptr, stream)
-                    : launch_one<false, false>(ctx, nmh, r, n, h, nullptr, nullptr, stream);
+        return occluder ? launch_one<true, true>(ctx, nmh, r, n, nullptr, occluder, counters, stream, rc)
+                        : launch_one<false, true>(ctx, nmh, r, n, h, nullptr, counters, stream, rc);
+    return occluder ? launch_one<true, false>(ctx, nmh, r, n, nullptr, occluder, nullptr, stream, rc)
+                    : launch_one<false, false>(ctx, nmh, r, n, h, nullptr, nullptr, stream, rc);
 }
 
 }  // namespace aur
@@ -164,14 +165,17 @@ aur_status check_trace_args(aur_ctx* ctx, const aur_nmh* nmh, const void* rays, 
     return AUR_OK;
 }
 
-// Host-buffer pipeline: chunks alternate between two device slots; the H2D
-// copy of chunk c+1 and the D2H copy of chunk c-1 overlap the traversal of c.
+// Host-buffer pipeline: chunks of 4M rays alternate between two device slots
+// and two launch streams (the context's and an internal one), so the H2D copy
+// of chunk c+1 and the D2H copy of chunk c-1 overlap the traversal of c, and
+// the traversal of c+1 starts while the last rays of c drain. Each slot has
+// its own ray counter, as its kernels may run concurrently with the other's.
 aur_status trace_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, void* out, bool any) {
     aur_status st = check_trace_args(ctx, nmh, rays, n, out);
     if (st != AUR_OK) return st;
     if (n == 0) return AUR_OK;
     AUR_CUDA(cudaSetDevice(ctx->device));
-    const uint32_t chunk = 1u << 20;
+    const uint32_t chunk = 1u << 22;
     const size_t out_sz = any ? sizeof(uint32_t) : sizeof(aur_hit);
     for (int s = 0; s < 2; ++s) {
         const size_t need_in = (size_t)chunk * sizeof(aur_ray), need_out = (size_t)chunk * out_sz;
@@ -191,9 +195,11 @@ aur_status trace_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uin
     cudaEvent_t* in_done = ctx->ev;
     cudaEvent_t* comp_done = ctx->ev + 2;
     cudaEvent_t* out_done = ctx->ev + 4;
-    // the copy streams start after work already queued on the launch stream
+    // the copy and second launch streams start after work already queued on the launch stream
     AUR_CUDA(cudaEventRecord(ctx->ev[6], ctx->stream));
     AUR_CUDA(cudaStreamWaitEvent(ctx->copy_in, ctx->ev[6], 0));
+    AUR_CUDA(cudaStreamWaitEvent(ctx->compute2, ctx->ev[6], 0));
+    cudaStream_t const launch[2] = {ctx->stream, ctx->compute2};
     bool used[2] = {false, false};
     for (uint32_t c0 = 0, c = 0; c0 < n; c0 += chunk, ++c) {
         const int s = (int)(c & 1);
@@ -202,11 +208,11 @@ aur_status trace_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uin
         AUR_CUDA(cudaMemcpyAsync(ctx->pipe[s].ptr, rays + c0, (size_t)m * sizeof(aur_ray), cudaMemcpyHostToDevice,
                                  ctx->copy_in));
         AUR_CUDA(cudaEventRecord(in_done[s], ctx->copy_in));
-        AUR_CUDA(cudaStreamWaitEvent(ctx->stream, in_done[s], 0));
+        AUR_CUDA(cudaStreamWaitEvent(launch[s], in_done[s], 0));
         st = launch_trace(ctx, nmh, (const aur_ray*)ctx->pipe[s].ptr, m, any ? nullptr : (aur_hit*)ctx->out[s].ptr,
-                          any ? (uint32_t*)ctx->out[s].ptr : nullptr, nullptr, ctx->stream, true);
+                          any ? (uint32_t*)ctx->out[s].ptr : nullptr, nullptr, launch[s], true, ctx->d_flags + 8 + s);
         if (st != AUR_OK) return st;
-        AUR_CUDA(cudaEventRecord(comp_done[s], ctx->stream));
+        AUR_CUDA(cudaEventRecord(comp_done[s], launch[s]));
         AUR_CUDA(cudaStreamWaitEvent(ctx->copy_out, comp_done[s], 0));
         AUR_CUDA(cudaMemcpyAsync((char*)out + (size_t)c0 * out_sz, ctx->out[s].ptr, (size_t)m * out_sz,
                                  cudaMemcpyDeviceToHost, ctx->copy_out));
@@ -214,6 +220,7 @@ aur_status trace_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uin
         used[s] = true;
     }
     AUR_CUDA(cudaStreamSynchronize(ctx->copy_out));
+    AUR_CUDA(cudaStreamSynchronize(ctx->compute2));
     AUR_CUDA(cudaStreamSynchronize(ctx->stream));
     return AUR_OK;
 }
