@@ -275,8 +275,9 @@ aur_status aur_trace_closest(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* ra
  * the original prim id of the first hit found in traversal order with
  * Epsilon < t < tmax, or AUR_NO_HIT. rays, occluder: device. */
 aur_status aur_trace_any(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, uint32_t* occluder);
-/* Same as above with HOST buffers: copies are chunked and overlapped with the
- * traversal on the context's stream plus two internal copy streams. */
+/* Same as above with HOST buffers: rays go in chunks of 4M, traced on the
+ * context's stream and one internal launch stream in turn, with two internal
+ * copy streams overlapping the copies; returns when all hits are back. */
 aur_status aur_trace_closest_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits);
 aur_status aur_trace_any_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, uint32_t* occluder);
 /* Counts the reference algorithm's traversal work for n device rays:
