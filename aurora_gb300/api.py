@@ -7,6 +7,7 @@ here computes on the CPU: the CUDA library must be built (build.py) and a
 GPU present, otherwise loading fails loudly.
 """
 import ctypes
+import json
 import os
 
 import numpy as np
@@ -28,6 +29,7 @@ class AuroraError(RuntimeError):
 SIGNATURES = {
     "aur_last_error": ([], ctypes.c_char_p),
     "aur_version": ([], ctypes.c_char_p),
+    "aur_debug_fail_allocation": ([U32], ctypes.c_int),
     "aur_ctx_create": ([ctypes.c_int, P], ctypes.c_int),
     "aur_ctx_destroy": ([P], ctypes.c_int),
     "aur_ctx_set_stream": ([P, P], ctypes.c_int),
@@ -67,6 +69,8 @@ SIGNATURES = {
     "aur_draw_pixels": ([P, U32, U32, ctypes.c_float, P, P], ctypes.c_int),
     "aur_clear_pixels": ([P, U32, U32, P], ctypes.c_int),
     "aur_filter_pixels": ([P, U32, U32, P, P, P], ctypes.c_int),
+    "aur_accum_save": ([P, ctypes.c_char_p, U32, U32, U32, U32, P], ctypes.c_int),
+    "aur_accum_load": ([P, ctypes.c_char_p, U32, U32, P, P, P], ctypes.c_int),
     "aur_debug_nmh_layout": ([U32, U32, P], ctypes.c_int),
     "aur_batch_create": ([P, P, P, P, U32, P, P], ctypes.c_int),
     "aur_batch_render": ([P, P, P], ctypes.c_int),
@@ -122,6 +126,7 @@ class Context:
     def __init__(self, device=0):
         torch = _torch()
         self.device = device
+        self.handle = None
         h = P()
         check(lib().aur_ctx_create(device, ctypes.byref(h)))
         self.handle = h
@@ -162,6 +167,7 @@ class Nmh:
     def __init__(self, ctx, vertices_dev, count=None, handle=None):
         self.ctx = ctx
         self.owned = handle is None
+        self.handle = None
         if handle is None:
             count = vertices_dev.numel() // 9 if count is None else count
             h = P()
@@ -254,6 +260,7 @@ class Scene:
     def __init__(self, ctx, sd):
         self.ctx = ctx
         self.data = sd
+        self.handle = None
         h = P()
         check(lib().aur_scene_create(ctx.handle, _ptr(sd.vertices), _ptr(sd.normals), _ptr(sd.shader_ids), sd.count,
                                      _ptr(sd.shaders), sd.shaders.shape[0], _ptr(sd.lights), sd.lights.shape[0],
@@ -358,6 +365,21 @@ def filter_pixels(ctx, W, H, in_dev, out_dev, region=None):
     check(lib().aur_filter_pixels(ctx.handle, W, H, _ptr(r), _ptr(in_dev), _ptr(out_dev)))
 
 
+def accum_save(ctx, path, accum_dev, samples_done, spp):
+    """Checkpoint of an (H, W, 4) device accumulation buffer."""
+    H, W = accum_dev.shape[:2]
+    check(lib().aur_accum_save(ctx.handle, os.fsencode(path), W, H, samples_done, spp, _ptr(accum_dev.contiguous())))
+
+
+def accum_load(ctx, path, accum_dev):
+    """Loads a checkpoint into an (H, W, 4) device buffer; returns (samples_done, spp)."""
+    H, W = accum_dev.shape[:2]
+    done, spp = ctypes.c_uint32(0), ctypes.c_uint32(0)
+    check(lib().aur_accum_load(ctx.handle, os.fsencode(path), W, H, ctypes.byref(done), ctypes.byref(spp),
+                               _ptr(accum_dev)))
+    return done.value, spp.value
+
+
 def clear_pixels(ctx, W, H, accum_dev):
     check(lib().aur_clear_pixels(ctx.handle, W, H, _ptr(accum_dev)))
 
@@ -402,6 +424,7 @@ class Batch:
 
     def __init__(self, ctx, scenes, params, tuning=None, cameras=None):
         self.ctx, self.scenes = ctx, list(scenes)
+        self.handle = None
         self._h, self._cams, self._prm = _batch_arrays(self.scenes, params, cameras)
         t = None if tuning is None else np.asarray(tuning, tuning_dtype).reshape(())
         h = P()
@@ -455,12 +478,59 @@ class Batch:
             pass
 
 
-def autotune(ctx, scenes, params, cameras=None):
-    """Runs the C-side autotuner; returns (tuning record, milliseconds of a 1-spp render)."""
-    h, cams, prm = _batch_arrays(list(scenes), params, cameras)
+def tuning_key(gpu_name, sm_count, scenes, params):
+    """Cache key of an autotuning result: the GPU and the batch's shape (per
+    scene: triangles, lights, frame size, spp, depth, mode)."""
+    shape = []
+    for sc, p in zip(scenes, params):
+        p = np.asarray(p, T.params_dtype).reshape(())
+        shape.append([int(sc.data.count), int(sc.data.lights.shape[0]), int(p["width"]), int(p["height"]),
+                      int(p["spp"]), int(p["max_depth"]), int(p["mode"])])
+    return json.dumps({"gpu": gpu_name, "sms": int(sm_count), "scenes": shape}, sort_keys=True)
+
+
+def tuning_cache_get(path, key):
+    """The cached tuning record for `key` in the JSON file `path`, or None."""
+    import json as _json
+    if not path or not os.path.exists(path):
+        return None
+    entry = _json.load(open(path)).get(key)
+    if entry is None:
+        return None
+    t = np.zeros((), tuning_dtype)
+    for k in tuning_dtype.names:
+        t[k] = entry["tuning"][k]
+    return t, float(entry["ms"])
+
+
+def tuning_cache_put(path, key, tuning, ms):
+    import json as _json
+    data = _json.load(open(path)) if os.path.exists(path) else {}
+    data[key] = {"tuning": {k: int(tuning[k]) for k in tuning_dtype.names}, "ms": float(ms)}
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        _json.dump(data, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
+def autotune(ctx, scenes, params, cameras=None, cache=None):
+    """Runs the C-side autotuner; returns (tuning record, milliseconds of a
+    1-spp render). With `cache` (a JSON file path), results are kept per GPU
+    and batch shape, and a hit skips the search."""
+    scenes = list(scenes)
+    key = None
+    if cache:
+        import torch
+        key = tuning_key(torch.cuda.get_device_name(ctx.device), ctx.sm_count(), scenes, params)
+        hit = tuning_cache_get(cache, key)
+        if hit is not None:
+            return hit
+    h, cams, prm = _batch_arrays(scenes, params, cameras)
     t = np.zeros((), tuning_dtype)
     ms = ctypes.c_float()
     check(lib().aur_batch_autotune(ctx.handle, h, _ptr(cams), _ptr(prm), len(scenes), _ptr(t), ctypes.byref(ms)))
+    if cache:
+        tuning_cache_put(cache, key, t, ms.value)
     return t, ms.value
 
 

@@ -1,10 +1,13 @@
 // abi.cu — contexts, errors, NMH and scene objects of the C ABI.
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "aur_integrate.cuh"
 #include "aur_internal.h"
@@ -33,6 +36,36 @@ aur_status cuda_fail(cudaError_t e, const char* what, const char* file, int line
 }
 
 void clear_error() { g_error[0] = 0; }
+
+namespace {
+// Allocation fault injection: 0 = off; k > 0 = the k-th allocation from now fails.
+std::atomic<uint32_t> g_fail_countdown{0};
+
+bool injected_failure() {
+    uint32_t k = g_fail_countdown.load();
+    while (k > 0)
+        if (g_fail_countdown.compare_exchange_weak(k, k - 1)) return k == 1;
+    return false;
+}
+}  // namespace
+
+cudaError_t alloc_device(void** p, size_t bytes) {
+    if (injected_failure()) { *p = nullptr; return cudaErrorMemoryAllocation; }
+    return cudaMalloc(p, bytes);
+}
+
+cudaError_t alloc_device_async(void** p, size_t bytes, cudaStream_t s) {
+    if (injected_failure()) { *p = nullptr; return cudaErrorMemoryAllocation; }
+    return cudaMallocAsync(p, bytes, s);
+}
+
+cudaError_t alloc_pinned(void** p, size_t bytes) {
+    if (injected_failure()) { *p = nullptr; return cudaErrorMemoryAllocation; }
+    return cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+}
+
+Range::Range(const char* name) { nvtxRangePushA(name); }
+Range::~Range() { nvtxRangePop(); }
 
 namespace {
 
@@ -110,24 +143,33 @@ aur_status aur_ctx_create(int device, aur_ctx** out) {
     aur_ctx* c = new aur_ctx();
     c->device = device;
     c->sm_count = prop.multiProcessorCount;
-    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->compute2, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc(&c->d_flags, 256) != cudaSuccess || cudaMemset(c->d_flags, 0, 256) != cudaSuccess) {
-        e = cudaGetLastError();
+    // keep the first failing call's own code (not the sticky last error)
+    e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->compute2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = ::aur::dev_malloc(&c->d_flags, 256);
+    if (e == cudaSuccess) e = cudaMemset(c->d_flags, 0, 256);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
         aur_ctx_destroy(c);
         return cuda_fail(e, "aur_ctx_create", __FILE__, __LINE__);
     }
     for (auto& ev : c->ev) {
-        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
-            e = cudaGetLastError();
+        e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
             aur_ctx_destroy(c);
             return cuda_fail(e, "aur_ctx_create events", __FILE__, __LINE__);
         }
     }
     c->stream = c->own_stream;
     *out = c;
+    return AUR_OK;
+}
+
+aur_status aur_debug_fail_allocation(uint32_t k) {
+    g_fail_countdown.store(k);
     return AUR_OK;
 }
 
@@ -182,6 +224,7 @@ aur_status aur_ctx_sm_count(aur_ctx* ctx, int* sm_count) {
 // ------------------------------------------------------------------ NMH
 
 aur_status aur_nmh_build(aur_ctx* ctx, const float* vertices, uint32_t count, aur_nmh** out) {
+    AUR_RANGE("aur_nmh_build");
     clear_error();
     return nmh_build_impl(ctx, vertices, count, out);
 }
@@ -216,6 +259,7 @@ aur_status aur_nmh_export(aur_ctx* ctx, const aur_nmh* nmh, uint32_t* perm, floa
 }
 
 aur_status aur_nmh_apply(aur_ctx* ctx, const aur_nmh* nmh, const void* src, uint32_t bytes_per_triangle, void* dst) {
+    AUR_RANGE("aur_nmh_apply");
     clear_error();
     AUR_CHECK(ctx && nmh, AUR_ERR_INVALID, "aur_nmh_apply: null context or NMH");
     AUR_CHECK(bytes_per_triangle > 0 && bytes_per_triangle % 2 == 0, AUR_ERR_INVALID,
@@ -244,8 +288,8 @@ aur_status aur_malloc(aur_ctx* ctx, size_t bytes, int policy, void** out) {
     }
     AUR_CUDA(cudaSetDevice(ctx->device));
     cudaError_t e;
-    if (policy == AUR_DEVICE_MEMORY) e = cudaMalloc(out, bytes);
-    else if (policy == AUR_PINNED_MEMORY) e = cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+    if (policy == AUR_DEVICE_MEMORY) e = ::aur::dev_malloc(out, bytes);
+    else if (policy == AUR_PINNED_MEMORY) e = alloc_pinned(out, bytes);
     else return fail(AUR_ERR_INVALID, "aur_malloc: unknown memory policy %d", policy);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -329,6 +373,7 @@ static uint32_t max_texture_id(const aur_shader* shaders, uint32_t n) {
 aur_status aur_scene_create(aur_ctx* ctx, const float* vertices, const float* normals, const uint16_t* shader_ids,
                             uint32_t count, const aur_shader* shaders, uint32_t num_shaders, const aur_light* lights,
                             uint32_t num_lights, aur_scene** out) {
+    AUR_RANGE("aur_scene_create");
     clear_error();
     AUR_CHECK(ctx && out, AUR_ERR_INVALID, "aur_scene_create: null context or output");
     AUR_CHECK(count == 0 || vertices, AUR_ERR_INVALID, "aur_scene_create: null vertices");
@@ -364,8 +409,8 @@ aur_status aur_scene_create(aur_ctx* ctx, const float* vertices, const float* no
     if (!shader_ids && count) { zeros.assign(count, 0); shader_ids = zeros.data(); }
     float* dv = nullptr; float* dn = nullptr; uint16_t* ds = nullptr;
     if (count) {
-        if (cudaMallocAsync(&dv, (size_t)count * 36, s) != cudaSuccess || cudaMallocAsync(&dn, (size_t)count * 36, s) != cudaSuccess ||
-            cudaMallocAsync(&ds, (size_t)count * 2, s) != cudaSuccess) {
+        if (::aur::dev_malloc_async(&dv, (size_t)count * 36, s) != cudaSuccess || ::aur::dev_malloc_async(&dn, (size_t)count * 36, s) != cudaSuccess ||
+            ::aur::dev_malloc_async(&ds, (size_t)count * 2, s) != cudaSuccess) {
             cudaGetLastError();
             cudaFreeAsync(dv, s); cudaFreeAsync(dn, s); cudaFreeAsync(ds, s);
             return bail(fail(AUR_ERR_OOM, "aur_scene_create: out of device memory"));
@@ -381,7 +426,7 @@ aur_status aur_scene_create(aur_ctx* ctx, const float* vertices, const float* no
     }
     const uint32_t N = sc->nmh->count;
     if (N) {
-        if (cudaMalloc(&sc->normals, (size_t)N * 36) != cudaSuccess || cudaMalloc(&sc->shader_ids, (size_t)N * 2) != cudaSuccess) {
+        if (::aur::dev_malloc(&sc->normals, (size_t)N * 36) != cudaSuccess || ::aur::dev_malloc(&sc->shader_ids, (size_t)N * 2) != cudaSuccess) {
             cudaGetLastError();
             cudaFreeAsync(dv, s); cudaFreeAsync(dn, s); cudaFreeAsync(ds, s);
             return bail(fail(AUR_ERR_OOM, "aur_scene_create: out of device memory"));
@@ -389,8 +434,8 @@ aur_status aur_scene_create(aur_ctx* ctx, const float* vertices, const float* no
         k_permute_attrs<<<(N + 255) / 256, 256, 0, s>>>(sc->nmh->perm, N, count, dn, ds, sc->normals, sc->shader_ids);
     }
     cudaFreeAsync(dv, s); cudaFreeAsync(dn, s); cudaFreeAsync(ds, s);
-    if (cudaMalloc(&sc->shaders, sizeof(aur_shader) * num_shaders) != cudaSuccess ||
-        (num_lights && cudaMalloc(&sc->lights, sizeof(aur_light) * num_lights) != cudaSuccess)) {
+    if (::aur::dev_malloc(&sc->shaders, sizeof(aur_shader) * num_shaders) != cudaSuccess ||
+        (num_lights && ::aur::dev_malloc(&sc->lights, sizeof(aur_light) * num_lights) != cudaSuccess)) {
         cudaGetLastError();
         return bail(fail(AUR_ERR_OOM, "aur_scene_create: out of device memory"));
     }
@@ -444,6 +489,7 @@ aur_status aur_scene_set_shaders(aur_ctx* ctx, aur_scene* sc, const aur_shader* 
 
 aur_status aur_scene_set_textures(aur_ctx* ctx, aur_scene* sc, const float* texcoords, const aur_texture* textures,
                                   uint32_t n) {
+    AUR_RANGE("aur_scene_set_textures");
     clear_error();
     AUR_CHECK(ctx && sc, AUR_ERR_INVALID, "aur_scene_set_textures: null argument");
     AUR_CHECK(n <= AUR_MAX_TEXTURES, AUR_ERR_INVALID, "aur_scene_set_textures: %u textures, at most %d", n,
@@ -461,8 +507,8 @@ aur_status aur_scene_set_textures(aur_ctx* ctx, aur_scene* sc, const float* texc
     const uint32_t N = sc->nmh->count;
     if (N) {
         float* staged = nullptr;
-        if (cudaMalloc(&sc->texcoords, (size_t)N * 24) != cudaSuccess ||
-            cudaMallocAsync(&staged, (size_t)count * 24, s) != cudaSuccess) {
+        if (::aur::dev_malloc(&sc->texcoords, (size_t)N * 24) != cudaSuccess ||
+            ::aur::dev_malloc_async(&staged, (size_t)count * 24, s) != cudaSuccess) {
             cudaGetLastError();
             free_textures(sc);
             return fail(AUR_ERR_OOM, "aur_scene_set_textures: out of device memory");
@@ -482,8 +528,8 @@ aur_status aur_scene_set_textures(aur_ctx* ctx, aur_scene* sc, const float* texc
         texels += (size_t)textures[i].width * textures[i].height;
         AUR_CHECK(texels < (1ull << 32), AUR_ERR_INVALID, "aur_scene_set_textures: more than 2^32 texels");
     }
-    if (cudaMalloc(&sc->tex_info, sizeof(info)) != cudaSuccess ||
-        (texels && cudaMalloc(&sc->texels, texels * sizeof(uchar4)) != cudaSuccess)) {
+    if (::aur::dev_malloc(&sc->tex_info, sizeof(info)) != cudaSuccess ||
+        (texels && ::aur::dev_malloc(&sc->texels, texels * sizeof(uchar4)) != cudaSuccess)) {
         cudaGetLastError();
         free_textures(sc);
         return fail(AUR_ERR_OOM, "aur_scene_set_textures: out of device memory");

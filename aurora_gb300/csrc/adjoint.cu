@@ -269,6 +269,7 @@ extern "C" {
 aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_camera* camera,
                               const aur_render_params* params, const float* d_image, float* d_diffuse,
                               float* d_light_color) {
+    AUR_RANGE("aur_render_adjoint");
     clear_error();
     AUR_CHECK(ctx && scene && camera && d_image && d_diffuse && (d_light_color || scene->num_lights == 0),
               AUR_ERR_INVALID, "aur_render_adjoint: null argument");
@@ -293,7 +294,7 @@ aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_ca
     const size_t smem_r = smem_p + 3 * kSharedLights * sizeof(float);
     AUR_CUDA(cudaFuncSetAttribute(k_adj_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
     float4* prim = nullptr;
-    AUR_CHECK(cudaMallocAsync(&prim, P * batch * sizeof(float4), ctx->stream) == cudaSuccess, AUR_ERR_OOM,
+    AUR_CHECK(::aur::dev_malloc_async(&prim, P * batch * sizeof(float4), ctx->stream) == cudaSuccess, AUR_ERR_OOM,
               "aur_render_adjoint: out of device memory");
     const SceneView sv = scene_view(scene);
     for (uint32_t s = s0; s < s1; s += batch) {

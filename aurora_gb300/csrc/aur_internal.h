@@ -25,6 +25,26 @@ void clear_error();
         if (!(cond)) return ::aur::fail((st), __VA_ARGS__);       \
     } while (0)
 
+// Every device and pinned allocation of the library goes through these, so
+// that tests can make the k-th one fail (aur_debug_fail_allocation) and check
+// each caller's out-of-memory path.
+cudaError_t alloc_device(void** p, size_t bytes);
+cudaError_t alloc_device_async(void** p, size_t bytes, cudaStream_t s);
+cudaError_t alloc_pinned(void** p, size_t bytes);
+template <typename T>
+inline cudaError_t dev_malloc(T** p, size_t bytes) { return alloc_device((void**)p, bytes); }
+template <typename T>
+inline cudaError_t dev_malloc_async(T** p, size_t bytes, cudaStream_t s) {
+    return alloc_device_async((void**)p, bytes, s);
+}
+
+// NVTX range over an entry point (a no-op unless a profiler is attached).
+struct Range {
+    explicit Range(const char* name);
+    ~Range();
+};
+#define AUR_RANGE(name) ::aur::Range aur_range_(name)
+
 // Grow-only device scratch owned by a context (stream-ordered allocation).
 struct Scratch {
     void* ptr = nullptr;

@@ -142,6 +142,7 @@ using namespace aur;
 extern "C" {
 
 aur_status aur_scene_emitters(aur_ctx* ctx, const aur_scene* sc, aur_emitter* emitters, uint32_t* num_emitters) {
+    AUR_RANGE("aur_scene_emitters");
     clear_error();
     AUR_CHECK(ctx && sc && num_emitters, AUR_ERR_INVALID, "aur_scene_emitters: null argument");
     *num_emitters = 0;
@@ -156,7 +157,7 @@ aur_status aur_scene_emitters(aur_ctx* ctx, const aur_scene* sc, aur_emitter* em
     const size_t o_ts = o_w + (((size_t)n * 8 + 255) & ~(size_t)255);
     const size_t bytes = o_ts + (size_t)(tiles + 1) * 8;
     char* scratch = nullptr;
-    AUR_CHECK(cudaMallocAsync((void**)&scratch, bytes, s) == cudaSuccess, AUR_ERR_OOM,
+    AUR_CHECK(::aur::dev_malloc_async((void**)&scratch, bytes, s) == cudaSuccess, AUR_ERR_OOM,
               "aur_scene_emitters: out of device memory");
     uint32_t* cnt = (uint32_t*)(scratch + o_cnt);
     double* w = (double*)(scratch + o_w);

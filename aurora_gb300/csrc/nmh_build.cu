@@ -644,9 +644,9 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
         cudaFree(nmh->verts);
         delete nmh;
     };
-    if (cudaMalloc(&nmh->node_recs, (size_t)n * kRecStride * sizeof(float4)) != cudaSuccess ||
-        cudaMalloc(&nmh->perm, (size_t)N * sizeof(uint32_t)) != cudaSuccess ||
-        cudaMalloc(&nmh->verts, (size_t)N * 9 * sizeof(float)) != cudaSuccess) {
+    if (::aur::dev_malloc(&nmh->node_recs, (size_t)n * kRecStride * sizeof(float4)) != cudaSuccess ||
+        ::aur::dev_malloc(&nmh->perm, (size_t)N * sizeof(uint32_t)) != cudaSuccess ||
+        ::aur::dev_malloc(&nmh->verts, (size_t)N * 9 * sizeof(float)) != cudaSuccess) {
         cudaGetLastError();
         cleanup();
         return fail(AUR_ERR_OOM, "aur_nmh_build: out of device memory for %u triangles", N);
@@ -669,7 +669,7 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
     const size_t o_tiles = take((size_t)2 * ntiles * sizeof(uint2));
     const size_t o_hist = take((size_t)3 * 256 * nb * 4), o_tot = take((size_t)3 * 256 * 4);
     char* base = nullptr;
-    if (cudaMallocAsync((void**)&base, off, st) != cudaSuccess) {
+    if (::aur::dev_malloc_async((void**)&base, off, st) != cudaSuccess) {
         cudaGetLastError();
         cleanup();
         return fail(AUR_ERR_OOM, "aur_nmh_build: out of device memory for %zu bytes of scratch", off);

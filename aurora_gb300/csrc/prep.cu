@@ -83,6 +83,7 @@ extern "C" {
 aur_status aur_transform(aur_ctx* ctx, const float* src_vertices, const float* src_normals, uint32_t count,
                          const aur_object_transform* transforms, uint32_t num_objects, float* dst_vertices,
                          float* dst_normals) {
+    AUR_RANGE("aur_transform");
     clear_error();
     AUR_CHECK(ctx, AUR_ERR_INVALID, "aur_transform: null context");
     AUR_CHECK(count == 0 || (src_vertices && src_normals && dst_vertices && dst_normals), AUR_ERR_INVALID,
@@ -94,7 +95,7 @@ aur_status aur_transform(aur_ctx* ctx, const float* src_vertices, const float* s
     if (count == 0 || num_objects == 0) return AUR_OK;
     AUR_CUDA(cudaSetDevice(ctx->device));
     aur_object_transform* dxf = nullptr;
-    AUR_CHECK(cudaMallocAsync(&dxf, sizeof(aur_object_transform) * num_objects, ctx->stream) == cudaSuccess, AUR_ERR_OOM,
+    AUR_CHECK(::aur::dev_malloc_async(&dxf, sizeof(aur_object_transform) * num_objects, ctx->stream) == cudaSuccess, AUR_ERR_OOM,
               "aur_transform: out of device memory");
     AUR_CUDA(cudaMemcpyAsync(dxf, transforms, sizeof(aur_object_transform) * num_objects, cudaMemcpyHostToDevice, ctx->stream));
     k_transform<<<(count + 255) / 256, 256, 0, ctx->stream>>>(src_vertices, src_normals, count, dxf, num_objects,
@@ -106,6 +107,7 @@ aur_status aur_transform(aur_ctx* ctx, const float* src_vertices, const float* s
 }
 
 aur_status aur_generate_tb(aur_ctx* ctx, const float* normals, uint32_t count, float* tangents, float* bitangents) {
+    AUR_RANGE("aur_generate_tb");
     clear_error();
     AUR_CHECK(ctx && (count == 0 || (normals && tangents && bitangents)), AUR_ERR_INVALID,
               "aur_generate_tb: null argument");

@@ -8,6 +8,9 @@
 // the samples to the frame in sample order — the same additions in the same
 // order as drawPixels, independent of the thread schedule.
 #include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
 
 #include "aur_integrate.cuh"
 #include "aur_internal.h"
@@ -24,6 +27,8 @@ constexpr int kRenderThreads = 128;
 constexpr int kRenderBlocksPerSm = 10;
 
 inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+const char kAccumMagic[8] = {'A', 'U', 'R', 'A', 'C', 'C', '1', '\0'};
 
 __device__ __forceinline__ StackRef stack_ref(uint32_t* smem, int cap) {
     StackRef s;
@@ -235,6 +240,7 @@ extern "C" {
 
 aur_status aur_render(aur_ctx* ctx, const aur_scene* scene, const aur_camera* camera, const aur_render_params* params,
                       float* accum) {
+    AUR_RANGE("aur_render");
     clear_error();
     AUR_CHECK(ctx && scene && camera && accum, AUR_ERR_INVALID, "aur_render: null argument");
     aur_status st = check_params(params);
@@ -247,7 +253,7 @@ aur_status aur_render(aur_ctx* ctx, const aur_scene* scene, const aur_camera* ca
     const uint64_t P = (uint64_t)p.width * p.height;
     const uint32_t batch = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(s1 - s0, (1ull << 24) / P));
     float4* colors = nullptr;
-    AUR_CHECK(cudaMallocAsync(&colors, P * batch * sizeof(float4), ctx->stream) == cudaSuccess, AUR_ERR_OOM,
+    AUR_CHECK(::aur::dev_malloc_async(&colors, P * batch * sizeof(float4), ctx->stream) == cudaSuccess, AUR_ERR_OOM,
               "aur_render: out of device memory");
     const int cap = stack_cap(scene);
     const size_t smem = (size_t)2 * cap * kRenderThreads * sizeof(uint32_t);
@@ -270,6 +276,7 @@ aur_status aur_render(aur_ctx* ctx, const aur_scene* scene, const aur_camera* ca
 
 aur_status aur_generate_rays(aur_ctx* ctx, uint32_t width, uint32_t height, uint32_t sample_id, uint32_t samples,
                              const aur_camera* camera, aur_path_ray* rays, aur_hitpoint* hits) {
+    AUR_RANGE("aur_generate_rays");
     AUR_CHECK(ctx && camera && rays && hits, AUR_ERR_INVALID, "aur_generate_rays: null argument");
     AUR_CHECK(width && height && samples >= 1 && sample_id < samples, AUR_ERR_INVALID,
               "aur_generate_rays: bad size or sample");
@@ -283,6 +290,7 @@ aur_status aur_generate_rays(aur_ctx* ctx, uint32_t width, uint32_t height, uint
 aur_status aur_raytrace_monte_carlo(aur_ctx* ctx, const aur_scene* scene, const aur_render_params* params,
                                     uint32_t sample_id, uint32_t offset, uint32_t num_rays, aur_path_ray* rays,
                                     aur_hitpoint* hits) {
+    AUR_RANGE("aur_raytrace_monte_carlo");
     AUR_CHECK(ctx && scene && params && rays && hits, AUR_ERR_INVALID, "aur_raytrace_monte_carlo: null argument");
     AUR_CHECK(params->max_depth <= AUR_MAX_DEPTH && params->mode <= AUR_MODE_PATH, AUR_ERR_INVALID,
               "aur_raytrace_monte_carlo: bad parameters");
@@ -304,6 +312,7 @@ aur_status aur_raytrace_monte_carlo(aur_ctx* ctx, const aur_scene* scene, const 
 
 aur_status aur_draw_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float weight, const aur_hitpoint* hits,
                            float* accum) {
+    AUR_RANGE("aur_draw_pixels");
     AUR_CHECK(ctx && hits && accum, AUR_ERR_INVALID, "aur_draw_pixels: null argument");
     AUR_CUDA(cudaSetDevice(ctx->device));
     const uint32_t P = width * height;
@@ -315,6 +324,7 @@ aur_status aur_draw_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float 
 
 aur_status aur_filter_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, const aur_rect* region, const float* in,
                              float* out) {
+    AUR_RANGE("aur_filter_pixels");
     clear_error();
     AUR_CHECK(ctx && in && out, AUR_ERR_INVALID, "aur_filter_pixels: null argument");
     AUR_CHECK(in != out, AUR_ERR_INVALID, "aur_filter_pixels: in and out must be distinct buffers");
@@ -332,6 +342,55 @@ aur_status aur_filter_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, cons
     k_filter_pixels<<<grid, block, 0, ctx->stream>>>(width, r, reinterpret_cast<const float4*>(in),
                                                     reinterpret_cast<float4*>(out));
     AUR_CUDA(cudaGetLastError());
+    return AUR_OK;
+}
+
+aur_status aur_accum_save(aur_ctx* ctx, const char* path, uint32_t width, uint32_t height, uint32_t samples_done,
+                          uint32_t spp, const float* accum) {
+    clear_error();
+    AUR_CHECK(ctx && path && accum, AUR_ERR_INVALID, "aur_accum_save: null argument");
+    AUR_CHECK(width && height && (uint64_t)width * height < (1ull << 31), AUR_ERR_INVALID,
+              "aur_accum_save: bad frame size %ux%u", width, height);
+    AUR_CHECK(samples_done <= spp, AUR_ERR_INVALID, "aur_accum_save: %u samples done of %u", samples_done, spp);
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    const size_t bytes = (size_t)width * height * sizeof(float4);
+    std::vector<unsigned char> host(bytes);
+    AUR_CUDA(cudaMemcpyAsync(host.data(), accum, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    FILE* f = std::fopen(path, "wb");
+    AUR_CHECK(f, AUR_ERR_INVALID, "aur_accum_save: cannot open %s for writing", path);
+    const uint32_t head[4] = {width, height, samples_done, spp};
+    const bool good = std::fwrite(kAccumMagic, 1, 8, f) == 8 && std::fwrite(head, 4, 4, f) == 4 &&
+                      std::fwrite(host.data(), 1, bytes, f) == bytes;
+    const bool closed = std::fclose(f) == 0;
+    AUR_CHECK(good && closed, AUR_ERR_INVALID, "aur_accum_save: write to %s failed", path);
+    return AUR_OK;
+}
+
+aur_status aur_accum_load(aur_ctx* ctx, const char* path, uint32_t width, uint32_t height, uint32_t* samples_done,
+                          uint32_t* spp, float* accum) {
+    clear_error();
+    AUR_CHECK(ctx && path && accum && samples_done && spp, AUR_ERR_INVALID, "aur_accum_load: null argument");
+    FILE* f = std::fopen(path, "rb");
+    AUR_CHECK(f, AUR_ERR_INVALID, "aur_accum_load: cannot open %s", path);
+    char magic[8];
+    uint32_t head[4];
+    const bool good = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kAccumMagic, 8) == 0 &&
+                      std::fread(head, 4, 4, f) == 4;
+    if (!good || head[0] != width || head[1] != height || head[2] > head[3]) {
+        std::fclose(f);
+        return fail(AUR_ERR_INVALID, "aur_accum_load: %s is not a %ux%u accumulation checkpoint", path, width, height);
+    }
+    const size_t bytes = (size_t)width * height * sizeof(float4);
+    std::vector<unsigned char> host(bytes);
+    const bool body = std::fread(host.data(), 1, bytes, f) == bytes;
+    std::fclose(f);
+    AUR_CHECK(body, AUR_ERR_INVALID, "aur_accum_load: %s is truncated", path);
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    AUR_CUDA(cudaMemcpyAsync(accum, host.data(), bytes, cudaMemcpyHostToDevice, ctx->stream));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    *samples_done = head[2];
+    *spp = head[3];
     return AUR_OK;
 }
 

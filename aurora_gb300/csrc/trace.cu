@@ -182,13 +182,13 @@ aur_status trace_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uin
         if (ctx->pipe[s].bytes < need_in) {
             cudaFree(ctx->pipe[s].ptr);
             ctx->pipe[s].ptr = nullptr; ctx->pipe[s].bytes = 0;
-            AUR_CHECK(cudaMalloc(&ctx->pipe[s].ptr, need_in) == cudaSuccess, AUR_ERR_OOM, "trace_host: out of memory");
+            AUR_CHECK(::aur::dev_malloc(&ctx->pipe[s].ptr, need_in) == cudaSuccess, AUR_ERR_OOM, "trace_host: out of memory");
             ctx->pipe[s].bytes = need_in;
         }
         if (ctx->out[s].bytes < need_out) {
             cudaFree(ctx->out[s].ptr);
             ctx->out[s].ptr = nullptr; ctx->out[s].bytes = 0;
-            AUR_CHECK(cudaMalloc(&ctx->out[s].ptr, need_out) == cudaSuccess, AUR_ERR_OOM, "trace_host: out of memory");
+            AUR_CHECK(::aur::dev_malloc(&ctx->out[s].ptr, need_out) == cudaSuccess, AUR_ERR_OOM, "trace_host: out of memory");
             ctx->out[s].bytes = need_out;
         }
     }
@@ -230,6 +230,7 @@ aur_status trace_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uin
 extern "C" {
 
 aur_status aur_trace_closest(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits) {
+    AUR_RANGE("aur_trace_closest");
     aur_status st = check_trace_args(ctx, nmh, rays, n, hits);
     if (st != AUR_OK) return st;
     AUR_CUDA(cudaSetDevice(ctx->device));
@@ -237,6 +238,7 @@ aur_status aur_trace_closest(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* ra
 }
 
 aur_status aur_trace_any(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, uint32_t* occluder) {
+    AUR_RANGE("aur_trace_any");
     aur_status st = check_trace_args(ctx, nmh, rays, n, occluder);
     if (st != AUR_OK) return st;
     AUR_CUDA(cudaSetDevice(ctx->device));
@@ -244,10 +246,12 @@ aur_status aur_trace_any(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, 
 }
 
 aur_status aur_trace_closest_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits) {
+    AUR_RANGE("aur_trace_closest_host");
     return trace_host(ctx, nmh, rays, n, hits, false);
 }
 
 aur_status aur_trace_any_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, uint32_t* occluder) {
+    AUR_RANGE("aur_trace_any_host");
     return trace_host(ctx, nmh, rays, n, occluder, true);
 }
 
@@ -261,7 +265,7 @@ aur_status count_work(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uin
     if (n == 0) return AUR_OK;
     void* scratch = nullptr;
     const size_t bytes = 256 + (size_t)n * sizeof(aur_hit);
-    AUR_CHECK(cudaMallocAsync(&scratch, bytes, ctx->stream) == cudaSuccess, AUR_ERR_OOM,
+    AUR_CHECK(::aur::dev_malloc_async(&scratch, bytes, ctx->stream) == cudaSuccess, AUR_ERR_OOM,
               "trace counters: out of memory");
     unsigned long long* cnt = (unsigned long long*)scratch;
     aur_hit* hits = (aur_hit*)((char*)scratch + 256);
@@ -281,6 +285,7 @@ aur_status count_work(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uin
 
 aur_status aur_trace_count_visits(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n,
                                   unsigned long long node_visits[2]) {
+    AUR_RANGE("aur_trace_count_visits");
     AUR_CHECK(node_visits, AUR_ERR_INVALID, "aur_trace_count_visits: null output");
     aur_status st = check_trace_args(ctx, nmh, rays, n, rays);
     if (st != AUR_OK) return st;
@@ -294,6 +299,7 @@ aur_status aur_trace_count_visits(aur_ctx* ctx, const aur_nmh* nmh, const aur_ra
 
 aur_status aur_trace_stats(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n,
                            aur_trace_work* closest, aur_trace_work* any) {
+    AUR_RANGE("aur_trace_stats");
     AUR_CHECK(closest && any, AUR_ERR_INVALID, "aur_trace_stats: null output");
     aur_status st = check_trace_args(ctx, nmh, rays, n, rays);
     if (st != AUR_OK) return st;

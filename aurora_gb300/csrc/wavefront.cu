@@ -617,6 +617,7 @@ extern "C" {
 aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const aur_camera* cameras,
                             const aur_render_params* params, uint32_t num_scenes, const aur_wavefront_tuning* tuning,
                             aur_batch** out) {
+    AUR_RANGE("aur_batch_create");
     clear_error();
     AUR_CHECK(ctx && scenes && cameras && params && out && num_scenes > 0, AUR_ERR_INVALID,
               "aur_batch_create: null argument or no scenes");
@@ -717,7 +718,7 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     const size_t o_fsh = take(16 * Q), o_emi = take(16 * Q), o_cj = take(16 * Q * M), o_vis = take(4 * Q);
     const size_t o_q0 = take(4 * Q), o_q1 = take(4 * Q), o_free = take(4 * Q);
     const size_t o_sho = take(16 * Q * M), o_shd = take(16 * Q * M), o_out = take(16 * out_items);
-    if (cudaMalloc(&bt->mem, off) != cudaSuccess) {
+    if (::aur::dev_malloc(&bt->mem, off) != cudaSuccess) {
         cudaGetLastError();
         batch_free(bt);
         return fail(AUR_ERR_OOM, "aur_batch_create: out of device memory (%zu bytes)", off);
@@ -756,10 +757,12 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     ctl.iter_limit = (uint32_t)std::min<uint64_t>(0x7FFFFFFFull, 4 * waves_of_pool * (p0.max_depth + 2) + 64);
     if (tn.max_iterations) ctl.iter_limit = tn.max_iterations;
     cudaMemcpy(a.ctl, &ctl, sizeof(ctl), cudaMemcpyHostToDevice);
-    if (cudaFuncSetAttribute(k_wf_extend, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem) != cudaSuccess ||
-        cudaFuncSetAttribute(k_wf_shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&bt->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
-        const cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaFuncSetAttribute(k_wf_extend, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_wf_shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&bt->cap_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
         batch_free(bt);
         return cuda_fail(e, "aur_batch_create set-up", __FILE__, __LINE__);
     }
@@ -774,6 +777,7 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
 }
 
 aur_status aur_batch_render(aur_ctx* ctx, aur_batch* bt, float* const* accum) {
+    AUR_RANGE("aur_batch_render");
     clear_error();
     AUR_CHECK(ctx && bt && accum, AUR_ERR_INVALID, "aur_batch_render: null argument");
     AUR_CHECK(ctx->device == bt->device, AUR_ERR_INVALID, "aur_batch_render: batch lives on another device");
@@ -898,6 +902,7 @@ aur_status aur_batch_profile(aur_ctx* ctx, aur_batch* bt, float* const* accum, f
 aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, const aur_camera* cameras,
                               const aur_render_params* params, uint32_t num_scenes, aur_wavefront_tuning* best,
                               float* best_ms) {
+    AUR_RANGE("aur_batch_autotune");
     clear_error();
     AUR_CHECK(ctx && scenes && cameras && params && best && num_scenes > 0, AUR_ERR_INVALID,
               "aur_batch_autotune: null argument");
@@ -908,7 +913,7 @@ aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, cons
     size_t pixels = 0;
     for (uint32_t i = 0; i < num_scenes; ++i) pixels += (size_t)p1[i].width * p1[i].height;
     float4* frames = nullptr;
-    AUR_CHECK(cudaMalloc(&frames, pixels * sizeof(float4)) == cudaSuccess, AUR_ERR_OOM, "aur_batch_autotune: out of memory");
+    AUR_CHECK(::aur::dev_malloc(&frames, pixels * sizeof(float4)) == cudaSuccess, AUR_ERR_OOM, "aur_batch_autotune: out of memory");
     std::vector<float*> acc(num_scenes);
     for (uint32_t i = 0, o = 0; i < num_scenes; o += p1[i].width * p1[i].height, ++i) acc[i] = (float*)(frames + o);
     // Larger pools mean fewer, fuller iterations: on the 64-scene sphere batch

@@ -50,6 +50,12 @@ const char* aur_last_error(void);
 /* Library version string. */
 const char* aur_version(void);
 
+/* Fault injection for tests of the out-of-memory paths: the k-th device or
+ * pinned allocation the library makes from now on (any thread, any context)
+ * fails as out of memory, after which injection is off again; k = 0 turns it
+ * off. No counterpart in the reference, which checks few of its allocations. */
+aur_status aur_debug_fail_allocation(uint32_t k);
+
 /* ------------------------------------------------------------ shared types */
 
 typedef struct aur_float3 { float x, y, z; } aur_float3;
@@ -394,6 +400,20 @@ aur_status aur_draw_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float 
                            const aur_hitpoint* hits, float* accum);
 /* Renderer::clearPixels (core/renderer.cpp:33-36). */
 aur_status aur_clear_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, float* accum);
+
+/* Checkpoints of an accumulation buffer (no counterpart in the reference,
+ * whose accumulation lives only in device memory). aur_accum_save writes the
+ * width*height float4 pixels of `accum` (device) with the frame's spp and the
+ * number of samples already added (samples_done) to `path`: 8-byte magic
+ * "AURACC1\0", uint32 width, height, samples_done, spp, then the pixels,
+ * little-endian. aur_accum_load reads such a file into `accum` (device) after
+ * checking its size, and returns samples_done and spp. The counter-based RNG
+ * makes a resumed render (sample_begin = samples_done) equal the
+ * uninterrupted one bit for bit. */
+aur_status aur_accum_save(aur_ctx* ctx, const char* path, uint32_t width, uint32_t height, uint32_t samples_done,
+                          uint32_t spp, const float* accum);
+aur_status aur_accum_load(aur_ctx* ctx, const char* path, uint32_t width, uint32_t height, uint32_t* samples_done,
+                          uint32_t* spp, float* accum);
 
 /* A pixel rectangle, bounds inclusive (Rect, util/math.h:283-313). */
 typedef struct aur_rect {
