@@ -42,12 +42,16 @@ __device__ __forceinline__ f3 box_inv(const f3& d) {
                1.0f / copysignf(fmaxf(fabsf(d.z), 1e-30f), d.z));
 }
 
-// Conservative ray/box overlap over (0, tlimit].
-__device__ __forceinline__ bool box_hit(float lx, float ly, float lz, float hx, float hy, float hz, const f3& pos,
+// Conservative ray/box overlap over (0, tlimit]. poi = pos * inv per axis, so
+// each slab distance is one fused multiply-add, (lo * inv - poi); its
+// rounding, like that of (lo - pos) * inv, is far inside the box padding and
+// the t margins, and a NaN (an overflowing poi with a 1e-30 component) can
+// only drop an axis from the test, never prune.
+__device__ __forceinline__ bool box_hit(float lx, float ly, float lz, float hx, float hy, float hz, const f3& poi,
                                         const f3& inv, float tlimit) {
-    const float x0 = (lx - pos.x) * inv.x, x1 = (hx - pos.x) * inv.x;
-    const float y0 = (ly - pos.y) * inv.y, y1 = (hy - pos.y) * inv.y;
-    const float z0 = (lz - pos.z) * inv.z, z1 = (hz - pos.z) * inv.z;
+    const float x0 = __fmaf_rn(lx, inv.x, -poi.x), x1 = __fmaf_rn(hx, inv.x, -poi.x);
+    const float y0 = __fmaf_rn(ly, inv.y, -poi.y), y1 = __fmaf_rn(hy, inv.y, -poi.y);
+    const float z0 = __fmaf_rn(lz, inv.z, -poi.z), z1 = __fmaf_rn(hz, inv.z, -poi.z);
     const float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), 0.0f));
     const float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), tlimit));
     return tn * kBoxNear <= tf * kBoxFar;
@@ -142,10 +146,11 @@ __device__ __forceinline__ void trav_descend(TravState& s, const float4* __restr
     bool h1 = c1 < nodes, h2 = c1 + 1 < nodes;
     if (kBoxes && h1) {
         const Sector s3 = ld_sector(recs + (size_t)s.k * kRecStride + 6);
+        const f3 poi = mk3(pos.x * inv.x, pos.y * inv.y, pos.z * inv.z);
         const float4& b1 = s3.a;
         const float4& b2 = s3.b;
-        h1 = box_hit(q5.x, q5.y, q5.z, q5.w, b1.x, b1.y, pos, inv, tlimit);
-        if (h2) h2 = box_hit(b1.z, b1.w, b2.x, b2.y, b2.z, b2.w, pos, inv, tlimit);
+        h1 = box_hit(q5.x, q5.y, q5.z, q5.w, b1.x, b1.y, poi, inv, tlimit);
+        if (h2) h2 = box_hit(b1.z, b1.w, b2.x, b2.y, b2.z, b2.w, poi, inv, tlimit);
     }
     const bool near_ok = neg ? h2 : h1;
     const bool far_ok = neg ? h1 : h2;
