@@ -54,6 +54,7 @@ def lib():
         L.orc_texfetch.argtypes = [P, P, U32, P]
         L.orc_filter_pixels.argtypes = [U32, P, P, P]
         L.orc_emitters.argtypes = [P, P, U32, P, P]
+        L.orc_draw2.argtypes = [U32, U32, U32, U32, U32, U32, P]
         L.orc_emitters.restype = U32
         _lib = L
     return _lib
@@ -70,6 +71,8 @@ def ref_lib():
         L = ctypes.CDLL(REF_SO)
         L.ref_trace_closest.argtypes = [P, U32, P, U32, P, P]
         L.ref_trace_any.argtypes = [P, U32, P, U32, P]
+        L.ref_uniform_order.restype = ctypes.c_int
+        L.ref_shade_hits.argtypes = [P, P, P, P, P, U32, P, U32, P, U32, P, P, P, U32, P, U32, P]
         _ref = L
     return _ref
 
@@ -252,6 +255,32 @@ def ref_trace_closest(V_nmh, rays):
     tuv = np.zeros((rays.shape[0], 3), np.float32); ids = np.zeros(rays.shape[0], np.int32)
     L.ref_trace_closest(_ptr(V), V.shape[0], _ptr(rays), rays.shape[0], _ptr(tuv), _ptr(ids))
     return tuv, ids
+
+
+def draw2(seed, scene, pixel, sample, ray, slot):
+    """The integrators' two uniforms at one counter-RNG slot."""
+    out = np.zeros(2, np.float32)
+    lib().orc_draw2(seed, scene, pixel, sample, ray, slot, _ptr(out))
+    return float(out[0]), float(out[1])
+
+
+def ref_uniform_order():
+    """0 if the reference's area-light sample scales e1 by the first uniform drawn, 1 if by the second."""
+    return ref_lib().ref_uniform_order()
+
+
+def ref_shade_hits(nscene, tangents, bitangents, rays8, tri, tuv, uniforms):
+    """Li at camera-ray hits through the reference's own shading code (raytrace()'s light loop)."""
+    n = rays8.shape[0]
+    u = np.ascontiguousarray(uniforms, np.float32).reshape(n, -1)
+    out = np.zeros((n, 3), np.float32)
+    ref_lib().ref_shade_hits(_ptr(nscene.V), _ptr(nscene.N), _ptr(np.ascontiguousarray(tangents, np.float32)),
+                             _ptr(np.ascontiguousarray(bitangents, np.float32)), _ptr(nscene.S), nscene.V.shape[0],
+                             _ptr(nscene.shaders), nscene.shaders.shape[0], _ptr(nscene.lights),
+                             nscene.lights.shape[0], _ptr(np.ascontiguousarray(rays8, np.float32)),
+                             _ptr(np.ascontiguousarray(tri, np.int32)), _ptr(np.ascontiguousarray(tuv, np.float32)),
+                             n, _ptr(u), u.shape[1], _ptr(out))
+    return out
 
 
 def ref_trace_any(V_nmh, rays):

@@ -937,6 +937,15 @@ uint32_t orc_emitters(const float* V, const uint16_t* S, uint32_t count, const a
     return m;
 }
 
+/* The two uniforms the integrators draw at one RNG slot (draw2): u1, u2. */
+void orc_draw2(uint32_t seed, uint32_t scene, uint32_t pixel, uint32_t sample, uint32_t ray, uint32_t slot,
+               float* out2) {
+    RngKey k;
+    k.seed = seed;
+    k.scene = scene;
+    draw2(k, pixel, sample, ray, slot, out2[0], out2[1]);
+}
+
 /* The texture fetch alone: rgb[3i..] = texFetch(t, uv[2i], uv[2i+1]). */
 void orc_texfetch(const aur_texture* t, const float* uv, uint32_t n, float* rgb) {
     for (uint32_t i = 0; i < n; ++i) {

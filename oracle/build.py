@@ -37,11 +37,13 @@ def build_ref(reference=None, force=False):
     ref = reference or os.environ.get("AURORA_REFERENCE", "/root/reference")
     if not os.path.isdir(os.path.join(ref, "src")):
         return None
-    src = os.path.join(HERE, "ref_shim", "ref_traverse.cpp")
-    if force or _stale(REF_SO, [src, __file__]):
+    srcs = [os.path.join(HERE, "ref_shim", "ref_traverse.cpp"), os.path.join(HERE, "ref_shim", "ref_shade.cpp")]
+    if force or _stale(REF_SO, srcs + [__file__]):
         os.makedirs(os.path.dirname(REF_SO), exist_ok=True)
-        subprocess.check_call(["g++", *FLAGS, "-w", "-I" + os.path.join(HERE, "ref_shim"),
-                               "-I" + os.path.join(ref, "src"), src, "-o", REF_SO])
+        # -fpermissive: util/bsdf.h declares a member with an extra class qualification, which MSVC accepts
+        subprocess.check_call(["g++", *FLAGS, "-w", "-fpermissive", "-I" + os.path.join(HERE, "ref_shim"),
+                               "-I" + os.path.join(ref, "src"), "-I" + os.path.join(HERE, "..", "include"),
+                               *srcs, "-o", REF_SO])
     return REF_SO
 
 
