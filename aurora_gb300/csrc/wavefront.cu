@@ -31,6 +31,10 @@ namespace aur {
 namespace {
 
 constexpr int kMaxLightSlots = 32;
+// WfCtl::error bits: 1 = iteration limit reached, 2 = a path needed more
+// light samples than the batch was sized for (aur_scene_set_lights after
+// aur_batch_create).
+constexpr uint32_t kWfErrLightSlots = 2u;
 // Largest block of the stage kernels: the traversal and shading stages are
 // compiled for it with at most 64 registers (4 blocks of 256 per SM), which
 // measured faster than their unconstrained 70-72 registers.
@@ -322,6 +326,10 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
             const aur_light& L = sc.lights[li];
             const uint32_t ns = L.type == AUR_LIGHT_AREA ? (uint32_t)L.samples : 1u;
             for (uint32_t j = 0; j < ns; ++j, ++q) {
+                if (q >= a.M) {   // lights given more samples since the batch was created
+                    atomicOr(&c->error, kWfErrLightSlots);
+                    break;
+                }
                 f3 wdir;
                 float wt, pdf;
                 const uint32_t lslot = L.type == AUR_LIGHT_AREA ? light_slot(li, j) : 0u;
@@ -438,14 +446,14 @@ __global__ void k_wf_combine(WfArgs a) {
             const aur_light& L = sc.lights[li];
             if (L.type == AUR_LIGHT_AMBIENT) Li = Li + f * ((from(L.color) * L.intensity) * L.ambient);
             if (L.type != AUR_LIGHT_AREA) {
-                const float4 v = cj[q];
+                const float4 v = q < a.M ? cj[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 if (v.w != 0.0f && ((vis >> q) & 1u)) Li = Li + mk3(v.x, v.y, v.z);
                 ++q;
             } else {
                 f3 acc = mk3(0.0f);
                 for (int32_t j = 0; j < L.samples; ++j, ++q) {
                     f3 Ls = mk3(0.0f);
-                    const float4 v = cj[q];
+                    const float4 v = q < a.M ? cj[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     if (v.w != 0.0f && ((vis >> q) & 1u)) Ls = Ls + mk3(v.x, v.y, v.z);
                     acc = acc + Ls;
                 }
@@ -803,8 +811,11 @@ aur_status aur_batch_status(aur_ctx* ctx, aur_batch* bt, uint32_t* iterations) {
     AUR_CUDA(cudaMemcpyAsync(&c, bt->args.ctl, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
     AUR_CUDA(cudaStreamSynchronize(ctx->stream));
     if (iterations) *iterations = c.total_iters;
+    AUR_CHECK(!(c.error & kWfErrLightSlots), AUR_ERR_INVALID,
+              "wavefront render stopped: a scene's lights now take more samples per hit than when the batch "
+              "was created; create the batch again");
     AUR_CHECK(c.error == 0, AUR_ERR_TIMEOUT,
-              "wavefront render stopped: iteration limit %u reached or traversal stack overflow (flags 0x%x)",
+              "wavefront render stopped: iteration limit %u reached (flags 0x%x)",
               c.iter_limit, c.error);
     AUR_CHECK(c.wave == c.num_waves, AUR_ERR_TIMEOUT, "wavefront render ended after %u of %u waves", c.wave,
               c.num_waves);

@@ -461,7 +461,12 @@ typedef struct aur_batch aur_batch;
  * frame with a host loop (render/monteCarloRaytracer.cpp:81-120); each scene's
  * frame equals aur_render's with the same parameters (same estimator, same
  * RNG streams keyed by params[i].scene_id). params[i] may differ in width,
- * height and scene_id only. Materials must be non-specular. */
+ * height and scene_id only. Materials must be non-specular. The batch reads
+ * the scenes' device data in place: each scene must outlive the batch, and
+ * its textures must not be replaced (aur_scene_set_textures) while the batch
+ * exists. Shaders and lights may be updated between renders, but the batch is
+ * sized for the light samples per hit at creation: a render after lights
+ * gained samples stops, and aur_batch_status reports AUR_ERR_INVALID. */
 aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const aur_camera* cameras,
                             const aur_render_params* params, uint32_t num_scenes,
                             const aur_wavefront_tuning* tuning, aur_batch** out);

@@ -87,3 +87,30 @@ def test_tuning_is_validated(ctx):
         with pytest.raises(api.AuroraError):
             api.Batch(ctx, [sc], p, tuning=api.make_tuning(**bad))
     api.Batch(ctx, [sc], p, tuning=api.make_tuning(block_size=256)).close()
+
+
+def test_lights_with_more_samples_after_creation_stop_the_render(ctx):
+    """The batch is sized for the light samples per hit at creation; a scene
+    whose lights gain samples afterwards must stop the render with an error
+    (no out-of-range writes), and the batch renders again once they are back."""
+    import torch
+    sd = scenes.cornell()
+    sc = api.Scene(ctx, sd)
+    p = [T.render_params(16, 16, 2, 2, mode=T.MODE_PATH)]
+    b = api.Batch(ctx, [sc], p, tuning=api.make_tuning(2048, 1, 128, 2))
+    ref = [torch.zeros((16, 16, 4), device="cuda")]
+    b.render(ref)
+    b.status()
+    more = sd.lights.copy()
+    more["samples"] = 4
+    sc.set_lights(more)
+    f = [torch.zeros((16, 16, 4), device="cuda")]
+    b.render(f)
+    with pytest.raises(api.AuroraError) as e:
+        b.status()
+    assert e.value.status == 1 and "samples" in str(e.value)
+    sc.set_lights(sd.lights)
+    f = [torch.zeros((16, 16, 4), device="cuda")]
+    b.render(f)
+    b.status()
+    assert torch.equal(f[0], ref[0])
