@@ -61,10 +61,10 @@ def parse():
                     help="only the large terrain workload (plain vs wavefront, RMSE against 16384 spp)")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling cases only)")
     ap.add_argument("--profile", nargs="?", const="trace", default=None,
-                    choices=["trace", "render", "wavefront", "adjoint", "build"],
+                    choices=["trace", "render", "wavefront", "adjoint", "build", "filter"],
                     help="small profiling case: trace = one closest-hit and one any-hit launch; render = Cornell "
                          "+ sphere frames; wavefront = stepped 8-scene batch; adjoint = one adjoint; "
-                         "build = NMH build of the 1M-triangle soup")
+                         "build = NMH build of the 1M-triangle soup; filter = pixel filter of a 3840x2160 frame")
     return ap.parse_args()
 
 
@@ -128,6 +128,14 @@ def run_profile(args):
         sc.adjoint(p, img.contiguous())
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": "adjoint"}))
+        return
+    if args.profile == "filter":
+        src = torch.rand((2160, 3840, 4), device="cuda")
+        out = torch.empty_like(src)
+        for _ in range(2):
+            api.filter_pixels(ctx, 3840, 2160, src, out)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "filter"}))
         return
     if args.profile == "build":
         V, _ = workload(16)
