@@ -62,6 +62,7 @@ SIGNATURES = {
     "aur_scene_set_textures": ([P, P, P, P, U32], ctypes.c_int),
     "aur_scene_texfetch": ([P, P, U32, P, U32, P], ctypes.c_int),
     "aur_scene_emitters": ([P, P, P, P], ctypes.c_int),
+    "aur_scene_mis_table": ([P, P, P, P, P, P], ctypes.c_int),
     "aur_camera_make": None,  # struct-by-value arguments; not bound
     "aur_render": ([P, P, P, P, P], ctypes.c_int),
     "aur_generate_rays": ([P, U32, U32, U32, U32, P, P, P], ctypes.c_int),
@@ -295,6 +296,18 @@ class Scene:
         m = ctypes.c_uint32(0)
         check(lib().aur_scene_emitters(self.ctx.handle, self.handle, _ptr(buf), ctypes.byref(m)))
         return buf[:m.value * T.emitter_dtype.itemsize].cpu().numpy().view(T.emitter_dtype)
+
+    def mis_table(self):
+        """The light-selection table of AUR_MODE_PATH_MIS as numpy arrays
+        (triangles, cdf, pa per NMH triangle)."""
+        n = self.nmh.info()[0]
+        tri = np.zeros(max(1, n), np.uint32)
+        cdf = np.zeros(max(1, n), np.float32)
+        pa = np.zeros(max(1, n), np.float32)
+        m = ctypes.c_uint32(0)
+        check(lib().aur_scene_mis_table(self.ctx.handle, self.handle, _ptr(tri), _ptr(cdf), _ptr(pa),
+                                        ctypes.byref(m)))
+        return tri[:m.value].copy(), cdf[:m.value].copy(), pa[:n].copy()
 
     def texfetch(self, texture, uv_dev):
         """RGB of texture `texture` (1-based) at n device (u, v) pairs."""

@@ -459,6 +459,7 @@ aur_status aur_scene_destroy(aur_scene* sc) {
     cudaFree(sc->shader_ids);
     cudaFree(sc->shaders);
     cudaFree(sc->lights);
+    free_mis_table(sc);
     free_textures(sc);
     aur_nmh_destroy(sc->nmh);
     delete sc;
@@ -484,6 +485,7 @@ aur_status aur_scene_set_shaders(aur_ctx* ctx, aur_scene* sc, const aur_shader* 
     for (uint32_t i = 0; i < n; ++i)
         sc->has_specular |= shaders[i].reflectivity > 0.0f || shaders[i].translucence > 0.0f;
     sc->max_texture = max_texture_id(shaders, n);
+    free_mis_table(sc);   // emission may have changed
     return AUR_OK;
 }
 

@@ -276,6 +276,8 @@ aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_ca
     aur_status st = check_params(params);
     if (st == AUR_OK) st = check_scene_textures(scene);
     if (st != AUR_OK) return st;
+    AUR_CHECK(params->mode != AUR_MODE_PATH_MIS, AUR_ERR_UNSUPPORTED,
+              "aur_render_adjoint: differentiates AUR_MODE_REFERENCE and AUR_MODE_PATH renders");
     AUR_CUDA(cudaSetDevice(ctx->device));
     {
         std::vector<aur_shader> sh(scene->num_shaders);

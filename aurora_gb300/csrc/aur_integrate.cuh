@@ -26,6 +26,12 @@ struct SceneView {
     const float* texcoords;    // NMH order, 6 floats per triangle (null without textures)
     const uchar4* texels;      // RGBA8 texels of all textures
     const uint4* tex_info;     // per texture: first texel, width, height
+    // AUR_MODE_PATH_MIS only:
+    const float* verts;        // NMH order, 9 floats per triangle (x1 x2 x3 y1 y2 y3 z1 z2 z3)
+    const uint32_t* mis_tri;   // light-selection table: NMH positions of the sampled emitters
+    const float* mis_cdf;      //   and their CDF (inclusive, normalised)
+    const float* mis_pa;       // per NMH triangle: selection probability / area (0 if not in the table)
+    uint32_t mis_count;
 };
 
 SceneView scene_view(const aur_scene* sc);
@@ -73,6 +79,7 @@ struct PathRay {
     f3 pos, dir;
     float weight, eta;
     f3 thr;
+    float pdf;   // AUR_MODE_PATH_MIS: solid-angle density of the diffuse bounce that made the ray, 0 otherwise
 };
 
 struct Bsdf { f3 N, S, T, color1; };
@@ -157,12 +164,221 @@ struct SampleResult {
     f3 last_pos, last_wo;
 };
 
+// ------------------------------------------------------------------- MIS
+// AUR_MODE_PATH_MIS: path mode with physically based direct lighting and
+// multiple importance sampling (Veach & Guibas, SIGGRAPH 1995), the half of
+// estimateDirectRadiance the reference compiles out (radiance.cuh:55-71).
+// * Area lights keep the reference's emission model, radiance
+//   Light::L(w) = colour * intensity * max(0, direction . w) (light.cuh:18-22),
+//   and are estimated by both strategies of estimateDirectRadiance: a point
+//   sampled on the quad (density t^2 / (cos_l * area) in solid angle, where
+//   the reference's Light::pdf returns 1 / |cos_l|, light.cuh:78-89) and a
+//   direction sampled from the BSDF (BSDF::samplef, bsdf.cuh:53-67) traced to
+//   the quad (Light::visibleArea, light.cuh:62-76), each weighted by the power
+//   heuristic against the other's density.
+// * Emissive triangles (shader emission > 0, emission colour at the hit as in
+//   raytrace()) are sampled once per hit from a table with probability
+//   proportional to emission * area; the emission a diffuse bounce finds is
+//   weighted against that density, and the sampled one against the bounce's.
+//   A hit from which no diffuse bounce follows gives its sample full weight.
+
+// Slots of the counter RNG: the BSDF half of light i's j-th sample, and the
+// two draws of the emitter sample (light indices < 32767).
+__host__ __device__ __forceinline__ uint32_t bsdf_light_slot(uint32_t light, uint32_t j) {
+    return light_slot(light, j) | 0x80000000u;
+}
+constexpr uint32_t kSlotEmitter = 0xFFFFFFF0u;
+
+// Power heuristic with exponent 2 (powerHeuristic, sampling.cuh:162-169) as
+// 1 / (1 + (p_other / p_this)^2), which does not overflow for large densities.
+__device__ __forceinline__ float mis_weight(float p_this, float p_other) {
+    const float r = p_other / p_this;
+    return 1.0f / (1.0f + r * r);
+}
+
+// BSDF::pdf (bsdf.cuh:22-30, 48-51): |cos| / pi on wo's side.
+__device__ __forceinline__ float bsdf_pdf(const Bsdf& b, const f3& wo, const f3& wi) {
+    const f3 lwo = world_to_local(wo, b.N, b.S, b.T);
+    const f3 lwi = world_to_local(wi, b.N, b.S, b.T);
+    return (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
+}
+
+// BSDF::samplef (bsdf.cuh:53-67): the direction and its density.
+__device__ __forceinline__ f3 bsdf_sample(const Bsdf& b, const f3& wo, float u1, float u2, float& pdf) {
+    const f3 lwo = world_to_local(wo, b.N, b.S, b.T);
+    f3 lwi = sample_hemisphere_cosine(u1, u2);
+    if (lwo.z < 0.0f) lwi.z *= -1.0f;
+    pdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
+    return local_to_world(lwi, b.N, b.S, b.T);
+}
+
+// Distance t > Epsilon along dir from pos to the parallelogram
+// p0 + a e1 + b e2 (a, b in [0, 1]), either face.
+__device__ __forceinline__ bool hit_quad(const f3& pos, const f3& dir, const f3& p0, const f3& e1, const f3& e2,
+                                         float& t) {
+    const f3 P = cross(dir, e2);
+    const float det = dot(e1, P);
+    if (det == 0.0f) return false;
+    const float inv = 1.0f / det;
+    const f3 T = pos - p0;
+    const float a = dot(T, P) * inv;
+    if (!(a >= 0.0f && a <= 1.0f)) return false;
+    const f3 Q = cross(T, e1);
+    const float b = dot(dir, Q) * inv;
+    if (!(b >= 0.0f && b <= 1.0f)) return false;
+    t = dot(e2, Q) * inv;
+    return t > kEpsilon;
+}
+
+__device__ __forceinline__ void tri_verts(const float* __restrict__ V, uint32_t tri, f3& v1, f3& v2, f3& v3) {
+    const float* v = V + (size_t)tri * 9;
+    v1 = mk3(v[0], v[3], v[6]);
+    v2 = mk3(v[1], v[4], v[7]);
+    v3 = mk3(v[2], v[5], v[8]);
+}
+
+// Cosine at an emitter seen along dir, as the culling test of the traversal
+// sees it: the Moller-Trumbore determinant e1 . (dir x e2) (ray.cuh:198-223)
+// over |e1 x e2|. Below Epsilon / |e1 x e2| the traversal cannot hit it.
+__device__ __forceinline__ float emitter_det(const f3& v1, const f3& v2, const f3& v3, const f3& dir, float& len) {
+    const f3 e1 = v2 - v1, e2 = v3 - v1;
+    len = length(cross(e1, e2));
+    return dot(e1, cross(dir, e2));
+}
+
+// Weight of the emission a ray found at triangle `tri` after travelling t
+// along dir from a diffuse bounce of density prev_pdf (0: camera or
+// specular ray, full weight).
+__device__ __forceinline__ float emission_weight(const SceneView& sc, uint32_t tri, const f3& dir, float t,
+                                                 float prev_pdf) {
+    if (!(prev_pdf > 0.0f)) return 1.0f;
+    const float pa = __ldg(sc.mis_pa + tri);
+    if (!(pa > 0.0f)) return 1.0f;
+    f3 v1, v2, v3;
+    tri_verts(sc.verts, tri, v1, v2, v3);
+    float len;
+    const float det = emitter_det(v1, v2, v3, dir, len);
+    const float epdf = (pa * (t * t)) / (det / len);
+    return mis_weight(prev_pdf, epdf);
+}
+
+// One area light, both strategies, averaged over its samples.
+__device__ __forceinline__ f3 area_light_mis(const SceneView& sc, const aur_light& L, uint32_t li, const Bsdf& b,
+                                             const f3& position, const f3& wo, uint32_t seed, uint32_t scene,
+                                             uint32_t pixel, uint32_t sample, uint32_t rix, const StackRef& stk,
+                                             uint32_t& visits, uint32_t* err) {
+    const f3 p0 = from(L.position), e1 = from(L.e1), e2 = from(L.e2), ldir = from(L.direction);
+    const f3 Le0 = from(L.color) * L.intensity;
+    const float area = length(cross(e1, e2));
+    const f3 f = bsdf_f(b);
+    f3 acc = mk3(0.0f);
+    if (area > 0.0f && !zero(f)) {
+        for (int32_t j = 0; j < L.samples; ++j) {
+            f3 Ls = mk3(0.0f);
+            float u1, u2, du = 0.0f, dv = 0.0f;
+            // light strategy
+            draw2(seed, scene, pixel, sample, rix, light_slot(li, (uint32_t)j), u1, u2);
+            const f3 P = p0 + ((e1 * u1) + (e2 * u2));
+            f3 wdir = P - position;
+            const float wt = length(wdir);
+            wdir = wdir / wt;
+            float cl = dot(ldir, -wdir);
+            float cs = fmaxf(0.0f, dot(wdir, b.N));
+            if (cl > 0.0f && cs > 0.0f) {
+                f3 wpos = position;
+                wpos.x += kEpsilon * wdir.x;
+                wpos.y += kEpsilon * wdir.y;
+                wpos.z += kEpsilon * wdir.z;
+                float tt = wt + kEpsilon;
+                if (traverse<true>(sc.recs, sc.nodes, sc.perm, wpos, wdir, tt, du, dv, stk, visits, err) == kNoPrim) {
+                    const float lpdf = (wt * wt) / (cl * area);
+                    const float w = mis_weight(lpdf, bsdf_pdf(b, wo, wdir));
+                    Ls = Ls + f * (Le0 * cl) * ((cs * w) / lpdf);
+                }
+            }
+            // BSDF strategy
+            draw2(seed, scene, pixel, sample, rix, bsdf_light_slot(li, (uint32_t)j), u1, u2);
+            float bpdf, tl;
+            const f3 wi = bsdf_sample(b, wo, u1, u2, bpdf);
+            if (bpdf > 0.0f && hit_quad(position, wi, p0, e1, e2, tl)) {
+                cl = dot(ldir, -wi);
+                cs = fmaxf(0.0f, dot(wi, b.N));
+                if (cl > 0.0f && cs > 0.0f) {
+                    f3 wpos = position;
+                    wpos.x += kEpsilon * wi.x;
+                    wpos.y += kEpsilon * wi.y;
+                    wpos.z += kEpsilon * wi.z;
+                    float tt = tl + kEpsilon;
+                    if (traverse<true>(sc.recs, sc.nodes, sc.perm, wpos, wi, tt, du, dv, stk, visits, err) ==
+                        kNoPrim) {
+                        const float lpdf = (tl * tl) / (cl * area);
+                        const float w = mis_weight(bpdf, lpdf);
+                        Ls = Ls + f * (Le0 * cl) * ((cs * w) / bpdf);
+                    }
+                }
+            }
+            acc = acc + Ls;
+        }
+    }
+    const float ns = (float)L.samples;
+    return mk3(acc.x / ns, acc.y / ns, acc.z / ns);
+}
+
+// One emitter sample: a table entry by its CDF, a uniform point on the
+// triangle (square-root parameterisation), a shadow ray that stops short of
+// the emitter.
+__device__ __forceinline__ f3 emitter_sample(const SceneView& sc, const Bsdf& b, const f3& position, const f3& wo,
+                                             bool bounce, uint32_t seed, uint32_t scene, uint32_t pixel,
+                                             uint32_t sample, uint32_t rix, const StackRef& stk, uint32_t& visits,
+                                             uint32_t* err) {
+    const f3 f = bsdf_f(b);
+    if (sc.mis_count == 0 || zero(f)) return mk3(0.0f);
+    float us, ua, ub, uc;
+    draw2(seed, scene, pixel, sample, rix, kSlotEmitter, us, ua);
+    draw2(seed, scene, pixel, sample, rix, kSlotEmitter + 1u, ub, uc);
+    uint32_t lo = 0, hi = sc.mis_count - 1;   // first entry with cdf >= us
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(sc.mis_cdf + mid) >= us) hi = mid; else lo = mid + 1;
+    }
+    const uint32_t tri = __ldg(sc.mis_tri + lo);
+    f3 v1, v2, v3;
+    tri_verts(sc.verts, tri, v1, v2, v3);
+    const float su = sqrtf(ua);
+    const f3 P = ((v1 * (1.0f - su)) + (v2 * (su * (1.0f - ub)))) + (v3 * (su * ub));
+    f3 wdir = P - position;
+    const float t = length(wdir);
+    if (!(t > kEpsilon)) return mk3(0.0f);
+    wdir = wdir / t;
+    float len;
+    const float det = emitter_det(v1, v2, v3, wdir, len);
+    const float cs = fmaxf(0.0f, dot(wdir, b.N));
+    if (det < kEpsilon || !(cs > 0.0f)) return mk3(0.0f);
+    f3 wpos = position;
+    wpos.x += kEpsilon * wdir.x;
+    wpos.y += kEpsilon * wdir.y;
+    wpos.z += kEpsilon * wdir.z;
+    float tt = t * 0.9999f;
+    float du = 0.0f, dv = 0.0f;
+    if (traverse<true>(sc.recs, sc.nodes, sc.perm, wpos, wdir, tt, du, dv, stk, visits, err) != kNoPrim)
+        return mk3(0.0f);
+    const float epdf = (__ldg(sc.mis_pa + tri) * (t * t)) / (det / len);
+    const float w = bounce ? mis_weight(epdf, bsdf_pdf(b, wo, wdir)) : 1.0f;
+    const uint32_t sid = sc.sids[tri];
+    const aur_shader* sh = sc.shaders + (sid > 0 ? sid - 1 : 0);
+    return f * from(sh->emission_color) * ((cs * w) / epdf);
+}
+
 // Li at a hit: emission + ambient + direct light of every light, in the
 // reference's order (monteCarloRaytracer.cu:42-52, radiance.cuh:13-80).
+// kMis: emission weighted by ew, area lights by area_light_mis, plus one
+// emitter sample; `bounce` says whether a diffuse bounce follows this hit.
+template <bool kMis>
 __device__ __forceinline__ f3 direct_light(const SceneView& sc, const aur_shader* sh, const Bsdf& b, const f3& position,
-                                           uint32_t seed, uint32_t scene, uint32_t pixel, uint32_t sample,
-                                           uint32_t rix, const StackRef& stk, uint32_t& visits, uint32_t* err) {
-    f3 Li = from(sh->emission_color);
+                                           const f3& wo, float ew, bool bounce, uint32_t seed, uint32_t scene,
+                                           uint32_t pixel, uint32_t sample, uint32_t rix, const StackRef& stk,
+                                           uint32_t& visits, uint32_t* err) {
+    f3 Li = kMis ? from(sh->emission_color) * ew : from(sh->emission_color);
     for (uint32_t i = 0; i < sc.num_lights; ++i) {
         const aur_light& L = sc.lights[i];
         if (L.type == AUR_LIGHT_AMBIENT) Li = Li + bsdf_f(b) * ((from(L.color) * L.intensity) * L.ambient);
@@ -177,6 +393,8 @@ __device__ __forceinline__ f3 direct_light(const SceneView& sc, const aur_shader
                     traverse<true>(sc.recs, sc.nodes, sc.perm, position, wdir, wt, du, dv, stk, visits, err) == kNoPrim)
                     Li = Li + f * Ls * fmaxf(0.0f, dot(wdir, b.N));
             }
+        } else if (kMis) {
+            Li = Li + area_light_mis(sc, L, i, b, position, wo, seed, scene, pixel, sample, rix, stk, visits, err);
         } else {
             // estimateDirectRadiance (radiance.cuh:35-80), light-sampling half
             f3 acc = mk3(0.0f);
@@ -204,6 +422,7 @@ __device__ __forceinline__ f3 direct_light(const SceneView& sc, const aur_shader
             Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
         }
     }
+    if (kMis) Li = Li + emitter_sample(sc, b, position, wo, bounce, seed, scene, pixel, sample, rix, stk, visits, err);
     return Li;
 }
 
@@ -211,13 +430,13 @@ __device__ __forceinline__ f3 direct_light(const SceneView& sc, const aur_shader
 // throughput f * |wi.N| / pdf. Returns false when the path ends here.
 __device__ __forceinline__ bool diffuse_bounce(const Bsdf& b, const f3& wo, const f3& thr, uint32_t seed,
                                                uint32_t scene, uint32_t pixel, uint32_t sample, uint32_t rix, f3& wi,
-                                               f3& nthr) {
+                                               f3& nthr, float& pdf) {
     float u1, u2;
     draw2(seed, scene, pixel, sample, rix, 0u, u1, u2);
     const f3 lwo = world_to_local(wo, b.N, b.S, b.T);
     f3 lwi = sample_hemisphere_cosine(u1, u2);
     if (lwo.z < 0.0f) lwi.z *= -1.0f;
-    const float pdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
+    pdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
     const f3 f = bsdf_f(b);
     wi = local_to_world(lwi, b.N, b.S, b.T);
     if (pdf > 0.0f && !zero(f)) {
@@ -228,7 +447,8 @@ __device__ __forceinline__ bool diffuse_bounce(const Bsdf& b, const f3& wo, cons
 }
 
 // Integrates one camera ray. RNG key: (seed, scene_id) x (pixel, sample,
-// ray index within the sample, slot).
+// ray index within the sample, slot). kMis: mode is AUR_MODE_PATH_MIS.
+template <bool kMis = false>
 __device__ __forceinline__ SampleResult integrate(const SceneView& sc, uint32_t max_depth, uint32_t mode,
                                                   uint32_t seed, uint32_t scene, uint32_t pixel, uint32_t sample,
                                                   const PathRay& primary, const StackRef& stk, uint32_t& visits,
@@ -245,6 +465,7 @@ __device__ __forceinline__ SampleResult integrate(const SceneView& sc, uint32_t 
     res.last_pos = res.last_wo = mk3(0.0f);
     uint32_t ray_index = 0;
     const int maxd = (int)max_depth;
+    const bool path = kMis || mode == AUR_MODE_PATH;
     while (depth <= maxd && sp > 0) {
         PathRay ray = stack[--sp];
         const uint32_t rix = ray_index++;
@@ -259,8 +480,10 @@ __device__ __forceinline__ SampleResult integrate(const SceneView& sc, uint32_t 
         const aur_shader* sh = sc.shaders + (sid > 0 ? sid - 1 : 0);   // getSafeID (util/array.h:16-17)
         const float refl = sh->reflectivity, trans = sh->translucence;
         const Bsdf b = get_bsdf(sc, sh, tri, u, v);
-        const f3 Li = direct_light(sc, sh, b, position, seed, scene, pixel, sample, rix, stk, visits, err);
         const bool specular = refl > 0.0f || trans > 0.0f;
+        const float ew = kMis ? emission_weight(sc, tri, ray.dir, t, ray.pdf) : 1.0f;
+        const f3 Li = direct_light<kMis>(sc, sh, b, position, wo, ew, !specular && depth + 1 <= maxd, seed, scene,
+                                         pixel, sample, rix, stk, visits, err);
         if (specular) depth++;
         if (depth <= maxd && refl > 0.0f) {
             PathRay nr;
@@ -268,9 +491,10 @@ __device__ __forceinline__ SampleResult integrate(const SceneView& sc, uint32_t 
             nr.dir = reflect(ray.dir, b.N);
             nr.weight = refl;
             nr.eta = ray.eta;
-            nr.thr = mode == AUR_MODE_PATH ? ray.thr * refl : mk3(nr.weight);
+            nr.thr = path ? ray.thr * refl : mk3(nr.weight);
+            nr.pdf = 0.0f;
             ray.weight *= (1.0f - refl);
-            ray.thr = mode == AUR_MODE_PATH ? ray.thr * (1.0f - refl) : mk3(ray.weight);
+            ray.thr = path ? ray.thr * (1.0f - refl) : mk3(ray.weight);
             if (sp < AUR_MAX_DEPTH + 2) stack[sp++] = nr; else atomicOr(err, 2u);
         }
         if (depth <= maxd && trans > 0.0f) {
@@ -284,20 +508,21 @@ __device__ __forceinline__ SampleResult integrate(const SceneView& sc, uint32_t 
                 nr.dir = tdir;
                 nr.weight = trans;
                 nr.eta = etat;
-                nr.thr = mode == AUR_MODE_PATH ? ray.thr * trans : mk3(nr.weight);
+                nr.thr = path ? ray.thr * trans : mk3(nr.weight);
+                nr.pdf = 0.0f;
                 ray.weight *= (1.0f - trans);
-                ray.thr = mode == AUR_MODE_PATH ? ray.thr * (1.0f - trans) : mk3(ray.weight);
+                ray.thr = path ? ray.thr * (1.0f - trans) : mk3(ray.weight);
                 if (sp < AUR_MAX_DEPTH + 2) stack[sp++] = nr; else atomicOr(err, 2u);
             }
         }
-        if (mode == AUR_MODE_PATH && !specular) {
+        if (path && !specular) {
             depth++;
             if (depth <= maxd) {
                 PathRay nr;
                 nr.pos = position;
                 nr.weight = 1.0f;
                 nr.eta = ray.eta;
-                if (diffuse_bounce(b, wo, ray.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr)) {
+                if (diffuse_bounce(b, wo, ray.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr, nr.pdf)) {
                     if (sp < AUR_MAX_DEPTH + 2) stack[sp++] = nr; else atomicOr(err, 2u);
                 }
             }
@@ -310,6 +535,7 @@ __device__ __forceinline__ SampleResult integrate(const SceneView& sc, uint32_t 
 // The same estimator for scenes without specular shaders: one ray in flight
 // per sample, no ray stack (a Lambert hit spawns at most the diffuse bounce).
 // Same operations in the same order as integrate().
+template <bool kMis = false>
 __device__ __forceinline__ SampleResult integrate_diffuse(const SceneView& sc, uint32_t max_depth, uint32_t mode,
                                                           uint32_t seed, uint32_t scene, uint32_t pixel,
                                                           uint32_t sample, const PathRay& primary, const StackRef& stk,
@@ -321,6 +547,8 @@ __device__ __forceinline__ SampleResult integrate_diffuse(const SceneView& sc, u
     res.last_u = res.last_v = 0.0f;
     res.last_pos = res.last_wo = mk3(0.0f);
     f3 pos = primary.pos, dir = primary.dir, thr = primary.thr;
+    float prev_pdf = 0.0f;
+    const bool path = kMis || mode == AUR_MODE_PATH;
     uint32_t depth = 0;
     for (uint32_t rix = 0;; ++rix) {
         float t = kInfinity, u = 0.0f, v = 0.0f;
@@ -333,15 +561,19 @@ __device__ __forceinline__ SampleResult integrate_diffuse(const SceneView& sc, u
         const uint32_t sid = sc.sids[tri];
         const aur_shader* sh = sc.shaders + (sid > 0 ? sid - 1 : 0);
         const Bsdf b = get_bsdf(sc, sh, tri, u, v);
-        const f3 Li = direct_light(sc, sh, b, position, seed, scene, pixel, sample, rix, stk, visits, err);
+        const float ew = kMis ? emission_weight(sc, tri, dir, t, prev_pdf) : 1.0f;
+        const f3 Li = direct_light<kMis>(sc, sh, b, position, wo, ew, depth + 1 <= max_depth, seed, scene, pixel,
+                                         sample, rix, stk, visits, err);
         res.color = res.color + Li * thr;
-        if (mode != AUR_MODE_PATH) break;
+        if (!path) break;
         if (++depth > max_depth) break;
         f3 wi, nthr;
-        if (!diffuse_bounce(b, wo, thr, seed, scene, pixel, sample, rix, wi, nthr)) break;
+        float bpdf;
+        if (!diffuse_bounce(b, wo, thr, seed, scene, pixel, sample, rix, wi, nthr, bpdf)) break;
         pos = position;
         dir = wi;
         thr = nthr;
+        prev_pdf = bpdf;
     }
     return res;
 }
@@ -367,6 +599,7 @@ __device__ __forceinline__ PathRay camera_ray(const aur_camera& cam, uint32_t W,
     r.weight = 1.0f;
     r.eta = 1.0f;
     r.thr = mk3(1.0f);
+    r.pdf = 0.0f;
     r.dir = normalize(px * from(cam.right) * cam.tanfov_x + py * from(cam.up) * cam.tanfov_y + from(cam.forward));
     return r;
 }

@@ -98,12 +98,23 @@ struct aur_scene {
     uint32_t num_textures = 0;
     uchar4* texels = nullptr;         // all textures' RGBA8 texels, row-major, one after another
     uint4* tex_info = nullptr;        // per texture: first texel, width, height
+    // Light-selection table of AUR_MODE_PATH_MIS, built by the first render
+    // that needs it and dropped when the shaders change.
+    mutable bool mis_ready = false;
+    mutable uint32_t mis_count = 0;
+    mutable uint32_t* mis_tri = nullptr;   // mis_count NMH positions
+    mutable float* mis_cdf = nullptr;      // mis_count
+    mutable float* mis_pa = nullptr;       // count: selection probability / area per NMH triangle
 };
 
 namespace aur {
 
 aur_status nmh_build_impl(aur_ctx* ctx, const float* vertices, uint32_t count, aur_nmh** out);
 aur_status check_params(const aur_render_params* p);
+// Builds the scene's light-selection table for AUR_MODE_PATH_MIS if it is
+// not built (stream-synchronous); free_mis_table drops it.
+aur_status build_mis_table(aur_ctx* ctx, const aur_scene* sc);
+void free_mis_table(const aur_scene* sc);
 // Every texture the scene's shaders name exists (and texcoords were given).
 aur_status check_scene_textures(const aur_scene* sc);
 // ray_counter: the persistent kernel's work counter (default d_flags[8]);

@@ -40,8 +40,9 @@ __device__ __forceinline__ StackRef stack_ref(uint32_t* smem, int cap) {
 }
 
 // colors[b * P + p] = (rgb, hit) of sample s0 + b at pixel p. kGeneric
-// selects the integrator with the specular ray stack.
-template <bool kGeneric>
+// selects the integrator with the specular ray stack, kMis the
+// AUR_MODE_PATH_MIS estimator.
+template <bool kGeneric, bool kMis>
 __global__ void __launch_bounds__(kRenderThreads, kRenderBlocksPerSm) k_render_samples(SceneView sc, aur_camera cam, aur_render_params p,
                                                                    uint32_t s0, uint32_t nb, float4* __restrict__ colors,
                                                                    uint32_t* __restrict__ err, int cap) {
@@ -55,8 +56,8 @@ __global__ void __launch_bounds__(kRenderThreads, kRenderBlocksPerSm) k_render_s
     const PathRay r = camera_ray(cam, p.width, p.height, pix % p.width, pix / p.width, s, p.spp);
     uint32_t visits = 0;
     const SampleResult res =
-        kGeneric ? integrate(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err)
-                 : integrate_diffuse(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err);
+        kGeneric ? integrate<kMis>(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err)
+                 : integrate_diffuse<kMis>(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err);
     colors[t] = make_float4(res.color.x, res.color.y, res.color.z, res.any_hit ? 1.0f : 0.0f);
 }
 
@@ -114,6 +115,7 @@ __global__ void __launch_bounds__(kRenderThreads) k_raytrace_mc(SceneView sc, au
     r.weight = in.weight;
     r.eta = in.eta;
     r.thr = mk3(in.weight);
+    r.pdf = 0.0f;
     uint32_t visits = 0;
     const SampleResult res =
         kGeneric ? integrate(sc, p.max_depth, p.mode, p.seed, p.scene_id, id, sample, r, stk, visits, err)
@@ -205,6 +207,11 @@ SceneView scene_view(const aur_scene* sc) {
     v.texcoords = sc->texcoords;
     v.texels = sc->texels;
     v.tex_info = sc->tex_info;
+    v.verts = sc->nmh->verts;
+    v.mis_tri = sc->mis_tri;
+    v.mis_cdf = sc->mis_cdf;
+    v.mis_pa = sc->mis_pa;
+    v.mis_count = sc->mis_count;
     return v;
 }
 
@@ -222,8 +229,8 @@ aur_status check_params(const aur_render_params* p) {
     AUR_CHECK(p->spp >= 1 && p->spp <= 65535, AUR_ERR_INVALID, "render: spp %u outside [1, 65535]", p->spp);
     AUR_CHECK(p->max_depth <= AUR_MAX_DEPTH, AUR_ERR_INVALID, "render: max_depth %u > %u", p->max_depth,
               AUR_MAX_DEPTH);
-    AUR_CHECK(p->mode == AUR_MODE_REFERENCE || p->mode == AUR_MODE_PATH, AUR_ERR_INVALID, "render: unknown mode %u",
-              p->mode);
+    AUR_CHECK(p->mode == AUR_MODE_REFERENCE || p->mode == AUR_MODE_PATH || p->mode == AUR_MODE_PATH_MIS,
+              AUR_ERR_INVALID, "render: unknown mode %u", p->mode);
     const uint32_t end = p->sample_end ? p->sample_end : p->spp;
     AUR_CHECK(p->sample_begin <= end && end <= p->spp, AUR_ERR_INVALID, "render: sample range [%u, %u) outside spp %u",
               p->sample_begin, end, p->spp);
@@ -246,7 +253,14 @@ aur_status aur_render(aur_ctx* ctx, const aur_scene* scene, const aur_camera* ca
     aur_status st = check_params(params);
     if (st == AUR_OK) st = check_scene_textures(scene);
     if (st != AUR_OK) return st;
+    const bool mis = params->mode == AUR_MODE_PATH_MIS;
+    AUR_CHECK(!mis || scene->num_lights < 32767, AUR_ERR_INVALID,
+              "aur_render: AUR_MODE_PATH_MIS takes at most 32766 lights (scene has %u)", scene->num_lights);
     AUR_CUDA(cudaSetDevice(ctx->device));
+    if (mis) {
+        st = build_mis_table(ctx, scene);
+        if (st != AUR_OK) return st;
+    }
     const aur_render_params p = *params;
     const uint32_t s0 = p.sample_begin, s1 = p.sample_end ? p.sample_end : p.spp;
     if (s1 == s0) return AUR_OK;
@@ -261,12 +275,22 @@ aur_status aur_render(aur_ctx* ctx, const aur_scene* scene, const aur_camera* ca
     const float weight = 1.0f / (float)p.spp;
     for (uint32_t s = s0; s < s1; s += batch) {
         const uint32_t nb = std::min(batch, s1 - s);
-        if (scene->has_specular)
-            k_render_samples<true><<<cdiv(P * nb, kRenderThreads), kRenderThreads, smem, ctx->stream>>>(
-                sv, *camera, p, s, nb, colors, ctx->d_flags, cap);
-        else
-            k_render_samples<false><<<cdiv(P * nb, kRenderThreads), kRenderThreads, smem, ctx->stream>>>(
-                sv, *camera, p, s, nb, colors, ctx->d_flags, cap);
+        const dim3 grid(cdiv(P * nb, kRenderThreads));
+        if (scene->has_specular) {
+            if (mis)
+                k_render_samples<true, true><<<grid, kRenderThreads, smem, ctx->stream>>>(sv, *camera, p, s, nb,
+                                                                                      colors, ctx->d_flags, cap);
+            else
+                k_render_samples<true, false><<<grid, kRenderThreads, smem, ctx->stream>>>(sv, *camera, p, s, nb,
+                                                                                       colors, ctx->d_flags, cap);
+        } else {
+            if (mis)
+                k_render_samples<false, true><<<grid, kRenderThreads, smem, ctx->stream>>>(sv, *camera, p, s, nb,
+                                                                                       colors, ctx->d_flags, cap);
+            else
+                k_render_samples<false, false><<<grid, kRenderThreads, smem, ctx->stream>>>(sv, *camera, p, s, nb,
+                                                                                        colors, ctx->d_flags, cap);
+        }
         k_accumulate<<<cdiv(P, 256), 256, 0, ctx->stream>>>(colors, (uint32_t)P, nb, weight, (float4*)accum);
     }
     cudaFreeAsync(colors, ctx->stream);

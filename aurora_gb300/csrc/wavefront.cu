@@ -632,6 +632,9 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     const aur_render_params& p0 = params[0];
     aur_status st = check_params(&p0);
     if (st != AUR_OK) return st;
+    AUR_CHECK(p0.mode != AUR_MODE_PATH_MIS, AUR_ERR_UNSUPPORTED,
+              "aur_batch_create: the wavefront batch renders AUR_MODE_REFERENCE and AUR_MODE_PATH (AUR_MODE_PATH_MIS "
+              "renders with aur_render)");
     uint64_t P_tot = 0;
     uint32_t M = 1, cap = 2;
     std::vector<WfScene> table(num_scenes);

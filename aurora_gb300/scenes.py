@@ -229,6 +229,32 @@ def cornell():
                      np.stack([cornell_light()]), cornell_camera())
 
 
+def cornell_emissive(area_light=False):
+    """The Cornell box lit by emissive geometry instead of an area light: a
+    0.3 x 0.3 quad under the ceiling (emission colour 12, weight 1), a small
+    glowing block on the floor (orange, weight 0.5) and, last, one emissive
+    triangle on the back wall, which makes the count odd so that the even
+    padding duplicates an emitter. `area_light` adds the Cornell area light."""
+    p1, p2, p3, sids = _cornell_parts()
+    P1, P2, P3, S = [p1], [p2], [p3], [sids]
+    q = _quad((0.35, 0.998, 0.35), (0.65, 0.998, 0.35), (0.65, 0.998, 0.65), (0.35, 0.998, 0.65), (0, -1, 0))
+    P1.append(q[0]); P2.append(q[1]); P3.append(q[2]); S.append(np.full(2, 4, np.uint16))
+    b = _box((0.82, 0.04, 0.2), (0.1, 0.08, 0.1), 30.0)
+    P1.append(b[0]); P2.append(b[1]); P3.append(b[2]); S.append(np.full(12, 5, np.uint16))
+    t = _orient(np.array([[0.1, 0.7, 0.001]]), np.array([[0.25, 0.7, 0.001]]), np.array([[0.17, 0.85, 0.001]]),
+                np.array([[0.0, 0.0, 1.0]]))
+    P1.append(t[0]); P2.append(t[1]); P3.append(t[2]); S.append(np.full(1, 6, np.uint16))
+    p1, p2, p3 = np.concatenate(P1), np.concatenate(P2), np.concatenate(P3)
+    fn = face_normals(p1, p2, p3)
+    lamp = T.lambert(WHITE, emission=(12.0, 12.0, 12.0)); lamp["emission"] = 1.0
+    glow = T.lambert((0.9, 0.5, 0.2), emission=(3.0, 1.6, 0.6)); glow["emission"] = 0.5
+    spot = T.lambert(WHITE, emission=(2.0, 4.0, 6.0)); spot["emission"] = 2.0
+    shaders = np.stack([T.lambert(WHITE), T.lambert(RED), T.lambert(GREEN), lamp, glow, spot])
+    lights = np.stack([cornell_light(intensity=1.5)]) if area_light else np.zeros(0, T.light_dtype)
+    return SceneData("cornell_emissive", tris_to_soa(p1, p2, p3), normals_to_aos(fn, fn, fn), np.concatenate(S),
+                     shaders, lights, cornell_camera())
+
+
 def planar_texcoords(vertices, scale=1.0):
     """Per-triangle texcoords (n, 6) = (u1 v1 u2 v2 u3 v3): each triangle's
     corners projected onto the two axes orthogonal to its dominant normal

@@ -52,7 +52,7 @@ class texture_ctype(ctypes.Structure):
 
 
 NO_HIT = 0xFFFFFFFF
-MODE_REFERENCE, MODE_PATH = 0, 1
+MODE_REFERENCE, MODE_PATH, MODE_PATH_MIS = 0, 1, 2
 SHADER_LAMBERT, SHADER_PHONG = 0, 1
 LIGHT_AMBIENT, LIGHT_POINT, LIGHT_DIRECTIONAL, LIGHT_AREA = 0, 1, 2, 3
 

@@ -383,6 +383,44 @@ def bench_cornell(ctx, cpu=True, textured=False):
     return out
 
 
+def bench_mis(ctx, size=256, spp=16, depth=3, ref_renders=256):
+    """AUR_MODE_PATH_MIS on the Cornell box lit by emissive geometry (a
+    ceiling lamp, a glowing block, a small wall emitter): samples/s of MIS at
+    depth d and of path mode at depth d + 1 (the same set of paths), the RMSE
+    of one spp-sample render of each against the mean of `ref_renders`
+    independent MIS renders of the same sub-pixel grid, and the efficiency
+    gain (rmse_path^2 * t_path) / (rmse_mis^2 * t_mis): how much less time
+    MIS needs for the same error."""
+    import torch
+    from aurora_gb300 import api, scenes, types as T
+    sc = api.Scene(ctx, scenes.cornell_emissive())
+    acc = None
+    for s in range(ref_renders):
+        acc = sc.render(T.render_params(size, size, spp, depth, seed=1000 + s, mode=T.MODE_PATH_MIS), accum=acc)
+    ref = (acc / ref_renders).cpu().numpy()[..., :3].astype(np.float64)
+    stream = torch.cuda.current_stream()
+    out = {"workload": "Cornell box lit by 15 emissive triangles, %dx%d, %d spp; MIS at depth %d vs path mode "
+                       "at depth %d" % (size, size, spp, depth, depth + 1)}
+    for name, mode, d in (("mis", T.MODE_PATH_MIS, depth), ("path", T.MODE_PATH, depth + 1)):
+        p = T.render_params(size, size, spp, d, seed=0, mode=mode)
+        sc.render(p)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 5
+        e0.record(stream)
+        for _ in range(reps):
+            img = sc.render(p)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        err = img.cpu().numpy()[..., :3].astype(np.float64) - ref
+        out[name + "_ms"] = ms
+        out[name + "_samples_per_s"] = size * size * spp / (ms * 1e-3)
+        out[name + "_rmse"] = float(np.sqrt(np.mean(err * err)))
+    out["efficiency_vs_path"] = (out["path_rmse"] ** 2 * out["path_ms"]) / (out["mis_rmse"] ** 2 * out["mis_ms"])
+    return out
+
+
 def bench_filter(ctx, width=3840, height=2160, reps=20):
     """aur_filter_pixels on a 3840x2160 float4 frame (133 MB in, 133 MB out,
     both larger than L2): algorithmic bytes 16 B read + 16 B written per pixel
@@ -723,6 +761,7 @@ def main():
         out["cornell_plain"] = bench_cornell(ctx, cpu=rank == 0 and not args.no_cpu_baseline)
         out["cornell_textured"] = bench_cornell(ctx, cpu=rank == 0 and not args.no_cpu_baseline, textured=True)
         out["filter_pixels"] = bench_filter(ctx)
+        out["mis"] = bench_mis(ctx)
         out["batched_wavefront"] = bench_batched(ctx)
         out["adjoint"] = bench_adjoint(ctx)
     if rank == 0:

@@ -125,8 +125,17 @@ typedef struct aur_camera {
  *    each hit, specular reflection/refraction rays, no diffuse bounce.
  *  AUR_MODE_PATH: the same, plus a cosine-sampled diffuse bounce
  *    (BSDF::samplef, kernels/lib/bsdf.cuh:222-236) at every non-specular hit
- *    while depth <= max_depth, with RGB path throughput. */
-enum { AUR_MODE_REFERENCE = 0, AUR_MODE_PATH = 1 };
+ *    while depth <= max_depth, with RGB path throughput.
+ *  AUR_MODE_PATH_MIS: path mode with physically based direct lighting and
+ *    multiple importance sampling (power heuristic): area lights by both
+ *    halves of estimateDirectRadiance (kernels/lib/radiance.cuh:41-71, the
+ *    BSDF half compiled out in the reference) with solid-angle densities and
+ *    the reference's emission model Light::L (light.cuh:18-22); emissive
+ *    triangles sampled from a table proportional to emission * area, their
+ *    emission found by diffuse bounces weighted against it. Images differ
+ *    from the other modes by design (the reference's light sample has no
+ *    area / distance^2 factor). aur_render only; at most 32766 lights. */
+enum { AUR_MODE_REFERENCE = 0, AUR_MODE_PATH = 1, AUR_MODE_PATH_MIS = 2 };
 
 /* Per-render parameters (Dim(width,height,samples), MAX_DEPTH, RNG seed). */
 typedef struct aur_render_params {
@@ -362,6 +371,16 @@ typedef struct aur_emitter {
  * scan order). `emitters`: device, room for one record per triangle;
  * *num_emitters (host) receives the count. */
 aur_status aur_scene_emitters(aur_ctx* ctx, const aur_scene* scene, aur_emitter* emitters, uint32_t* num_emitters);
+/* The light-selection table AUR_MODE_PATH_MIS samples emissive triangles
+ * from (no reference counterpart; built on first use, rebuilt after
+ * aur_scene_set_shaders): the triangles with emission > 0 and positive area,
+ * the even-padding copy left out, in NMH order; `cdf` the inclusive CDF of
+ * emission * area (summed in double, normalised, rounded to float); `pa` per
+ * NMH triangle (aur_nmh_info count) the selection probability / area, 0 for
+ * triangles not in the table. Outputs may be NULL, host or device memory;
+ * `triangles` and `cdf` need room for one entry per triangle. */
+aur_status aur_scene_mis_table(aur_ctx* ctx, const aur_scene* scene, uint32_t* triangles, float* cdf, float* pa,
+                               uint32_t* count);
 /* texel(texture - 1, uv) for n device (u, v) pairs into n device RGB triples
  * (the fetch the integrators use; no reference counterpart). */
 aur_status aur_scene_texfetch(aur_ctx* ctx, const aur_scene* scene, uint32_t texture, const float* uv, uint32_t n,

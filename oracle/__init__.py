@@ -56,6 +56,10 @@ def lib():
         L.orc_emitters.argtypes = [P, P, U32, P, P]
         L.orc_draw2.argtypes = [U32, U32, U32, U32, U32, U32, P]
         L.orc_emitters.restype = U32
+        L.orc_render_ex.argtypes = [P, P, P, P, U32, P, U32, P, U32, P, P, P, ctypes.c_int, P, P, U32, P, P, P, U32]
+        L.orc_render_ex.restype = ctypes.c_uint64
+        L.orc_mis_table.argtypes = [P, P, P, U32, U32, P, P, P, P]
+        L.orc_mis_table.restype = U32
         _lib = L
     return _lib
 
@@ -201,6 +205,7 @@ class NmhScene:
     """A scene reordered into NMH order, as the renderer consumes it."""
 
     def __init__(self, scene, perm=None):
+        self.input_count = int(np.asarray(scene.vertices).reshape(-1, 9).shape[0])
         V = pad_even(scene.vertices)
         N = pad_even(scene.normals)
         S = scene.shader_ids
@@ -225,14 +230,42 @@ class NmhScene:
             self.TC = np.ascontiguousarray(tc[self.perm])
 
 
-def render(nscene, params, camera=None, accum=None, nthreads=None):
+def mis_table(nscene):
+    """The light-selection table of AUR_MODE_PATH_MIS: (triangles, cdf, pa)
+    with pa per NMH triangle."""
+    n = nscene.V.shape[0]
+    tri = np.zeros(n, np.uint32)
+    cdf = np.zeros(n, np.float32)
+    pa = np.zeros(n, np.float32)
+    m = lib().orc_mis_table(_ptr(nscene.V), _ptr(nscene.S), _ptr(nscene.perm), n, nscene.input_count,
+                            _ptr(nscene.shaders), _ptr(tri), _ptr(cdf), _ptr(pa))
+    return tri[:m].copy(), cdf[:m].copy(), pa
+
+
+def render(nscene, params, camera=None, accum=None, nthreads=None, table=None):
     """Adds the requested samples into accum (H, W, 4) float32 and returns
-    (accum, node fetches)."""
+    (accum, node fetches). For AUR_MODE_PATH_MIS, `table` is the
+    light-selection table (triangles, cdf, pa) to sample; default the
+    oracle's own (mis_table)."""
     p = np.asarray(params, T.params_dtype).reshape(())
     W, H = int(p["width"]), int(p["height"])
     if accum is None:
         accum = np.zeros((H, W, 4), np.float32)
     cam = np.asarray(nscene.camera if camera is None else camera, T.camera_dtype).reshape(())
+    if int(p["mode"]) == T.MODE_PATH_MIS:
+        tri, cdf, pa = mis_table(nscene) if table is None else table
+        tri = np.ascontiguousarray(tri, np.uint32)
+        cdf = np.ascontiguousarray(cdf, np.float32)
+        pa = np.ascontiguousarray(pa, np.float32)
+        assert pa.shape[0] == nscene.V.shape[0] and tri.shape[0] == cdf.shape[0]
+        table_t, keep = _texture_table(nscene.textures)
+        tot = lib().orc_render_ex(_ptr(nscene.V), _ptr(nscene.N), _ptr(nscene.S), _ptr(nscene.perm),
+                                  nscene.V.shape[0], _ptr(nscene.shaders), nscene.shaders.shape[0],
+                                  _ptr(nscene.lights), nscene.lights.shape[0], _ptr(cam), _ptr(p), _ptr(accum),
+                                  nthreads or nthreads_default(), _ptr(nscene.TC),
+                                  ctypes.c_void_p(ctypes.addressof(table_t)) if keep else ctypes.c_void_p(0),
+                                  len(keep), _ptr(tri), _ptr(cdf), _ptr(pa), tri.shape[0])
+        return accum, int(tot)
     if nscene.TC is not None:
         table, keep = _texture_table(nscene.textures)
         tot = lib().orc_render_textured(_ptr(nscene.V), _ptr(nscene.N), _ptr(nscene.S), _ptr(nscene.perm),

@@ -204,6 +204,7 @@ struct Ray {
     F3 pos, dir;
     float t, weight, eta;
     F3 thr;          // RGB path throughput (path mode); (weight,weight,weight) otherwise
+    float pdf = 0.0f; // AUR_MODE_PATH_MIS: density of the diffuse bounce that made the ray, 0 otherwise
 };
 
 // kernels/lib/ray.cuh:198-223 (Moller-Trumbore with back-face culling)
@@ -538,6 +539,11 @@ struct Scene {
     const float* TC = nullptr;          // NMH-ordered texcoords, count*6
     const aur_texture* tex = nullptr;
     uint32_t ntex = 0;
+    // AUR_MODE_PATH_MIS light-selection table (see orc_mis_table)
+    const uint32_t* misTri = nullptr;
+    const float* misCdf = nullptr;
+    const float* misPa = nullptr;        // per NMH triangle
+    uint32_t misCount = 0;
 };
 
 // ------------------------------------------------------------ textures
@@ -700,6 +706,171 @@ inline F3 directArea(const Scene& sc, const aur_light& L, uint32_t li, const BSD
     return mk3(acc.x / ns, acc.y / ns, acc.z / ns);
 }
 
+// ------------------------------------------------------ AUR_MODE_PATH_MIS
+// Path mode with physically based direct lighting and multiple importance
+// sampling (Veach & Guibas 1995); the half of estimateDirectRadiance the
+// reference compiles out (radiance.cuh:55-71). Area lights: the reference's
+// emission model Light::L = colour * intensity * max(0, direction . w)
+// (light.cuh:18-22), both strategies (a point on the quad, density
+// t^2 / (cos_l * area); a BSDF direction traced to the quad, visibleArea,
+// light.cuh:62-76), power heuristic (sampling.cuh:162-169) written as
+// 1 / (1 + (p_other / p_this)^2). Emissive triangles: one sample per hit from
+// the table (probability ~ emission * area, uniform point by the square-root
+// parameterisation), weighted against the diffuse bounce's density; emission
+// found by a diffuse bounce weighted against the table's. A hit from which no
+// diffuse bounce follows gives its emitter sample full weight.
+// RNG slots: BSDF half of light li's j-th sample = light slot | 2^31; the
+// emitter sample draws at 0xFFFFFFF0 and 0xFFFFFFF1.
+
+const uint32_t kSlotEmitter = 0xFFFFFFF0u;
+inline uint32_t bsdfLightSlot(uint32_t li, uint32_t j) { return (1u + (li << 16) + j) | 0x80000000u; }
+
+inline float misWeight(float pThis, float pOther) {
+    const float r = pOther / pThis;
+    return 1.0f / (1.0f + r * r);
+}
+
+// BSDF::pdf (bsdf.cuh:22-30, 48-51)
+inline float bsdfPdf(const BSDF& b, const F3& wo, const F3& wi) {
+    const F3 lwo = worldToLocal(wo, b.N, b.S, b.T);
+    const F3 lwi = worldToLocal(wi, b.N, b.S, b.T);
+    return (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
+}
+
+// BSDF::samplef (bsdf.cuh:53-67)
+inline F3 bsdfSample(const BSDF& b, const F3& wo, float u1, float u2, float& pdf) {
+    const F3 lwo = worldToLocal(wo, b.N, b.S, b.T);
+    F3 lwi = sampleHemisphereCosine(u1, u2);
+    if (lwo.z < 0.0f) lwi.z *= -1.0f;
+    pdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
+    return localToWorld(lwi, b.N, b.S, b.T);
+}
+
+// Distance t > Epsilon from pos along dir to the parallelogram p0 + a e1 + b e2.
+inline bool hitQuad(const F3& pos, const F3& dir, const F3& p0, const F3& e1, const F3& e2, float& t) {
+    const F3 P = cross(dir, e2);
+    const float det = dot(e1, P);
+    if (det == 0.0f) return false;
+    const float inv = 1.0f / det;
+    const F3 T = pos - p0;
+    const float a = dot(T, P) * inv;
+    if (!(a >= 0.0f && a <= 1.0f)) return false;
+    const F3 Q = cross(T, e1);
+    const float b = dot(dir, Q) * inv;
+    if (!(b >= 0.0f && b <= 1.0f)) return false;
+    t = dot(e2, Q) * inv;
+    return t > kEpsilon;
+}
+
+inline void triVerts(const float* V, uint32_t tri, F3& v1, F3& v2, F3& v3) {
+    const float* v = V + (size_t)tri * 9;
+    v1 = mk3(v[0], v[3], v[6]);
+    v2 = mk3(v[1], v[4], v[7]);
+    v3 = mk3(v[2], v[5], v[8]);
+}
+
+// Moller-Trumbore's determinant e1 . (dir x e2) (ray.cuh:198-223) and |e1 x e2|.
+inline float emitterDet(const F3& v1, const F3& v2, const F3& v3, const F3& dir, float& len) {
+    const F3 e1 = v2 - v1, e2 = v3 - v1;
+    len = length(cross(e1, e2));
+    return dot(e1, cross(dir, e2));
+}
+
+inline float emissionWeight(const Scene& sc, uint32_t tri, const F3& dir, float t, float prevPdf) {
+    if (!(prevPdf > 0.0f)) return 1.0f;
+    const float pa = sc.misPa[tri];
+    if (!(pa > 0.0f)) return 1.0f;
+    F3 v1, v2, v3;
+    triVerts(sc.V, tri, v1, v2, v3);
+    float len;
+    const float det = emitterDet(v1, v2, v3, dir, len);
+    const float epdf = (pa * (t * t)) / (det / len);
+    return misWeight(prevPdf, epdf);
+}
+
+// A shadow ray from pos, offset by Epsilon along dir (Ray::offset, ray.cuh:184-191).
+inline Ray offsetRay(const F3& pos, const F3& dir, float t) {
+    Ray r = pointRay(pos);
+    r.dir = dir;
+    r.pos.x += kEpsilon * dir.x;
+    r.pos.y += kEpsilon * dir.y;
+    r.pos.z += kEpsilon * dir.z;
+    r.t = t;
+    return r;
+}
+
+inline F3 areaLightMis(const Scene& sc, const aur_light& L, uint32_t li, const BSDF& b, const F3& pos, const F3& wo,
+                       const PixelCtx& pc, uint64_t* vis) {
+    const F3 p0 = from(L.position), e1 = from(L.e1), e2 = from(L.e2), ldir = from(L.direction);
+    const F3 Le0 = from(L.color) * L.intensity;
+    const float area = length(cross(e1, e2));
+    const F3 f = bsdfF(b);
+    F3 acc = mk3(0.0f);
+    if (area > 0.0f && !zero(f)) {
+        for (int32_t j = 0; j < L.samples; ++j) {
+            F3 Ls = mk3(0.0f);
+            float u1, u2;
+            draw2(pc.key, pc.pixel, pc.sample, pc.ray, 1u + (li << 16) + (uint32_t)j, u1, u2);
+            const F3 P = from(L.position) + ((e1 * u1) + (e2 * u2));
+            F3 wdir = P - pos;
+            const float wt = length(wdir);
+            wdir = wdir / wt;
+            float cl = dot(ldir, -wdir);
+            float cs = fmaxf(0.0f, dot(wdir, b.N));
+            if (cl > 0.0f && cs > 0.0f && traceAny(sc.V, sc.count, offsetRay(pos, wdir, wt + kEpsilon), vis) < 0) {
+                const float lpdf = (wt * wt) / (cl * area);
+                const float w = misWeight(lpdf, bsdfPdf(b, wo, wdir));
+                Ls = Ls + f * (Le0 * cl) * ((cs * w) / lpdf);
+            }
+            draw2(pc.key, pc.pixel, pc.sample, pc.ray, bsdfLightSlot(li, (uint32_t)j), u1, u2);
+            float bpdf, tl;
+            const F3 wi = bsdfSample(b, wo, u1, u2, bpdf);
+            if (bpdf > 0.0f && hitQuad(pos, wi, p0, e1, e2, tl)) {
+                cl = dot(ldir, -wi);
+                cs = fmaxf(0.0f, dot(wi, b.N));
+                if (cl > 0.0f && cs > 0.0f && traceAny(sc.V, sc.count, offsetRay(pos, wi, tl + kEpsilon), vis) < 0) {
+                    const float lpdf = (tl * tl) / (cl * area);
+                    const float w = misWeight(bpdf, lpdf);
+                    Ls = Ls + f * (Le0 * cl) * ((cs * w) / bpdf);
+                }
+            }
+            acc = acc + Ls;
+        }
+    }
+    const float ns = (float)L.samples;
+    return mk3(acc.x / ns, acc.y / ns, acc.z / ns);
+}
+
+inline F3 emitterSample(const Scene& sc, const BSDF& b, const F3& pos, const F3& wo, bool bounce, const PixelCtx& pc,
+                        uint64_t* vis) {
+    const F3 f = bsdfF(b);
+    if (sc.misCount == 0 || zero(f)) return mk3(0.0f);
+    float us, ua, ub, uc;
+    draw2(pc.key, pc.pixel, pc.sample, pc.ray, kSlotEmitter, us, ua);
+    draw2(pc.key, pc.pixel, pc.sample, pc.ray, kSlotEmitter + 1u, ub, uc);
+    // first entry whose CDF value is >= us (the last one if rounding left it below)
+    const uint32_t k = (uint32_t)(std::lower_bound(sc.misCdf, sc.misCdf + (sc.misCount - 1), us) - sc.misCdf);
+    const uint32_t tri = sc.misTri[k];
+    F3 v1, v2, v3;
+    triVerts(sc.V, tri, v1, v2, v3);
+    const float su = sqrtf(ua);
+    const F3 P = ((v1 * (1.0f - su)) + (v2 * (su * (1.0f - ub)))) + (v3 * (su * ub));
+    F3 wdir = P - pos;
+    const float t = length(wdir);
+    if (!(t > kEpsilon)) return mk3(0.0f);
+    wdir = wdir / t;
+    float len;
+    const float det = emitterDet(v1, v2, v3, wdir, len);
+    const float cs = fmaxf(0.0f, dot(wdir, b.N));
+    if (det < kEpsilon || !(cs > 0.0f)) return mk3(0.0f);
+    if (traceAny(sc.V, sc.count, offsetRay(pos, wdir, t * 0.9999f), vis) >= 0) return mk3(0.0f);
+    const float epdf = (sc.misPa[tri] * (t * t)) / (det / len);
+    const float w = bounce ? misWeight(epdf, bsdfPdf(b, wo, wdir)) : 1.0f;
+    const uint32_t sid = sc.S[tri];
+    const aur_shader& sh = sc.shaders[sid > 0 ? sid - 1 : 0];
+    return f * from(sh.emission_color) * ((cs * w) / epdf);
+}
+
 // utility.cu:18-77: camera ray for pixel (x, y), sample s of `samples`.
 inline Ray cameraRay(const aur_camera& cam, uint32_t W, uint32_t H, uint32_t x, uint32_t y, uint32_t s,
                      uint32_t samples) {
@@ -739,6 +910,8 @@ SampleOut integrate(const Scene& sc, const aur_render_params& p, const Ray& prim
     bool anyHit = false;
     uint32_t rayIndex = 0;
     const int maxDepth = (int)p.max_depth;
+    const bool mis = p.mode == AUR_MODE_PATH_MIS;
+    const bool path = mis || p.mode == AUR_MODE_PATH;
     while (depth <= maxDepth && sp > 0) {
         Ray ray = stack[--sp];
         PixelCtx pc = pc0;
@@ -753,23 +926,26 @@ SampleOut integrate(const Scene& sc, const aur_render_params& p, const Ray& prim
         const uint32_t sid = sc.S[tri];
         const aur_shader& sh = sc.shaders[sid > 0 ? sid - 1 : 0];   // getSafeID, util/array.h:16-17
         const BSDF b = getBSDF(sc, sh, tri, u, v);
-        F3 Li = from(sh.emission_color);
+        const bool specular = sh.reflectivity > 0.0f || sh.translucence > 0.0f;
+        F3 Li = mis ? from(sh.emission_color) * emissionWeight(sc, tri, ray.dir, ray.t, ray.pdf)
+                    : from(sh.emission_color);
         for (uint32_t i = 0; i < sc.nlights; ++i) {
             const aur_light& L = sc.lights[i];
             if (L.type == AUR_LIGHT_AMBIENT) Li = Li + ambientRadiance(L, b);
             if (L.type != AUR_LIGHT_AREA) Li = Li + directDelta(sc, L, b, position, vis);
+            else if (mis) Li = Li + areaLightMis(sc, L, i, b, position, wo, pc, vis);
             else Li = Li + directArea(sc, L, i, b, position, pc, vis);
         }
-        const bool specular = sh.reflectivity > 0.0f || sh.translucence > 0.0f;
+        if (mis) Li = Li + emitterSample(sc, b, position, wo, !specular && depth + 1 <= maxDepth, pc, vis);
         if (specular) depth++;
         if (depth <= maxDepth && sh.reflectivity > 0.0f) {
             Ray nr = pointRay(position);
             nr.dir = reflect(ray.dir, b.N);
             nr.weight = sh.reflectivity;
             nr.eta = ray.eta;
-            nr.thr = p.mode == AUR_MODE_PATH ? ray.thr * sh.reflectivity : mk3(nr.weight);
+            nr.thr = path ? ray.thr * sh.reflectivity : mk3(nr.weight);
             ray.weight *= (1.0f - sh.reflectivity);
-            ray.thr = p.mode == AUR_MODE_PATH ? ray.thr * (1.0f - sh.reflectivity) : mk3(ray.weight);
+            ray.thr = path ? ray.thr * (1.0f - sh.reflectivity) : mk3(ray.weight);
             stack[sp++] = nr;
         }
         if (depth <= maxDepth && sh.translucence > 0.0f) {
@@ -782,13 +958,13 @@ SampleOut integrate(const Scene& sc, const aur_render_params& p, const Ray& prim
                 nr.dir = tdir;
                 nr.weight = sh.translucence;
                 nr.eta = etat;
-                nr.thr = p.mode == AUR_MODE_PATH ? ray.thr * sh.translucence : mk3(nr.weight);
+                nr.thr = path ? ray.thr * sh.translucence : mk3(nr.weight);
                 ray.weight *= (1.0f - sh.translucence);
-                ray.thr = p.mode == AUR_MODE_PATH ? ray.thr * (1.0f - sh.translucence) : mk3(ray.weight);
+                ray.thr = path ? ray.thr * (1.0f - sh.translucence) : mk3(ray.weight);
                 stack[sp++] = nr;
             }
         }
-        if (p.mode == AUR_MODE_PATH && !specular) {
+        if (path && !specular) {
             depth++;
             if (depth <= maxDepth) {
                 // BSDF::samplef (bsdf.cuh:222-236)
@@ -805,6 +981,7 @@ SampleOut integrate(const Scene& sc, const aur_render_params& p, const Ray& prim
                     nr.dir = wi;
                     nr.eta = ray.eta;
                     nr.thr = ray.thr * (f * (fabsf(dot(wi, b.N)) / pdf));
+                    nr.pdf = pdf;
                     stack[sp++] = nr;
                 }
             }
@@ -934,6 +1111,57 @@ uint32_t orc_emitters(const float* V, const uint16_t* S, uint32_t count, const a
         run += w[j];
         out[j].cdf = (float)(run / total);
     }
+    return m;
+}
+
+/* orc_render with everything optional: TC/tex (textures; ntex 0 for none)
+ * and the AUR_MODE_PATH_MIS light-selection table (mis_pa per NMH triangle;
+ * mis_count 0 for none). */
+uint64_t orc_render_ex(const float* V, const float* N, const uint16_t* S, const uint32_t* perm, uint32_t count,
+                       const aur_shader* shaders, uint32_t nshaders, const aur_light* lights, uint32_t nlights,
+                       const aur_camera* cam, const aur_render_params* p, float* accum, int nthreads, const float* TC,
+                       const aur_texture* tex, uint32_t ntex, const uint32_t* mis_tri, const float* mis_cdf,
+                       const float* mis_pa, uint32_t mis_count) {
+    Scene sc;
+    sc.V = V; sc.N = N; sc.S = S; sc.perm = perm; sc.count = count;
+    sc.shaders = shaders; sc.nshaders = nshaders; sc.lights = lights; sc.nlights = nlights;
+    sc.TC = TC; sc.tex = tex; sc.ntex = ntex;
+    sc.misTri = mis_tri; sc.misCdf = mis_cdf; sc.misPa = mis_pa; sc.misCount = mis_count;
+    return render_scene(sc, cam, p, accum, nthreads);
+}
+
+/* The light-selection table of AUR_MODE_PATH_MIS, sequentially: NMH
+ * positions i (V: count*9 NMH-ordered, S: 1-based shader ids) whose shader
+ * has emission > 0, whose area 0.5 |(v2 - v1) x (v3 - v1)| is positive and
+ * which are not the even-padding copy (perm[i] >= input_count); weights
+ * emission * area summed in double, cdf = (float)(running / total);
+ * pa[i] = (cdf[k] - cdf[k-1]) / area for the k-th entry, 0 elsewhere.
+ * tri and cdf need room for count entries. Returns the number of entries. */
+uint32_t orc_mis_table(const float* V, const uint16_t* S, const uint32_t* perm, uint32_t count, uint32_t input_count,
+                       const aur_shader* shaders, uint32_t* tri, float* cdf, float* pa) {
+    std::vector<double> w;
+    std::vector<float> area;
+    uint32_t m = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        pa[i] = 0.0f;
+        const aur_shader& sh = shaders[S[i] > 0 ? S[i] - 1 : 0];
+        if (!(sh.emission > 0.0f) || perm[i] >= input_count) continue;
+        F3 v1, v2, v3;
+        triVerts(V, i, v1, v2, v3);
+        const float a = 0.5f * length(cross(v2 - v1, v3 - v1));
+        if (!(a > 0.0f)) continue;
+        tri[m++] = i;
+        w.push_back((double)sh.emission * (double)a);
+        area.push_back(a);
+    }
+    double total = 0.0;
+    for (double x : w) total += x;
+    double run = 0.0;
+    for (uint32_t k = 0; k < m; ++k) {
+        run += w[k];
+        cdf[k] = (float)(run / total);
+    }
+    for (uint32_t k = 0; k < m; ++k) pa[tri[k]] = (cdf[k] - (k > 0 ? cdf[k - 1] : 0.0f)) / area[k];
     return m;
 }
 

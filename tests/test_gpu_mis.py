@@ -1,0 +1,131 @@
+"""AUR_MODE_PATH_MIS on the GPU: the light-selection table and the images
+against the oracle, unbiasedness at high sample counts, and the entry points
+that do not take the mode."""
+import numpy as np
+import pytest
+
+import oracle
+from aurora_gb300 import api, scenes, types as T
+
+pytestmark = pytest.mark.gpu
+
+
+def _specular(sd):
+    sh = np.concatenate([sd.shaders, np.stack([T.lambert((0.9, 0.9, 0.9)), T.lambert((0.8, 0.9, 1.0))])])
+    k = sd.shaders.shape[0]
+    sh["reflectivity"][k] = 0.6
+    sh["translucence"][k + 1] = 0.7
+    sh["refractive_index"][k + 1] = 1.5
+    sids = sd.shader_ids.copy()
+    sids[10:22] = k + 1
+    sids[22:34] = k + 2
+    return scenes.SceneData(sd.name + "_specular", sd.vertices, sd.normals, sids, sh, sd.lights, sd.camera)
+
+
+def test_table_matches_oracle(ctx):
+    for sd in (scenes.cornell_emissive(), scenes.cornell_emissive(area_light=True), scenes.cornell()):
+        sc = api.Scene(ctx, sd)
+        tri, cdf, pa = sc.mis_table()
+        otri, ocdf, opa = oracle.mis_table(oracle.NmhScene(sd))
+        assert np.array_equal(tri, otri)
+        assert np.allclose(cdf, ocdf, rtol=3e-7, atol=0) and (len(cdf) == 0 or cdf[-1] == np.float32(1.0))
+        assert np.allclose(pa, opa, rtol=1e-5, atol=0) and np.array_equal(pa > 0, opa > 0)
+
+
+def test_table_of_many_emitters_matches_oracle(ctx):
+    """Multi-tile scans: 300,001 triangles, a third of them emitting."""
+    V = scenes.random_soup(300_001, seed=7)
+    n = V.shape[0]
+    sh = np.stack([T.lambert((0.5, 0.5, 0.5)), T.lambert((0.5, 0.5, 0.5), emission=(1.0, 2.0, 3.0)),
+                   T.lambert((0.5, 0.5, 0.5), emission=(4.0, 0.0, 0.0))])
+    sh["emission"][1], sh["emission"][2] = 0.7, 2.5
+    sids = (np.arange(n) % 3 + 1).astype(np.uint16)
+    sd = scenes.SceneData("soup", V, np.zeros_like(V), sids, sh, np.zeros(0, T.light_dtype), scenes.cornell_camera())
+    sc = api.Scene(ctx, sd)
+    tri, cdf, pa = sc.mis_table()
+    otri, ocdf, opa = oracle.mis_table(oracle.NmhScene(sd, perm=sc.nmh.export()[0]))
+    assert len(tri) > 190_000 and np.array_equal(tri, otri)
+    assert np.max(np.abs(cdf.astype(np.float64) - ocdf)) <= 2.0 ** -23
+    assert np.allclose(pa, opa, rtol=2e-3, atol=0)      # cdf differences of an ulp, divided
+
+
+@pytest.mark.parametrize("scene", ["cornell", "emissive", "emissive_area", "emissive_specular"])
+def test_render_matches_oracle(ctx, scene):
+    sd = {"cornell": scenes.cornell, "emissive": scenes.cornell_emissive,
+          "emissive_area": lambda: scenes.cornell_emissive(area_light=True),
+          "emissive_specular": lambda: _specular(scenes.cornell_emissive(area_light=True))}[scene]()
+    sc = api.Scene(ctx, sd)
+    p = T.render_params(40, 40, 4, 4, seed=9, mode=T.MODE_PATH_MIS)
+    img = sc.render(p).cpu().numpy()
+    ref, _ = oracle.render(oracle.NmhScene(sd), p, table=sc.mis_table())
+    assert np.array_equal(img, ref)                 # same arithmetic, same order: bit-exact
+    assert img[..., :3].mean() > 0.01
+
+
+def test_mis_matches_path_mode_one_bounce_deeper(ctx):
+    """Emissive geometry only: E[MIS at depth d] = E[path mode at depth d + 1];
+    48 x 48 pixels, 8 independent 1024-sample renders of each. Path mode's
+    per-pixel estimates are far from normal in dark corners (rare large
+    contributions), so the comparison is on the image mean (a z-test over
+    the 8 renders) and on 8 x 8-pixel block means."""
+    sc = api.Scene(ctx, scenes.cornell_emissive())
+    W = 48
+
+    def renders(mode, d):
+        return np.stack([sc.render(T.render_params(W, W, 1024, d, seed=s, mode=mode)).cpu().numpy()[..., :3]
+                         for s in range(8)]).astype(np.float64)
+
+    mis, path = renders(T.MODE_PATH_MIS, 2), renders(T.MODE_PATH, 3)
+    im, ip = mis.mean(axis=(1, 2, 3)), path.mean(axis=(1, 2, 3))
+    z = (im.mean() - ip.mean()) / np.sqrt(im.var(ddof=1) / 8 + ip.var(ddof=1) / 8)
+    assert abs(z) < 4.0, z
+    bm = mis.mean(0).reshape(6, 8, 6, 8, 3).mean(axis=(1, 3))
+    bp = path.mean(0).reshape(6, 8, 6, 8, 3).mean(axis=(1, 3))
+    assert np.max(np.abs(bm / bp - 1.0)) < 0.03
+    assert im.std() < 0.25 * ip.std()                                # variance of the image mean
+    assert mis.std(0).mean() < 0.5 * path.std(0).mean()              # and per pixel
+
+
+def test_other_entry_points_reject_the_mode(ctx):
+    import torch
+    sd = scenes.cornell_emissive(area_light=True)
+    sc = api.Scene(ctx, sd)
+    p = T.render_params(16, 16, 1, 2, mode=T.MODE_PATH_MIS)
+    with pytest.raises(api.AuroraError) as e:
+        api.Batch(ctx, [sc], [p], cameras=[sd.camera])
+    assert e.value.status == 6                          # AUR_ERR_UNSUPPORTED
+    d_img = torch.ones((16, 16, 4), dtype=torch.float32, device="cuda")
+    with pytest.raises(api.AuroraError) as e:
+        sc.adjoint(p, d_img)
+    assert e.value.status == 6
+    rays = torch.zeros((256, 9), dtype=torch.float32, device="cuda")
+    hits = torch.zeros((256, 12), dtype=torch.float32, device="cuda")
+    with pytest.raises(api.AuroraError):
+        api.raytrace_monte_carlo(ctx, sc, p, 0, 0, 256, rays, hits)
+
+
+def test_too_many_lights_for_the_rng_slots(ctx):
+    sd = scenes.cornell()
+    lights = np.repeat(sd.lights, 32767)
+    sd2 = scenes.SceneData("many", sd.vertices, sd.normals, sd.shader_ids, sd.shaders, lights, sd.camera)
+    sc = api.Scene(ctx, sd2)
+    with pytest.raises(api.AuroraError) as e:
+        sc.render(T.render_params(4, 4, 1, 1, mode=T.MODE_PATH_MIS))
+    assert e.value.status == 1                          # AUR_ERR_INVALID
+
+
+def test_table_follows_shader_changes(ctx):
+    sd = scenes.cornell_emissive()
+    sc = api.Scene(ctx, sd)
+    p = T.render_params(24, 24, 4, 3, seed=2, mode=T.MODE_PATH_MIS)
+    before = sc.render(p).cpu().numpy()
+    assert len(sc.mis_table()[0]) == 15
+    sh = sd.shaders.copy()
+    sh["emission"][4] = 0.0                     # the floor block no longer in the table
+    sc.set_shaders(sh)
+    tri, _, _ = sc.mis_table()
+    assert len(tri) == 3
+    sd2 = scenes.SceneData("e2", sd.vertices, sd.normals, sd.shader_ids, sh, sd.lights, sd.camera)
+    after = sc.render(p).cpu().numpy()
+    ref, _ = oracle.render(oracle.NmhScene(sd2), p, table=sc.mis_table())
+    assert np.array_equal(after, ref) and not np.array_equal(after, before)
