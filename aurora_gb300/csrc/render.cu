@@ -97,7 +97,7 @@ __global__ void k_generate_rays(uint32_t W, uint32_t H, uint32_t sample, uint32_
 }
 
 // cudaRaytraceKernel (monteCarloRaytracer.cu:90-113) on caller-provided rays.
-template <bool kGeneric>
+template <bool kGeneric, bool kMis>
 __global__ void __launch_bounds__(kRenderThreads) k_raytrace_mc(SceneView sc, aur_render_params p, uint32_t sample,
                                                                 uint32_t offset, uint32_t num,
                                                                 const aur_path_ray* __restrict__ rays,
@@ -118,8 +118,9 @@ __global__ void __launch_bounds__(kRenderThreads) k_raytrace_mc(SceneView sc, au
     r.pdf = 0.0f;
     uint32_t visits = 0;
     const SampleResult res =
-        kGeneric ? integrate(sc, p.max_depth, p.mode, p.seed, p.scene_id, id, sample, r, stk, visits, err)
-                 : integrate_diffuse(sc, p.max_depth, p.mode, p.seed, p.scene_id, id, sample, r, stk, visits, err);
+        kGeneric ? integrate<kMis>(sc, p.max_depth, p.mode, p.seed, p.scene_id, id, sample, r, stk, visits, err)
+                 : integrate_diffuse<kMis>(sc, p.max_depth, p.mode, p.seed, p.scene_id, id, sample, r, stk, visits,
+                                           err);
     aur_hitpoint h = hits[id];
     h.color = to(from(h.color) + res.color);
     if (res.any_hit) {
@@ -316,20 +317,42 @@ aur_status aur_raytrace_monte_carlo(aur_ctx* ctx, const aur_scene* scene, const 
                                     aur_hitpoint* hits) {
     AUR_RANGE("aur_raytrace_monte_carlo");
     AUR_CHECK(ctx && scene && params && rays && hits, AUR_ERR_INVALID, "aur_raytrace_monte_carlo: null argument");
-    AUR_CHECK(params->max_depth <= AUR_MAX_DEPTH && params->mode <= AUR_MODE_PATH, AUR_ERR_INVALID,
+    AUR_CHECK(params->max_depth <= AUR_MAX_DEPTH && params->mode <= AUR_MODE_PATH_MIS, AUR_ERR_INVALID,
               "aur_raytrace_monte_carlo: bad parameters");
-    const aur_status st = check_scene_textures(scene);
+    aur_status st = check_scene_textures(scene);
     if (st != AUR_OK) return st;
+    const bool mis = params->mode == AUR_MODE_PATH_MIS;
+    AUR_CHECK(!mis || scene->num_lights < 32767, AUR_ERR_INVALID,
+              "aur_raytrace_monte_carlo: AUR_MODE_PATH_MIS takes at most 32766 lights (scene has %u)",
+              scene->num_lights);
     AUR_CUDA(cudaSetDevice(ctx->device));
     if (num_rays == 0) return AUR_OK;
+    if (mis) {
+        st = build_mis_table(ctx, scene);
+        if (st != AUR_OK) return st;
+    }
     const int cap = stack_cap(scene);
     const size_t smem = (size_t)2 * cap * kRenderThreads * sizeof(uint32_t);
-    if (scene->has_specular)
-        k_raytrace_mc<true><<<cdiv(num_rays, kRenderThreads), kRenderThreads, smem, ctx->stream>>>(
-            scene_view(scene), *params, sample_id, offset, num_rays, rays, hits, ctx->d_flags, cap);
-    else
-        k_raytrace_mc<false><<<cdiv(num_rays, kRenderThreads), kRenderThreads, smem, ctx->stream>>>(
-            scene_view(scene), *params, sample_id, offset, num_rays, rays, hits, ctx->d_flags, cap);
+    const dim3 grid(cdiv(num_rays, kRenderThreads));
+    const SceneView sv = scene_view(scene);
+    const aur_render_params& p = *params;
+    aur_path_ray* r = rays;
+    aur_hitpoint* h = hits;
+    if (scene->has_specular) {
+        if (mis)
+            k_raytrace_mc<true, true><<<grid, kRenderThreads, smem, ctx->stream>>>(sv, p, sample_id, offset, num_rays,
+                                                                                  r, h, ctx->d_flags, cap);
+        else
+            k_raytrace_mc<true, false><<<grid, kRenderThreads, smem, ctx->stream>>>(sv, p, sample_id, offset,
+                                                                                   num_rays, r, h, ctx->d_flags, cap);
+    } else {
+        if (mis)
+            k_raytrace_mc<false, true><<<grid, kRenderThreads, smem, ctx->stream>>>(sv, p, sample_id, offset,
+                                                                                   num_rays, r, h, ctx->d_flags, cap);
+        else
+            k_raytrace_mc<false, false><<<grid, kRenderThreads, smem, ctx->stream>>>(sv, p, sample_id, offset,
+                                                                                    num_rays, r, h, ctx->d_flags, cap);
+    }
     AUR_CUDA(cudaGetLastError());
     return AUR_OK;
 }

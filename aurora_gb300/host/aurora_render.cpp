@@ -2,7 +2,7 @@
 // (src/maya/renderCommand.cpp, core/engine.cpp:171-251).
 //
 //   aurora_render SCENE.bin OUT.pfm [--width W] [--height H] [--spp S]
-//                 [--depth D] [--seed N] [--mode reference|path] [--device K]
+//                 [--depth D] [--seed N] [--mode reference|path|mis] [--device K]
 //                 [--filter] [--progressive]
 //   aurora_render SCENE.bin --dry-run          parse the scene file only
 //   aurora_render SCENE.bin --geometry-check   Geometry upload + rebuild + TB
@@ -34,7 +34,7 @@ static int fail(const char* what) {
 int main(int argc, char** argv) {
     if (argc < 2) {
         std::fprintf(stderr, "usage: aurora_render SCENE.bin OUT.pfm [--width W] [--height H] [--spp S] [--depth D] "
-                             "[--seed N] [--mode reference|path] [--device K] | --dry-run | --geometry-check\n");
+                             "[--seed N] [--mode reference|path|mis] [--device K] | --dry-run | --geometry-check\n");
         return 2;
     }
     std::string scenePath = argv[1], outPath;
@@ -50,7 +50,10 @@ int main(int argc, char** argv) {
         else if (a == "--depth") depth = (unsigned)next();
         else if (a == "--seed") seed = (unsigned)next();
         else if (a == "--device") device = (int)next();
-        else if (a == "--mode") mode = (i + 1 < argc && std::string(argv[++i]) == "reference") ? AUR_MODE_REFERENCE : AUR_MODE_PATH;
+        else if (a == "--mode") {
+            const std::string m = i + 1 < argc ? argv[++i] : "";
+            mode = m == "reference" ? AUR_MODE_REFERENCE : (m == "mis" ? AUR_MODE_PATH_MIS : AUR_MODE_PATH);
+        }
         else if (a == "--dry-run") dry = true;
         else if (a == "--geometry-check") geomCheck = true;
         else if (a == "--filter") filter = true;

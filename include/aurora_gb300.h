@@ -134,7 +134,8 @@ typedef struct aur_camera {
  *    triangles sampled from a table proportional to emission * area, their
  *    emission found by diffuse bounces weighted against it. Images differ
  *    from the other modes by design (the reference's light sample has no
- *    area / distance^2 factor). aur_render only; at most 32766 lights. */
+ *    area / distance^2 factor). aur_render and aur_raytrace_monte_carlo
+ *    (not the wavefront batch or the adjoint); at most 32766 lights. */
 enum { AUR_MODE_REFERENCE = 0, AUR_MODE_PATH = 1, AUR_MODE_PATH_MIS = 2 };
 
 /* Per-render parameters (Dim(width,height,samples), MAX_DEPTH, RNG seed). */

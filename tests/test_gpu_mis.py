@@ -86,7 +86,7 @@ def test_mis_matches_path_mode_one_bounce_deeper(ctx):
     assert mis.std(0).mean() < 0.5 * path.std(0).mean()              # and per pixel
 
 
-def test_other_entry_points_reject_the_mode(ctx):
+def test_batch_and_adjoint_reject_the_mode(ctx):
     import torch
     sd = scenes.cornell_emissive(area_light=True)
     sc = api.Scene(ctx, sd)
@@ -98,10 +98,29 @@ def test_other_entry_points_reject_the_mode(ctx):
     with pytest.raises(api.AuroraError) as e:
         sc.adjoint(p, d_img)
     assert e.value.status == 6
-    rays = torch.zeros((256, 9), dtype=torch.float32, device="cuda")
-    hits = torch.zeros((256, 12), dtype=torch.float32, device="cuda")
-    with pytest.raises(api.AuroraError):
-        api.raytrace_monte_carlo(ctx, sc, p, 0, 0, 256, rays, hits)
+
+
+def test_helper_entry_points_match_fused_render(ctx):
+    """generateRays + raytraceMonteCarlo tiles + drawPixels in MIS mode give
+    the fused render bit for bit (the tile kernel builds the same table)."""
+    import torch
+    sd = scenes.cornell_emissive(area_light=True)
+    sc = api.Scene(ctx, sd)
+    W = H = 40
+    spp = 4
+    p = T.render_params(W, H, spp, 3, seed=2, mode=T.MODE_PATH_MIS)
+    fused = sc.render(p).cpu().numpy()
+    sc2 = api.Scene(ctx, sd)                          # table built by the tile path
+    rays = torch.zeros((W * H, 9), dtype=torch.float32, device="cuda")
+    hits = torch.zeros((W * H, 12), dtype=torch.float32, device="cuda")
+    accum = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    api.clear_pixels(ctx, W, H, accum)
+    for s in range(spp):
+        api.generate_rays(ctx, W, H, s, spp, sd.camera, rays, hits)
+        for off in range(0, W * H, 512):
+            api.raytrace_monte_carlo(ctx, sc2, p, s, off, min(512, W * H - off), rays, hits)
+        api.draw_pixels(ctx, W, H, 1.0 / spp, hits, accum)
+    assert np.array_equal(accum.cpu().numpy(), fused)
 
 
 def test_too_many_lights_for_the_rng_slots(ctx):

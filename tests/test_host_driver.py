@@ -51,7 +51,7 @@ def test_malformed_scene_file_fails(driver, tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode,textured", [("path", False), ("reference", False), ("path", True)])
+@pytest.mark.parametrize("mode,textured", [("path", False), ("reference", False), ("path", True), ("mis", False)])
 def test_driver_render_matches_api(driver, ctx, tmp_path, mode, textured):
     """MonteCarloRaytracer::render (per-sample, 65,536-ray tiles) gives the
     image of the fused renderer bit for bit."""
@@ -63,7 +63,7 @@ def test_driver_render_matches_api(driver, ctx, tmp_path, mode, textured):
     _run([driver, str(path), str(out), "--width", str(W), "--height", str(H), "--spp", str(spp),
           "--depth", str(depth), "--seed", str(seed), "--mode", mode])
     img = scenes.read_pfm(str(out))
-    m = T.MODE_PATH if mode == "path" else T.MODE_REFERENCE
+    m = {"path": T.MODE_PATH, "reference": T.MODE_REFERENCE, "mis": T.MODE_PATH_MIS}[mode]
     sc = api.Scene(ctx, sd)
     if textured:
         sc.set_textures(sd.texcoords, sd.textures)
