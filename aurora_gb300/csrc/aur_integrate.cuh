@@ -262,61 +262,119 @@ __device__ __forceinline__ float emission_weight(const SceneView& sc, uint32_t t
     return mis_weight(prev_pdf, epdf);
 }
 
+// A sample of the direct-lighting estimator up to its shadow ray: the
+// contribution `c` it adds if the segment from o along d over (Epsilon, tmax)
+// is unoccluded; cand false when it adds nothing whatever the visibility.
+// The plain integrators trace the ray at once, the wavefront queues it.
+struct ShadowSample {
+    f3 c, o, d;
+    float tmax;
+    bool cand;
+};
+
+__device__ __forceinline__ f3 offset_origin(const f3& position, const f3& dir) {
+    f3 p = position;   // Ray::offset(Epsilon) (ray.cuh:184-191)
+    p.x += kEpsilon * dir.x;
+    p.y += kEpsilon * dir.y;
+    p.z += kEpsilon * dir.z;
+    return p;
+}
+
+// An area light seen by the MIS estimator: quad, emission, area, and whether
+// it can contribute at all (positive area, non-black BSDF).
+struct AreaLightMis {
+    f3 p0, e1, e2, ldir, Le0;
+    float area;
+    bool active;
+};
+__device__ __forceinline__ AreaLightMis area_light_setup(const aur_light& L, const f3& f) {
+    AreaLightMis q;
+    q.p0 = from(L.position);
+    q.e1 = from(L.e1);
+    q.e2 = from(L.e2);
+    q.ldir = from(L.direction);
+    q.Le0 = from(L.color) * L.intensity;
+    q.area = length(cross(q.e1, q.e2));
+    q.active = q.area > 0.0f && !zero(f);
+    return q;
+}
+
+// Light strategy of sample j of area light li: a point on the quad.
+__device__ __forceinline__ ShadowSample area_light_sample(const AreaLightMis& q, uint32_t li, uint32_t j, const Bsdf& b,
+                                                          const f3& f, const f3& position, const f3& wo,
+                                                          uint32_t seed, uint32_t scene, uint32_t pixel,
+                                                          uint32_t sample, uint32_t rix) {
+    ShadowSample s;
+    s.cand = false;
+    s.c = mk3(0.0f);
+    float u1, u2;
+    draw2(seed, scene, pixel, sample, rix, light_slot(li, j), u1, u2);
+    const f3 P = q.p0 + ((q.e1 * u1) + (q.e2 * u2));
+    f3 wdir = P - position;
+    const float wt = length(wdir);
+    wdir = wdir / wt;
+    const float cl = dot(q.ldir, -wdir);
+    const float cs = fmaxf(0.0f, dot(wdir, b.N));
+    if (cl > 0.0f && cs > 0.0f) {
+        const float lpdf = (wt * wt) / (cl * q.area);
+        const float w = mis_weight(lpdf, bsdf_pdf(b, wo, wdir));
+        s.c = f * (q.Le0 * cl) * ((cs * w) / lpdf);
+        s.o = offset_origin(position, wdir);
+        s.d = wdir;
+        s.tmax = wt + kEpsilon;
+        s.cand = true;
+    }
+    return s;
+}
+
+// BSDF strategy of sample j of area light li: a direction traced to the quad.
+__device__ __forceinline__ ShadowSample area_bsdf_sample(const AreaLightMis& q, uint32_t li, uint32_t j, const Bsdf& b,
+                                                         const f3& f, const f3& position, const f3& wo,
+                                                         uint32_t seed, uint32_t scene, uint32_t pixel,
+                                                         uint32_t sample, uint32_t rix) {
+    ShadowSample s;
+    s.cand = false;
+    s.c = mk3(0.0f);
+    float u1, u2;
+    draw2(seed, scene, pixel, sample, rix, bsdf_light_slot(li, j), u1, u2);
+    float bpdf, tl;
+    const f3 wi = bsdf_sample(b, wo, u1, u2, bpdf);
+    if (bpdf > 0.0f && hit_quad(position, wi, q.p0, q.e1, q.e2, tl)) {
+        const float cl = dot(q.ldir, -wi);
+        const float cs = fmaxf(0.0f, dot(wi, b.N));
+        if (cl > 0.0f && cs > 0.0f) {
+            const float lpdf = (tl * tl) / (cl * q.area);
+            const float w = mis_weight(bpdf, lpdf);
+            s.c = f * (q.Le0 * cl) * ((cs * w) / bpdf);
+            s.o = offset_origin(position, wi);
+            s.d = wi;
+            s.tmax = tl + kEpsilon;
+            s.cand = true;
+        }
+    }
+    return s;
+}
+
 // One area light, both strategies, averaged over its samples.
 __device__ __forceinline__ f3 area_light_mis(const SceneView& sc, const aur_light& L, uint32_t li, const Bsdf& b,
                                              const f3& position, const f3& wo, uint32_t seed, uint32_t scene,
                                              uint32_t pixel, uint32_t sample, uint32_t rix, const StackRef& stk,
                                              uint32_t& visits, uint32_t* err) {
-    const f3 p0 = from(L.position), e1 = from(L.e1), e2 = from(L.e2), ldir = from(L.direction);
-    const f3 Le0 = from(L.color) * L.intensity;
-    const float area = length(cross(e1, e2));
     const f3 f = bsdf_f(b);
+    const AreaLightMis q = area_light_setup(L, f);
     f3 acc = mk3(0.0f);
-    if (area > 0.0f && !zero(f)) {
+    if (q.active) {
         for (int32_t j = 0; j < L.samples; ++j) {
             f3 Ls = mk3(0.0f);
-            float u1, u2, du = 0.0f, dv = 0.0f;
-            // light strategy
-            draw2(seed, scene, pixel, sample, rix, light_slot(li, (uint32_t)j), u1, u2);
-            const f3 P = p0 + ((e1 * u1) + (e2 * u2));
-            f3 wdir = P - position;
-            const float wt = length(wdir);
-            wdir = wdir / wt;
-            float cl = dot(ldir, -wdir);
-            float cs = fmaxf(0.0f, dot(wdir, b.N));
-            if (cl > 0.0f && cs > 0.0f) {
-                f3 wpos = position;
-                wpos.x += kEpsilon * wdir.x;
-                wpos.y += kEpsilon * wdir.y;
-                wpos.z += kEpsilon * wdir.z;
-                float tt = wt + kEpsilon;
-                if (traverse<true>(sc.recs, sc.nodes, sc.perm, wpos, wdir, tt, du, dv, stk, visits, err) == kNoPrim) {
-                    const float lpdf = (wt * wt) / (cl * area);
-                    const float w = mis_weight(lpdf, bsdf_pdf(b, wo, wdir));
-                    Ls = Ls + f * (Le0 * cl) * ((cs * w) / lpdf);
-                }
-            }
-            // BSDF strategy
-            draw2(seed, scene, pixel, sample, rix, bsdf_light_slot(li, (uint32_t)j), u1, u2);
-            float bpdf, tl;
-            const f3 wi = bsdf_sample(b, wo, u1, u2, bpdf);
-            if (bpdf > 0.0f && hit_quad(position, wi, p0, e1, e2, tl)) {
-                cl = dot(ldir, -wi);
-                cs = fmaxf(0.0f, dot(wi, b.N));
-                if (cl > 0.0f && cs > 0.0f) {
-                    f3 wpos = position;
-                    wpos.x += kEpsilon * wi.x;
-                    wpos.y += kEpsilon * wi.y;
-                    wpos.z += kEpsilon * wi.z;
-                    float tt = tl + kEpsilon;
-                    if (traverse<true>(sc.recs, sc.nodes, sc.perm, wpos, wi, tt, du, dv, stk, visits, err) ==
-                        kNoPrim) {
-                        const float lpdf = (tl * tl) / (cl * area);
-                        const float w = mis_weight(bpdf, lpdf);
-                        Ls = Ls + f * (Le0 * cl) * ((cs * w) / bpdf);
-                    }
-                }
-            }
+            float du = 0.0f, dv = 0.0f;
+            ShadowSample s = area_light_sample(q, li, (uint32_t)j, b, f, position, wo, seed, scene, pixel, sample, rix);
+            if (s.cand && traverse<true>(sc.recs, sc.nodes, sc.perm, s.o, s.d, s.tmax, du, dv, stk, visits, err) ==
+                              kNoPrim)
+                Ls = Ls + s.c;
+            s = area_bsdf_sample(q, li, (uint32_t)j, b, f, position, wo, seed, scene, pixel, sample, rix);
+            if (s.cand && traverse<true>(sc.recs, sc.nodes, sc.perm, s.o, s.d, s.tmax, du, dv, stk, visits, err) ==
+                              kNoPrim)
+                Ls = Ls + s.c;
             acc = acc + Ls;
         }
     }
@@ -324,15 +382,17 @@ __device__ __forceinline__ f3 area_light_mis(const SceneView& sc, const aur_ligh
     return mk3(acc.x / ns, acc.y / ns, acc.z / ns);
 }
 
-// One emitter sample: a table entry by its CDF, a uniform point on the
-// triangle (square-root parameterisation), a shadow ray that stops short of
-// the emitter.
-__device__ __forceinline__ f3 emitter_sample(const SceneView& sc, const Bsdf& b, const f3& position, const f3& wo,
-                                             bool bounce, uint32_t seed, uint32_t scene, uint32_t pixel,
-                                             uint32_t sample, uint32_t rix, const StackRef& stk, uint32_t& visits,
-                                             uint32_t* err) {
-    const f3 f = bsdf_f(b);
-    if (sc.mis_count == 0 || zero(f)) return mk3(0.0f);
+// One emitter sample up to its shadow ray: a table entry by its CDF, a
+// uniform point on the triangle (square-root parameterisation); the shadow
+// ray stops short of the emitter.
+__device__ __forceinline__ ShadowSample emitter_shadow_sample(const SceneView& sc, const Bsdf& b, const f3& f,
+                                                              const f3& position, const f3& wo, bool bounce,
+                                                              uint32_t seed, uint32_t scene, uint32_t pixel,
+                                                              uint32_t sample, uint32_t rix) {
+    ShadowSample s;
+    s.cand = false;
+    s.c = mk3(0.0f);
+    if (sc.mis_count == 0 || zero(f)) return s;
     float us, ua, ub, uc;
     draw2(seed, scene, pixel, sample, rix, kSlotEmitter, us, ua);
     draw2(seed, scene, pixel, sample, rix, kSlotEmitter + 1u, ub, uc);
@@ -348,25 +408,33 @@ __device__ __forceinline__ f3 emitter_sample(const SceneView& sc, const Bsdf& b,
     const f3 P = ((v1 * (1.0f - su)) + (v2 * (su * (1.0f - ub)))) + (v3 * (su * ub));
     f3 wdir = P - position;
     const float t = length(wdir);
-    if (!(t > kEpsilon)) return mk3(0.0f);
+    if (!(t > kEpsilon)) return s;
     wdir = wdir / t;
     float len;
     const float det = emitter_det(v1, v2, v3, wdir, len);
     const float cs = fmaxf(0.0f, dot(wdir, b.N));
-    if (det < kEpsilon || !(cs > 0.0f)) return mk3(0.0f);
-    f3 wpos = position;
-    wpos.x += kEpsilon * wdir.x;
-    wpos.y += kEpsilon * wdir.y;
-    wpos.z += kEpsilon * wdir.z;
-    float tt = t * 0.9999f;
-    float du = 0.0f, dv = 0.0f;
-    if (traverse<true>(sc.recs, sc.nodes, sc.perm, wpos, wdir, tt, du, dv, stk, visits, err) != kNoPrim)
-        return mk3(0.0f);
+    if (det < kEpsilon || !(cs > 0.0f)) return s;
     const float epdf = (__ldg(sc.mis_pa + tri) * (t * t)) / (det / len);
     const float w = bounce ? mis_weight(epdf, bsdf_pdf(b, wo, wdir)) : 1.0f;
     const uint32_t sid = sc.sids[tri];
     const aur_shader* sh = sc.shaders + (sid > 0 ? sid - 1 : 0);
-    return f * from(sh->emission_color) * ((cs * w) / epdf);
+    s.c = f * from(sh->emission_color) * ((cs * w) / epdf);
+    s.o = offset_origin(position, wdir);
+    s.d = wdir;
+    s.tmax = t * 0.9999f;
+    s.cand = true;
+    return s;
+}
+
+__device__ __forceinline__ f3 emitter_sample(const SceneView& sc, const Bsdf& b, const f3& position, const f3& wo,
+                                             bool bounce, uint32_t seed, uint32_t scene, uint32_t pixel,
+                                             uint32_t sample, uint32_t rix, const StackRef& stk, uint32_t& visits,
+                                             uint32_t* err) {
+    ShadowSample s = emitter_shadow_sample(sc, b, bsdf_f(b), position, wo, bounce, seed, scene, pixel, sample, rix);
+    float du = 0.0f, dv = 0.0f;
+    if (!s.cand || traverse<true>(sc.recs, sc.nodes, sc.perm, s.o, s.d, s.tmax, du, dv, stk, visits, err) != kNoPrim)
+        return mk3(0.0f);
+    return s.c;
 }
 
 // Li at a hit: emission + ambient + direct light of every light, in the

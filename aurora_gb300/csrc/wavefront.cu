@@ -4,7 +4,10 @@
 // kernels/monteCarloRaytracer.cu:23-113) for non-specular materials — same
 // counter-RNG keys (seed, scene id) x (pixel, sample, ray index, slot), same
 // arithmetic in the same order — so every path sample has the same value as
-// in aur_render and the frames are identical.
+// in aur_render and the frames are identical. In AUR_MODE_PATH_MIS the
+// shade stage queues both strategies of every area-light sample and the
+// emitter sample (the ShadowSample helpers of aur_integrate.cuh), and the
+// combine stage adds them in the plain integrator's order.
 //
 // Structure (Laine, Karras, Aila, "Megakernels considered harmful", HPG'13):
 // a pool of paths in flight (SoA state) and index queues; each iteration runs
@@ -50,6 +53,12 @@ struct WfScene {
     const float* texcoords;
     const uchar4* texels;
     const uint4* tex_info;
+    // AUR_MODE_PATH_MIS: NMH-ordered vertices and the light-selection table
+    const float* verts;
+    const uint32_t* mis_tri;
+    const float* mis_cdf;
+    const float* mis_pa;
+    uint32_t mis_count;
     uint32_t nodes;
     uint32_t num_lights;
     uint32_t width, height;
@@ -87,12 +96,12 @@ struct WfArgs {
     // path state, indexed by pool slot
     float4* o;      // origin
     float4* d;      // direction
-    float4* thr;    // throughput
+    float4* thr;    // throughput, w = density of the bounce that made the ray (0: camera ray)
     float4* col;    // colour, w = any hit
     float4* hit;    // t, u, v, tri
     uint4* meta;    // item, depth, ray index, scene
     float4* ndir;   // bounce direction, w = 1 if the path continues
-    float4* nthr;   // bounce throughput
+    float4* nthr;   // bounce throughput, w = the bounce's density (AUR_MODE_PATH_MIS)
     float4* fsh;    // f = color1 / pi
     float4* emi;    // emission
     float4* cj;     // Q * M light-sample contributions, w = candidate
@@ -287,7 +296,8 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_extend(WfArgs a) {
 }
 
 // Shading: misses finish; hits get their light samples (shadow rays queued)
-// and, in path mode, their bounce.
+// and, in path mode, their bounce. kMis: the mode is AUR_MODE_PATH_MIS.
+template <bool kMis>
 __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
     WfCtl* c = a.ctl;
     const uint32_t cur = c->iter & 1u;
@@ -310,20 +320,60 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
         const f3 wo = -dir;
         const uint32_t sid = sc.sids[tri];
         const aur_shader* sh = sc.shaders + (sid > 0 ? sid - 1 : 0);
+        constexpr bool mis = kMis;
         SceneView sv;
         sv.normals = sc.normals;
         sv.texcoords = sc.texcoords;
         sv.texels = sc.texels;
         sv.tex_info = sc.tex_info;
+        sv.sids = sc.sids;
+        sv.shaders = sc.shaders;
+        sv.verts = sc.verts;
+        sv.mis_tri = sc.mis_tri;
+        sv.mis_cdf = sc.mis_cdf;
+        sv.mis_pa = sc.mis_pa;
+        sv.mis_count = sc.mis_count;
         const Bsdf bs = get_bsdf(sv, sh, tri, h.y, h.z);
         const f3 f = bsdf_f(bs);
+        const uint32_t depth = m.y + 1u;
         a.fsh[slot] = make_float4(f.x, f.y, f.z, 0.0f);
-        a.emi[slot] = make_float4(sh->emission_color.x, sh->emission_color.y, sh->emission_color.z, 0.0f);
+        const f3 em = mis ? from(sh->emission_color) * emission_weight(sv, tri, dir, h.x, a.thr[slot].w)
+                          : from(sh->emission_color);
+        a.emi[slot] = make_float4(em.x, em.y, em.z, 0.0f);
         a.vis[slot] = 0u;
         float4* cj = a.cj + (size_t)slot * a.M;
         uint32_t q = 0;
+        // queues one shadow ray of light-sample slot q
+        auto queue = [&](const ShadowSample& ss, uint32_t qq) {
+            cj[qq] = make_float4(ss.c.x, ss.c.y, ss.c.z, ss.cand ? 1.0f : 0.0f);
+            if (ss.cand) {
+                const uint32_t e = agg_inc(&c->shadow_count);
+                a.sh_o[e] = make_float4(ss.o.x, ss.o.y, ss.o.z, ss.tmax);
+                a.sh_d[e] = make_float4(ss.d.x, ss.d.y, ss.d.z, __uint_as_float((slot << 5) | qq));
+            }
+        };
         for (uint32_t li = 0; li < sc.num_lights; ++li) {
             const aur_light& L = sc.lights[li];
+            if (mis && L.type == AUR_LIGHT_AREA) {
+                // both strategies of every sample (area_light_mis), two slots each
+                const AreaLightMis al = area_light_setup(L, f);
+                for (uint32_t j = 0; j < (uint32_t)L.samples; ++j, q += 2) {
+                    if (q + 1 >= a.M) {   // lights given more samples since the batch was created
+                        atomicOr(&c->error, kWfErrLightSlots);
+                        break;
+                    }
+                    ShadowSample ss;
+                    ss.cand = false;
+                    ss.c = mk3(0.0f);
+                    if (al.active)
+                        ss = area_light_sample(al, li, j, bs, f, position, wo, a.seed, sc.scene_id, pix, sample, rix);
+                    queue(ss, q);
+                    if (al.active)
+                        ss = area_bsdf_sample(al, li, j, bs, f, position, wo, a.seed, sc.scene_id, pix, sample, rix);
+                    queue(ss, q + 1);
+                }
+                continue;
+            }
             const uint32_t ns = L.type == AUR_LIGHT_AREA ? (uint32_t)L.samples : 1u;
             for (uint32_t j = 0; j < ns; ++j, ++q) {
                 if (q >= a.M) {   // lights given more samples since the batch was created
@@ -351,17 +401,25 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
                 }
             }
         }
+        if (mis) {   // the emitter sample (emitter_sample), last slot
+            if (q >= a.M) {
+                atomicOr(&c->error, kWfErrLightSlots);
+            } else {
+                queue(emitter_shadow_sample(sv, bs, f, position, wo, depth <= a.max_depth, a.seed, sc.scene_id, pix,
+                                            sample, rix),
+                      q);
+            }
+        }
         // bounce (BSDF::samplef, bsdf.cuh:222-236)
-        float cont = 0.0f;
+        float cont = 0.0f, bpdf = 0.0f;
         f3 wi = mk3(0.0f), nt = mk3(0.0f);
-        const uint32_t depth = m.y + 1u;
-        if (a.mode == AUR_MODE_PATH && depth <= a.max_depth) {
+        if ((mis || a.mode == AUR_MODE_PATH) && depth <= a.max_depth) {
             float u1, u2;
             draw2(a.seed, sc.scene_id, pix, sample, rix, 0u, u1, u2);
             const f3 lwo = world_to_local(wo, bs.N, bs.S, bs.T);
             f3 lwi = sample_hemisphere_cosine(u1, u2);
             if (lwo.z < 0.0f) lwi.z *= -1.0f;
-            const float bpdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
+            bpdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
             wi = local_to_world(lwi, bs.N, bs.S, bs.T);
             if (bpdf > 0.0f && !zero(f)) {
                 const float4 t4 = a.thr[slot];
@@ -370,7 +428,7 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
             }
         }
         a.ndir[slot] = make_float4(wi.x, wi.y, wi.z, cont);
-        a.nthr[slot] = make_float4(nt.x, nt.y, nt.z, 0.0f);
+        a.nthr[slot] = make_float4(nt.x, nt.y, nt.z, bpdf);
         a.meta[slot].y = depth;
     }
 }
@@ -425,7 +483,8 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shadow(WfArgs a) {
 }
 
 // Li in the reference's order (radiance.cuh:13-80, monteCarloRaytracer.cu:42-52),
-// colour update, then continue or finish.
+// colour update, then continue or finish. kMis as in k_wf_shade.
+template <bool kMis>
 __global__ void k_wf_combine(WfArgs a) {
     WfCtl* c = a.ctl;
     const uint32_t cur = c->iter & 1u, nxt = cur ^ 1u;
@@ -440,12 +499,26 @@ __global__ void k_wf_combine(WfArgs a) {
         const f3 f = mk3(f4.x, f4.y, f4.z);
         const uint32_t vis = a.vis[slot];
         const float4* cj = a.cj + (size_t)slot * a.M;
+        constexpr bool mis = kMis;
         f3 Li = mk3(e4.x, e4.y, e4.z);
         uint32_t q = 0;
         for (uint32_t li = 0; li < sc.num_lights; ++li) {
             const aur_light& L = sc.lights[li];
             if (L.type == AUR_LIGHT_AMBIENT) Li = Li + f * ((from(L.color) * L.intensity) * L.ambient);
-            if (L.type != AUR_LIGHT_AREA) {
+            if (mis && L.type == AUR_LIGHT_AREA) {
+                // area_light_mis: per sample, the light then the BSDF strategy
+                f3 acc = mk3(0.0f);
+                for (int32_t j = 0; j < L.samples; ++j) {
+                    f3 Ls = mk3(0.0f);
+                    for (int h2 = 0; h2 < 2; ++h2, ++q) {
+                        const float4 v = q < a.M ? cj[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        if (v.w != 0.0f && ((vis >> q) & 1u)) Ls = Ls + mk3(v.x, v.y, v.z);
+                    }
+                    acc = acc + Ls;
+                }
+                const float ns = (float)L.samples;
+                Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
+            } else if (L.type != AUR_LIGHT_AREA) {
                 const float4 v = q < a.M ? cj[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 if (v.w != 0.0f && ((vis >> q) & 1u)) Li = Li + mk3(v.x, v.y, v.z);
                 ++q;
@@ -460,6 +533,10 @@ __global__ void k_wf_combine(WfArgs a) {
                 const float ns = (float)L.samples;
                 Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
             }
+        }
+        if (mis) {   // emitter_sample: added whether or not it contributes
+            const float4 v = q < a.M ? cj[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            Li = Li + ((v.w != 0.0f && ((vis >> q) & 1u)) ? mk3(v.x, v.y, v.z) : mk3(0.0f));
         }
         const float4 t4 = a.thr[slot];
         float4 col = a.col[slot];
@@ -548,6 +625,8 @@ struct aur_batch {
     uint32_t grid = 0, block = 0;
     size_t smem = 0;
     std::vector<float4*> accum_host;
+    std::vector<const aur_scene*> scene_ptrs;   // AUR_MODE_PATH_MIS: tables to keep current
+    std::vector<WfScene> table_host;            // host copy of the device scene table
 };
 
 namespace {
@@ -593,9 +672,11 @@ aur_status make_graph(aur_batch* bt) {
     k_wf_generate<<<g, bs, 0, s>>>(a);
     k_wf_generate_commit<<<1, 1, 0, s>>>(a);
     k_wf_extend<<<g, bs, bt->smem, s>>>(a);
-    k_wf_shade<<<g, bs, 0, s>>>(a);
+    if (a.mode == AUR_MODE_PATH_MIS) k_wf_shade<true><<<g, bs, 0, s>>>(a);
+    else k_wf_shade<false><<<g, bs, 0, s>>>(a);
     k_wf_shadow<<<g, bs, bt->smem, s>>>(a);
-    k_wf_combine<<<g, bs, 0, s>>>(a);
+    if (a.mode == AUR_MODE_PATH_MIS) k_wf_combine<true><<<g, bs, 0, s>>>(a);
+    else k_wf_combine<false><<<g, bs, 0, s>>>(a);
     k_wf_end<<<1, 1, 0, s>>>(a);
     AUR_CUDA(cudaStreamEndCapture(s, &tmp));
     // wave body part 2: accumulate after the inner loop
@@ -605,6 +686,30 @@ aur_status make_graph(aur_batch* bt) {
     AUR_CUDA(cudaStreamEndCapture(s, &tmp));
     AUR_CUDA(cudaGraphInstantiate(&bt->exec, bt->graph, 0));
     a.in_graph = 0;   // the host-launched (profiling) form must not touch the conditionals
+    return AUR_OK;
+}
+
+// AUR_MODE_PATH_MIS: a scene whose shaders changed since the last render
+// dropped its light-selection table; rebuild it and point the device scene
+// table at the new one, so that the frames keep equalling aur_render's.
+aur_status refresh_mis_tables(aur_ctx* ctx, aur_batch* bt) {
+    if (bt->params.mode != AUR_MODE_PATH_MIS) return AUR_OK;
+    for (uint32_t i = 0; i < bt->num_scenes; ++i) {
+        const aur_scene* sc = bt->scene_ptrs[i];
+        const aur_status st = build_mis_table(ctx, sc);
+        if (st != AUR_OK) return st;
+        WfScene& w = bt->table_host[i];
+        if (w.mis_tri == sc->mis_tri && w.mis_cdf == sc->mis_cdf && w.mis_pa == sc->mis_pa &&
+            w.mis_count == sc->mis_count)
+            continue;
+        w.mis_tri = sc->mis_tri;
+        w.mis_cdf = sc->mis_cdf;
+        w.mis_pa = sc->mis_pa;
+        w.mis_count = sc->mis_count;
+        AUR_CUDA(cudaMemcpyAsync((void*)(bt->args.scenes + i), &w, sizeof(WfScene), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+        AUR_CUDA(cudaStreamSynchronize(ctx->stream));   // w is pageable host memory
+    }
     return AUR_OK;
 }
 
@@ -632,9 +737,7 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     const aur_render_params& p0 = params[0];
     aur_status st = check_params(&p0);
     if (st != AUR_OK) return st;
-    AUR_CHECK(p0.mode != AUR_MODE_PATH_MIS, AUR_ERR_UNSUPPORTED,
-              "aur_batch_create: the wavefront batch renders AUR_MODE_REFERENCE and AUR_MODE_PATH (AUR_MODE_PATH_MIS "
-              "renders with aur_render)");
+    const bool mis = p0.mode == AUR_MODE_PATH_MIS;
     uint64_t P_tot = 0;
     uint32_t M = 1, cap = 2;
     std::vector<WfScene> table(num_scenes);
@@ -659,8 +762,18 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
         std::vector<aur_light> lt(sc->num_lights);
         if (sc->num_lights)
             AUR_CUDA(cudaMemcpy(lt.data(), sc->lights, sizeof(aur_light) * sc->num_lights, cudaMemcpyDeviceToHost));
-        uint32_t m = 0;
-        for (const aur_light& l : lt) m += l.type == AUR_LIGHT_AREA ? (uint32_t)l.samples : 1u;
+        // light-sample slots per hit: one per sample (MIS: two per area-light
+        // sample, plus the emitter sample)
+        uint32_t m = mis ? 1u : 0u;
+        for (const aur_light& l : lt) m += l.type == AUR_LIGHT_AREA ? (mis ? 2u : 1u) * (uint32_t)l.samples : 1u;
+        if (mis) {
+            AUR_CHECK(sc->num_lights < 32767, AUR_ERR_INVALID,
+                      "aur_batch_create: AUR_MODE_PATH_MIS takes at most 32766 lights (scene %u has %u)", i,
+                      sc->num_lights);
+            AUR_CUDA(cudaSetDevice(ctx->device));
+            st = build_mis_table(ctx, sc);
+            if (st != AUR_OK) return st;
+        }
         AUR_CHECK(m <= (uint32_t)kMaxLightSlots, AUR_ERR_UNSUPPORTED,
                   "aur_batch_create: scene %u needs %u light samples per hit (limit %d)", i, m, kMaxLightSlots);
         M = std::max(M, m);
@@ -675,6 +788,11 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
         w.texcoords = sc->texcoords;
         w.texels = sc->texels;
         w.tex_info = sc->tex_info;
+        w.verts = sc->nmh->verts;
+        w.mis_tri = sc->mis_tri;
+        w.mis_cdf = sc->mis_cdf;
+        w.mis_pa = sc->mis_pa;
+        w.mis_count = sc->mis_count;
         w.nodes = sc->nmh->nodes;
         w.num_lights = sc->num_lights;
         w.width = p.width;
@@ -718,6 +836,8 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     bt->grid = (uint32_t)ctx->sm_count * tn.blocks_per_sm;
     bt->smem = (size_t)2 * cap * tn.block_size * sizeof(uint32_t);
     bt->accum_host.assign(num_scenes, nullptr);
+    bt->scene_ptrs.assign(scenes, scenes + num_scenes);
+    bt->table_host = table;
     const uint64_t Q = tn.paths_in_flight;
     const uint64_t out_items = P_tot * tn.samples_per_wave;
     size_t off = 0;
@@ -797,6 +917,8 @@ aur_status aur_batch_render(aur_ctx* ctx, aur_batch* bt, float* const* accum) {
         AUR_CHECK(accum[i], AUR_ERR_INVALID, "aur_batch_render: frame %u is null", i);
         bt->accum_host[i] = (float4*)accum[i];
     }
+    const aur_status st = refresh_mis_tables(ctx, bt);
+    if (st != AUR_OK) return st;
     const WfArgs& a = bt->args;
     AUR_CUDA(cudaMemcpyAsync((void*)a.accum, bt->accum_host.data(), sizeof(float4*) * bt->num_scenes,
                              cudaMemcpyHostToDevice, ctx->stream));
@@ -858,6 +980,8 @@ aur_status aur_batch_profile(aur_ctx* ctx, aur_batch* bt, float* const* accum, f
     AUR_CHECK(ctx && bt && accum && stage_ms, AUR_ERR_INVALID, "aur_batch_profile: null argument");
     AUR_CUDA(cudaSetDevice(ctx->device));
     for (uint32_t i = 0; i < bt->num_scenes; ++i) bt->accum_host[i] = (float4*)accum[i];
+    const aur_status rs = refresh_mis_tables(ctx, bt);
+    if (rs != AUR_OK) return rs;
     const WfArgs& a = bt->args;
     cudaStream_t st = ctx->stream;
     AUR_CUDA(cudaMemcpyAsync((void*)a.accum, bt->accum_host.data(), sizeof(float4*) * bt->num_scenes,
@@ -888,11 +1012,13 @@ aur_status aur_batch_profile(aur_ctx* ctx, aur_batch* bt, float* const* accum, f
             cudaEventRecord(ev[1], st);
             k_wf_extend<<<g, bs, bt->smem, st>>>(a);
             cudaEventRecord(ev[2], st);
-            k_wf_shade<<<g, bs, 0, st>>>(a);
+            if (a.mode == AUR_MODE_PATH_MIS) k_wf_shade<true><<<g, bs, 0, st>>>(a);
+            else k_wf_shade<false><<<g, bs, 0, st>>>(a);
             cudaEventRecord(ev[3], st);
             k_wf_shadow<<<g, bs, bt->smem, st>>>(a);
             cudaEventRecord(ev[4], st);
-            k_wf_combine<<<g, bs, 0, st>>>(a);
+            if (a.mode == AUR_MODE_PATH_MIS) k_wf_combine<true><<<g, bs, 0, st>>>(a);
+            else k_wf_combine<false><<<g, bs, 0, st>>>(a);
             k_wf_end<<<1, 1, 0, st>>>(a);
             cudaEventRecord(ev[5], st);
             AUR_CUDA(cudaMemcpyAsync(&c, a.ctl, sizeof(c), cudaMemcpyDeviceToHost, st));

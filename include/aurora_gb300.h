@@ -134,8 +134,8 @@ typedef struct aur_camera {
  *    triangles sampled from a table proportional to emission * area, their
  *    emission found by diffuse bounces weighted against it. Images differ
  *    from the other modes by design (the reference's light sample has no
- *    area / distance^2 factor). aur_render and aur_raytrace_monte_carlo
- *    (not the wavefront batch or the adjoint); at most 32766 lights. */
+ *    area / distance^2 factor). aur_render, aur_raytrace_monte_carlo and
+ *    the wavefront batch (not the adjoint); at most 32766 lights. */
 enum { AUR_MODE_REFERENCE = 0, AUR_MODE_PATH = 1, AUR_MODE_PATH_MIS = 2 };
 
 /* Per-render parameters (Dim(width,height,samples), MAX_DEPTH, RNG seed). */
@@ -484,9 +484,12 @@ typedef struct aur_batch aur_batch;
  * height and scene_id only. Materials must be non-specular. The batch reads
  * the scenes' device data in place: each scene must outlive the batch, and
  * its textures must not be replaced (aur_scene_set_textures) while the batch
- * exists. Shaders and lights may be updated between renders, but the batch is
- * sized for the light samples per hit at creation: a render after lights
- * gained samples stops, and aur_batch_status reports AUR_ERR_INVALID. */
+ * exists. Shaders and lights may be updated between renders (in
+ * AUR_MODE_PATH_MIS the next render rebuilds the light-selection tables of
+ * scenes whose shaders changed), but the batch is sized for the light
+ * samples per hit at creation (AUR_MODE_PATH_MIS: two per area-light sample
+ * plus one, at most 32 in all): a render after lights gained samples stops,
+ * and aur_batch_status reports AUR_ERR_INVALID. */
 aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const aur_camera* cameras,
                             const aur_render_params* params, uint32_t num_scenes,
                             const aur_wavefront_tuning* tuning, aur_batch** out);

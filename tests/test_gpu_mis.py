@@ -1,6 +1,7 @@
 """AUR_MODE_PATH_MIS on the GPU: the light-selection table and the images
-against the oracle, unbiasedness at high sample counts, and the entry points
-that do not take the mode."""
+against the oracle, unbiasedness at high sample counts, the tile entry point
+and the wavefront batch against the fused renderer, and the adjoint's
+refusal."""
 import numpy as np
 import pytest
 
@@ -86,18 +87,65 @@ def test_mis_matches_path_mode_one_bounce_deeper(ctx):
     assert mis.std(0).mean() < 0.5 * path.std(0).mean()              # and per pixel
 
 
-def test_batch_and_adjoint_reject_the_mode(ctx):
+def _mis_batch_scenes():
+    sph = scenes.sphere_scene(5, max_tris=20000)
+    sph.shaders = sph.shaders.copy()
+    sph.shaders["emission"][0] = 1.0          # the first shader's triangles emit (colour set below)
+    sph.shaders["emission_color"][0] = (0.5, 0.4, 0.3)
+    return [scenes.cornell_emissive(area_light=True), scenes.cornell_emissive(), scenes.cornell(), sph]
+
+
+@pytest.mark.parametrize("tuning", [dict(paths_in_flight=1024, samples_per_wave=1, block_size=64, blocks_per_sm=2),
+                                    dict()])
+def test_wavefront_equals_plain(ctx, tuning):
+    """The wavefront batch in MIS mode: every frame equals aur_render's."""
+    sds = _mis_batch_scenes()
+    scs = [api.Scene(ctx, sd) for sd in sds]
+    sizes = [(40, 32), (24, 24), (33, 17), (16, 40)]
+    prm = [T.render_params(w, h, 4, 3, seed=7, mode=T.MODE_PATH_MIS, scene_id=i) for i, (w, h) in enumerate(sizes)]
+    batch = api.Batch(ctx, scs, prm, tuning=api.make_tuning(**tuning) if tuning else None)
+    frames = batch.render()
+    assert batch.status() > 0
+    for sc, p, f in zip(scs, prm, frames):
+        assert np.array_equal(f.cpu().numpy(), sc.render(p).cpu().numpy())
+    # shaders change between renders: the batch picks up the rebuilt tables
+    sh = sds[1].shaders.copy()
+    sh["emission"][4] = 0.0
+    scs[1].set_shaders(sh)
+    frames = batch.render()
+    batch.status()
+    for sc, p, f in zip(scs, prm, frames):
+        assert np.array_equal(f.cpu().numpy(), sc.render(p).cpu().numpy())
+
+
+def test_adjoint_rejects_the_mode(ctx):
     import torch
     sd = scenes.cornell_emissive(area_light=True)
     sc = api.Scene(ctx, sd)
     p = T.render_params(16, 16, 1, 2, mode=T.MODE_PATH_MIS)
-    with pytest.raises(api.AuroraError) as e:
-        api.Batch(ctx, [sc], [p], cameras=[sd.camera])
-    assert e.value.status == 6                          # AUR_ERR_UNSUPPORTED
     d_img = torch.ones((16, 16, 4), dtype=torch.float32, device="cuda")
     with pytest.raises(api.AuroraError) as e:
         sc.adjoint(p, d_img)
+    assert e.value.status == 6                          # AUR_ERR_UNSUPPORTED
+
+
+def test_wavefront_light_slot_limit(ctx):
+    """MIS takes two slots per area-light sample plus one: 16 samples need 33
+    of the 32 a path has."""
+    sd = scenes.cornell()
+    sd.lights = sd.lights.copy()
+    sd.lights["samples"][0] = 16
+    sc = api.Scene(ctx, sd)
+    with pytest.raises(api.AuroraError) as e:
+        api.Batch(ctx, [sc], [T.render_params(8, 8, 1, 2, mode=T.MODE_PATH_MIS)])
     assert e.value.status == 6
+    sd.lights["samples"][0] = 15
+    sc2 = api.Scene(ctx, sd)
+    p = T.render_params(8, 8, 1, 2, mode=T.MODE_PATH_MIS)
+    b = api.Batch(ctx, [sc2], [p])
+    fr = b.render()
+    b.status()
+    assert np.array_equal(fr[0].cpu().numpy(), sc2.render(p).cpu().numpy())
 
 
 def test_helper_entry_points_match_fused_render(ctx):
