@@ -47,6 +47,10 @@ __device__ __forceinline__ float light_scale(const aur_light& L, const f3& dir, 
 // gradient contributions (scaled by g per colour channel).
 // Gradients of light 0 are summed in `gl0` (reduced once per block by the
 // caller); those of further lights go to d_light with atomics.
+// kMis: AUR_MODE_PATH_MIS, whose MIS weights do not depend on the colours
+// (Lambert densities are |cos| / pi), so every direct term stays linear in
+// the vertex colour and in the light colour.
+template <bool kMis>
 __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, uint32_t seed, uint32_t scene,
                        uint32_t pixel, uint32_t sample, PathRay ray, const StackRef& stk, const f3& C, const f3& g,
                        float* __restrict__ d_diffuse, float* __restrict__ d_light, f3& gl0, uint32_t& visits,
@@ -65,7 +69,8 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
         const Bsdf b = get_bsdf(sc, sh, tri, u, v);
         const f3 f = bsdf_f(b);
         const f3 thr = ray.thr;
-        f3 Li = from(sh->emission_color);
+        f3 Li = kMis ? from(sh->emission_color) * emission_weight(sc, tri, ray.dir, t, ray.pdf)
+                     : from(sh->emission_color);
         f3 Dp = mk3(0.0f);   // direct light per unit Lambert colour
         for (uint32_t i = 0; i < sc.num_lights; ++i) {
             const aur_light& L = sc.lights[i];
@@ -89,6 +94,34 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
                         dl = dl + f * (light_scale(L, wdir, wt) * cs);
                     }
                 }
+            } else if (kMis) {
+                // area_light_mis, both strategies
+                f3 acc = mk3(0.0f), accp = mk3(0.0f), accl = mk3(0.0f);
+                const AreaLightMis q = area_light_setup(L, f);
+                if (q.active) {
+                    for (int32_t j = 0; j < L.samples; ++j) {
+                        f3 Ls = mk3(0.0f);
+                        for (int h2 = 0; h2 < 2; ++h2) {
+                            const ShadowSample ss =
+                                h2 == 0 ? area_light_sample(q, i, (uint32_t)j, b, f, position, wo, seed, scene, pixel,
+                                                            sample, rix)
+                                        : area_bsdf_sample(q, i, (uint32_t)j, b, f, position, wo, seed, scene, pixel,
+                                                           sample, rix);
+                            float du = 0.0f, dv = 0.0f, tt = ss.tmax;
+                            if (ss.cand && traverse<true>(sc.recs, sc.nodes, sc.perm, ss.o, ss.d, tt, du, dv, stk,
+                                                          visits, err) == kNoPrim) {
+                                Ls = Ls + ss.c;
+                                accp = accp + ss.e * (ss.geo * kInvPi);
+                                accl = accl + f * (L.intensity * ss.geo);
+                            }
+                        }
+                        acc = acc + Ls;
+                    }
+                }
+                const float ns = (float)L.samples;
+                Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
+                Dp = Dp + mk3(accp.x / ns, accp.y / ns, accp.z / ns);
+                dl = dl + mk3(accl.x / ns, accl.y / ns, accl.z / ns);
             } else {
                 f3 acc = mk3(0.0f), accp = mk3(0.0f), accl = mk3(0.0f);
                 for (int32_t j = 0; j < L.samples; ++j) {
@@ -125,11 +158,20 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
                 atomicAdd(d_light + 3 * i + 2, gl.z);
             }
         }
+        if (kMis) {   // the emitter sample (emitter_sample)
+            const ShadowSample ss =
+                emitter_shadow_sample(sc, b, f, position, wo, depth + 1 <= max_depth, seed, scene, pixel, sample, rix);
+            float du = 0.0f, dv = 0.0f, tt = ss.tmax;
+            const bool vis = ss.cand && traverse<true>(sc.recs, sc.nodes, sc.perm, ss.o, ss.d, tt, du, dv, stk,
+                                                       visits, err) == kNoPrim;
+            Li = Li + (vis ? ss.c : mk3(0.0f));
+            if (vis) Dp = Dp + ss.e * (ss.geo * kInvPi);
+        }
         Lrem = Lrem - Li * thr;
         // bounce, as in the primal
         bool cont = false;
         PathRay nr;
-        if (mode == AUR_MODE_PATH) {
+        if (kMis || mode == AUR_MODE_PATH) {
             depth++;
             if (depth <= max_depth) {
                 float u1, u2;
@@ -145,6 +187,7 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
                     nr.weight = 1.0f;
                     nr.eta = ray.eta;
                     nr.thr = thr * (f * (fabsf(dot(wi, b.N)) / pdf));
+                    nr.pdf = pdf;
                     cont = true;
                 }
             }
@@ -189,6 +232,7 @@ __device__ __forceinline__ StackRef adj_stack(uint32_t* smem, int cap) {
 
 // Primal pass: the radiance C of every camera sample (the estimator of
 // aur_render), w = 1 when the sample hit something.
+template <bool kMis>
 __global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_primal(SceneView sc, aur_camera cam, aur_render_params p, uint32_t s0,
                                                             uint32_t nb, float4* __restrict__ prim,
                                                             uint32_t* __restrict__ err, int cap) {
@@ -201,11 +245,13 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_primal(Sce
     const uint32_t s = s0 + (uint32_t)(t / P);
     const PathRay r = camera_ray(cam, p.width, p.height, pix % p.width, pix / p.width, s, p.spp);
     uint32_t visits = 0;
-    const SampleResult res = integrate_diffuse(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err);
+    const SampleResult res =
+        integrate_diffuse<kMis>(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err);
     prim[t] = make_float4(res.color.x, res.color.y, res.color.z, res.any_hit ? 1.0f : 0.0f);
 }
 
 // Replay pass.
+template <bool kMis>
 __global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_replay(SceneView sc, aur_camera cam, aur_render_params p, uint32_t s0,
                                                             uint32_t nb, const float4* __restrict__ prim,
                                                             const float4* __restrict__ d_image,
@@ -232,7 +278,7 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_replay(Sce
             const float w = 1.0f / (float)p.spp;
             const f3 g = mk3(di.x * w, di.y * w, di.z * w);
             uint32_t visits = 0;
-            replay(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, mk3(c.x, c.y, c.z), g, d_diffuse,
+            replay<kMis>(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, mk3(c.x, c.y, c.z), g, d_diffuse,
                    shared_lights ? s_light : d_light, gl0, visits, err);
         }
     }
@@ -276,9 +322,14 @@ aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_ca
     aur_status st = check_params(params);
     if (st == AUR_OK) st = check_scene_textures(scene);
     if (st != AUR_OK) return st;
-    AUR_CHECK(params->mode != AUR_MODE_PATH_MIS, AUR_ERR_UNSUPPORTED,
-              "aur_render_adjoint: differentiates AUR_MODE_REFERENCE and AUR_MODE_PATH renders");
+    const bool mis = params->mode == AUR_MODE_PATH_MIS;
+    AUR_CHECK(!mis || scene->num_lights < 32767, AUR_ERR_INVALID,
+              "aur_render_adjoint: AUR_MODE_PATH_MIS takes at most 32766 lights (scene has %u)", scene->num_lights);
     AUR_CUDA(cudaSetDevice(ctx->device));
+    if (mis) {
+        st = build_mis_table(ctx, scene);
+        if (st != AUR_OK) return st;
+    }
     {
         std::vector<aur_shader> sh(scene->num_shaders);
         AUR_CUDA(cudaMemcpy(sh.data(), scene->shaders, sizeof(aur_shader) * sh.size(), cudaMemcpyDeviceToHost));
@@ -294,7 +345,8 @@ aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_ca
     const int cap = (int)scene->nmh->levels + 1;
     const size_t smem_p = (size_t)2 * cap * kAdjThreads * sizeof(uint32_t);
     const size_t smem_r = smem_p + 3 * kSharedLights * sizeof(float);
-    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
+    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
+    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
     float4* prim = nullptr;
     AUR_CHECK(::aur::dev_malloc_async(&prim, P * batch * sizeof(float4), ctx->stream) == cudaSuccess, AUR_ERR_OOM,
               "aur_render_adjoint: out of device memory");
@@ -302,9 +354,17 @@ aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_ca
     for (uint32_t s = s0; s < s1; s += batch) {
         const uint32_t nb = std::min(batch, s1 - s);
         const uint32_t grid = cdiv(P * nb, kAdjThreads);
-        k_adj_primal<<<grid, kAdjThreads, smem_p, ctx->stream>>>(sv, *camera, p, s, nb, prim, ctx->d_flags, cap);
-        k_adj_replay<<<grid, kAdjThreads, smem_r, ctx->stream>>>(sv, *camera, p, s, nb, prim, (const float4*)d_image,
-                                                                d_diffuse, d_light_color, ctx->d_flags, cap);
+        if (mis) {
+            k_adj_primal<true><<<grid, kAdjThreads, smem_p, ctx->stream>>>(sv, *camera, p, s, nb, prim, ctx->d_flags,
+                                                                           cap);
+            k_adj_replay<true><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
+                sv, *camera, p, s, nb, prim, (const float4*)d_image, d_diffuse, d_light_color, ctx->d_flags, cap);
+        } else {
+            k_adj_primal<false><<<grid, kAdjThreads, smem_p, ctx->stream>>>(sv, *camera, p, s, nb, prim, ctx->d_flags,
+                                                                            cap);
+            k_adj_replay<false><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
+                sv, *camera, p, s, nb, prim, (const float4*)d_image, d_diffuse, d_light_color, ctx->d_flags, cap);
+        }
     }
     cudaFreeAsync(prim, ctx->stream);
     AUR_CUDA(cudaGetLastError());

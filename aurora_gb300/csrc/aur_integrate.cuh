@@ -266,9 +266,11 @@ __device__ __forceinline__ float emission_weight(const SceneView& sc, uint32_t t
 // contribution `c` it adds if the segment from o along d over (Epsilon, tmax)
 // is unoccluded; cand false when it adds nothing whatever the visibility.
 // The plain integrators trace the ray at once, the wavefront queues it.
+// For the adjoint, c = f * e * geo up to rounding: e is the emitted colour
+// scale (an area light's colour * intensity, an emitter's emission colour).
 struct ShadowSample {
-    f3 c, o, d;
-    float tmax;
+    f3 c, o, d, e;
+    float tmax, geo;
     bool cand;
 };
 
@@ -319,6 +321,8 @@ __device__ __forceinline__ ShadowSample area_light_sample(const AreaLightMis& q,
         const float lpdf = (wt * wt) / (cl * q.area);
         const float w = mis_weight(lpdf, bsdf_pdf(b, wo, wdir));
         s.c = f * (q.Le0 * cl) * ((cs * w) / lpdf);
+        s.e = q.Le0;
+        s.geo = cl * ((cs * w) / lpdf);
         s.o = offset_origin(position, wdir);
         s.d = wdir;
         s.tmax = wt + kEpsilon;
@@ -346,6 +350,8 @@ __device__ __forceinline__ ShadowSample area_bsdf_sample(const AreaLightMis& q, 
             const float lpdf = (tl * tl) / (cl * q.area);
             const float w = mis_weight(bpdf, lpdf);
             s.c = f * (q.Le0 * cl) * ((cs * w) / bpdf);
+            s.e = q.Le0;
+            s.geo = cl * ((cs * w) / bpdf);
             s.o = offset_origin(position, wi);
             s.d = wi;
             s.tmax = tl + kEpsilon;
@@ -419,6 +425,8 @@ __device__ __forceinline__ ShadowSample emitter_shadow_sample(const SceneView& s
     const uint32_t sid = sc.sids[tri];
     const aur_shader* sh = sc.shaders + (sid > 0 ? sid - 1 : 0);
     s.c = f * from(sh->emission_color) * ((cs * w) / epdf);
+    s.e = from(sh->emission_color);
+    s.geo = (cs * w) / epdf;
     s.o = offset_origin(position, wdir);
     s.d = wdir;
     s.tmax = t * 0.9999f;

@@ -134,8 +134,8 @@ typedef struct aur_camera {
  *    triangles sampled from a table proportional to emission * area, their
  *    emission found by diffuse bounces weighted against it. Images differ
  *    from the other modes by design (the reference's light sample has no
- *    area / distance^2 factor). aur_render, aur_raytrace_monte_carlo and
- *    the wavefront batch (not the adjoint); at most 32766 lights. */
+ *    area / distance^2 factor). Every render entry point and the adjoint
+ *    take it; at most 32766 lights. */
 enum { AUR_MODE_REFERENCE = 0, AUR_MODE_PATH = 1, AUR_MODE_PATH_MIS = 2 };
 
 /* Per-render parameters (Dim(width,height,samples), MAX_DEPTH, RNG seed). */
@@ -456,8 +456,9 @@ aur_status aur_filter_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, cons
  * reference. d_image: device, width*height float4 = dLoss/d(accum) of
  * aur_render with the same parameters (alpha ignored). d_diffuse
  * (num_shaders*3) and d_light_color (num_lights*3), device: gradients are
- * ADDED. Same estimator and RNG streams as aur_render; materials must be
- * non-specular (AUR_ERR_UNSUPPORTED otherwise). */
+ * ADDED. Same estimator and RNG streams as aur_render, in every mode
+ * (AUR_MODE_PATH_MIS included: its weights do not depend on the colours);
+ * materials must be non-specular (AUR_ERR_UNSUPPORTED otherwise). */
 aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_camera* camera,
                               const aur_render_params* params, const float* d_image, float* d_diffuse,
                               float* d_light_color);

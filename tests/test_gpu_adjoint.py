@@ -16,13 +16,13 @@ def _loss(img, target):
     return float((d[..., :3] ** 2).sum())
 
 
-def _setup(ctx, mode, W=48, spp=8, depth=4):
-    sd = scenes.cornell_sphere(seed=3)
+def _setup(ctx, mode, W=48, spp=8, depth=4, sd=None):
+    sd = scenes.cornell_sphere(seed=3) if sd is None else sd
     sc = api.Scene(ctx, sd)
     p = T.render_params(W, W, spp, depth, seed=5, mode=mode)
     rng = np.random.default_rng(1)
     target_sh = sd.shaders.copy()
-    target_sh["diffuse_color"] = np.clip(target_sh["diffuse_color"] + rng.normal(0, 0.05, (sd.count, 3)), 0, 1)
+    target_sh["diffuse_color"] = np.clip(target_sh["diffuse_color"] + rng.normal(0, 0.05, (len(target_sh), 3)), 0, 1)
     sc.set_shaders(target_sh)
     target = sc.render(p)
     sc.set_shaders(sd.shaders)
@@ -45,9 +45,12 @@ def _fd(sc, sd, p, target, kind, idx, ch):
     return (vals[0] - vals[1]) / (2 * H)
 
 
-@pytest.mark.parametrize("mode", [T.MODE_PATH, T.MODE_REFERENCE])
-def test_adjoint_matches_finite_differences(ctx, mode):
-    sd, sc, p, target = _setup(ctx, mode)
+@pytest.mark.parametrize("mode,scene", [(T.MODE_PATH, "sphere"), (T.MODE_REFERENCE, "sphere"),
+                                        (T.MODE_PATH_MIS, "sphere"), (T.MODE_PATH_MIS, "emissive")])
+def test_adjoint_matches_finite_differences(ctx, mode, scene):
+    """MIS: the area light by both strategies (sphere), and emissive
+    triangles sampled from the table plus the area light (emissive)."""
+    sd, sc, p, target = _setup(ctx, mode, sd=None if scene == "sphere" else scenes.cornell_emissive(area_light=True))
     img = sc.render(p)
     d_image = (2.0 * (img - target)).contiguous()
     d_image[..., 3] = 0.0

@@ -1,7 +1,7 @@
 """AUR_MODE_PATH_MIS on the GPU: the light-selection table and the images
 against the oracle, unbiasedness at high sample counts, the tile entry point
-and the wavefront batch against the fused renderer, and the adjoint's
-refusal."""
+and and the wavefront batch against the fused renderer (the adjoint's
+finite-difference checks are in test_gpu_adjoint.py)."""
 import numpy as np
 import pytest
 
@@ -116,17 +116,6 @@ def test_wavefront_equals_plain(ctx, tuning):
     batch.status()
     for sc, p, f in zip(scs, prm, frames):
         assert np.array_equal(f.cpu().numpy(), sc.render(p).cpu().numpy())
-
-
-def test_adjoint_rejects_the_mode(ctx):
-    import torch
-    sd = scenes.cornell_emissive(area_light=True)
-    sc = api.Scene(ctx, sd)
-    p = T.render_params(16, 16, 1, 2, mode=T.MODE_PATH_MIS)
-    d_img = torch.ones((16, 16, 4), dtype=torch.float32, device="cuda")
-    with pytest.raises(api.AuroraError) as e:
-        sc.adjoint(p, d_img)
-    assert e.value.status == 6                          # AUR_ERR_UNSUPPORTED
 
 
 def test_wavefront_light_slot_limit(ctx):
