@@ -582,6 +582,19 @@ def bench_terrain(ctx, res=2048, samples=1, ref_spp=16384, small=(64, 36), small
     def rmse(a):
         return float(torch.sqrt(((a[..., :3].double() - ref[..., :3].double()) ** 2).mean()))
 
+    # CPU baseline on a bounded sample of the workload: the oracle renders the
+    # small crop at 1 spp on all host cores (the GPU's NMH permutation, equal
+    # to the oracle's own build, saves the host build of 8.4M triangles); the
+    # GPU's image of the same crop must be bit-identical
+    import oracle
+    ns = oracle.NmhScene(sd, perm=sc.nmh.export(with_vertices=False)[0])
+    pc = T.render_params(sw, sh, 1, 8, seed=0, mode=T.MODE_PATH)
+    nth = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    cimg, _ = oracle.render(ns, pc, camera=cam, nthreads=nth)
+    cpu_s = time.perf_counter() - t0
+    cpu_exact = bool(np.array_equal(sc.render(pc, camera=cam).cpu().numpy(), cimg))
+
     n_samples = W * H * samples
     return {"workload": "fBm terrain %dx%d vertices (%d triangles), 16 area lights, %dx%d, 256 spp, depth 8, path mode; "
                         "samples [0, %d) timed" % (res, res, sd.count, W, H, samples),
@@ -595,7 +608,10 @@ def bench_terrain(ctx, res=2048, samples=1, ref_spp=16384, small=(64, 36), small
             "wavefront_rays": {"closest": ext, "shadow": shadow, "iterations": iters,
                                "mrays_per_s": (ext + shadow) / (wf_ms * 1e-3) / 1e6},
             "rmse": {"reference": "%dx%d at %d spp (seed 1)" % (sw, sh, ref_spp), "spp": small_spp,
-                     "plain": rmse(pl), "wavefront": rmse(wfs)}}
+                     "plain": rmse(pl), "wavefront": rmse(wfs)},
+            "cpu_baseline": {"samples_per_s": sw * sh / cpu_s, "cores": nth, "kind": "port",
+                             "sample": "%dx%d crop of the same camera, 1 spp, depth 8, oracle C++ restatement" % (sw, sh),
+                             "gpu_bit_exact": cpu_exact}}
 
 
 def run_reference(args):
