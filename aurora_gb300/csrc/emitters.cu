@@ -8,6 +8,8 @@
 // as thrust::copy_if keeps order), then the emitter records, then an
 // inclusive scan of the weights in double (tile sums, one-block scan,
 // per-tile apply) rounded to float after normalisation.
+#include <mutex>
+
 #include "aur_internal.h"
 #include "aur_math.cuh"
 
@@ -213,9 +215,11 @@ __global__ void k_mis_pa(const uint32_t* __restrict__ tri, const float* __restri
     pa[i] = psel / mis_area(verts, i);
 }
 
-}  // namespace
+// Guards the lazily built tables: renders of one scene from several threads
+// (each on its own context) may ask for the table at the same time.
+std::mutex g_mis_mutex;
 
-void free_mis_table(const aur_scene* sc) {
+void free_mis_table_locked(const aur_scene* sc) {
     cudaFree(sc->mis_tri);
     cudaFree(sc->mis_cdf);
     cudaFree(sc->mis_pa);
@@ -226,9 +230,17 @@ void free_mis_table(const aur_scene* sc) {
     sc->mis_ready = false;
 }
 
+}  // namespace
+
+void free_mis_table(const aur_scene* sc) {
+    std::lock_guard<std::mutex> lock(g_mis_mutex);
+    free_mis_table_locked(sc);
+}
+
 aur_status build_mis_table(aur_ctx* ctx, const aur_scene* sc) {
+    std::lock_guard<std::mutex> lock(g_mis_mutex);
     if (sc->mis_ready) return AUR_OK;
-    free_mis_table(sc);
+    free_mis_table_locked(sc);
     const uint32_t n = sc->nmh->count;
     if (n == 0) {
         sc->mis_ready = true;
@@ -282,7 +294,7 @@ aur_status build_mis_table(aur_ctx* ctx, const aur_scene* sc) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) st = cuda_fail(e, "render (light-selection table)", __FILE__, __LINE__);
     if (st != AUR_OK) {
-        free_mis_table(sc);
+        free_mis_table_locked(sc);
         return st;
     }
     sc->mis_count = m;
