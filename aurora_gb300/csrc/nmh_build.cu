@@ -498,6 +498,282 @@ __global__ void __launch_bounds__(kThreads) k_partition(ListSet ls, uint32_t M, 
     }
 }
 
+// ------------------------------------------------ subtree finish in shared memory
+// Once every node segment of a level holds at most kLocalMax triangles, one
+// block per node of that level finishes its whole subtree with the same
+// per-level steps (select, emit, split, partition) on shared-memory copies of
+// the three lists, instead of 8 launches per remaining level over the whole
+// soup. Triangles get block-local ids (their position in the first list);
+// lists hold local ids, the global node_of array is reused as the pid ->
+// local id map while the block loads its segment.
+constexpr uint32_t kLocalMax = 2048;
+constexpr int kLocalThreads = 512;
+constexpr int kLocalPer = (int)kLocalMax / kLocalThreads;   // elements per thread in block scans
+constexpr uint16_t kLocalDone = 0xFFFFu;
+
+struct LocalSmem {
+    uint16_t list[2][3][kLocalMax];       // local ids, double-buffered, per axis
+    uint16_t node[kLocalMax];             // local node index at the current depth, kLocalDone once paired
+    uint16_t nnode[kLocalMax];            // child index at the next depth
+    uint16_t pre0[kLocalMax];             // block-scan outputs (exclusive prefix counts)
+    uint16_t pre1[kLocalMax];
+    uint32_t pid[kLocalMax];              // global prim id of each local id
+    uint16_t off[kLocalMax / 2 + 1];      // segment offsets of the depth's nodes (+ end)
+    uint16_t numl[kLocalMax / 2];         // triangles going to the left child
+    uint16_t p0[kLocalMax / 2];           // pair[0] (local id) per node
+    unsigned long long best[kLocalMax / 2];
+    uint32_t warp_tot[kLocalThreads / 32][2];
+};
+
+// Exclusive prefix counts of two flags over positions [0, m) (each thread a
+// contiguous chunk of kLocalPer), written to out0 and (if not null) out1;
+// returns the totals.
+template <typename F>
+__device__ __forceinline__ void local_scan2(LocalSmem& s, uint32_t m, F flags, uint16_t* out0, uint16_t* out1,
+                                            uint32_t& tot0, uint32_t& tot1) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t b = (uint32_t)t * kLocalPer;
+    uint32_t f0[kLocalPer], f1[kLocalPer];
+    uint32_t c0 = 0, c1 = 0;
+#pragma unroll
+    for (int i = 0; i < kLocalPer; ++i) {
+        f0[i] = f1[i] = 0;
+        if (b + i < m) flags(b + i, f0[i], f1[i]);
+        c0 += f0[i];
+        c1 += f1[i];
+    }
+    uint32_t x0 = c0, x1 = c1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y0 = __shfl_up_sync(0xffffffffu, x0, o), y1 = __shfl_up_sync(0xffffffffu, x1, o);
+        if (lane >= o) { x0 += y0; x1 += y1; }
+    }
+    if (lane == 31) { s.warp_tot[warp][0] = x0; s.warp_tot[warp][1] = x1; }
+    __syncthreads();
+    uint32_t w0 = 0, w1 = 0, a0 = 0, a1 = 0;
+    for (int w = 0; w < kLocalThreads / 32; ++w) {
+        if (w < warp) { w0 += s.warp_tot[w][0]; w1 += s.warp_tot[w][1]; }
+        a0 += s.warp_tot[w][0];
+        a1 += s.warp_tot[w][1];
+    }
+    uint32_t r0 = w0 + x0 - c0, r1 = w1 + x1 - c1;
+#pragma unroll
+    for (int i = 0; i < kLocalPer; ++i) {
+        if (b + i < m) {
+            out0[b + i] = (uint16_t)r0;
+            if (out1) out1[b + i] = (uint16_t)r1;
+        }
+        r0 += f0[i];
+        r1 += f1[i];
+    }
+    tot0 = a0;
+    tot1 = a1;
+    __syncthreads();
+}
+
+// Finishes the subtree of node L0 + blockIdx.x (levels lv0 .. levels-1).
+// Lists: the level-lv0 lists (axis x at list + x * S), node segments in heap
+// order. Writes heap[2g], heap[2g+1] for every node g of the subtree.
+__global__ void __launch_bounds__(kLocalThreads) k_local_finish(const uint32_t* __restrict__ list, size_t S,
+                                                                 const float* __restrict__ mn,
+                                                                 const float* __restrict__ mx, uint32_t n,
+                                                                 uint32_t lv0, uint32_t L0,
+                                                                 const uint32_t* __restrict__ nstart,
+                                                                 uint32_t npids, uint32_t* __restrict__ lid_of,
+                                                                 uint32_t* __restrict__ heap,
+                                                                 float* __restrict__ sbox,
+                                                                 uint32_t* __restrict__ err) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    LocalSmem& s = *reinterpret_cast<LocalSmem*>(smem_raw);
+    const uint32_t k = L0 + blockIdx.x;
+    const int t = threadIdx.x;
+    const uint32_t seg0 = nstart[k];
+    const uint32_t len = (uint32_t)(2 * subtree_nodes(k, n));
+    if (len > kLocalMax) {   // the host chose lv0 so that this cannot happen
+        if (t == 0) atomicOr(err, 4u);
+        return;
+    }
+    const uint32_t a0 = lv0 % 3u;
+    // local ids: positions in the select axis' list
+    for (uint32_t j = t; j < len; j += kLocalThreads) {
+        const uint32_t gp = list[a0 * S + seg0 + j];
+        s.pid[j] = gp;
+        s.list[0][a0][j] = (uint16_t)j;
+        s.node[j] = 0;
+        lid_of[gp] = j;
+    }
+    __syncthreads();
+    for (uint32_t j = t; j < len; j += kLocalThreads) {
+#pragma unroll
+        for (uint32_t x = 0; x < 3; ++x)
+            if (x != a0) s.list[0][x][j] = (uint16_t)lid_of[list[x * S + seg0 + j]];
+    }
+    for (uint32_t r = t; r < kLocalMax / 2; r += kLocalThreads) s.best[r] = 0ull;
+    __syncthreads();
+    int cur = 0;
+    uint32_t depth_last = 0;
+    for (uint32_t d = 0;; ++d) {
+        depth_last = d;
+        const uint32_t lv = lv0 + d;
+        const uint64_t G0 = (uint64_t)(k + 1) * (1ull << d) - 1ull;
+        if (G0 >= n) break;
+        const uint64_t avail = (uint64_t)n - G0;
+        const uint32_t nd = (uint32_t)((1ull << d) < avail ? (1ull << d) : avail);
+        const uint32_t a = lv % 3u, b = (lv + 1) % 3u, c = (lv + 2) % 3u;
+        // node table of this depth: segment lengths and left sizes, offsets by a scan
+        {
+            uint32_t tot0, tot1;
+            local_scan2(
+                s, nd,
+                [&](uint32_t r, uint32_t& f0, uint32_t& f1) {
+                    const uint64_t g = G0 + r;
+                    f0 = (uint32_t)(2 * subtree_nodes(g, n));
+                    f1 = 0;
+                    s.numl[r] = (uint16_t)((2 * g + 1 < n) ? 2 * subtree_nodes(2 * g + 1, n) : 0);
+                },
+                s.off, nullptr, tot0, tot1);
+            if (t == 0) s.off[nd] = (uint16_t)tot0;
+            __syncthreads();
+        }
+        const uint32_t m = s.off[nd];
+        // select: pair[0] = first of the segment on axis a, pair[1] = arg-max
+        // of (max-key, lowest prim id) over the rest (k_select)
+        for (uint32_t j = t; j < m; j += kLocalThreads) {
+            const uint16_t lid = s.list[cur][a][j];
+            const uint32_t r = lid < len ? s.node[lid] : kLocalDone;
+            if (r >= nd) {   // consistency check: every listed triangle belongs to a node of this depth
+                atomicOr(err, 4u);
+                continue;
+            }
+            if (j == s.off[r]) {
+                s.p0[r] = lid;
+            } else {
+                const uint32_t gp = s.pid[lid];
+                const unsigned long long key =
+                    ((unsigned long long)orderable(mx[a * S + gp]) << 32) | (unsigned long long)(0xFFFFFFFFu - gp);
+                atomicMax(&s.best[r], key);
+            }
+        }
+        __syncthreads();
+        // emit (k_emit_pairs)
+        for (uint32_t r = t; r < nd; r += kLocalThreads) {
+            const uint32_t g = (uint32_t)(G0 + r);
+            const uint32_t q0 = s.p0[r];
+            const uint32_t p1 = 0xFFFFFFFFu - (uint32_t)(s.best[r] & 0xFFFFFFFFull);
+            s.best[r] = 0ull;
+            const uint32_t q1 = p1 < npids ? lid_of[p1] : kLocalMax;
+            if (q0 >= len || q1 >= len) {
+                atomicOr(err, 4u);
+                continue;
+            }
+            heap[2 * g] = s.pid[q0];
+            heap[2 * g + 1] = p1;
+            s.node[q0] = kLocalDone;
+            s.node[q1] = kLocalDone;
+        }
+        __syncthreads();
+        if (2 * G0 + 1 >= n) break;   // no node below this depth
+        const int nxt = cur ^ 1;
+        // split the next axis' list: drop the pairs, rank within the node's
+        // remainder decides left / right (k_split_next)
+        {
+            uint32_t td, tu;
+            local_scan2(
+                s, m,
+                [&](uint32_t j, uint32_t& f0, uint32_t& f1) {
+                    const uint16_t lid = s.list[cur][b][j];
+                    f0 = lid < len && s.node[lid] == kLocalDone;
+                    f1 = 0;
+                },
+                s.pre0, nullptr, td, tu);
+            for (uint32_t j = t; j < m; j += kLocalThreads) {
+                const uint16_t lid = s.list[cur][b][j];
+                const uint32_t r = lid < len ? s.node[lid] : kLocalDone;
+                if (r == kLocalDone) continue;
+                if (r >= nd) {
+                    atomicOr(err, 4u);
+                    continue;
+                }
+                const uint32_t db = s.pre0[j];
+                const uint32_t rpos = (j - s.off[r]) - (db - 2u * r);
+                s.nnode[lid] = (uint16_t)(rpos < s.numl[r] ? 2u * r : 2u * r + 1u);
+                s.list[nxt][b][j - db] = lid;
+            }
+            __syncthreads();
+        }
+        // stable partition of the other two lists into left then right child
+        // segments (k_partition)
+        for (int which = 0; which < 2; ++which) {
+            const uint32_t x = which == 0 ? a : c;
+            uint32_t td, tl;
+            local_scan2(
+                s, m,
+                [&](uint32_t j, uint32_t& f0, uint32_t& f1) {
+                    const uint16_t lid = s.list[cur][x][j];
+                    const bool done = lid >= len || s.node[lid] == kLocalDone;
+                    f0 = done;
+                    f1 = !done && !(s.nnode[lid] & 1u);
+                },
+                s.pre0, s.pre1, td, tl);
+            for (uint32_t j = t; j < m; j += kLocalThreads) {
+                const uint16_t lid = s.list[cur][x][j];
+                const uint32_t r = lid < len ? s.node[lid] : kLocalDone;
+                if (r == kLocalDone) continue;
+                if (r >= nd) {
+                    atomicOr(err, 4u);
+                    continue;
+                }
+                const uint32_t o = s.off[r];
+                const uint32_t base = o - 2u * r;                 // left child's segment at the next depth
+                const uint32_t lb = s.pre1[j] - s.pre1[o];        // left elements of this node before j
+                const uint32_t db = s.pre0[j] - s.pre0[o];        // retired elements of this node before j
+                uint32_t dst;
+                if (!(s.nnode[lid] & 1u)) dst = base + lb;
+                else dst = base + s.numl[r] + ((j - o) - lb - db);
+                if (dst < m - 2u * nd) s.list[nxt][x][dst] = lid;
+                else atomicOr(err, 4u);
+            }
+            __syncthreads();
+        }
+        for (uint32_t j = t; j < len; j += kLocalThreads)
+            if (s.node[j] != kLocalDone) s.node[j] = s.nnode[j];
+        __syncthreads();
+        cur = nxt;
+    }
+    // subtree boxes of the subtree's nodes, bottom-up: the pair's bounds
+    // (k_bounds' per-triangle min / max) and the children's subtree boxes,
+    // written by this block one depth earlier
+    for (int d = (int)depth_last; d >= 0; --d) {
+        const uint64_t G0 = (uint64_t)(k + 1) * (1ull << d) - 1ull;
+        const uint64_t avail = (uint64_t)n - G0;
+        const uint32_t nd = (uint32_t)((1ull << d) < avail ? (1ull << d) : avail);
+        for (uint32_t r = t; r < nd; r += kLocalThreads) {
+            const uint32_t g = (uint32_t)(G0 + r);
+            const uint32_t p = heap[2 * g], q = heap[2 * g + 1];
+            float b[6];
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+                b[ax] = fminf(mn[ax * S + p], mn[ax * S + q]);
+                b[3 + ax] = fmaxf(mx[ax * S + p], mx[ax * S + q]);
+            }
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                const uint32_t c = 2 * g + 1 + j;
+                if (c < n) {
+#pragma unroll
+                    for (int ax = 0; ax < 3; ++ax) {
+                        b[ax] = fminf(b[ax], sbox[6 * (size_t)c + ax]);
+                        b[3 + ax] = fmaxf(b[3 + ax], sbox[6 * (size_t)c + 3 + ax]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int q6 = 0; q6 < 6; ++q6) sbox[6 * (size_t)g + q6] = b[q6];
+        }
+        __syncthreads();
+    }
+}
+
 // Orders each pair by (min-key on the last level's axis, prim id).
 __global__ void k_pair_order(uint32_t n, const uint32_t* __restrict__ heap, const float* __restrict__ mn_last,
                              uint32_t* __restrict__ perm) {
@@ -564,17 +840,21 @@ __device__ __forceinline__ void pad_interval(float lo, float hi, float& plo, flo
     phi = hi + p;
 }
 
-// One heap level, bottom-up: box[k] becomes the bounding box of node k's
-// subtree (its pair and its children's subtrees, computed one launch
-// earlier), and the padded subtree boxes of the children go into record
-// words 5..7 of node k (an empty box where a child does not exist).
-__global__ void k_node_boxes(uint32_t L0, uint32_t L1, uint32_t n, float* __restrict__ box,
-                             float4* __restrict__ recs) {
+// Nodes [L0, L1) (kUnion: one heap level, bottom-up): with kUnion, sbox[k]
+// becomes the bounding box of node k's subtree (its pair's box pbox[k] and
+// its children's subtree boxes, computed one launch earlier); in both forms
+// the padded subtree boxes of the children go into record words 5..7 of
+// node k (an empty box where a child does not exist).
+template <bool kUnion>
+__global__ void k_node_boxes(uint32_t L0, uint32_t L1, uint32_t n, const float* __restrict__ pbox,
+                             float* __restrict__ box, float4* __restrict__ recs) {
     const uint32_t k = L0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= L1) return;
     float b[6];
+    if (kUnion) {
 #pragma unroll
-    for (int q = 0; q < 6; ++q) b[q] = box[6 * (size_t)k + q];
+        for (int q = 0; q < 6; ++q) b[q] = pbox[6 * (size_t)k + q];
+    }
     float cb[2][6];
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
@@ -592,8 +872,10 @@ __global__ void k_node_boxes(uint32_t L0, uint32_t L1, uint32_t n, float* __rest
             for (int ax = 0; ax < 3; ++ax) { cb[j][ax] = 1.0f; cb[j][3 + ax] = -1.0f; }
         }
     }
+    if (kUnion) {
 #pragma unroll
-    for (int q = 0; q < 6; ++q) box[6 * (size_t)k + q] = b[q];
+        for (int q = 0; q < 6; ++q) box[6 * (size_t)k + q] = b[q];
+    }
     float4* rec = recs + (size_t)k * kRecStride + 5;
     rec[0] = make_float4(cb[0][0], cb[0][1], cb[0][2], cb[0][3]);
     rec[1] = make_float4(cb[0][4], cb[0][5], cb[1][0], cb[1][1]);
@@ -608,15 +890,42 @@ uint32_t log2i(uint32_t x) {
     return r;
 }
 
-// Node records: pairs and slabs, then the children's subtree boxes level by
-// level from the bottom. box: 6 floats per node of scratch.
-void emit_records(const float* V, uint32_t count, const uint32_t* perm, uint32_t n, uint32_t levels, float* verts,
-                  float4* recs, float* box, cudaStream_t st) {
-    k_emit_nodes<<<cdiv(n, 128), 128, 0, st>>>(V, count, perm, n, verts, recs, box);
-    for (int lv = (int)levels - 1; lv >= 0; --lv) {
+// First level whose node segments all fit k_local_finish (the leftmost
+// subtree of a level of a complete heap is its largest).
+uint32_t local_level(uint32_t n, uint32_t levels) {
+    for (uint32_t lv = 0; lv < levels; ++lv)
+        if (2 * subtree_nodes((1ull << lv) - 1ull, n) <= kLocalMax) return lv;
+    return levels;
+}
+
+// The remaining levels lv0 .. levels-1, one block per node of level lv0.
+cudaError_t finish_local(const uint32_t* list, size_t S, const float* mn, const float* mx, uint32_t n,
+                         uint32_t lv0, const uint32_t* nstart, uint32_t* node_of, uint32_t* heap, float* sbox,
+                         uint32_t* err, cudaStream_t st) {
+    const uint32_t L0 = (1u << lv0) - 1u;
+    const uint32_t L1 = ((2u << lv0) - 1u) < n ? ((2u << lv0) - 1u) : n;
+    const cudaError_t e = cudaFuncSetAttribute(k_local_finish, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)sizeof(LocalSmem));
+    if (e != cudaSuccess) return e;
+    k_local_finish<<<L1 - L0, kLocalThreads, sizeof(LocalSmem), st>>>(list, S, mn, mx, n, lv0, L0, nstart, 2 * n,
+                                                                      node_of, heap, sbox, err);
+    return cudaGetLastError();
+}
+
+// Node records: pairs and slabs, then the children's subtree boxes. The
+// subtree boxes of levels >= lv0 are in sbox already (k_local_finish); the
+// levels above are unions, level by level from the bottom, of the pair boxes
+// (pbox, written by k_emit_nodes) and the children's subtree boxes.
+// pbox and sbox: 6 floats per node of scratch each.
+void emit_records(const float* V, uint32_t count, const uint32_t* perm, uint32_t n, uint32_t lv0, float* verts,
+                  float4* recs, float* pbox, float* sbox, cudaStream_t st) {
+    k_emit_nodes<<<cdiv(n, 128), 128, 0, st>>>(V, count, perm, n, verts, recs, pbox);
+    const uint32_t Lb = (1u << lv0) - 1u;   // first node of level lv0
+    if (Lb < n) k_node_boxes<false><<<cdiv(n - Lb, 256), 256, 0, st>>>(Lb, n, n, pbox, sbox, recs);
+    for (int lv = (int)lv0 - 1; lv >= 0; --lv) {
         const uint32_t L0 = (1u << lv) - 1u;
         const uint32_t L1 = ((2u << lv) - 1u) < n ? ((2u << lv) - 1u) : n;
-        k_node_boxes<<<cdiv(L1 - L0, 256), 256, 0, st>>>(L0, L1, n, box, recs);
+        k_node_boxes<true><<<cdiv(L1 - L0, 256), 256, 0, st>>>(L0, L1, n, pbox, sbox, recs);
     }
 }
 
@@ -711,7 +1020,9 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
     cudaMemsetAsync(node_of, 0, (size_t)N * 4, st);
     cudaMemsetAsync(best, 0, (size_t)n * 8, st);
 
-    for (uint32_t lv = 0; lv < nmh->levels; ++lv) {
+    // levels above lv0 over the whole soup, the rest per subtree in shared memory
+    const uint32_t lv0 = local_level(n, nmh->levels);
+    for (uint32_t lv = 0; lv < lv0; ++lv) {
         const uint32_t L0 = (1u << lv) - 1u;
         const uint32_t L1 = ((2u << lv) - 1u) < n ? ((2u << lv) - 1u) : n;
         const uint32_t M = N - 2u * L0;
@@ -735,10 +1046,18 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
                                                       M - 2u * (L1 - L0), ctx->d_flags);
         uint32_t* t = listA; listA = listB; listB = t;
     }
+    if (lv0 < nmh->levels) {
+        const cudaError_t le = finish_local(listA, S, mn, mx, n, lv0, ns, node_of, heap, (float*)k2, ctx->d_flags, st);
+        if (le != cudaSuccess) {
+            cudaFreeAsync(base, st);
+            cleanup();
+            return cuda_fail(le, "aur_nmh_build (subtree finish)", __FILE__, __LINE__);
+        }
+    }
     const int al = (int)((nmh->levels - 1) % 3);
     k_pair_order<<<cdiv(n, 256), 256, 0, st>>>(n, heap, mn + al * S, nmh->perm);
-    // mx is free once the levels are placed: 3*S >= 6*n floats for the boxes
-    emit_records(V, count, nmh->perm, n, nmh->levels, nmh->verts, nmh->node_recs, mx, st);
+    // mx and k2 are free once the levels are placed: 3*S >= 6*n floats each for the boxes
+    emit_records(V, count, nmh->perm, n, lv0, nmh->verts, nmh->node_recs, mx, (float*)k2, st);
     cudaFreeAsync(base, st);
     cudaError_t e = cudaGetLastError();
     uint32_t flags = 0;
@@ -893,7 +1212,8 @@ aur_status nmh_build_noalloc_impl(const float* V, uint32_t count, cudaStream_t s
     uint32_t* listA = vals;
     uint32_t* listB = v2;
     k_node_table<<<cdiv(n, 256), 256, 0, st>>>(n, ns, nl, nlb);
-    for (uint32_t lv = 0; lv < levels; ++lv) {
+    const uint32_t lv0 = local_level(n, levels);
+    for (uint32_t lv = 0; lv < lv0; ++lv) {
         const uint32_t L0 = (1u << lv) - 1u;
         const uint32_t L1 = ((2u << lv) - 1u) < n ? ((2u << lv) - 1u) : n;
         const uint32_t M = N - 2u * L0;
@@ -917,9 +1237,10 @@ aur_status nmh_build_noalloc_impl(const float* V, uint32_t count, cudaStream_t s
                                                       flags);
         uint32_t* t = listA; listA = listB; listB = t;
     }
+    if (lv0 < levels) AUR_CUDA(finish_local(listA, S, mn, mx, n, lv0, ns, node_of, heap, (float*)k2, flags, st));
     const int al = (int)((levels - 1) % 3);
     k_pair_order<<<cdiv(n, 256), 256, 0, st>>>(n, heap, mn + al * S, perm);
-    emit_records(V, count, perm, n, levels, verts, recs, mx, st);
+    emit_records(V, count, perm, n, lv0, verts, recs, mx, (float*)k2, st);
     AUR_CUDA(cudaGetLastError());
     uint32_t h_flags = 0;
     AUR_CUDA(cudaMemcpyAsync(&h_flags, flags, 4, cudaMemcpyDeviceToHost, st));

@@ -18,7 +18,8 @@ def _gpu_build(ctx, V):
     return nmh, perm, verts, levels
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 6, 7, 33, 34, 100, 1001, 4096, 65537, 300000])
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 6, 7, 33, 34, 100, 1001, 2047, 2048, 2049, 2050, 3071, 4096, 4099,
+                               8191, 65537, 300000])
 def test_build_matches_oracle(ctx, n):
     V = scenes.random_soup(n, seed=n)
     nmh, perm, verts, levels = _gpu_build(ctx, V)
