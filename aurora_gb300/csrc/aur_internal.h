@@ -79,6 +79,7 @@ struct aur_nmh {
     uint32_t input_count = 0; // triangles as given
     uint32_t levels = 0;
     uint32_t nodes = 0;       // count / 2
+    void* mem = nullptr;          // one allocation holding the three arrays below
     float4* node_recs = nullptr;  // nodes * 8 float4 (slab, 2 x (v1, e1, e2), children's boxes)
     uint32_t* perm = nullptr;     // NMH position -> original prim id
     float* verts = nullptr;       // count * 9, NMH order, reference layout

@@ -511,17 +511,23 @@ constexpr int kLocalThreads = 512;
 constexpr int kLocalPer = (int)kLocalMax / kLocalThreads;   // elements per thread in block scans
 constexpr uint16_t kLocalDone = 0xFFFFu;
 
+// 53.6 KB: four blocks fit an SM, so the 512 subtrees of a 1M-triangle
+// build run as one wave on 152 SMs.
 struct LocalSmem {
     uint16_t list[2][3][kLocalMax];       // local ids, double-buffered, per axis
     uint16_t node[kLocalMax];             // local node index at the current depth, kLocalDone once paired
-    uint16_t nnode[kLocalMax];            // child index at the next depth
-    uint16_t pre0[kLocalMax];             // block-scan outputs (exclusive prefix counts)
-    uint16_t pre1[kLocalMax];
+    uint8_t right[kLocalMax];             // 1: goes to the right child at the next depth
+    union {                               // select / emit use best, split / partition the scans
+        struct {
+            uint16_t pre0[kLocalMax];     // block-scan outputs (exclusive prefix counts)
+            uint16_t pre1[kLocalMax];
+        };
+        unsigned long long best[kLocalMax / 2];
+    };
     uint32_t pid[kLocalMax];              // global prim id of each local id
     uint16_t off[kLocalMax / 2 + 1];      // segment offsets of the depth's nodes (+ end)
     uint16_t numl[kLocalMax / 2];         // triangles going to the left child
     uint16_t p0[kLocalMax / 2];           // pair[0] (local id) per node
-    unsigned long long best[kLocalMax / 2];
     uint32_t warp_tot[kLocalThreads / 32][2];
 };
 
@@ -608,8 +614,6 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_finish(const uint32_t* 
         for (uint32_t x = 0; x < 3; ++x)
             if (x != a0) s.list[0][x][j] = (uint16_t)lid_of[list[x * S + seg0 + j]];
     }
-    for (uint32_t r = t; r < kLocalMax / 2; r += kLocalThreads) s.best[r] = 0ull;
-    __syncthreads();
     int cur = 0;
     uint32_t depth_last = 0;
     for (uint32_t d = 0;; ++d) {
@@ -636,6 +640,8 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_finish(const uint32_t* 
             __syncthreads();
         }
         const uint32_t m = s.off[nd];
+        for (uint32_t r = t; r < nd; r += kLocalThreads) s.best[r] = 0ull;   // shares storage with the scans
+        __syncthreads();
         // select: pair[0] = first of the segment on axis a, pair[1] = arg-max
         // of (max-key, lowest prim id) over the rest (k_select)
         for (uint32_t j = t; j < m; j += kLocalThreads) {
@@ -660,7 +666,6 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_finish(const uint32_t* 
             const uint32_t g = (uint32_t)(G0 + r);
             const uint32_t q0 = s.p0[r];
             const uint32_t p1 = 0xFFFFFFFFu - (uint32_t)(s.best[r] & 0xFFFFFFFFull);
-            s.best[r] = 0ull;
             const uint32_t q1 = p1 < npids ? lid_of[p1] : kLocalMax;
             if (q0 >= len || q1 >= len) {
                 atomicOr(err, 4u);
@@ -696,7 +701,7 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_finish(const uint32_t* 
                 }
                 const uint32_t db = s.pre0[j];
                 const uint32_t rpos = (j - s.off[r]) - (db - 2u * r);
-                s.nnode[lid] = (uint16_t)(rpos < s.numl[r] ? 2u * r : 2u * r + 1u);
+                s.right[lid] = rpos < s.numl[r] ? 0 : 1;
                 s.list[nxt][b][j - db] = lid;
             }
             __syncthreads();
@@ -712,7 +717,7 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_finish(const uint32_t* 
                     const uint16_t lid = s.list[cur][x][j];
                     const bool done = lid >= len || s.node[lid] == kLocalDone;
                     f0 = done;
-                    f1 = !done && !(s.nnode[lid] & 1u);
+                    f1 = !done && !s.right[lid];
                 },
                 s.pre0, s.pre1, td, tl);
             for (uint32_t j = t; j < m; j += kLocalThreads) {
@@ -728,7 +733,7 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_finish(const uint32_t* 
                 const uint32_t lb = s.pre1[j] - s.pre1[o];        // left elements of this node before j
                 const uint32_t db = s.pre0[j] - s.pre0[o];        // retired elements of this node before j
                 uint32_t dst;
-                if (!(s.nnode[lid] & 1u)) dst = base + lb;
+                if (!s.right[lid]) dst = base + lb;
                 else dst = base + s.numl[r] + ((j - o) - lb - db);
                 if (dst < m - 2u * nd) s.list[nxt][x][dst] = lid;
                 else atomicOr(err, 4u);
@@ -736,7 +741,7 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_finish(const uint32_t* 
             __syncthreads();
         }
         for (uint32_t j = t; j < len; j += kLocalThreads)
-            if (s.node[j] != kLocalDone) s.node[j] = s.nnode[j];
+            if (s.node[j] != kLocalDone) s.node[j] = (uint16_t)(2u * s.node[j] + s.right[j]);
         __syncthreads();
         cur = nxt;
     }
@@ -948,18 +953,20 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
     if (N == 0) { *out = nmh; return AUR_OK; }
 
     auto cleanup = [&]() {
-        cudaFree(nmh->node_recs);
-        cudaFree(nmh->perm);
-        cudaFree(nmh->verts);
+        cudaFree(nmh->mem);
         delete nmh;
     };
-    if (::aur::dev_malloc(&nmh->node_recs, (size_t)n * kRecStride * sizeof(float4)) != cudaSuccess ||
-        ::aur::dev_malloc(&nmh->perm, (size_t)N * sizeof(uint32_t)) != cudaSuccess ||
-        ::aur::dev_malloc(&nmh->verts, (size_t)N * 9 * sizeof(float)) != cudaSuccess) {
+    // records, permutation and vertices in one allocation (records first: 128-byte aligned)
+    const size_t b_recs = ((size_t)n * kRecStride * sizeof(float4) + 255) & ~(size_t)255;
+    const size_t b_perm = ((size_t)N * sizeof(uint32_t) + 255) & ~(size_t)255;
+    if (::aur::dev_malloc(&nmh->mem, b_recs + b_perm + (size_t)N * 9 * sizeof(float)) != cudaSuccess) {
         cudaGetLastError();
         cleanup();
         return fail(AUR_ERR_OOM, "aur_nmh_build: out of device memory for %u triangles", N);
     }
+    nmh->node_recs = (float4*)nmh->mem;
+    nmh->perm = (uint32_t*)((char*)nmh->mem + b_recs);
+    nmh->verts = (float*)((char*)nmh->mem + b_recs + b_perm);
 
     cudaStream_t st = ctx->stream;
     const uint32_t nb = cdiv(N, kSortTile);

@@ -56,7 +56,7 @@ def test_nmh_build_and_trace(ctx):
         nmh = api.Nmh(ctx, Vd, count=V.shape[0])
         hits = api.hits_to_numpy(api.trace_closest(ctx, nmh, api.rays_tensor(rays)))
         return [nmh.export()[0], hits.view(np.uint32), np.array(api.count_visits(ctx, nmh, api.rays_tensor(rays)))]
-    assert _sweep(op) >= 5
+    assert _sweep(op) >= 3          # NMH arrays, build scratch, trace counters
 
 
 def test_scene_textures_render_emitters_adjoint(ctx):
