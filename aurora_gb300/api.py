@@ -107,6 +107,15 @@ def check(status):
         raise AuroraError(status, lib().aur_last_error().decode())
 
 
+def _dense(t):
+    """The tensor itself if it is contiguous. The library reads device memory
+    asynchronously on its own stream, so a temporary contiguous copy could be
+    freed and reused before the read: callers pass contiguous tensors."""
+    if not t.is_contiguous():
+        raise ValueError("aurora_gb300: pass a contiguous tensor (the library reads it asynchronously)")
+    return t
+
+
 def _ptr(x):
     """Address of a numpy array / torch tensor / None."""
     if x is None:
@@ -313,8 +322,8 @@ class Scene:
         """RGB of texture `texture` (1-based) at n device (u, v) pairs."""
         import torch
         out = torch.empty((uv_dev.shape[0], 3), dtype=torch.float32, device="cuda")
-        check(lib().aur_scene_texfetch(self.ctx.handle, self.handle, texture, _ptr(uv_dev.contiguous()),
-                                       uv_dev.shape[0], _ptr(out)))
+        uv = _dense(uv_dev)
+        check(lib().aur_scene_texfetch(self.ctx.handle, self.handle, texture, _ptr(uv), uv.shape[0], _ptr(out)))
         return out
 
     def set_lights(self, lights):
@@ -341,7 +350,7 @@ class Scene:
             d_light = torch.zeros((max(1, self.data.lights.shape[0]), 3), dtype=torch.float32, device="cuda")
         cam = np.asarray(self.data.camera if camera is None else camera, T.camera_dtype).reshape(())
         check(lib().aur_render_adjoint(self.ctx.handle, self.handle, _ptr(cam), _ptr(p),
-                                       _ptr(d_image.contiguous()), _ptr(d_diffuse), _ptr(d_light)))
+                                       _ptr(_dense(d_image)), _ptr(d_diffuse), _ptr(d_light)))
         return d_diffuse, d_light
 
     def close(self):
@@ -381,7 +390,7 @@ def filter_pixels(ctx, W, H, in_dev, out_dev, region=None):
 def accum_save(ctx, path, accum_dev, samples_done, spp):
     """Checkpoint of an (H, W, 4) device accumulation buffer."""
     H, W = accum_dev.shape[:2]
-    check(lib().aur_accum_save(ctx.handle, os.fsencode(path), W, H, samples_done, spp, _ptr(accum_dev.contiguous())))
+    check(lib().aur_accum_save(ctx.handle, os.fsencode(path), W, H, samples_done, spp, _ptr(_dense(accum_dev))))
 
 
 def accum_load(ctx, path, accum_dev):

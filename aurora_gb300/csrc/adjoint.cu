@@ -171,7 +171,20 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
         // bounce, as in the primal
         bool cont = false;
         PathRay nr;
-        if (kMis || mode == AUR_MODE_PATH) {
+        if (kMis) {
+            depth++;
+            f3 wi, nt;
+            float pdf;
+            if (depth <= max_depth && mis_bounce(b, wo, thr, seed, scene, pixel, sample, rix, wi, nt, pdf)) {
+                nr.pos = position;
+                nr.dir = wi;
+                nr.weight = 1.0f;
+                nr.eta = ray.eta;
+                nr.thr = nt;
+                nr.pdf = pdf;
+                cont = true;
+            }
+        } else if (mode == AUR_MODE_PATH) {
             depth++;
             if (depth <= max_depth) {
                 float u1, u2;

@@ -196,20 +196,50 @@ __device__ __forceinline__ float mis_weight(float p_this, float p_other) {
     return 1.0f / (1.0f + r * r);
 }
 
-// BSDF::pdf (bsdf.cuh:22-30, 48-51): |cos| / pi on wo's side.
+// The Lambert density of BSDF::pdf (bsdf.cuh:22-30), |cos| / pi on wo's
+// side, with the cosine taken against the shading normal in world space.
 __device__ __forceinline__ float bsdf_pdf(const Bsdf& b, const f3& wo, const f3& wi) {
-    const f3 lwo = world_to_local(wo, b.N, b.S, b.T);
-    const f3 lwi = world_to_local(wi, b.N, b.S, b.T);
-    return (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
+    const float co = dot(wo, b.N), ci = dot(wi, b.N);
+    return (co * ci > 0.0f) ? fabsf(ci) * kInvPi : 0.0f;
 }
 
-// BSDF::samplef (bsdf.cuh:53-67): the direction and its density.
+// BSDF::samplef (bsdf.cuh:53-67) in an orthonormal frame about the shading
+// normal: the tangent made orthogonal to N (Gram-Schmidt), bitangent N x S.
+// The reference's interpolated tangent frame is not orthonormal on curved
+// meshes, so its directions are neither unit nor distributed as |cos| / pi;
+// in this frame they are (up to rounding), and the returned density is
+// bsdf_pdf of the returned direction, the one the light strategies weigh
+// against.
 __device__ __forceinline__ f3 bsdf_sample(const Bsdf& b, const f3& wo, float u1, float u2, float& pdf) {
-    const f3 lwo = world_to_local(wo, b.N, b.S, b.T);
+    f3 S = b.S - b.N * dot(b.N, b.S);
+    float l = length(S);
+    if (!(l > 1e-6f)) {   // tangent (anti)parallel to N: any perpendicular
+        S = fabsf(b.N.x) < 0.9f ? cross(b.N, mk3(1.0f, 0.0f, 0.0f)) : cross(b.N, mk3(0.0f, 1.0f, 0.0f));
+        l = length(S);
+    }
+    S = S / l;
+    const f3 T = cross(b.N, S);
     f3 lwi = sample_hemisphere_cosine(u1, u2);
-    if (lwo.z < 0.0f) lwi.z *= -1.0f;
-    pdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
-    return local_to_world(lwi, b.N, b.S, b.T);
+    if (dot(wo, b.N) < 0.0f) lwi.z *= -1.0f;
+    const f3 wi = local_to_world(lwi, b.N, S, T);
+    pdf = bsdf_pdf(b, wo, wi);
+    return wi;
+}
+
+// The diffuse bounce of the MIS mode (slot 0, as diffuse_bounce): the
+// direction from bsdf_sample, throughput f * |wi.N| / pdf.
+__device__ __forceinline__ bool mis_bounce(const Bsdf& b, const f3& wo, const f3& thr, uint32_t seed, uint32_t scene,
+                                           uint32_t pixel, uint32_t sample, uint32_t rix, f3& wi, f3& nthr,
+                                           float& pdf) {
+    float u1, u2;
+    draw2(seed, scene, pixel, sample, rix, 0u, u1, u2);
+    wi = bsdf_sample(b, wo, u1, u2, pdf);
+    const f3 f = bsdf_f(b);
+    if (pdf > 0.0f && !zero(f)) {
+        nthr = thr * (f * (fabsf(dot(wi, b.N)) / pdf));
+        return true;
+    }
+    return false;
 }
 
 // Distance t > Epsilon along dir from pos to the parallelogram
@@ -598,7 +628,8 @@ __device__ __forceinline__ SampleResult integrate(const SceneView& sc, uint32_t 
                 nr.pos = position;
                 nr.weight = 1.0f;
                 nr.eta = ray.eta;
-                if (diffuse_bounce(b, wo, ray.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr, nr.pdf)) {
+                if (kMis ? mis_bounce(b, wo, ray.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr, nr.pdf)
+                         : diffuse_bounce(b, wo, ray.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr, nr.pdf)) {
                     if (sp < AUR_MAX_DEPTH + 2) stack[sp++] = nr; else atomicOr(err, 2u);
                 }
             }
@@ -645,7 +676,9 @@ __device__ __forceinline__ SampleResult integrate_diffuse(const SceneView& sc, u
         if (++depth > max_depth) break;
         f3 wi, nthr;
         float bpdf;
-        if (!diffuse_bounce(b, wo, thr, seed, scene, pixel, sample, rix, wi, nthr, bpdf)) break;
+        if (!(kMis ? mis_bounce(b, wo, thr, seed, scene, pixel, sample, rix, wi, nthr, bpdf)
+                   : diffuse_bounce(b, wo, thr, seed, scene, pixel, sample, rix, wi, nthr, bpdf)))
+            break;
         pos = position;
         dir = wi;
         thr = nthr;

@@ -413,7 +413,11 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
         // bounce (BSDF::samplef, bsdf.cuh:222-236)
         float cont = 0.0f, bpdf = 0.0f;
         f3 wi = mk3(0.0f), nt = mk3(0.0f);
-        if ((mis || a.mode == AUR_MODE_PATH) && depth <= a.max_depth) {
+        if (mis && depth <= a.max_depth) {
+            const float4 t4 = a.thr[slot];
+            if (mis_bounce(bs, wo, mk3(t4.x, t4.y, t4.z), a.seed, sc.scene_id, pix, sample, rix, wi, nt, bpdf))
+                cont = 1.0f;
+        } else if (a.mode == AUR_MODE_PATH && depth <= a.max_depth) {
             float u1, u2;
             draw2(a.seed, sc.scene_id, pix, sample, rix, 0u, u1, u2);
             const f3 lwo = world_to_local(wo, bs.N, bs.S, bs.T);

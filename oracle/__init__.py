@@ -60,6 +60,11 @@ def lib():
         L.orc_render_ex.restype = ctypes.c_uint64
         L.orc_mis_table.argtypes = [P, P, P, U32, U32, P, P, P, P]
         L.orc_mis_table.restype = U32
+        L.orc_bsdf_hits.argtypes = [P, P, P, U32, P, U32, P, P, P, U32, P, P, ctypes.c_int, P]
+        L.orc_mis_weight.argtypes = [ctypes.c_float, ctypes.c_float]
+        L.orc_mis_weight.restype = ctypes.c_float
+        L.orc_hit_quad.argtypes = [P, P, P, P]
+        L.orc_hit_quad.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -77,6 +82,11 @@ def ref_lib():
         L.ref_trace_any.argtypes = [P, U32, P, U32, P]
         L.ref_uniform_order.restype = ctypes.c_int
         L.ref_shade_hits.argtypes = [P, P, P, P, P, U32, P, U32, P, U32, P, P, P, U32, P, U32, P]
+        L.ref_bsdf_hits.argtypes = [P, P, P, P, P, U32, P, U32, P, P, P, U32, P, P, P]
+        L.ref_power_heuristic.argtypes = [ctypes.c_float, ctypes.c_float]
+        L.ref_power_heuristic.restype = ctypes.c_float
+        L.ref_area_hit.argtypes = [P, P, P, P]
+        L.ref_area_hit.restype = ctypes.c_int
         _ref = L
     return _ref
 
@@ -307,12 +317,13 @@ def ref_shade_hits(nscene, tangents, bitangents, rays8, tri, tuv, uniforms):
     n = rays8.shape[0]
     u = np.ascontiguousarray(uniforms, np.float32).reshape(n, -1)
     out = np.zeros((n, 3), np.float32)
-    ref_lib().ref_shade_hits(_ptr(nscene.V), _ptr(nscene.N), _ptr(np.ascontiguousarray(tangents, np.float32)),
-                             _ptr(np.ascontiguousarray(bitangents, np.float32)), _ptr(nscene.S), nscene.V.shape[0],
+    # converted copies are held in locals: the call reads them through pointers
+    tg, bt = np.ascontiguousarray(tangents, np.float32), np.ascontiguousarray(bitangents, np.float32)
+    r8, tr, tv = (np.ascontiguousarray(rays8, np.float32), np.ascontiguousarray(tri, np.int32),
+                  np.ascontiguousarray(tuv, np.float32))
+    ref_lib().ref_shade_hits(_ptr(nscene.V), _ptr(nscene.N), _ptr(tg), _ptr(bt), _ptr(nscene.S), nscene.V.shape[0],
                              _ptr(nscene.shaders), nscene.shaders.shape[0], _ptr(nscene.lights),
-                             nscene.lights.shape[0], _ptr(np.ascontiguousarray(rays8, np.float32)),
-                             _ptr(np.ascontiguousarray(tri, np.int32)), _ptr(np.ascontiguousarray(tuv, np.float32)),
-                             n, _ptr(u), u.shape[1], _ptr(out))
+                             nscene.lights.shape[0], _ptr(r8), _ptr(tr), _ptr(tv), n, _ptr(u), u.shape[1], _ptr(out))
     return out
 
 
@@ -340,3 +351,41 @@ def generate_tb(normals):
     t = np.zeros_like(N); b = np.zeros_like(N)
     lib().orc_generate_tb(_ptr(N), N.shape[0], _ptr(t), _ptr(b))
     return t, b
+
+
+def bsdf_hits(nscene, rays8, tri, tuv, uniforms, probes, tangents=None, bitangents=None, reference=False,
+              mis=False):
+    """BSDF sampling at hits: (n, 6) = sampled wi.xyz, its pdf, pdf(wo, wi),
+    pdf(wo, probe). The oracle's path-mode bounce (or, mis=True, the MIS
+    mode's orthonormal-frame sampling), or (reference=True, with the tangent
+    frames) the reference's own BSDF::samplef and BSDF::pdf."""
+    n = rays8.shape[0]
+    out = np.zeros((n, 6), np.float32)
+    keep = [np.ascontiguousarray(a, t) for a, t in ((rays8, np.float32), (tri, np.int32), (tuv, np.float32),
+                                                    (uniforms, np.float32), (probes, np.float32))]
+    args = [_ptr(keep[0]), _ptr(keep[1]), _ptr(keep[2]), n, _ptr(keep[3]), _ptr(keep[4]), _ptr(out)]
+    if reference:
+        tb = [np.ascontiguousarray(tangents, np.float32), np.ascontiguousarray(bitangents, np.float32)]
+        ref_lib().ref_bsdf_hits(_ptr(nscene.V), _ptr(nscene.N), _ptr(tb[0]), _ptr(tb[1]), _ptr(nscene.S),
+                                nscene.V.shape[0], _ptr(nscene.shaders), nscene.shaders.shape[0], *args)
+    else:
+        lib().orc_bsdf_hits(_ptr(nscene.V), _ptr(nscene.N), _ptr(nscene.S), nscene.V.shape[0], _ptr(nscene.shaders),
+                            nscene.shaders.shape[0], *args[:-1], 1 if mis else 0, args[-1])
+    return out
+
+
+def mis_weight(a, b, reference=False):
+    """The oracle's MIS weight 1 / (1 + (b/a)^2), or the reference's powerHeuristic(1, a, 1, b)."""
+    return (ref_lib().ref_power_heuristic if reference else lib().orc_mis_weight)(a, b)
+
+
+def area_hit(light, pos, direction, reference=False):
+    """(hit, t) of a ray against an area light's quad: the oracle's hitQuad or
+    the reference's Light::visibleArea with nothing to occlude."""
+    lt = np.ascontiguousarray(light, T.light_dtype).reshape(())
+    p = np.ascontiguousarray(pos, np.float32)           # held here: the call reads them through pointers
+    d = np.ascontiguousarray(direction, np.float32)
+    t = np.zeros(1, np.float32)
+    f = ref_lib().ref_area_hit if reference else lib().orc_hit_quad
+    h = f(_ptr(lt), _ptr(p), _ptr(d), _ptr(t))
+    return bool(h), float(t[0])

@@ -730,20 +730,30 @@ inline float misWeight(float pThis, float pOther) {
     return 1.0f / (1.0f + r * r);
 }
 
-// BSDF::pdf (bsdf.cuh:22-30, 48-51)
+// The Lambert density of BSDF::pdf (bsdf.cuh:22-30), |cos| / pi on wo's
+// side, the cosine taken against the shading normal in world space.
 inline float bsdfPdf(const BSDF& b, const F3& wo, const F3& wi) {
-    const F3 lwo = worldToLocal(wo, b.N, b.S, b.T);
-    const F3 lwi = worldToLocal(wi, b.N, b.S, b.T);
-    return (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
+    const float co = dot(wo, b.N), ci = dot(wi, b.N);
+    return (co * ci > 0.0f) ? fabsf(ci) * kInvPi : 0.0f;
 }
 
-// BSDF::samplef (bsdf.cuh:53-67)
+// BSDF::samplef (bsdf.cuh:53-67) in an orthonormal frame about N: the
+// tangent made orthogonal to N (Gram-Schmidt), bitangent N x S; the density
+// returned is bsdfPdf of the returned direction.
 inline F3 bsdfSample(const BSDF& b, const F3& wo, float u1, float u2, float& pdf) {
-    const F3 lwo = worldToLocal(wo, b.N, b.S, b.T);
+    F3 S = b.S - b.N * dot(b.N, b.S);
+    float l = length(S);
+    if (!(l > 1e-6f)) {
+        S = fabsf(b.N.x) < 0.9f ? cross(b.N, mk3(1.0f, 0.0f, 0.0f)) : cross(b.N, mk3(0.0f, 1.0f, 0.0f));
+        l = length(S);
+    }
+    S = S / l;
+    const F3 T = cross(b.N, S);
     F3 lwi = sampleHemisphereCosine(u1, u2);
-    if (lwo.z < 0.0f) lwi.z *= -1.0f;
-    pdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
-    return localToWorld(lwi, b.N, b.S, b.T);
+    if (dot(wo, b.N) < 0.0f) lwi.z *= -1.0f;
+    const F3 wi = localToWorld(lwi, b.N, S, T);
+    pdf = bsdfPdf(b, wo, wi);
+    return wi;
 }
 
 // Distance t > Epsilon from pos along dir to the parallelogram p0 + a e1 + b e2.
@@ -964,7 +974,23 @@ SampleOut integrate(const Scene& sc, const aur_render_params& p, const Ray& prim
                 stack[sp++] = nr;
             }
         }
-        if (path && !specular) {
+        if (mis && !specular) {
+            depth++;
+            if (depth <= maxDepth) {
+                float u1, u2, pdf;
+                draw2(pc.key, pc.pixel, pc.sample, pc.ray, 0u, u1, u2);
+                const F3 wi = bsdfSample(b, wo, u1, u2, pdf);
+                const F3 f = bsdfF(b);
+                if (pdf > 0.0f && !zero(f)) {
+                    Ray nr = pointRay(position);
+                    nr.dir = wi;
+                    nr.eta = ray.eta;
+                    nr.thr = ray.thr * (f * (fabsf(dot(wi, b.N)) / pdf));
+                    nr.pdf = pdf;
+                    stack[sp++] = nr;
+                }
+            }
+        } else if (path && !specular) {
             depth++;
             if (depth <= maxDepth) {
                 // BSDF::samplef (bsdf.cuh:222-236)
@@ -1163,6 +1189,53 @@ uint32_t orc_mis_table(const float* V, const uint16_t* S, const uint32_t* perm, 
     }
     for (uint32_t k = 0; k < m; ++k) pa[tri[k]] = (cdf[k] - (k > 0 ? cdf[k - 1] : 0.0f)) / area[k];
     return m;
+}
+
+/* BSDF sampling at hits (NMH-ordered V, N, S; hit i: ray rays8[8i..] =
+ * origin, tmax, direction, pad; NMH triangle tri[i] (skipped when < 0);
+ * t/u/v tuv[3i..]) with uniforms[2i], [2i+1]: the MIS mode's bsdfSample
+ * (mis != 0) or the path-mode bounce; then bsdfPdf of the sampled direction
+ * and of probes[3i..]. out, 6 floats per hit: wi.xyz, the sample's pdf,
+ * pdf(wo, wi), pdf(wo, probe). */
+void orc_bsdf_hits(const float* V, const float* N, const uint16_t* S, uint32_t count, const aur_shader* shaders,
+                   uint32_t nshaders, const float* rays8, const int32_t* tri, const float* tuv, uint32_t n,
+                   const float* uniforms, const float* probes, int mis, float* out) {
+    Scene sc;
+    sc.V = V; sc.N = N; sc.S = S; sc.perm = nullptr; sc.count = count;
+    sc.shaders = shaders; sc.nshaders = nshaders; sc.lights = nullptr; sc.nlights = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        float* o = out + (size_t)i * 6;
+        for (int q = 0; q < 6; ++q) o[q] = 0.0f;
+        if (tri[i] < 0) continue;
+        const float* r = rays8 + (size_t)i * 8;
+        const F3 wo = -mk3(r[4], r[5], r[6]);
+        const aur_shader& sh = shaders[S[tri[i]] > 0 ? S[tri[i]] - 1 : 0];
+        const BSDF b = getBSDF(sc, sh, (uint32_t)tri[i], tuv[3 * i + 1], tuv[3 * i + 2]);
+        float pdf;
+        F3 wi;
+        if (mis) {
+            wi = bsdfSample(b, wo, uniforms[2 * i], uniforms[2 * i + 1], pdf);
+        } else {   // the path-mode bounce: BSDF::samplef in the reference's frame
+            const F3 lwo = worldToLocal(wo, b.N, b.S, b.T);
+            F3 lwi = sampleHemisphereCosine(uniforms[2 * i], uniforms[2 * i + 1]);
+            if (lwo.z < 0.0f) lwi.z *= -1.0f;
+            pdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
+            wi = localToWorld(lwi, b.N, b.S, b.T);
+        }
+        o[0] = wi.x; o[1] = wi.y; o[2] = wi.z;
+        o[3] = pdf;
+        o[4] = bsdfPdf(b, wo, wi);
+        o[5] = bsdfPdf(b, wo, mk3(probes[3 * i], probes[3 * i + 1], probes[3 * i + 2]));
+    }
+}
+
+/* The MIS weight of the oracle (and the GPU): 1 / (1 + (b / a)^2). */
+float orc_mis_weight(float a, float b) { return misWeight(a, b); }
+
+/* hitQuad against an area light's quad: 1 and the distance, else 0. */
+int orc_hit_quad(const aur_light* l, const float* pos, const float* dir, float* t) {
+    return hitQuad(mk3(pos[0], pos[1], pos[2]), mk3(dir[0], dir[1], dir[2]), from(l->position), from(l->e1),
+                   from(l->e2), *t) ? 1 : 0;
 }
 
 /* The two uniforms the integrators draw at one RNG slot (draw2): u1, u2. */

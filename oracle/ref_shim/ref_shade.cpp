@@ -8,7 +8,9 @@
  *   Shader::getBSDF (kernels/lib/shader.cuh), BSDF::f (bsdf.cuh),
  *   Light::sampleL / visiblePoint (light.cuh), sampleRectangle (sampling.cuh),
  *   estimateAmbientRadiance / estimateDirectRadianceDelta /
- *   estimateDirectRadiance (radiance.cuh), intersectAny (intersect.cuh).
+ *   estimateDirectRadiance (radiance.cuh), intersectAny (intersect.cuh);
+ * and the pieces of the MIS mode the reference has: BSDF::samplef / pdf
+ * (bsdf.cuh), powerHeuristic (sampling.cuh), Light::visibleArea (light.cuh).
  * The shim supplies what nvcc would (keywords, CUDA vector types, device
  * min/max of floats) and stands in for cuRAND: curand_uniform() replays the
  * numbers the caller passes, in the order the reference's code asks for them.
@@ -207,6 +209,63 @@ void ref_shade_hits(const float* V, const float* N, const float* TG, const float
     }
     delete[] sh;
     delete[] lt;
+}
+
+/* The BSDF sampling pieces of the MIS mode, through the reference's code at
+ * each hit (located as in ref_shade_hits): BSDF::samplef with two replayed
+ * uniforms per hit, then BSDF::pdf of the sampled direction and of a given
+ * probe direction (bsdf.cuh:22-30, 48-67). out, 6 floats per hit: sampled
+ * wi.xyz, samplef's pdf, pdf(wo, wi), pdf(wo, probe). */
+void ref_bsdf_hits(const float* V, const float* N, const float* TG, const float* BT, const uint16_t* S,
+                   uint32_t count, const aur_shader* shaders, uint32_t nshaders, const float* rays8,
+                   const int32_t* tri, const float* tuv, uint32_t n, const float* uniforms, const float* probes,
+                   float* out) {
+    Geometry g;
+    std::memset(&g, 0, sizeof(g));
+    g.vertices = const_cast<float*>(V);
+    g.normals = const_cast<float*>(N);
+    g.tangents = const_cast<float*>(TG);
+    g.bitangents = const_cast<float*>(BT);
+    g.shaders = const_cast<unsigned short*>(S);
+    g.count = count;
+    Shader* sh = new Shader[nshaders];
+    for (uint32_t k = 0; k < nshaders; ++k) sh[k] = to_shader(shaders[k]);
+    for (uint32_t i = 0; i < n; ++i) {
+        float* o = out + (size_t)i * 6;
+        for (int q = 0; q < 6; ++q) o[q] = 0.0f;
+        if (tri[i] < 0) continue;
+        const float* r = rays8 + (size_t)i * 8;
+        Ray ray(make_float3(r[0], r[1], r[2]), make_float3(r[4], r[5], r[6]), tuv[3 * i]);
+        const float3 wo = -ray.dir;
+        const Shader& shader = sh[getSafeID(g.shaders[tri[i]])];
+        BSDF bsdf = shader.getBSDF(g, tri[i], tuv[3 * i + 1], tuv[3 * i + 2]);
+        RNG rng = {uniforms + (size_t)i * 2, 2, 0};
+        float3 wi;
+        float pdf;
+        bsdf.samplef(&rng, wo, wi, pdf);
+        const float3 pr = make_float3(probes[3 * i], probes[3 * i + 1], probes[3 * i + 2]);
+        o[0] = wi.x; o[1] = wi.y; o[2] = wi.z;
+        o[3] = pdf;
+        o[4] = bsdf.pdf(wo, wi);
+        o[5] = bsdf.pdf(wo, pr);
+    }
+    delete[] sh;
+}
+
+/* powerHeuristic(1, a, 1, b) (sampling.cuh:162-169). */
+float ref_power_heuristic(float a, float b) { return powerHeuristic(1, a, 1, b); }
+
+/* Light::visibleArea (light.cuh:62-76) with no geometry to occlude: 1 and
+ * the distance to the light's quad when the ray meets one of its two
+ * triangles (Ray::intersect, culled), else 0. */
+int ref_area_hit(const aur_light* l, const float* pos, const float* dir, float* t) {
+    const Light L = to_light(*l);
+    Geometry g;
+    std::memset(&g, 0, sizeof(g));
+    Ray ray(make_float3(pos[0], pos[1], pos[2]), make_float3(dir[0], dir[1], dir[2]), Infinity);
+    const bool hit = L.visibleArea(g, ray);
+    *t = ray.t;
+    return hit ? 1 : 0;
 }
 
 }  // extern "C"
