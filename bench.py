@@ -373,13 +373,29 @@ def bench_cornell(ctx, cpu=True, textured=False):
         import oracle
         ns = oracle.NmhScene(sd)
         t0 = time.perf_counter()
-        ref, _ = oracle.render(ns, p, nthreads=os.cpu_count() or 1)
+        if textured:
+            ref, _ = oracle.render(ns, p, nthreads=os.cpu_count() or 1)
+        else:
+            ref, fetches, shaded = oracle.render_counted(ns, p, nthreads=os.cpu_count() or 1)
         dt = time.perf_counter() - t0
         out["cpu_samples_per_s"] = 256 * 256 * 16 / dt
         out["cpu_cores"] = os.cpu_count()
         g = img.cpu().numpy()
         out["matches_oracle"] = bool(np.all(np.abs(g - ref) <= 1e-4 * np.abs(ref) + 1e-7))
         out["bit_exact"] = bool(np.array_equal(g, ref))
+        if not textured:
+            # path-sampling roofline: per sample, 72 B per node fetch of the
+            # reference algorithm (closest and any hit), 36 B of normals and an
+            # 80-byte shader per shading point, 16 B of accumulation (counted
+            # by the oracle on the same render); the 34-triangle scene itself
+            # is 2 KB, so these bytes come from L1 and L2
+            n = 256 * 256 * 16
+            per_sample = (72.0 * fetches + (36.0 + 80.0) * shaded + 16.0 * n) / n
+            peak, _ = load_peaks()
+            gbs = per_sample * out["gpu_samples_per_s"] / 1e9
+            out["roofline"] = {"algorithmic_bytes_per_sample": per_sample,
+                               "node_fetches_per_sample": fetches / n, "shading_points_per_sample": shaded / n,
+                               "achieved_GBps": gbs, "frac_of_hbm_peak": gbs / peak}
     return out
 
 

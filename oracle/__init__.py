@@ -60,6 +60,8 @@ def lib():
         L.orc_render_ex.restype = ctypes.c_uint64
         L.orc_mis_table.argtypes = [P, P, P, U32, U32, P, P, P, P]
         L.orc_mis_table.restype = U32
+        L.orc_render_counted.argtypes = [P, P, P, P, U32, P, U32, P, U32, P, P, P, ctypes.c_int, P]
+        L.orc_render_counted.restype = ctypes.c_uint64
         L.orc_bsdf_hits.argtypes = [P, P, P, U32, P, U32, P, P, P, U32, P, P, ctypes.c_int, P]
         L.orc_mis_weight.argtypes = [ctypes.c_float, ctypes.c_float]
         L.orc_mis_weight.restype = ctypes.c_float
@@ -389,3 +391,17 @@ def area_hit(light, pos, direction, reference=False):
     f = ref_lib().ref_area_hit if reference else lib().orc_hit_quad
     h = f(_ptr(lt), _ptr(p), _ptr(d), _ptr(t))
     return bool(h), float(t[0])
+
+
+def render_counted(nscene, params, camera=None, nthreads=None):
+    """orc_render of an untextured scene in reference or path mode: (accum,
+    node fetches of the reference algorithm, shading points)."""
+    p = np.asarray(params, T.params_dtype).reshape(())
+    accum = np.zeros((int(p["height"]), int(p["width"]), 4), np.float32)
+    cam = np.asarray(nscene.camera if camera is None else camera, T.camera_dtype).reshape(())
+    sp = np.zeros(1, np.uint64)
+    tot = lib().orc_render_counted(_ptr(nscene.V), _ptr(nscene.N), _ptr(nscene.S), _ptr(nscene.perm),
+                                   nscene.V.shape[0], _ptr(nscene.shaders), nscene.shaders.shape[0],
+                                   _ptr(nscene.lights), nscene.lights.shape[0], _ptr(cam), _ptr(p), _ptr(accum),
+                                   nthreads or nthreads_default(), _ptr(sp))
+    return accum, int(tot), int(sp[0])

@@ -930,6 +930,7 @@ SampleOut integrate(const Scene& sc, const aur_render_params& p, const Ray& prim
         const int64_t h = traceClosest(sc.V, sc.count, sc.perm, ray, u, v, vis);
         if (h < 0) continue;
         anyHit = true;
+        ++vis[1];   // shading points (vis[0]: node fetches)
         const uint32_t tri = (uint32_t)h;
         const F3 position = ray.pos + (ray.dir * ray.t);
         const F3 wo = -ray.dir;
@@ -1060,7 +1061,7 @@ void orc_generate_rays(const aur_camera* cam, uint32_t W, uint32_t H, uint32_t s
  * Returns the number of node fetches (closest + any).
  */
 static uint64_t render_scene(const Scene& sc, const aur_camera* cam, const aur_render_params* p, float* accum,
-                             int nthreads);
+                             int nthreads, uint64_t* shading_points = nullptr);
 
 uint64_t orc_render(const float* V, const float* N, const uint16_t* S, const uint32_t* perm, uint32_t count,
                     const aur_shader* shaders, uint32_t nshaders, const aur_light* lights, uint32_t nlights,
@@ -1154,6 +1155,20 @@ uint64_t orc_render_ex(const float* V, const float* N, const uint16_t* S, const 
     sc.TC = TC; sc.tex = tex; sc.ntex = ntex;
     sc.misTri = mis_tri; sc.misCdf = mis_cdf; sc.misPa = mis_pa; sc.misCount = mis_count;
     return render_scene(sc, cam, p, accum, nthreads);
+}
+
+/* orc_render, also returning the number of shading points (ray hits that
+ * were shaded) in *shading_points: the units of the path-sampling roofline
+ * (node fetches of the reference algorithm, normals and shader reads per
+ * shading point, the accumulation per sample). */
+uint64_t orc_render_counted(const float* V, const float* N, const uint16_t* S, const uint32_t* perm, uint32_t count,
+                            const aur_shader* shaders, uint32_t nshaders, const aur_light* lights, uint32_t nlights,
+                            const aur_camera* cam, const aur_render_params* p, float* accum, int nthreads,
+                            uint64_t* shading_points) {
+    Scene sc;
+    sc.V = V; sc.N = N; sc.S = S; sc.perm = perm; sc.count = count;
+    sc.shaders = shaders; sc.nshaders = nshaders; sc.lights = lights; sc.nlights = nlights;
+    return render_scene(sc, cam, p, accum, nthreads, shading_points);
 }
 
 /* The light-selection table of AUR_MODE_PATH_MIS, sequentially: NMH
@@ -1258,11 +1273,12 @@ void orc_texfetch(const aur_texture* t, const float* uv, uint32_t n, float* rgb)
 }  // extern "C"
 
 static uint64_t render_scene(const Scene& sc, const aur_camera* cam, const aur_render_params* p, float* accum,
-                             int nthreads) {
+                             int nthreads, uint64_t* shading_points) {
     const uint32_t W = p->width, H = p->height;
     const uint32_t s0 = p->sample_begin, s1 = p->sample_end ? p->sample_end : p->spp;
     const float weight = 1.0f / (float)p->spp;
-    std::vector<uint64_t> tot((size_t)std::max(1, nthreads), 0);
+    // per worker: node fetches, shading points
+    std::vector<uint64_t> tot(2 * (size_t)std::max(1, nthreads), 0);
     parallel_for(W * H, nthreads, [&](uint32_t pix, int w) {
         const uint32_t x = pix % W, y = pix / W;
         float* px = accum + (size_t)pix * 4;
@@ -1271,7 +1287,7 @@ static uint64_t render_scene(const Scene& sc, const aur_camera* cam, const aur_r
             PixelCtx pc;
             pc.key.seed = p->seed; pc.key.scene = p->scene_id;
             pc.pixel = pix; pc.sample = s; pc.ray = 0;
-            const SampleOut o = integrate(sc, *p, r, pc, &tot[(size_t)w]);
+            const SampleOut o = integrate(sc, *p, r, pc, &tot[2 * (size_t)w]);
             if (o.hit) {
                 px[0] += o.color.x * weight;
                 px[1] += o.color.y * weight;
@@ -1280,8 +1296,12 @@ static uint64_t render_scene(const Scene& sc, const aur_camera* cam, const aur_r
             }
         }
     });
-    uint64_t s = 0;
-    for (uint64_t x : tot) s += x;
+    uint64_t s = 0, h = 0;
+    for (size_t i = 0; i < tot.size(); i += 2) {
+        s += tot[i];
+        h += tot[i + 1];
+    }
+    if (shading_points) *shading_points = h;
     return s;
 }
 

@@ -147,3 +147,21 @@ def test_render_sample_ranges_add_up():
     part, _ = oracle.render(ns, T.render_params(16, 16, 4, 3, seed=5, sample_begin=0, sample_end=2))
     part, _ = oracle.render(ns, T.render_params(16, 16, 4, 3, seed=5, sample_begin=2, sample_end=4), accum=part)
     assert np.array_equal(full, part)
+
+
+def test_render_counted_counts_fetches_and_shading_points():
+    """The path-sampling roofline's units: the counted render gives the same
+    image; in reference mode without specular shaders every sample is shaded
+    exactly once per camera hit, and path mode adds one shading point per
+    bounce that hits."""
+    from aurora_gb300 import scenes, types as T
+    ns = oracle.NmhScene(scenes.cornell())
+    p = T.render_params(16, 16, 4, 3, seed=2, mode=T.MODE_REFERENCE)
+    img, fetches, shaded = oracle.render_counted(ns, p)
+    ref, fetches2 = oracle.render(ns, p)
+    assert np.array_equal(img, ref) and fetches == fetches2
+    hits = int(round(img[..., 3].sum() * 4))                       # alpha: 1/spp per hitting sample
+    assert shaded == hits
+    pp = T.render_params(16, 16, 4, 3, seed=2, mode=T.MODE_PATH)
+    _, _, shaded_path = oracle.render_counted(ns, pp)
+    assert hits < shaded_path <= 4 * hits
