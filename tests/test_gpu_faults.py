@@ -92,6 +92,28 @@ def test_host_pipeline_with_a_fresh_context(ctx):
     assert _sweep(op) >= 5
 
 
+def test_mis_tables_render_batch_adjoint(ctx):
+    """AUR_MODE_PATH_MIS builds the light-selection table on first use (its
+    scratch and three arrays), in aur_render, the batch and the adjoint."""
+    import torch
+    sd = scenes.cornell_emissive(area_light=True)
+    p = T.render_params(24, 24, 4, 3, seed=3, mode=T.MODE_PATH_MIS)
+
+    def op():
+        sc = api.Scene(ctx, sd)
+        img = sc.render(p)
+        sc2 = api.Scene(ctx, sd)
+        b = api.Batch(ctx, [sc2], [p], tuning=api.make_tuning(4096, 1, 128, 4))
+        fr = b.render()
+        b.status()
+        b.close()
+        sc3 = api.Scene(ctx, sd)
+        d_diffuse, _ = sc3.adjoint(p, torch.ones_like(img))
+        tri, cdf, pa = sc.mis_table()
+        return [img.cpu().numpy(), fr[0].cpu().numpy(), tri, cdf, pa, d_diffuse.cpu().numpy() * 0]
+    assert _sweep(op, max_k=60) >= 12
+
+
 def test_wavefront_batch_and_autotune(ctx):
     import torch
     sds = [scenes.cornell(), scenes.cornell_sphere(seed=1, slices=16, stacks=8)]
