@@ -94,16 +94,23 @@ __host__ __device__ __forceinline__ uint64_t left_base(uint64_t k, uint64_t L0, 
 
 // Bounds and sort keys (computeTriangleBounds, rebuilder.cu:72-91). Position
 // i >= count_in is the even-padding duplicate of the last triangle.
+// A coordinate that is NaN or infinite sets bit 8 of *err: the reference's
+// float sorts have no defined order for NaN, so the build refuses such soups.
 __global__ void k_bounds(const float* __restrict__ V, uint32_t N, size_t S, uint32_t count_in,
                          float* __restrict__ mn, float* __restrict__ mx, uint32_t* __restrict__ keys,
-                         uint32_t* __restrict__ vals) {
+                         uint32_t* __restrict__ vals, uint32_t* __restrict__ err) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const uint32_t src = i < count_in ? i : count_in - 1;
     const float* v = V + (size_t)src * 9;
     float c[9];
+    bool finite = true;
 #pragma unroll
-    for (int q = 0; q < 9; ++q) c[q] = v[q];
+    for (int q = 0; q < 9; ++q) {
+        c[q] = v[q];
+        finite = finite && isfinite(c[q]);
+    }
+    if (!finite) atomicOr(err, 8u);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const float lo = fminf(fminf(c[3 * a], c[3 * a + 1]), c[3 * a + 2]);
@@ -1007,7 +1014,7 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
     uint32_t* hist = (uint32_t*)(base + o_hist);
     uint32_t* tot = (uint32_t*)(base + o_tot);
 
-    k_bounds<<<cdiv(N, 256), 256, 0, st>>>(V, N, S, count, mn, mx, keys, vals);
+    k_bounds<<<cdiv(N, 256), 256, 0, st>>>(V, N, S, count, mn, mx, keys, vals, ctx->d_flags);
     // three stable LSD radix sorts of (min-key, prim id); result in keys/vals
     for (int pass = 0; pass < 4; ++pass) {
         const int shift = pass * 8;
@@ -1074,9 +1081,12 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
         cleanup();
         return cuda_fail(e, "aur_nmh_build kernels", __FILE__, __LINE__);
     }
-    if (flags & 4u) {
+    if (flags & (4u | 8u)) {
         cudaMemsetAsync(ctx->d_flags, 0, 4, st);
+        cudaStreamSynchronize(st);
         cleanup();
+        if (flags & 8u)
+            return fail(AUR_ERR_INVALID, "aur_nmh_build: a vertex coordinate is NaN or infinite");
         return fail(AUR_ERR_CUDA, "aur_nmh_build: internal partition check failed (flags 0x%x)", flags);
     }
     *out = nmh;
@@ -1205,7 +1215,7 @@ aur_status nmh_build_noalloc_impl(const float* V, uint32_t count, cudaStream_t s
     AUR_CUDA(cudaMemsetAsync(flags, 0, 4, st));
     AUR_CUDA(cudaMemsetAsync(node_of, 0, (size_t)N * 4, st));
     AUR_CUDA(cudaMemsetAsync(best, 0, (size_t)n * 8, st));
-    k_bounds<<<cdiv(N, 256), 256, 0, st>>>(V, N, S, count, mn, mx, keys, vals);
+    k_bounds<<<cdiv(N, 256), 256, 0, st>>>(V, N, S, count, mn, mx, keys, vals, flags);
     for (int pass = 0; pass < 4; ++pass) {
         const int shift = pass * 8;
         uint32_t* kin = (pass & 1) ? k2 : keys;
@@ -1252,6 +1262,7 @@ aur_status nmh_build_noalloc_impl(const float* V, uint32_t count, cudaStream_t s
     uint32_t h_flags = 0;
     AUR_CUDA(cudaMemcpyAsync(&h_flags, flags, 4, cudaMemcpyDeviceToHost, st));
     AUR_CUDA(cudaStreamSynchronize(st));
+    AUR_CHECK(!(h_flags & 8u), AUR_ERR_INVALID, "aur_nmh_build_noalloc: a vertex coordinate is NaN or infinite");
     AUR_CHECK(!(h_flags & 4u), AUR_ERR_CUDA, "aur_nmh_build_noalloc: internal partition check failed (flags 0x%x)",
               h_flags);
     return AUR_OK;

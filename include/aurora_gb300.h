@@ -215,7 +215,9 @@ typedef struct aur_nmh aur_nmh;
  * by duplicating the last triangle (Geometry::padToEven, data/geometry.cpp:164-176);
  * the duplicate gets prim id `count`. Ties in every ordering are broken by the
  * lower original prim id, which makes the result deterministic where the
- * reference's atomicCAS swap (rebuilder.cu:93-125) is not. */
+ * reference's atomicCAS swap (rebuilder.cu:93-125) is not. A NaN or infinite
+ * coordinate returns AUR_ERR_INVALID (the reference's float sorts have no
+ * order for NaN). */
 aur_status aur_nmh_build(aur_ctx* ctx, const float* vertices, uint32_t count, aur_nmh** out);
 aur_status aur_nmh_destroy(aur_nmh* nmh);
 /* Triangle count after padding and number of heap levels (log2i(count/2)+1). */

@@ -56,3 +56,20 @@ def test_build_is_deterministic(ctx):
 def test_empty_build(ctx):
     nmh, perm, verts, levels = _gpu_build(ctx, np.zeros((0, 9), np.float32))
     assert levels == 0 and perm.size == 0
+
+
+@pytest.mark.parametrize("bad", [np.nan, np.inf, -np.inf])
+def test_non_finite_vertices_are_refused(ctx, bad):
+    """The reference's float sorts have no order for NaN: a soup with a NaN or
+    infinite coordinate is refused (AUR_ERR_INVALID), and the context then
+    builds a finite soup normally."""
+    import torch
+    V = scenes.random_soup(5001, seed=6)
+    V[4321, 4] = bad
+    Vd = torch.from_numpy(np.ascontiguousarray(V, np.float32).reshape(-1)).cuda()
+    with pytest.raises(api.AuroraError) as e:
+        api.Nmh(ctx, Vd, count=V.shape[0])
+    assert e.value.status == 1 and "NaN or infinite" in str(e.value)
+    V[4321, 4] = 0.5
+    _, perm, _, _ = _gpu_build(ctx, V)
+    assert np.array_equal(perm, oracle.nmh_build(V)[0])
