@@ -100,3 +100,24 @@ def test_trace_edge_cases(ctx):
     assert np.array_equal(h2["t"], rays["tmax"])
     z = api.trace_closest(ctx, nmh, api.rays_tensor(rays[:0]))
     assert z.shape[0] == 0
+
+
+def test_trace_non_finite_rays(ctx):
+    """Rays with a NaN or infinite origin or direction component hit nothing,
+    as the reference's arithmetic gives (NaN fails every t test), and do not
+    disturb the other rays of the launch."""
+    V = scenes.random_soup(20000, seed=8)
+    nmh, perm, verts = _setup(ctx, V)
+    rays = scenes.microbench_rays(4096, seed=9)
+    bad = np.arange(0, 4096, 7)
+    for j, k in enumerate(bad):
+        field = ("ox", "oy", "oz", "dx", "dy", "dz")[j % 6]
+        rays[field][k] = (np.nan, np.inf, -np.inf)[j % 3]
+    hits, occ = _gpu_trace(ctx, nmh, rays)
+    ohits, _, _ = oracle.trace_closest(verts, perm, rays)
+    oocc, _, _ = oracle.trace_any(verts, perm, rays)
+    assert hits_equal(hits, ohits) and np.array_equal(occ, oocc)
+    nan_rays = bad[np.arange(len(bad)) % 3 == 0]
+    assert np.all(hits["prim"][nan_rays] == T.NO_HIT)
+    good = np.setdiff1d(np.arange(4096), bad)
+    assert (hits["prim"][good] != T.NO_HIT).mean() > 0.05
