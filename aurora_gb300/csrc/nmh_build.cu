@@ -13,7 +13,10 @@
 //         within the remainder decides left/right (calcPartition sizes,
 //         :40-50, :189-215);
 //      c. the other two lists are stably partitioned left/right.
-//      Stable partitions are warp-ballot scans over 4096-element tiles.
+//      Stable partitions are warp-ballot scans over 4096-element tiles in a
+//      single pass, the tile prefixes by decoupled look-back;
+//   3'. once every node's segment fits 2048 triangles, one block per node
+//      finishes its subtree in shared memory (k_local_finish).
 //   4. each pair is ordered by the last level's axis key (the reference's
 //      final sort, :381-385), then vertices are gathered into NMH order
 //      (applyIndices, :217-245) and traversal node records are written.
@@ -356,65 +359,77 @@ __device__ __forceinline__ void flags_of(uint32_t nd, bool& D, bool& Lf) {
     Lf = kPart && !D && (nd & 1u);
 }
 
-// Tile counts of (D, L) for list blockIdx.y.
-template <bool kPart>
-__global__ void __launch_bounds__(kThreads) k_tile_count(ListSet ls, uint32_t M, const uint32_t* __restrict__ node_of,
-                                                         uint2* __restrict__ cnt, uint32_t ntiles) {
-    __shared__ uint32_t s_d[kThreads / 32], s_l[kThreads / 32];
-    const uint32_t* list = ls.in[blockIdx.y];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t wbase = blockIdx.x * kTile + warp * 32 * kTileItems;
-    uint32_t cd = 0, cl = 0;
-#pragma unroll 4
-    for (int i = 0; i < kTileItems; ++i) {
-        const uint32_t j = wbase + i * 32 + lane;
-        bool D = false, Lf = false;
-        if (j < M) flags_of<kPart>(node_of[list[j]], D, Lf);
-        cd += __popc(__ballot_sync(0xffffffffu, D));
-        cl += __popc(__ballot_sync(0xffffffffu, Lf));
-    }
-    if (lane == 0) { s_d[warp] = cd; s_l[warp] = cl; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t d = 0, l = 0;
-        for (int w = 0; w < kThreads / 32; ++w) { d += s_d[w]; l += s_l[w]; }
-        cnt[(size_t)blockIdx.y * ntiles + blockIdx.x] = make_uint2(d, l);
-    }
+// Single-pass tile prefix (decoupled look-back, D. Merrill and M. Garland,
+// "Single-pass Parallel Prefix Scan with Decoupled Look-back", NVIDIA
+// NVR-2016-002): each tile publishes its (D, L) counts, then walks back over
+// its predecessors' words until one holds an inclusive prefix. A status word
+// packs the state (bits 62-63: 0 not ready, 1 counts of the tile, 2
+// inclusive prefix) with the D count (bits 31-61) and the L count (bits
+// 0-30), so one 64-bit store publishes all of it. Tiles are taken in launch
+// order from a counter, so every tile a block waits for belongs to a block
+// that is already running; the wait is still bounded, and a block that gives
+// up sets bit 16 of *err and publishes what it has.
+constexpr unsigned long long kStTile = 1ull << 62, kStPrefix = 2ull << 62;
+constexpr uint32_t kLookbackSpins = 1u << 22;
+
+__device__ __forceinline__ unsigned long long st_word(unsigned long long state, uint64_t d, uint64_t l) {
+    return state | ((d & 0x7FFFFFFFull) << 31) | (l & 0x7FFFFFFFull);
 }
 
-// In-place exclusive scan of the tile counts of list blockIdx.x.
-__global__ void k_tile_scan(uint2* __restrict__ cnt, uint32_t ntiles) {
-    __shared__ uint32_t s_warp[32];
-    uint2* c = cnt + (size_t)blockIdx.x * ntiles;
-    uint32_t cd = 0, cl = 0;
-    for (uint32_t b = 0; b < ntiles; b += blockDim.x) {
-        const uint32_t i = b + threadIdx.x;
-        const uint2 v = i < ntiles ? c[i] : make_uint2(0, 0);
-        uint32_t td, tl;
-        const uint32_t ed = block_exclusive_scan(v.x, s_warp, td);
-        const uint32_t el = block_exclusive_scan(v.y, s_warp, tl);
-        if (i < ntiles) c[i] = make_uint2(cd + ed, cl + el);
-        cd += td;
-        cl += tl;
+// One thread: exclusive (D, L) prefix of `tile` given its own counts.
+__device__ uint2 tile_lookback(unsigned long long* status, uint32_t tile, uint32_t cd, uint32_t cl,
+                               uint32_t* err) {
+    if (tile == 0) {
+        atomicExch(status, st_word(kStPrefix, cd, cl));
+        return make_uint2(0u, 0u);
     }
+    atomicExch(status + tile, st_word(kStTile, cd, cl));
+    uint64_t ed = 0, el = 0;
+    uint32_t spins = 0;
+    for (int64_t p = (int64_t)tile - 1; p >= 0;) {
+        const unsigned long long w = atomicAdd(status + p, 0ull);   // coherent read
+        const unsigned long long state = w >> 62;
+        if (state == 0) {
+            if (++spins > kLookbackSpins) {
+                atomicOr(err, 16u);
+                break;
+            }
+            __nanosleep(32);
+            continue;
+        }
+        ed += (w >> 31) & 0x7FFFFFFFull;
+        el += w & 0x7FFFFFFFull;
+        if (state == 2) break;
+        --p;
+    }
+    atomicExch(status + tile, st_word(kStPrefix, ed + cd, el + cl));
+    return make_uint2((uint32_t)ed, (uint32_t)el);
 }
 
-// Per-tile scan helper: for each of a warp's 16 items, exclusive global
-// counts of D and L flags before position j.
+// Per-tile scan helper: the block takes the next tile, and for each of a
+// warp's 16 items gets the exclusive global counts of D and L flags before
+// position j (tile prefix by look-back).
 template <bool kPart>
 struct TileScan {
     uint32_t pid[kTileItems];
     uint32_t nd[kTileItems];
     uint32_t dmask[kTileItems], lmask[kTileItems];
     uint32_t wd, wl;  // warp offsets within the tile + tile prefix
+    uint32_t tile;
 };
 
 template <bool kPart>
 __device__ __forceinline__ void tile_scan(const uint32_t* __restrict__ list, uint32_t M,
-                                          const uint32_t* __restrict__ node_of, uint2 pre, TileScan<kPart>& s) {
+                                          const uint32_t* __restrict__ node_of, unsigned long long* status,
+                                          uint32_t* tile_counter, uint32_t* err, TileScan<kPart>& s) {
     __shared__ uint32_t s_d[kThreads / 32], s_l[kThreads / 32];
+    __shared__ uint32_t s_tile;
+    __shared__ uint2 s_pre;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t wbase = blockIdx.x * kTile + warp * 32 * kTileItems;
+    if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1u);
+    __syncthreads();
+    s.tile = s_tile;
+    const uint32_t wbase = s.tile * kTile + warp * 32 * kTileItems;
 #pragma unroll
     for (int i = 0; i < kTileItems; ++i) {
         const uint32_t j = wbase + i * 32 + lane;
@@ -434,7 +449,13 @@ __device__ __forceinline__ void tile_scan(const uint32_t* __restrict__ list, uin
     }
     if (lane == 0) { s_d[warp] = cd; s_l[warp] = cl; }
     __syncthreads();
-    uint32_t od = pre.x, ol = pre.y;
+    if (threadIdx.x == 0) {
+        uint32_t td = 0, tl = 0;
+        for (int w = 0; w < kThreads / 32; ++w) { td += s_d[w]; tl += s_l[w]; }
+        s_pre = tile_lookback(status, s.tile, td, tl, err);
+    }
+    __syncthreads();
+    uint32_t od = s_pre.x, ol = s_pre.y;
     for (int w = 0; w < warp; ++w) { od += s_d[w]; ol += s_l[w]; }
     s.wd = od;
     s.wl = ol;
@@ -445,11 +466,13 @@ __device__ __forceinline__ void tile_scan(const uint32_t* __restrict__ list, uin
 __global__ void __launch_bounds__(kThreads) k_split_next(ListSet ls, uint32_t M, uint32_t* __restrict__ node_of,
                                                          const uint32_t* __restrict__ nstart,
                                                          const uint32_t* __restrict__ nnuml, uint32_t L0,
-                                                         const uint2* __restrict__ pre) {
+                                                         unsigned long long* __restrict__ status,
+                                                         uint32_t* __restrict__ tile_counter,
+                                                         uint32_t* __restrict__ err) {
     TileScan<false> s;
-    tile_scan<false>(ls.in[0], M, node_of, pre[blockIdx.x], s);
+    tile_scan<false>(ls.in[0], M, node_of, status, tile_counter, err, s);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t wbase = blockIdx.x * kTile + warp * 32 * kTileItems;
+    const uint32_t wbase = s.tile * kTile + warp * 32 * kTileItems;
     const uint32_t lt = lanemask_lt();
     uint32_t gd = s.wd;
     uint32_t* out = ls.out[0];
@@ -472,12 +495,14 @@ __global__ void __launch_bounds__(kThreads) k_partition(ListSet ls, uint32_t M, 
                                                         const uint32_t* __restrict__ nstart,
                                                         const uint32_t* __restrict__ nnuml,
                                                         const uint32_t* __restrict__ nlbase, uint32_t L0,
-                                                        const uint2* __restrict__ pre, uint32_t ntiles,
-                                                        uint32_t m_next, uint32_t* __restrict__ err) {
+                                                        unsigned long long* __restrict__ status, uint32_t ntiles,
+                                                        uint32_t* __restrict__ tile_counter, uint32_t m_next,
+                                                        uint32_t* __restrict__ err) {
     TileScan<true> s;
-    tile_scan<true>(ls.in[blockIdx.y], M, node_of, pre[(size_t)blockIdx.y * ntiles + blockIdx.x], s);
+    tile_scan<true>(ls.in[blockIdx.y], M, node_of, status + (size_t)blockIdx.y * ntiles, tile_counter + blockIdx.y,
+                    err, s);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t wbase = blockIdx.x * kTile + warp * 32 * kTileItems;
+    const uint32_t wbase = s.tile * kTile + warp * 32 * kTileItems;
     const uint32_t lt = lanemask_lt();
     uint32_t gd = s.wd, gl = s.wl;
     uint32_t* out = ls.out[blockIdx.y];
@@ -902,6 +927,23 @@ uint32_t log2i(uint32_t x) {
     return r;
 }
 
+// Look-back scratch: per list (the split list and the two partitioned ones)
+// one status word per tile, then the three tile counters.
+constexpr size_t lookback_bytes(size_t ntiles) { return 3 * ntiles * sizeof(unsigned long long) + 16; }
+
+// One level's split of the next axis' list and partition of the other two,
+// each a single pass with look-back tile prefixes; the status words and
+// tile counters are cleared first.
+void split_and_partition(const ListSet& sb, const ListSet& sac, uint32_t M, uint32_t mt, uint32_t ntiles,
+                         uint32_t* node_of, const uint32_t* ns, const uint32_t* nl, const uint32_t* nlb, uint32_t L0,
+                         uint32_t m_next, unsigned long long* lb, uint32_t* err, cudaStream_t st) {
+    uint32_t* counters = reinterpret_cast<uint32_t*>(lb + 3 * (size_t)ntiles);
+    cudaMemsetAsync(lb, 0, lookback_bytes(ntiles), st);
+    k_split_next<<<mt, kThreads, 0, st>>>(sb, M, node_of, ns, nl, L0, lb, counters, err);
+    k_partition<<<dim3(mt, 2), kThreads, 0, st>>>(sac, M, node_of, ns, nl, nlb, L0, lb + ntiles, ntiles, counters + 1,
+                                                  m_next, err);
+}
+
 // First level whose node segments all fit k_local_finish (the leftmost
 // subtree of a level of a complete heap is its largest).
 uint32_t local_level(uint32_t n, uint32_t levels) {
@@ -989,7 +1031,7 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
     const size_t o_nodeof = take((size_t)N * 4), o_heap = take((size_t)N * 4);
     const size_t o_pair0 = take((size_t)n * 4), o_best = take((size_t)n * 8);
     const size_t o_ns = take((size_t)n * 4), o_nl = take((size_t)n * 4), o_nlb = take((size_t)n * 4);
-    const size_t o_tiles = take((size_t)2 * ntiles * sizeof(uint2));
+    const size_t o_tiles = take(lookback_bytes(ntiles));
     const size_t o_hist = take((size_t)3 * 256 * nb * 4), o_tot = take((size_t)3 * 256 * 4);
     char* base = nullptr;
     if (::aur::dev_malloc_async((void**)&base, off, st) != cudaSuccess) {
@@ -1010,7 +1052,7 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
     uint32_t* ns = (uint32_t*)(base + o_ns);
     uint32_t* nl = (uint32_t*)(base + o_nl);
     uint32_t* nlb = (uint32_t*)(base + o_nlb);
-    uint2* tiles = (uint2*)(base + o_tiles);
+    unsigned long long* tiles = (unsigned long long*)(base + o_tiles);
     uint32_t* hist = (uint32_t*)(base + o_hist);
     uint32_t* tot = (uint32_t*)(base + o_tot);
 
@@ -1048,16 +1090,11 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
         ListSet sb;
         sb.in[0] = listA + b * S; sb.out[0] = listB + b * S;
         sb.in[1] = nullptr; sb.out[1] = nullptr;
-        k_tile_count<false><<<dim3(mt, 1), kThreads, 0, st>>>(sb, M, node_of, tiles, mt);
-        k_tile_scan<<<1, 1024, 0, st>>>(tiles, mt);
-        k_split_next<<<mt, kThreads, 0, st>>>(sb, M, node_of, ns, nl, L0, tiles);
         ListSet sac;
         sac.in[0] = listA + a * S; sac.out[0] = listB + a * S;
         sac.in[1] = listA + c * S; sac.out[1] = listB + c * S;
-        k_tile_count<true><<<dim3(mt, 2), kThreads, 0, st>>>(sac, M, node_of, tiles, mt);
-        k_tile_scan<<<2, 1024, 0, st>>>(tiles, mt);
-        k_partition<<<dim3(mt, 2), kThreads, 0, st>>>(sac, M, node_of, ns, nl, nlb, L0, tiles, mt,
-                                                      M - 2u * (L1 - L0), ctx->d_flags);
+        split_and_partition(sb, sac, M, mt, ntiles, node_of, ns, nl, nlb, L0, M - 2u * (L1 - L0), tiles,
+                            ctx->d_flags, st);
         uint32_t* t = listA; listA = listB; listB = t;
     }
     if (lv0 < nmh->levels) {
@@ -1081,12 +1118,13 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
         cleanup();
         return cuda_fail(e, "aur_nmh_build kernels", __FILE__, __LINE__);
     }
-    if (flags & (4u | 8u)) {
+    if (flags & (4u | 8u | 16u)) {
         cudaMemsetAsync(ctx->d_flags, 0, 4, st);
         cudaStreamSynchronize(st);
         cleanup();
         if (flags & 8u)
             return fail(AUR_ERR_INVALID, "aur_nmh_build: a vertex coordinate is NaN or infinite");
+        if (flags & 16u) return fail(AUR_ERR_TIMEOUT, "aur_nmh_build: a tile prefix wait gave up (flags 0x%x)", flags);
         return fail(AUR_ERR_CUDA, "aur_nmh_build: internal partition check failed (flags 0x%x)", flags);
     }
     *out = nmh;
@@ -1138,7 +1176,7 @@ constexpr NoAllocLayout noalloc_layout(size_t N) {
     L.ns = off; off += na_round(n * 4);
     L.nl = off; off += na_round(n * 4);
     L.nlb = off; off += na_round(n * 4);
-    L.tiles = off; off += na_round(2 * ntiles * 8);
+    L.tiles = off; off += na_round(lookback_bytes(ntiles));
     L.hist = off; off += na_round(3 * 256 * nb * 4);
     L.tot = off; off += na_round(3 * 256 * 4);
     L.end = off;
@@ -1206,10 +1244,11 @@ aur_status nmh_build_noalloc_impl(const float* V, uint32_t count, cudaStream_t s
     uint32_t* ns = (uint32_t*)(base + L.ns);
     uint32_t* nl = (uint32_t*)(base + L.nl);
     uint32_t* nlb = (uint32_t*)(base + L.nlb);
-    uint2* tiles = (uint2*)(base + L.tiles);
+    unsigned long long* tiles = (unsigned long long*)(base + L.tiles);
     uint32_t* hist = (uint32_t*)(base + L.hist);
     uint32_t* tot = (uint32_t*)(base + L.tot);
     const uint32_t nb = cdiv(N, kSortTile);
+    const uint32_t ntiles = cdiv(N, kTile);
 
     // The array keeps the previous call's contents: clear what must start at zero.
     AUR_CUDA(cudaMemsetAsync(flags, 0, 4, st));
@@ -1242,16 +1281,10 @@ aur_status nmh_build_noalloc_impl(const float* V, uint32_t count, cudaStream_t s
         ListSet sb;
         sb.in[0] = listA + b * S; sb.out[0] = listB + b * S;
         sb.in[1] = nullptr; sb.out[1] = nullptr;
-        k_tile_count<false><<<dim3(mt, 1), kThreads, 0, st>>>(sb, M, node_of, tiles, mt);
-        k_tile_scan<<<1, 1024, 0, st>>>(tiles, mt);
-        k_split_next<<<mt, kThreads, 0, st>>>(sb, M, node_of, ns, nl, L0, tiles);
         ListSet sac;
         sac.in[0] = listA + a * S; sac.out[0] = listB + a * S;
         sac.in[1] = listA + c * S; sac.out[1] = listB + c * S;
-        k_tile_count<true><<<dim3(mt, 2), kThreads, 0, st>>>(sac, M, node_of, tiles, mt);
-        k_tile_scan<<<2, 1024, 0, st>>>(tiles, mt);
-        k_partition<<<dim3(mt, 2), kThreads, 0, st>>>(sac, M, node_of, ns, nl, nlb, L0, tiles, mt, M - 2u * (L1 - L0),
-                                                      flags);
+        split_and_partition(sb, sac, M, mt, ntiles, node_of, ns, nl, nlb, L0, M - 2u * (L1 - L0), tiles, flags, st);
         uint32_t* t = listA; listA = listB; listB = t;
     }
     if (lv0 < levels) AUR_CUDA(finish_local(listA, S, mn, mx, n, lv0, ns, node_of, heap, (float*)k2, flags, st));
@@ -1263,6 +1296,8 @@ aur_status nmh_build_noalloc_impl(const float* V, uint32_t count, cudaStream_t s
     AUR_CUDA(cudaMemcpyAsync(&h_flags, flags, 4, cudaMemcpyDeviceToHost, st));
     AUR_CUDA(cudaStreamSynchronize(st));
     AUR_CHECK(!(h_flags & 8u), AUR_ERR_INVALID, "aur_nmh_build_noalloc: a vertex coordinate is NaN or infinite");
+    AUR_CHECK(!(h_flags & 16u), AUR_ERR_TIMEOUT, "aur_nmh_build_noalloc: a tile prefix wait gave up (flags 0x%x)",
+              h_flags);
     AUR_CHECK(!(h_flags & 4u), AUR_ERR_CUDA, "aur_nmh_build_noalloc: internal partition check failed (flags 0x%x)",
               h_flags);
     return AUR_OK;
