@@ -63,6 +63,23 @@ def test_render_matches_oracle(ctx, scene):
     assert img[..., :3].mean() > 0.01
 
 
+def test_textured_render_matches_oracle(ctx):
+    """Textured shaders in the MIS mode: the colour of a textured shader enters
+    f, and both strategies and the emitter sample, bit for bit."""
+    sd = scenes.cornell_textured(seed=2)
+    sd.shaders = np.concatenate([sd.shaders, np.stack([T.lambert((1.0, 1.0, 1.0), emission=(3.0, 2.0, 1.0))])])
+    sd.shaders["emission"][-1] = 1.0
+    sd.shader_ids = sd.shader_ids.copy()
+    sd.shader_ids[2:4] = len(sd.shaders)              # the ceiling emits
+    sc = api.Scene(ctx, sd)
+    sc.set_textures(sd.texcoords, sd.textures)
+    p = T.render_params(40, 40, 4, 3, seed=5, mode=T.MODE_PATH_MIS)
+    img = sc.render(p).cpu().numpy()
+    ref, _ = oracle.render(oracle.NmhScene(sd), p, table=sc.mis_table())
+    assert np.array_equal(img, ref)
+    assert len(sc.mis_table()[0]) == 2
+
+
 def test_mis_matches_path_mode_one_bounce_deeper(ctx):
     """Emissive geometry only: E[MIS at depth d] = E[path mode at depth d + 1];
     48 x 48 pixels, 8 independent 1024-sample renders of each. Path mode's
