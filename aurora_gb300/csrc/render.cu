@@ -25,6 +25,10 @@ constexpr int kRenderThreads = 128;
 // kernel (k_raytrace_mc) runs grids of one 65,536-ray tile, too small for
 // occupancy to matter, and is left unconstrained (a cap made it slower).
 constexpr int kRenderBlocksPerSm = 10;
+// The MIS instantiations carry more live state (two strategies per light
+// sample, the emitter sample): 8 blocks per SM (64 registers) measured 9-17 %
+// faster than 10 or 12, and 4-9 % faster than 6.
+constexpr int kRenderBlocksPerSmMis = 8;
 
 inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
@@ -43,7 +47,7 @@ __device__ __forceinline__ StackRef stack_ref(uint32_t* smem, int cap) {
 // selects the integrator with the specular ray stack, kMis the
 // AUR_MODE_PATH_MIS estimator.
 template <bool kGeneric, bool kMis>
-__global__ void __launch_bounds__(kRenderThreads, kRenderBlocksPerSm) k_render_samples(SceneView sc, aur_camera cam, aur_render_params p,
+__global__ void __launch_bounds__(kRenderThreads, kMis ? kRenderBlocksPerSmMis : kRenderBlocksPerSm) k_render_samples(SceneView sc, aur_camera cam, aur_render_params p,
                                                                    uint32_t s0, uint32_t nb, float4* __restrict__ colors,
                                                                    uint32_t* __restrict__ err, int cap) {
     extern __shared__ uint32_t smem[];
