@@ -1,10 +1,13 @@
 // wavefront.cu — batched wavefront path tracer: many scenes, one graph launch.
 //
 // Estimator: exactly the plain integrator's (aur_integrate.cuh, after
-// kernels/monteCarloRaytracer.cu:23-113) for non-specular materials — same
-// counter-RNG keys (seed, scene id) x (pixel, sample, ray index, slot), same
-// arithmetic in the same order — so every path sample has the same value as
-// in aur_render and the frames are identical. In AUR_MODE_PATH_MIS the
+// kernels/monteCarloRaytracer.cu:23-113) — same counter-RNG keys (seed,
+// scene id) x (pixel, sample, ray index, slot), same arithmetic in the same
+// order — so every path sample has the same value as in aur_render and the
+// frames are identical. A path slot carries one camera sample; in batches
+// with specular shaders it also keeps the sample's ray stack, so the
+// reflection, refraction and bounce rays are traced one after the other in
+// the plain integrator's order. In AUR_MODE_PATH_MIS the
 // shade stage queues both strategies of every area-light sample and the
 // emitter sample (the ShadowSample helpers of aur_integrate.cuh), and the
 // combine stage adds them in the plain integrator's order.
@@ -38,6 +41,12 @@ constexpr int kMaxLightSlots = 32;
 // light samples than the batch was sized for (aur_scene_set_lights after
 // aur_batch_create).
 constexpr uint32_t kWfErrLightSlots = 2u;
+// WfCtl::error bit 4: a path's ray stack would have overflowed (the plain
+// integrator's stack check; cannot happen within AUR_MAX_DEPTH).
+constexpr uint32_t kWfErrStack = 4u;
+// Specular batches keep each sample's pending rays (the ray stack of the
+// plain integrator, monteCarloRaytracer.cu:26-88) with its path.
+constexpr uint32_t kWfStack = AUR_MAX_DEPTH + 2;
 // Largest block of the stage kernels: the traversal and shading stages are
 // compiled for it with at most 64 registers (4 blocks of 256 per SM), which
 // measured faster than their unconstrained 70-72 registers.
@@ -112,6 +121,10 @@ struct WfArgs {
     float4* sh_o;   // shadow ray origin, w = tmax
     float4* sh_d;   // shadow ray direction, w = (slot << 5 | light slot) bits
     float4* out;    // per wave: nb * P_tot sample colours, indexed by item
+    // specular batches: per slot a stack of kWfStack pending rays, entry e
+    // component k (pos + weight, dir + eta, thr + pdf) at stk[(e * 3 + k) * Q + slot]
+    float4* stk;
+    uint32_t* sp;   // stack depth per slot
     cudaGraphConditionalHandle h_inner, h_outer;
     uint32_t in_graph;   // 1 when launched by the graph: only then may kernels set its conditionals
 };
@@ -227,11 +240,12 @@ __global__ void k_wf_generate(WfArgs a) {
         const ItemRef ir = decode_item(item, c->nb, sc);
         const uint32_t lp = ir.pix;
         const PathRay r = camera_ray(sc.cam, sc.width, sc.height, lp % sc.width, lp / sc.width, c->s0 + ir.b, a.spp);
-        a.o[slot] = make_float4(r.pos.x, r.pos.y, r.pos.z, 0.0f);
-        a.d[slot] = make_float4(r.dir.x, r.dir.y, r.dir.z, 0.0f);
+        a.o[slot] = make_float4(r.pos.x, r.pos.y, r.pos.z, r.weight);   // w: the ray's weight (specular batches)
+        a.d[slot] = make_float4(r.dir.x, r.dir.y, r.dir.z, r.eta);      // w: the ray's eta
         a.thr[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         a.col[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         a.meta[slot] = make_uint4(item, 0u, 0u, s);
+        if (a.sp) a.sp[slot] = 0u;
         a.ext_q[cur][base + i] = slot;
     }
 }
@@ -295,9 +309,40 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_extend(WfArgs a) {
     }
 }
 
-// Shading: misses finish; hits get their light samples (shadow rays queued)
-// and, in path mode, their bounce. kMis: the mode is AUR_MODE_PATH_MIS.
-template <bool kMis>
+// The per-slot ray stack of specular batches.
+__device__ __forceinline__ void wf_push(const WfArgs& a, uint32_t slot, uint32_t& sp, const PathRay& r, WfCtl* c) {
+    if (sp >= kWfStack) {
+        atomicOr(&c->error, kWfErrStack);
+        return;
+    }
+    const size_t b = (size_t)sp * 3 * a.Q + slot;
+    a.stk[b] = make_float4(r.pos.x, r.pos.y, r.pos.z, r.weight);
+    a.stk[b + a.Q] = make_float4(r.dir.x, r.dir.y, r.dir.z, r.eta);
+    a.stk[b + 2 * (size_t)a.Q] = make_float4(r.thr.x, r.thr.y, r.thr.z, r.pdf);
+    ++sp;
+}
+
+// Pops the slot's next pending ray into its current-ray state (the plain
+// integrator's `while (depth <= maxd && sp > 0)` loop); false when the
+// sample is done.
+__device__ __forceinline__ bool wf_pop_next(const WfArgs& a, uint32_t slot, uint32_t depth, uint32_t sp) {
+    if (!(depth <= a.max_depth && sp > 0)) return false;
+    --sp;
+    const size_t b = (size_t)sp * 3 * a.Q + slot;
+    a.o[slot] = a.stk[b];
+    a.d[slot] = a.stk[b + a.Q];
+    a.thr[slot] = a.stk[b + 2 * (size_t)a.Q];
+    a.sp[slot] = sp;
+    a.meta[slot].z += 1u;   // the sample's next ray index
+    return true;
+}
+
+// Shading: misses finish (specular batches: the sample's next pending ray
+// goes on); hits get their light samples (shadow rays queued) and, in path
+// mode, their bounce; specular batches push reflection, refraction and
+// bounce rays on the slot's stack in the plain integrator's order.
+// kMis: the mode is AUR_MODE_PATH_MIS; kSpec: the batch has specular shaders.
+template <bool kMis, bool kSpec>
 __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
     WfCtl* c = a.ctl;
     const uint32_t cur = c->iter & 1u;
@@ -308,6 +353,10 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
         const float4 h = a.hit[slot];
         const uint32_t tri = __float_as_uint(h.w);
         if (tri == kNoPrim) {
+            if (kSpec && wf_pop_next(a, slot, m.y, a.sp[slot])) {
+                a.ext_q[cur ^ 1u][agg_inc(&c->ext_count[cur ^ 1u])] = slot;
+                continue;
+            }
             finish_path(a, slot, m.x, a.col[slot]);
             continue;
         }
@@ -336,6 +385,9 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
         const Bsdf bs = get_bsdf(sv, sh, tri, h.y, h.z);
         const f3 f = bsdf_f(bs);
         const uint32_t depth = m.y + 1u;
+        const bool specular = kSpec && (sh->reflectivity > 0.0f || sh->translucence > 0.0f);
+        // does a diffuse bounce follow this hit (the emitter sample's weight)?
+        const bool bounce = kSpec ? !specular && m.y + 1u <= a.max_depth : depth <= a.max_depth;
         a.fsh[slot] = make_float4(f.x, f.y, f.z, 0.0f);
         const f3 em = mis ? from(sh->emission_color) * emission_weight(sv, tri, dir, h.x, a.thr[slot].w)
                           : from(sh->emission_color);
@@ -405,10 +457,67 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
             if (q >= a.M) {
                 atomicOr(&c->error, kWfErrLightSlots);
             } else {
-                queue(emitter_shadow_sample(sv, bs, f, position, wo, depth <= a.max_depth, a.seed, sc.scene_id, pix,
-                                            sample, rix),
-                      q);
+                queue(emitter_shadow_sample(sv, bs, f, position, wo, bounce, a.seed, sc.scene_id, pix, sample, rix), q);
             }
+        }
+        if (kSpec) {
+            // integrate(): specular splits and the diffuse bounce onto the stack
+            const float4 t4 = a.thr[slot];
+            f3 thr = mk3(t4.x, t4.y, t4.z);
+            float weight = o4.w;
+            const float eta = d4.w;
+            const bool path = kMis || a.mode == AUR_MODE_PATH;
+            const float refl = sh->reflectivity, trans = sh->translucence;
+            uint32_t dep = m.y, sp = a.sp[slot];
+            if (specular) dep++;
+            if (dep <= a.max_depth && refl > 0.0f) {
+                PathRay nr;
+                nr.pos = position;
+                nr.dir = reflect(dir, bs.N);
+                nr.weight = refl;
+                nr.eta = eta;
+                nr.thr = path ? thr * refl : mk3(nr.weight);
+                nr.pdf = 0.0f;
+                weight *= (1.0f - refl);
+                thr = path ? thr * (1.0f - refl) : mk3(weight);
+                wf_push(a, slot, sp, nr, c);
+            }
+            if (dep <= a.max_depth && trans > 0.0f) {
+                f3 rN = bs.N;
+                float etai = eta, etat = sh->refractive_index;
+                if (dot(rN, wo) < 0.0f) { rN = -rN; etai = sh->refractive_index; etat = 1.0f; }
+                f3 tdir;
+                if (refract(tdir, dir, rN, etai, etat)) {
+                    PathRay nr;
+                    nr.pos = position;
+                    nr.dir = tdir;
+                    nr.weight = trans;
+                    nr.eta = etat;
+                    nr.thr = path ? thr * trans : mk3(nr.weight);
+                    nr.pdf = 0.0f;
+                    weight *= (1.0f - trans);
+                    thr = path ? thr * (1.0f - trans) : mk3(weight);
+                    wf_push(a, slot, sp, nr, c);
+                }
+            }
+            if (path && !specular) {
+                dep++;
+                if (dep <= a.max_depth) {
+                    PathRay nr;
+                    nr.pos = position;
+                    nr.weight = 1.0f;
+                    nr.eta = eta;
+                    const bool ok = kMis ? mis_bounce(bs, wo, thr, a.seed, sc.scene_id, pix, sample, rix, nr.dir,
+                                                      nr.thr, nr.pdf)
+                                         : diffuse_bounce(bs, wo, thr, a.seed, sc.scene_id, pix, sample, rix, nr.dir,
+                                                          nr.thr, nr.pdf);
+                    if (ok) wf_push(a, slot, sp, nr, c);
+                }
+            }
+            a.thr[slot] = make_float4(thr.x, thr.y, thr.z, 0.0f);   // the colour update's throughput
+            a.sp[slot] = sp;
+            a.meta[slot].y = dep;
+            continue;
         }
         // bounce (BSDF::samplef, bsdf.cuh:222-236)
         float cont = 0.0f, bpdf = 0.0f;
@@ -487,8 +596,8 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shadow(WfArgs a) {
 }
 
 // Li in the reference's order (radiance.cuh:13-80, monteCarloRaytracer.cu:42-52),
-// colour update, then continue or finish. kMis as in k_wf_shade.
-template <bool kMis>
+// colour update, then continue or finish. kMis and kSpec as in k_wf_shade.
+template <bool kMis, bool kSpec>
 __global__ void k_wf_combine(WfArgs a) {
     WfCtl* c = a.ctl;
     const uint32_t cur = c->iter & 1u, nxt = cur ^ 1u;
@@ -546,6 +655,14 @@ __global__ void k_wf_combine(WfArgs a) {
         float4 col = a.col[slot];
         const f3 cc = mk3(col.x, col.y, col.z) + Li * mk3(t4.x, t4.y, t4.z);
         col = make_float4(cc.x, cc.y, cc.z, 1.0f);
+        if (kSpec) {
+            a.col[slot] = col;
+            if (wf_pop_next(a, slot, a.meta[slot].y, a.sp[slot]))
+                a.ext_q[nxt][agg_inc(&c->ext_count[nxt])] = slot;
+            else
+                finish_path(a, slot, m.x, col);
+            continue;
+        }
         const float4 nd = a.ndir[slot];
         if (nd.w != 0.0f) {
             const float4 o4 = a.o[slot], d4 = a.d[slot];
@@ -635,6 +752,22 @@ struct aur_batch {
 
 namespace {
 
+// The shade and combine instantiations for the batch's mode and materials.
+void launch_shade(const WfArgs& a, uint32_t g, uint32_t bs, cudaStream_t s) {
+    const bool mis = a.mode == AUR_MODE_PATH_MIS, spec = a.stk != nullptr;
+    if (mis && spec) k_wf_shade<true, true><<<g, bs, 0, s>>>(a);
+    else if (mis) k_wf_shade<true, false><<<g, bs, 0, s>>>(a);
+    else if (spec) k_wf_shade<false, true><<<g, bs, 0, s>>>(a);
+    else k_wf_shade<false, false><<<g, bs, 0, s>>>(a);
+}
+void launch_combine(const WfArgs& a, uint32_t g, uint32_t bs, cudaStream_t s) {
+    const bool mis = a.mode == AUR_MODE_PATH_MIS, spec = a.stk != nullptr;
+    if (mis && spec) k_wf_combine<true, true><<<g, bs, 0, s>>>(a);
+    else if (mis) k_wf_combine<true, false><<<g, bs, 0, s>>>(a);
+    else if (spec) k_wf_combine<false, true><<<g, bs, 0, s>>>(a);
+    else k_wf_combine<false, false><<<g, bs, 0, s>>>(a);
+}
+
 aur_status make_graph(aur_batch* bt) {
     WfArgs& a = bt->args;
     a.in_graph = 1;
@@ -676,11 +809,9 @@ aur_status make_graph(aur_batch* bt) {
     k_wf_generate<<<g, bs, 0, s>>>(a);
     k_wf_generate_commit<<<1, 1, 0, s>>>(a);
     k_wf_extend<<<g, bs, bt->smem, s>>>(a);
-    if (a.mode == AUR_MODE_PATH_MIS) k_wf_shade<true><<<g, bs, 0, s>>>(a);
-    else k_wf_shade<false><<<g, bs, 0, s>>>(a);
+    launch_shade(a, g, bs, s);
     k_wf_shadow<<<g, bs, bt->smem, s>>>(a);
-    if (a.mode == AUR_MODE_PATH_MIS) k_wf_combine<true><<<g, bs, 0, s>>>(a);
-    else k_wf_combine<false><<<g, bs, 0, s>>>(a);
+    launch_combine(a, g, bs, s);
     k_wf_end<<<1, 1, 0, s>>>(a);
     AUR_CUDA(cudaStreamEndCapture(s, &tmp));
     // wave body part 2: accumulate after the inner loop
@@ -744,6 +875,7 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     const bool mis = p0.mode == AUR_MODE_PATH_MIS;
     uint64_t P_tot = 0;
     uint32_t M = 1, cap = 2;
+    bool spec = false;
     std::vector<WfScene> table(num_scenes);
     std::vector<uint32_t> pix_off(num_scenes + 1);
     for (uint32_t i = 0; i < num_scenes; ++i) {
@@ -758,11 +890,7 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
                   AUR_ERR_INVALID, "aur_batch_create: scene %u differs in spp/depth/mode/seed/sample range", i);
         AUR_CHECK(sc->nmh->device == ctx->device, AUR_ERR_INVALID, "aur_batch_create: scene %u on another device", i);
         // specular materials need the per-sample ray stack of the plain path
-        std::vector<aur_shader> sh(sc->num_shaders);
-        AUR_CUDA(cudaMemcpy(sh.data(), sc->shaders, sizeof(aur_shader) * sc->num_shaders, cudaMemcpyDeviceToHost));
-        for (const aur_shader& s : sh)
-            AUR_CHECK(!(s.reflectivity > 0.0f) && !(s.translucence > 0.0f), AUR_ERR_UNSUPPORTED,
-                      "aur_batch_create: scene %u has a specular shader; use aur_render", i);
+        spec = spec || sc->has_specular;
         std::vector<aur_light> lt(sc->num_lights);
         if (sc->num_lights)
             AUR_CUDA(cudaMemcpy(lt.data(), sc->lights, sizeof(aur_light) * sc->num_lights, cudaMemcpyDeviceToHost));
@@ -853,6 +981,7 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     const size_t o_fsh = take(16 * Q), o_emi = take(16 * Q), o_cj = take(16 * Q * M), o_vis = take(4 * Q);
     const size_t o_q0 = take(4 * Q), o_q1 = take(4 * Q), o_free = take(4 * Q);
     const size_t o_sho = take(16 * Q * M), o_shd = take(16 * Q * M), o_out = take(16 * out_items);
+    const size_t o_stk = spec ? take(16 * 3 * (size_t)kWfStack * Q) : 0, o_sp = spec ? take(4 * Q) : 0;
     if (::aur::dev_malloc(&bt->mem, off) != cudaSuccess) {
         cudaGetLastError();
         batch_free(bt);
@@ -880,6 +1009,8 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     a.ext_q[0] = (uint32_t*)(base + o_q0); a.ext_q[1] = (uint32_t*)(base + o_q1);
     a.free_list = (uint32_t*)(base + o_free);
     a.sh_o = (float4*)(base + o_sho); a.sh_d = (float4*)(base + o_shd); a.out = (float4*)(base + o_out);
+    a.stk = spec ? (float4*)(base + o_stk) : nullptr;
+    a.sp = spec ? (uint32_t*)(base + o_sp) : nullptr;
     cudaMemcpy(base + o_tab, table.data(), sizeof(WfScene) * num_scenes, cudaMemcpyHostToDevice);
     cudaMemcpy(base + o_pix, pix_off.data(), 4 * (num_scenes + 1), cudaMemcpyHostToDevice);
     WfCtl ctl{};
@@ -919,6 +1050,9 @@ aur_status aur_batch_render(aur_ctx* ctx, aur_batch* bt, float* const* accum) {
     AUR_CUDA(cudaSetDevice(ctx->device));
     for (uint32_t i = 0; i < bt->num_scenes; ++i) {
         AUR_CHECK(accum[i], AUR_ERR_INVALID, "aur_batch_render: frame %u is null", i);
+        AUR_CHECK(!bt->scene_ptrs[i]->has_specular || bt->args.stk, AUR_ERR_INVALID,
+                  "aur_batch_render: scene %u has specular shaders now; the batch was created without: create it "
+                  "again", i);
         bt->accum_host[i] = (float4*)accum[i];
     }
     const aur_status st = refresh_mis_tables(ctx, bt);
@@ -1016,13 +1150,11 @@ aur_status aur_batch_profile(aur_ctx* ctx, aur_batch* bt, float* const* accum, f
             cudaEventRecord(ev[1], st);
             k_wf_extend<<<g, bs, bt->smem, st>>>(a);
             cudaEventRecord(ev[2], st);
-            if (a.mode == AUR_MODE_PATH_MIS) k_wf_shade<true><<<g, bs, 0, st>>>(a);
-            else k_wf_shade<false><<<g, bs, 0, st>>>(a);
+            launch_shade(a, g, bs, st);
             cudaEventRecord(ev[3], st);
             k_wf_shadow<<<g, bs, bt->smem, st>>>(a);
             cudaEventRecord(ev[4], st);
-            if (a.mode == AUR_MODE_PATH_MIS) k_wf_combine<true><<<g, bs, 0, st>>>(a);
-            else k_wf_combine<false><<<g, bs, 0, st>>>(a);
+            launch_combine(a, g, bs, st);
             k_wf_end<<<1, 1, 0, st>>>(a);
             cudaEventRecord(ev[5], st);
             AUR_CUDA(cudaMemcpyAsync(&c, a.ctl, sizeof(c), cudaMemcpyDeviceToHost, st));

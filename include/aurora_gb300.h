@@ -484,7 +484,11 @@ typedef struct aur_batch aur_batch;
  * frame with a host loop (render/monteCarloRaytracer.cpp:81-120); each scene's
  * frame equals aur_render's with the same parameters (same estimator, same
  * RNG streams keyed by params[i].scene_id). params[i] may differ in width,
- * height and scene_id only. Materials must be non-specular. The batch reads
+ * height and scene_id only. With specular shaders (reflectivity or
+ * translucence > 0) each path keeps its sample's pending rays, the plain
+ * integrator's ray stack, in device memory (864 bytes per path in flight);
+ * a scene given specular shaders after the batch was created needs a new
+ * batch (aur_batch_render returns AUR_ERR_INVALID). The batch reads
  * the scenes' device data in place: each scene must outlive the batch, and
  * its textures must not be replaced (aur_scene_set_textures) while the batch
  * exists. Shaders and lights may be updated between renders (in

@@ -39,14 +39,55 @@ def test_wavefront_equals_plain(ctx, mode, tuning):
         assert np.array_equal(f.cpu().numpy(), twice.cpu().numpy())
 
 
-def test_wavefront_rejects_specular(ctx):
+def _specular(sd, k0=10, k1=22, k2=34):
+    """The scene with a mirror-like block (reflectivity 0.6) and a glass-like
+    one (translucence 0.7, index 1.5)."""
+    sh = np.concatenate([sd.shaders, np.stack([T.lambert((0.9, 0.9, 0.9)), T.lambert((0.8, 0.9, 1.0))])])
+    n = sd.shaders.shape[0]
+    sh["reflectivity"][n] = 0.6
+    sh["translucence"][n + 1] = 0.7
+    sh["refractive_index"][n + 1] = 1.5
+    sids = sd.shader_ids.copy()
+    sids[k0:k1] = n + 1
+    sids[k1:k2] = n + 2
+    return scenes.SceneData(sd.name + "_specular", sd.vertices, sd.normals, sids, sh, sd.lights, sd.camera)
+
+
+@pytest.mark.parametrize("mode", [T.MODE_REFERENCE, T.MODE_PATH, T.MODE_PATH_MIS])
+@pytest.mark.parametrize("tuning", [dict(paths_in_flight=1024, samples_per_wave=1, block_size=64, blocks_per_sm=2),
+                                    dict()])
+def test_wavefront_specular_equals_plain(ctx, mode, tuning):
+    """Specular shaders: each path keeps its sample's pending rays (the plain
+    integrator's ray stack), so reflection and refraction rays are traced in
+    the same order with the same ray indices; the frames equal aur_render's,
+    with specular and Lambert scenes in one batch."""
+    sds = [_specular(scenes.cornell()), scenes.cornell_sphere(seed=2),
+           _specular(scenes.cornell_emissive(area_light=True))]
+    scs = [api.Scene(ctx, sd) for sd in sds]
+    sizes = [(40, 32), (24, 24), (33, 17)]
+    prm = [T.render_params(w, h, 4, 5, seed=7, mode=mode, scene_id=i) for i, (w, h) in enumerate(sizes)]
+    batch = api.Batch(ctx, scs, prm, tuning=api.make_tuning(**tuning) if tuning else None)
+    frames = batch.render()
+    assert batch.status() > 0
+    for sc, p, f in zip(scs, prm, frames):
+        assert np.array_equal(f.cpu().numpy(), sc.render(p).cpu().numpy())
+
+
+def test_wavefront_needs_a_new_batch_for_new_specular_shaders(ctx):
     sd = scenes.cornell()
-    sd.shaders = sd.shaders.copy()
-    sd.shaders["reflectivity"][0] = 0.5
     sc = api.Scene(ctx, sd)
+    p = _params(T.MODE_PATH, [(8, 8)])
+    b = api.Batch(ctx, [sc], p)
+    sh = sd.shaders.copy()
+    sh["reflectivity"][0] = 0.5
+    sc.set_shaders(sh)
     with pytest.raises(api.AuroraError) as e:
-        api.Batch(ctx, [sc], _params(T.MODE_PATH, [(8, 8)]))
-    assert e.value.status == 6
+        b.render()
+    assert e.value.status == 1
+    b2 = api.Batch(ctx, [sc], p)
+    fr = b2.render()
+    b2.status()
+    assert np.array_equal(fr[0].cpu().numpy(), sc.render(p[0]).cpu().numpy())
 
 
 def test_autotune_returns_a_working_tuning(ctx):
