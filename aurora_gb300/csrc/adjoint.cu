@@ -43,6 +43,138 @@ __device__ __forceinline__ float light_scale(const aur_light& L, const f3& dir, 
     return L.intensity * fmaxf(0.0f, dot(from(L.direction), -dir));
 }
 
+// Adds g_c1 * d(colour1)/d(diffuse_color) = g_c1 * diffuse to shader si's
+// gradient (colour1 = diffuse_color * diffuse; a textured shader's colour is
+// not its diffuse_color, so it gets none). Lanes that hit the same shader
+// (large triangles are hit by most of a warp) are summed first, so a warp
+// issues one atomic per shader instead of one per lane.
+__device__ __forceinline__ void add_diffuse_grad(float* __restrict__ d_diffuse, uint32_t si, const aur_shader* sh,
+                                                 const f3& g_c1) {
+    const f3 gd = sh->texture > 0 ? mk3(0.0f) : g_c1 * sh->diffuse;
+    namespace cg = cooperative_groups;
+    const cg::coalesced_group active = cg::coalesced_threads();
+    const cg::coalesced_group same = cg::labeled_partition(active, si);
+    const float sx = cg::reduce(same, gd.x, cg::plus<float>());
+    const float sy = cg::reduce(same, gd.y, cg::plus<float>());
+    const float sz = cg::reduce(same, gd.z, cg::plus<float>());
+    if (same.thread_rank() == 0 && (sx != 0.0f || sy != 0.0f || sz != 0.0f)) {
+        atomicAdd(d_diffuse + 3 * si + 0, sx);
+        atomicAdd(d_diffuse + 3 * si + 1, sy);
+        atomicAdd(d_diffuse + 3 * si + 2, sz);
+    }
+}
+
+// Direct light at a hit as the primal computes it (direct_light), with its
+// derivatives: Dp receives the direct light per unit Lambert colour, and the
+// light-colour gradients g * thr * d(direct)/d(colour_l) are added (light 0
+// into gl0, the others to d_light). ew: the emission's MIS weight; bounce:
+// whether a diffuse bounce follows the hit (both for AUR_MODE_PATH_MIS).
+template <bool kMis>
+__device__ __forceinline__ f3 direct_grad(const SceneView& sc, const aur_shader* sh, const Bsdf& b, const f3& f,
+                                          const f3& position, const f3& wo, float ew, bool bounce, uint32_t seed,
+                                          uint32_t scene, uint32_t pixel, uint32_t sample, uint32_t rix, const f3& thr,
+                                          const f3& g, float* __restrict__ d_light, f3& gl0, f3& Dp,
+                                          const StackRef& stk, uint32_t& visits, uint32_t* err) {
+    f3 Li = kMis ? from(sh->emission_color) * ew : from(sh->emission_color);
+    Dp = mk3(0.0f);   // direct light per unit Lambert colour
+    for (uint32_t i = 0; i < sc.num_lights; ++i) {
+        const aur_light& L = sc.lights[i];
+        f3 dl = mk3(0.0f);   // d(direct)/d(light colour), per channel
+        if (L.type == AUR_LIGHT_AMBIENT) {
+            const f3 X = (from(L.color) * L.intensity) * L.ambient;
+            Li = Li + f * X;
+            Dp = Dp + X * kInvPi;
+            dl = dl + f * (L.intensity * L.ambient);
+        }
+        if (L.type != AUR_LIGHT_AREA) {
+            f3 wdir; float wt, pdf;
+            const f3 Ls = sample_light(L, position, seed, scene, pixel, sample, rix, 0u, wdir, wt, pdf);
+            if (pdf > 0.0f && !zero(Ls)) {
+                float du = 0.0f, dv = 0.0f;
+                if (!zero(f) &&
+                    traverse<true>(sc.recs, sc.nodes, sc.perm, position, wdir, wt, du, dv, stk, visits, err) == kNoPrim) {
+                    const float cs = fmaxf(0.0f, dot(wdir, b.N));
+                    Li = Li + f * Ls * cs;
+                    Dp = Dp + Ls * (kInvPi * cs);
+                    dl = dl + f * (light_scale(L, wdir, wt) * cs);
+                }
+            }
+        } else if (kMis) {
+            // area_light_mis, both strategies
+            f3 acc = mk3(0.0f), accp = mk3(0.0f), accl = mk3(0.0f);
+            const AreaLightMis q = area_light_setup(L, f);
+            if (q.active) {
+                for (int32_t j = 0; j < L.samples; ++j) {
+                    f3 Ls = mk3(0.0f);
+                    for (int h2 = 0; h2 < 2; ++h2) {
+                        const ShadowSample ss =
+                            h2 == 0 ? area_light_sample(q, i, (uint32_t)j, b, f, position, wo, seed, scene, pixel,
+                                                        sample, rix)
+                                    : area_bsdf_sample(q, i, (uint32_t)j, b, f, position, wo, seed, scene, pixel,
+                                                       sample, rix);
+                        float du = 0.0f, dv = 0.0f, tt = ss.tmax;
+                        if (ss.cand && traverse<true>(sc.recs, sc.nodes, sc.perm, ss.o, ss.d, tt, du, dv, stk,
+                                                      visits, err) == kNoPrim) {
+                            Ls = Ls + ss.c;
+                            accp = accp + ss.e * (ss.geo * kInvPi);
+                            accl = accl + f * (L.intensity * ss.geo);
+                        }
+                    }
+                    acc = acc + Ls;
+                }
+            }
+            const float ns = (float)L.samples;
+            Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
+            Dp = Dp + mk3(accp.x / ns, accp.y / ns, accp.z / ns);
+            dl = dl + mk3(accl.x / ns, accl.y / ns, accl.z / ns);
+        } else {
+            f3 acc = mk3(0.0f), accp = mk3(0.0f), accl = mk3(0.0f);
+            for (int32_t j = 0; j < L.samples; ++j) {
+                f3 wdir; float wt, lpdf;
+                const f3 Lr = sample_light(L, position, seed, scene, pixel, sample, rix, light_slot(i, (uint32_t)j),
+                                           wdir, wt, lpdf);
+                f3 wpos = position;
+                wpos.x += kEpsilon * wdir.x;
+                wpos.y += kEpsilon * wdir.y;
+                wpos.z += kEpsilon * wdir.z;
+                wt += kEpsilon;
+                if (lpdf > 0.0f && !zero(Lr)) {
+                    float du = 0.0f, dv = 0.0f;
+                    if (!zero(f) &&
+                        traverse<true>(sc.recs, sc.nodes, sc.perm, wpos, wdir, wt, du, dv, stk, visits, err) == kNoPrim) {
+                        const float cs = fmaxf(0.0f, dot(wdir, b.N));
+                        acc = acc + f * Lr * cs;
+                        accp = accp + Lr * (kInvPi * cs);
+                        accl = accl + f * (light_scale(L, wdir, wt - kEpsilon) * cs);
+                    }
+                }
+            }
+            const float ns = (float)L.samples;
+            Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
+            Dp = Dp + mk3(accp.x / ns, accp.y / ns, accp.z / ns);
+            dl = dl + mk3(accl.x / ns, accl.y / ns, accl.z / ns);
+        }
+        const f3 gl = g * thr * dl;
+        if (i == 0) {
+            gl0 = gl0 + gl;
+        } else if (gl.x != 0.0f || gl.y != 0.0f || gl.z != 0.0f) {
+            atomicAdd(d_light + 3 * i + 0, gl.x);
+            atomicAdd(d_light + 3 * i + 1, gl.y);
+            atomicAdd(d_light + 3 * i + 2, gl.z);
+        }
+    }
+    if (kMis) {   // the emitter sample (emitter_sample)
+        const ShadowSample ss =
+            emitter_shadow_sample(sc, b, f, position, wo, bounce, seed, scene, pixel, sample, rix);
+        float du = 0.0f, dv = 0.0f, tt = ss.tmax;
+        const bool vis = ss.cand && traverse<true>(sc.recs, sc.nodes, sc.perm, ss.o, ss.d, tt, du, dv, stk,
+                                                   visits, err) == kNoPrim;
+        Li = Li + (vis ? ss.c : mk3(0.0f));
+        if (vis) Dp = Dp + ss.e * (ss.geo * kInvPi);
+    }
+    return Li;
+}
+
 // Replays one camera sample whose primal radiance is C and adds its
 // gradient contributions (scaled by g per colour channel).
 // Gradients of light 0 are summed in `gl0` (reduced once per block by the
@@ -69,104 +201,10 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
         const Bsdf b = get_bsdf(sc, sh, tri, u, v);
         const f3 f = bsdf_f(b);
         const f3 thr = ray.thr;
-        f3 Li = kMis ? from(sh->emission_color) * emission_weight(sc, tri, ray.dir, t, ray.pdf)
-                     : from(sh->emission_color);
-        f3 Dp = mk3(0.0f);   // direct light per unit Lambert colour
-        for (uint32_t i = 0; i < sc.num_lights; ++i) {
-            const aur_light& L = sc.lights[i];
-            f3 dl = mk3(0.0f);   // d(direct)/d(light colour), per channel
-            if (L.type == AUR_LIGHT_AMBIENT) {
-                const f3 X = (from(L.color) * L.intensity) * L.ambient;
-                Li = Li + f * X;
-                Dp = Dp + X * kInvPi;
-                dl = dl + f * (L.intensity * L.ambient);
-            }
-            if (L.type != AUR_LIGHT_AREA) {
-                f3 wdir; float wt, pdf;
-                const f3 Ls = sample_light(L, position, seed, scene, pixel, sample, rix, 0u, wdir, wt, pdf);
-                if (pdf > 0.0f && !zero(Ls)) {
-                    float du = 0.0f, dv = 0.0f;
-                    if (!zero(f) &&
-                        traverse<true>(sc.recs, sc.nodes, sc.perm, position, wdir, wt, du, dv, stk, visits, err) == kNoPrim) {
-                        const float cs = fmaxf(0.0f, dot(wdir, b.N));
-                        Li = Li + f * Ls * cs;
-                        Dp = Dp + Ls * (kInvPi * cs);
-                        dl = dl + f * (light_scale(L, wdir, wt) * cs);
-                    }
-                }
-            } else if (kMis) {
-                // area_light_mis, both strategies
-                f3 acc = mk3(0.0f), accp = mk3(0.0f), accl = mk3(0.0f);
-                const AreaLightMis q = area_light_setup(L, f);
-                if (q.active) {
-                    for (int32_t j = 0; j < L.samples; ++j) {
-                        f3 Ls = mk3(0.0f);
-                        for (int h2 = 0; h2 < 2; ++h2) {
-                            const ShadowSample ss =
-                                h2 == 0 ? area_light_sample(q, i, (uint32_t)j, b, f, position, wo, seed, scene, pixel,
-                                                            sample, rix)
-                                        : area_bsdf_sample(q, i, (uint32_t)j, b, f, position, wo, seed, scene, pixel,
-                                                           sample, rix);
-                            float du = 0.0f, dv = 0.0f, tt = ss.tmax;
-                            if (ss.cand && traverse<true>(sc.recs, sc.nodes, sc.perm, ss.o, ss.d, tt, du, dv, stk,
-                                                          visits, err) == kNoPrim) {
-                                Ls = Ls + ss.c;
-                                accp = accp + ss.e * (ss.geo * kInvPi);
-                                accl = accl + f * (L.intensity * ss.geo);
-                            }
-                        }
-                        acc = acc + Ls;
-                    }
-                }
-                const float ns = (float)L.samples;
-                Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
-                Dp = Dp + mk3(accp.x / ns, accp.y / ns, accp.z / ns);
-                dl = dl + mk3(accl.x / ns, accl.y / ns, accl.z / ns);
-            } else {
-                f3 acc = mk3(0.0f), accp = mk3(0.0f), accl = mk3(0.0f);
-                for (int32_t j = 0; j < L.samples; ++j) {
-                    f3 wdir; float wt, lpdf;
-                    const f3 Lr = sample_light(L, position, seed, scene, pixel, sample, rix, light_slot(i, (uint32_t)j),
-                                               wdir, wt, lpdf);
-                    f3 wpos = position;
-                    wpos.x += kEpsilon * wdir.x;
-                    wpos.y += kEpsilon * wdir.y;
-                    wpos.z += kEpsilon * wdir.z;
-                    wt += kEpsilon;
-                    if (lpdf > 0.0f && !zero(Lr)) {
-                        float du = 0.0f, dv = 0.0f;
-                        if (!zero(f) &&
-                            traverse<true>(sc.recs, sc.nodes, sc.perm, wpos, wdir, wt, du, dv, stk, visits, err) == kNoPrim) {
-                            const float cs = fmaxf(0.0f, dot(wdir, b.N));
-                            acc = acc + f * Lr * cs;
-                            accp = accp + Lr * (kInvPi * cs);
-                            accl = accl + f * (light_scale(L, wdir, wt - kEpsilon) * cs);
-                        }
-                    }
-                }
-                const float ns = (float)L.samples;
-                Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
-                Dp = Dp + mk3(accp.x / ns, accp.y / ns, accp.z / ns);
-                dl = dl + mk3(accl.x / ns, accl.y / ns, accl.z / ns);
-            }
-            const f3 gl = g * thr * dl;
-            if (i == 0) {
-                gl0 = gl0 + gl;
-            } else if (gl.x != 0.0f || gl.y != 0.0f || gl.z != 0.0f) {
-                atomicAdd(d_light + 3 * i + 0, gl.x);
-                atomicAdd(d_light + 3 * i + 1, gl.y);
-                atomicAdd(d_light + 3 * i + 2, gl.z);
-            }
-        }
-        if (kMis) {   // the emitter sample (emitter_sample)
-            const ShadowSample ss =
-                emitter_shadow_sample(sc, b, f, position, wo, depth + 1 <= max_depth, seed, scene, pixel, sample, rix);
-            float du = 0.0f, dv = 0.0f, tt = ss.tmax;
-            const bool vis = ss.cand && traverse<true>(sc.recs, sc.nodes, sc.perm, ss.o, ss.d, tt, du, dv, stk,
-                                                       visits, err) == kNoPrim;
-            Li = Li + (vis ? ss.c : mk3(0.0f));
-            if (vis) Dp = Dp + ss.e * (ss.geo * kInvPi);
-        }
+        const float ew = kMis ? emission_weight(sc, tri, ray.dir, t, ray.pdf) : 1.0f;
+        f3 Dp;
+        const f3 Li = direct_grad<kMis>(sc, sh, b, f, position, wo, ew, depth + 1 <= max_depth, seed, scene, pixel,
+                                        sample, rix, thr, g, d_light, gl0, Dp, stk, visits, err);
         Lrem = Lrem - Li * thr;
         // bounce, as in the primal
         bool cont = false;
@@ -212,26 +250,138 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
             dc.y += c1.y != 0.0f ? Lrem.y / c1.y : 0.0f;
             dc.z += c1.z != 0.0f ? Lrem.z / c1.z : 0.0f;
         }
-        // color1 = diffuse_color * diffuse. Lanes that hit the same shader
-        // (large triangles are hit by most of a warp) are summed first, so a
-        // warp issues one atomic per shader instead of one per lane.
-        const f3 gd = sh->texture > 0 ? mk3(0.0f) : g * dc * sh->diffuse;   // textured: colour is not diffuse_color
-        {
-            namespace cg = cooperative_groups;
-            const cg::coalesced_group active = cg::coalesced_threads();
-            const cg::coalesced_group same = cg::labeled_partition(active, si);
-            const float sx = cg::reduce(same, gd.x, cg::plus<float>());
-            const float sy = cg::reduce(same, gd.y, cg::plus<float>());
-            const float sz = cg::reduce(same, gd.z, cg::plus<float>());
-            if (same.thread_rank() == 0 && (sx != 0.0f || sy != 0.0f || sz != 0.0f)) {
-                atomicAdd(d_diffuse + 3 * si + 0, sx);
-                atomicAdd(d_diffuse + 3 * si + 1, sy);
-                atomicAdd(d_diffuse + 3 * si + 2, sz);
-            }
-        }
+        add_diffuse_grad(d_diffuse, si, sh, g * dc);
         if (!cont) return;
         ray = nr;
     }
+}
+
+
+// The replay for scenes with specular shaders: integrate()'s ray stack
+// (monteCarloRaytracer.cu:26-88) walked again with the same draws. A hit's
+// colour Li * thr depends on its own vertex's colour through the direct
+// light, and on the colour of every vertex whose diffuse bounce lies on its
+// way from the camera through thr, as a factor. The rays that descend from a
+// diffuse bounce are exactly those traced between its pop and the return of
+// the stack to the height it had before the bounce was pushed (depth first),
+// so a marker per pending bounce sums its subtree's radiance; when the
+// subtree ends, g * subtree / c_k goes to the bouncing vertex's shader.
+template <bool kMis>
+__device__ void replay_stack(const SceneView& sc, uint32_t max_depth, uint32_t mode, uint32_t seed, uint32_t scene,
+                             uint32_t pixel, uint32_t sample, const PathRay& primary, const StackRef& stk,
+                             const f3& g, float* __restrict__ d_diffuse, float* __restrict__ d_light, f3& gl0,
+                             uint32_t& visits, uint32_t* err) {
+    struct Marker {
+        f3 col0, c1;          // colour before the subtree, the bouncing vertex's Lambert colour
+        const aur_shader* sh;
+        uint32_t si;
+        int base;             // stack height before the bounce was pushed
+    };
+    PathRay stack[AUR_MAX_DEPTH + 2];
+    Marker mk[AUR_MAX_DEPTH + 2];
+    int sp = 0, nm = 0;
+    stack[sp++] = primary;
+    int depth = 0;
+    f3 col = mk3(0.0f);
+    uint32_t ray_index = 0;
+    const int maxd = (int)max_depth;
+    const bool path = kMis || mode == AUR_MODE_PATH;
+    auto close = [&](const Marker& m) {
+        const f3 sub = col - m.col0;
+        f3 dc;
+        dc.x = m.c1.x != 0.0f ? sub.x / m.c1.x : 0.0f;
+        dc.y = m.c1.y != 0.0f ? sub.y / m.c1.y : 0.0f;
+        dc.z = m.c1.z != 0.0f ? sub.z / m.c1.z : 0.0f;
+        add_diffuse_grad(d_diffuse, m.si, m.sh, g * dc);
+    };
+    for (;;) {
+        while (nm > 0 && sp <= mk[nm - 1].base) close(mk[--nm]);
+        if (!(depth <= maxd && sp > 0)) break;
+        PathRay ray = stack[--sp];
+        const uint32_t rix = ray_index++;
+        float t = kInfinity, u = 0.0f, v = 0.0f;
+        const uint32_t tri = traverse<false>(sc.recs, sc.nodes, sc.perm, ray.pos, ray.dir, t, u, v, stk, visits, err);
+        if (tri == kNoPrim) continue;
+        const f3 position = ray.pos + (ray.dir * t);
+        const f3 wo = -ray.dir;
+        const uint32_t sid = sc.sids[tri];
+        const uint32_t si = sid > 0 ? sid - 1 : 0;
+        const aur_shader* sh = sc.shaders + si;
+        const float refl = sh->reflectivity, trans = sh->translucence;
+        const Bsdf b = get_bsdf(sc, sh, tri, u, v);
+        const f3 f = bsdf_f(b);
+        const bool specular = refl > 0.0f || trans > 0.0f;
+        const bool bounce_follows = !specular && depth + 1 <= maxd;   // as direct_light is told in the primal
+        const float ew = kMis ? emission_weight(sc, tri, ray.dir, t, ray.pdf) : 1.0f;
+        // the splits below change ray.thr before the colour update; the direct
+        // light's derivatives are scaled by the throughput it is added with
+        PathRay cur = ray;
+        if (specular) depth++;
+        PathRay kids[3];
+        int nk = 0;
+        if (depth <= maxd && refl > 0.0f) {
+            PathRay nr;
+            nr.pos = position;
+            nr.dir = reflect(cur.dir, b.N);
+            nr.weight = refl;
+            nr.eta = cur.eta;
+            nr.thr = path ? cur.thr * refl : mk3(nr.weight);
+            nr.pdf = 0.0f;
+            cur.weight *= (1.0f - refl);
+            cur.thr = path ? cur.thr * (1.0f - refl) : mk3(cur.weight);
+            kids[nk++] = nr;
+        }
+        if (depth <= maxd && trans > 0.0f) {
+            f3 rN = b.N;
+            float etai = cur.eta, etat = sh->refractive_index;
+            if (dot(rN, wo) < 0.0f) { rN = -rN; etai = sh->refractive_index; etat = 1.0f; }
+            f3 tdir;
+            if (refract(tdir, cur.dir, rN, etai, etat)) {
+                PathRay nr;
+                nr.pos = position;
+                nr.dir = tdir;
+                nr.weight = trans;
+                nr.eta = etat;
+                nr.thr = path ? cur.thr * trans : mk3(nr.weight);
+                nr.pdf = 0.0f;
+                cur.weight *= (1.0f - trans);
+                cur.thr = path ? cur.thr * (1.0f - trans) : mk3(cur.weight);
+                kids[nk++] = nr;
+            }
+        }
+        bool bounced = false;
+        if (path && !specular) {
+            depth++;
+            if (depth <= maxd) {
+                PathRay nr;
+                nr.pos = position;
+                nr.weight = 1.0f;
+                nr.eta = cur.eta;
+                bounced = kMis ? mis_bounce(b, wo, cur.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr, nr.pdf)
+                               : diffuse_bounce(b, wo, cur.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr,
+                                                nr.pdf);
+                if (bounced) kids[nk++] = nr;
+            }
+        }
+        f3 Dp;
+        const f3 Li = direct_grad<kMis>(sc, sh, b, f, position, wo, ew, bounce_follows, seed, scene, pixel, sample, rix,
+                                        cur.thr, g, d_light, gl0, Dp, stk, visits, err);
+        add_diffuse_grad(d_diffuse, si, sh, g * (cur.thr * Dp));
+        col = col + Li * cur.thr;
+        for (int q = 0; q < nk; ++q) {
+            if (bounced && q == nk - 1) {   // the diffuse bounce: its subtree scales with this vertex's colour
+                Marker m;
+                m.col0 = col;
+                m.c1 = b.color1;
+                m.sh = sh;
+                m.si = si;
+                m.base = sp;
+                mk[nm++] = m;
+            }
+            if (sp < AUR_MAX_DEPTH + 2) stack[sp++] = kids[q]; else atomicOr(err, 2u);
+        }
+    }
+    while (nm > 0) close(mk[--nm]);
 }
 
 __device__ __forceinline__ StackRef adj_stack(uint32_t* smem, int cap) {
@@ -263,8 +413,9 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_primal(Sce
     prim[t] = make_float4(res.color.x, res.color.y, res.color.z, res.any_hit ? 1.0f : 0.0f);
 }
 
-// Replay pass.
-template <bool kMis>
+// Replay pass. kGeneric: scenes with specular shaders, replayed through the
+// ray stack (replay_stack) without the primal pass.
+template <bool kMis, bool kGeneric>
 __global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_replay(SceneView sc, aur_camera cam, aur_render_params p, uint32_t s0,
                                                             uint32_t nb, const float4* __restrict__ prim,
                                                             const float4* __restrict__ d_image,
@@ -281,7 +432,17 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_replay(Sce
     const uint64_t P = (uint64_t)p.width * p.height;
     const uint64_t t = (uint64_t)blockIdx.x * kAdjThreads + threadIdx.x;
     f3 gl0 = mk3(0.0f);
-    if (t < P * nb) {
+    if (kGeneric && t < P * nb) {
+        const uint32_t pix = (uint32_t)(t % P);
+        const uint32_t s = s0 + (uint32_t)(t / P);
+        const PathRay r = camera_ray(cam, p.width, p.height, pix % p.width, pix / p.width, s, p.spp);
+        const float4 di = d_image[pix];
+        const float w = 1.0f / (float)p.spp;
+        const f3 g = mk3(di.x * w, di.y * w, di.z * w);
+        uint32_t visits = 0;
+        replay_stack<kMis>(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, g, d_diffuse,
+                           shared_lights ? s_light : d_light, gl0, visits, err);
+    } else if (!kGeneric && t < P * nb) {
         const float4 c = prim[t];
         if (c.w != 0.0f) {
             const uint32_t pix = (uint32_t)(t % P);
@@ -343,13 +504,7 @@ aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_ca
         st = build_mis_table(ctx, scene);
         if (st != AUR_OK) return st;
     }
-    {
-        std::vector<aur_shader> sh(scene->num_shaders);
-        AUR_CUDA(cudaMemcpy(sh.data(), scene->shaders, sizeof(aur_shader) * sh.size(), cudaMemcpyDeviceToHost));
-        for (const aur_shader& s : sh)
-            AUR_CHECK(!(s.reflectivity > 0.0f) && !(s.translucence > 0.0f), AUR_ERR_UNSUPPORTED,
-                      "aur_render_adjoint: specular shaders are not differentiated");
-    }
+    const bool generic = scene->has_specular;
     const aur_render_params p = *params;
     const uint32_t s0 = p.sample_begin, s1 = p.sample_end ? p.sample_end : p.spp;
     if (s1 == s0) return AUR_OK;
@@ -358,8 +513,10 @@ aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_ca
     const int cap = (int)scene->nmh->levels + 1;
     const size_t smem_p = (size_t)2 * cap * kAdjThreads * sizeof(uint32_t);
     const size_t smem_r = smem_p + 3 * kSharedLights * sizeof(float);
-    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
-    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
+    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
+    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
+    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
+    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
     float4* prim = nullptr;
     AUR_CHECK(::aur::dev_malloc_async(&prim, P * batch * sizeof(float4), ctx->stream) == cudaSuccess, AUR_ERR_OOM,
               "aur_render_adjoint: out of device memory");
@@ -367,16 +524,24 @@ aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_ca
     for (uint32_t s = s0; s < s1; s += batch) {
         const uint32_t nb = std::min(batch, s1 - s);
         const uint32_t grid = cdiv(P * nb, kAdjThreads);
-        if (mis) {
+        const float4* di = (const float4*)d_image;
+        if (generic) {   // the stack replay needs no primal radiance
+            if (mis)
+                k_adj_replay<true, true><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
+                    sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, ctx->d_flags, cap);
+            else
+                k_adj_replay<false, true><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
+                    sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, ctx->d_flags, cap);
+        } else if (mis) {
             k_adj_primal<true><<<grid, kAdjThreads, smem_p, ctx->stream>>>(sv, *camera, p, s, nb, prim, ctx->d_flags,
                                                                            cap);
-            k_adj_replay<true><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
-                sv, *camera, p, s, nb, prim, (const float4*)d_image, d_diffuse, d_light_color, ctx->d_flags, cap);
+            k_adj_replay<true, false><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
+                sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, ctx->d_flags, cap);
         } else {
             k_adj_primal<false><<<grid, kAdjThreads, smem_p, ctx->stream>>>(sv, *camera, p, s, nb, prim, ctx->d_flags,
                                                                             cap);
-            k_adj_replay<false><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
-                sv, *camera, p, s, nb, prim, (const float4*)d_image, d_diffuse, d_light_color, ctx->d_flags, cap);
+            k_adj_replay<false, false><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
+                sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, ctx->d_flags, cap);
         }
     }
     cudaFreeAsync(prim, ctx->stream);

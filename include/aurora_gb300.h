@@ -459,8 +459,10 @@ aur_status aur_filter_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, cons
  * aur_render with the same parameters (alpha ignored). d_diffuse
  * (num_shaders*3) and d_light_color (num_lights*3), device: gradients are
  * ADDED. Same estimator and RNG streams as aur_render, in every mode
- * (AUR_MODE_PATH_MIS included: its weights do not depend on the colours);
- * materials must be non-specular (AUR_ERR_UNSUPPORTED otherwise). */
+ * (AUR_MODE_PATH_MIS included: its weights do not depend on the colours)
+ * and for every material (scenes with specular shaders are replayed
+ * through the integrator's ray stack). A textured shader's colour is not
+ * its diffuse_color: its gradient entries stay zero. */
 aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_camera* camera,
                               const aur_render_params* params, const float* d_image, float* d_diffuse,
                               float* d_light_color);

@@ -45,12 +45,32 @@ def _fd(sc, sd, p, target, kind, idx, ch):
     return (vals[0] - vals[1]) / (2 * H)
 
 
+def _specular_cornell():
+    """Cornell with a mirror-like block (reflectivity 0.6, diffuse remainder)
+    and a glass-like one (translucence 0.7, index 1.5)."""
+    sd = scenes.cornell()
+    sh = np.concatenate([sd.shaders, np.stack([T.lambert((0.9, 0.8, 0.7)), T.lambert((0.7, 0.8, 0.9))])])
+    sh["reflectivity"][3] = 0.6
+    sh["translucence"][4] = 0.7
+    sh["refractive_index"][4] = 1.5
+    sids = sd.shader_ids.copy()
+    sids[10:22] = 4
+    sids[22:34] = 5
+    return scenes.SceneData("cornell_specular", sd.vertices, sd.normals, sids, sh, sd.lights, sd.camera)
+
+
 @pytest.mark.parametrize("mode,scene", [(T.MODE_PATH, "sphere"), (T.MODE_REFERENCE, "sphere"),
-                                        (T.MODE_PATH_MIS, "sphere"), (T.MODE_PATH_MIS, "emissive")])
+                                        (T.MODE_PATH_MIS, "sphere"), (T.MODE_PATH_MIS, "emissive"),
+                                        (T.MODE_REFERENCE, "specular"), (T.MODE_PATH, "specular"),
+                                        (T.MODE_PATH_MIS, "specular")])
 def test_adjoint_matches_finite_differences(ctx, mode, scene):
     """MIS: the area light by both strategies (sphere), and emissive
-    triangles sampled from the table plus the area light (emissive)."""
-    sd, sc, p, target = _setup(ctx, mode, sd=None if scene == "sphere" else scenes.cornell_emissive(area_light=True))
+    triangles sampled from the table plus the area light (emissive).
+    Specular: the ray-stack replay, with reflected and refracted rays and
+    diffuse bounces under them."""
+    sd = {"sphere": None, "emissive": scenes.cornell_emissive(area_light=True),
+          "specular": _specular_cornell()}[scene]
+    sd, sc, p, target = _setup(ctx, mode, sd=sd)
     img = sc.render(p)
     d_image = (2.0 * (img - target)).contiguous()
     d_image[..., 3] = 0.0
