@@ -313,63 +313,18 @@ __device__ void replay_stack(const SceneView& sc, uint32_t max_depth, uint32_t m
         const bool specular = refl > 0.0f || trans > 0.0f;
         const bool bounce_follows = !specular && depth + 1 <= maxd;   // as direct_light is told in the primal
         const float ew = kMis ? emission_weight(sc, tri, ray.dir, t, ray.pdf) : 1.0f;
-        // the splits below change ray.thr before the colour update; the direct
-        // light's derivatives are scaled by the throughput it is added with
+        // the continuation changes the ray's throughput before the colour
+        // update; the direct light's derivatives scale with that throughput
         PathRay cur = ray;
-        if (specular) depth++;
-        PathRay kids[3];
-        int nk = 0;
-        if (depth <= maxd && refl > 0.0f) {
-            PathRay nr;
-            nr.pos = position;
-            nr.dir = reflect(cur.dir, b.N);
-            nr.weight = refl;
-            nr.eta = cur.eta;
-            nr.thr = path ? cur.thr * refl : mk3(nr.weight);
-            nr.pdf = 0.0f;
-            cur.weight *= (1.0f - refl);
-            cur.thr = path ? cur.thr * (1.0f - refl) : mk3(cur.weight);
-            kids[nk++] = nr;
-        }
-        if (depth <= maxd && trans > 0.0f) {
-            f3 rN = b.N;
-            float etai = cur.eta, etat = sh->refractive_index;
-            if (dot(rN, wo) < 0.0f) { rN = -rN; etai = sh->refractive_index; etat = 1.0f; }
-            f3 tdir;
-            if (refract(tdir, cur.dir, rN, etai, etat)) {
-                PathRay nr;
-                nr.pos = position;
-                nr.dir = tdir;
-                nr.weight = trans;
-                nr.eta = etat;
-                nr.thr = path ? cur.thr * trans : mk3(nr.weight);
-                nr.pdf = 0.0f;
-                cur.weight *= (1.0f - trans);
-                cur.thr = path ? cur.thr * (1.0f - trans) : mk3(cur.weight);
-                kids[nk++] = nr;
-            }
-        }
-        bool bounced = false;
-        if (path && !specular) {
-            depth++;
-            if (depth <= maxd) {
-                PathRay nr;
-                nr.pos = position;
-                nr.weight = 1.0f;
-                nr.eta = cur.eta;
-                bounced = kMis ? mis_bounce(b, wo, cur.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr, nr.pdf)
-                               : diffuse_bounce(b, wo, cur.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr,
-                                                nr.pdf);
-                if (bounced) kids[nk++] = nr;
-            }
-        }
+        const Continuation kc =
+            continue_ray<kMis>(sh, b, cur, position, wo, path, depth, maxd, seed, scene, pixel, sample, rix);
         f3 Dp;
         const f3 Li = direct_grad<kMis>(sc, sh, b, f, position, wo, ew, bounce_follows, seed, scene, pixel, sample, rix,
                                         cur.thr, g, d_light, gl0, Dp, stk, visits, err);
         add_diffuse_grad(d_diffuse, si, sh, g * (cur.thr * Dp));
         col = col + Li * cur.thr;
-        for (int q = 0; q < nk; ++q) {
-            if (bounced && q == nk - 1) {   // the diffuse bounce: its subtree scales with this vertex's colour
+        for (int q = 0; q < kc.n; ++q) {
+            if (kc.bounced && q == kc.n - 1) {   // the diffuse bounce: its subtree scales with this vertex's colour
                 Marker m;
                 m.col0 = col;
                 m.c1 = b.color1;
@@ -378,7 +333,7 @@ __device__ void replay_stack(const SceneView& sc, uint32_t max_depth, uint32_t m
                 m.base = sp;
                 mk[nm++] = m;
             }
-            if (sp < AUR_MAX_DEPTH + 2) stack[sp++] = kids[q]; else atomicOr(err, 2u);
+            if (sp < AUR_MAX_DEPTH + 2) stack[sp++] = kc.ray[q]; else atomicOr(err, 2u);
         }
     }
     while (nm > 0) close(mk[--nm]);

@@ -552,6 +552,74 @@ __device__ __forceinline__ bool diffuse_bounce(const Bsdf& b, const f3& wo, cons
     return false;
 }
 
+// The rays a hit hands on (monteCarloRaytracer.cu:54-85): a specular
+// shader's reflection and refraction rays, path mode's diffuse bounce
+// otherwise, in the order they are pushed on the sample's ray stack. Updates
+// the ray's weight and throughput (the throughput its colour is added with)
+// and the sample's depth counter. Shared by the plain integrator, the
+// wavefront's specular batches and the adjoint's stack replay.
+struct Continuation {
+    PathRay ray[3];
+    int n;
+    bool bounced;   // the last ray is the diffuse bounce
+};
+
+template <bool kMis>
+__device__ __forceinline__ Continuation continue_ray(const aur_shader* sh, const Bsdf& b, PathRay& ray,
+                                                     const f3& position, const f3& wo, bool path, int& depth, int maxd,
+                                                     uint32_t seed, uint32_t scene, uint32_t pixel, uint32_t sample,
+                                                     uint32_t rix) {
+    Continuation k;
+    k.n = 0;
+    k.bounced = false;
+    const float refl = sh->reflectivity, trans = sh->translucence;
+    const bool specular = refl > 0.0f || trans > 0.0f;
+    if (specular) depth++;
+    if (depth <= maxd && refl > 0.0f) {
+        PathRay& nr = k.ray[k.n++];
+        nr.pos = position;
+        nr.dir = reflect(ray.dir, b.N);
+        nr.weight = refl;
+        nr.eta = ray.eta;
+        nr.thr = path ? ray.thr * refl : mk3(nr.weight);
+        nr.pdf = 0.0f;
+        ray.weight *= (1.0f - refl);
+        ray.thr = path ? ray.thr * (1.0f - refl) : mk3(ray.weight);
+    }
+    if (depth <= maxd && trans > 0.0f) {
+        f3 rN = b.N;
+        float etai = ray.eta, etat = sh->refractive_index;
+        if (dot(rN, wo) < 0.0f) { rN = -rN; etai = sh->refractive_index; etat = 1.0f; }
+        f3 tdir;
+        if (refract(tdir, ray.dir, rN, etai, etat)) {
+            PathRay& nr = k.ray[k.n++];
+            nr.pos = position;
+            nr.dir = tdir;
+            nr.weight = trans;
+            nr.eta = etat;
+            nr.thr = path ? ray.thr * trans : mk3(nr.weight);
+            nr.pdf = 0.0f;
+            ray.weight *= (1.0f - trans);
+            ray.thr = path ? ray.thr * (1.0f - trans) : mk3(ray.weight);
+        }
+    }
+    if (path && !specular) {
+        depth++;
+        if (depth <= maxd) {
+            PathRay& nr = k.ray[k.n];
+            nr.pos = position;
+            nr.weight = 1.0f;
+            nr.eta = ray.eta;
+            if (kMis ? mis_bounce(b, wo, ray.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr, nr.pdf)
+                     : diffuse_bounce(b, wo, ray.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr, nr.pdf)) {
+                ++k.n;
+                k.bounced = true;
+            }
+        }
+    }
+    return k;
+}
+
 // Integrates one camera ray. RNG key: (seed, scene_id) x (pixel, sample,
 // ray index within the sample, slot). kMis: mode is AUR_MODE_PATH_MIS.
 template <bool kMis = false>
@@ -590,49 +658,10 @@ __device__ __forceinline__ SampleResult integrate(const SceneView& sc, uint32_t 
         const float ew = kMis ? emission_weight(sc, tri, ray.dir, t, ray.pdf) : 1.0f;
         const f3 Li = direct_light<kMis>(sc, sh, b, position, wo, ew, !specular && depth + 1 <= maxd, seed, scene,
                                          pixel, sample, rix, stk, visits, err);
-        if (specular) depth++;
-        if (depth <= maxd && refl > 0.0f) {
-            PathRay nr;
-            nr.pos = position;
-            nr.dir = reflect(ray.dir, b.N);
-            nr.weight = refl;
-            nr.eta = ray.eta;
-            nr.thr = path ? ray.thr * refl : mk3(nr.weight);
-            nr.pdf = 0.0f;
-            ray.weight *= (1.0f - refl);
-            ray.thr = path ? ray.thr * (1.0f - refl) : mk3(ray.weight);
-            if (sp < AUR_MAX_DEPTH + 2) stack[sp++] = nr; else atomicOr(err, 2u);
-        }
-        if (depth <= maxd && trans > 0.0f) {
-            f3 rN = b.N;
-            float etai = ray.eta, etat = sh->refractive_index;
-            if (dot(rN, wo) < 0.0f) { rN = -rN; etai = sh->refractive_index; etat = 1.0f; }
-            f3 tdir;
-            if (refract(tdir, ray.dir, rN, etai, etat)) {
-                PathRay nr;
-                nr.pos = position;
-                nr.dir = tdir;
-                nr.weight = trans;
-                nr.eta = etat;
-                nr.thr = path ? ray.thr * trans : mk3(nr.weight);
-                nr.pdf = 0.0f;
-                ray.weight *= (1.0f - trans);
-                ray.thr = path ? ray.thr * (1.0f - trans) : mk3(ray.weight);
-                if (sp < AUR_MAX_DEPTH + 2) stack[sp++] = nr; else atomicOr(err, 2u);
-            }
-        }
-        if (path && !specular) {
-            depth++;
-            if (depth <= maxd) {
-                PathRay nr;
-                nr.pos = position;
-                nr.weight = 1.0f;
-                nr.eta = ray.eta;
-                if (kMis ? mis_bounce(b, wo, ray.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr, nr.pdf)
-                         : diffuse_bounce(b, wo, ray.thr, seed, scene, pixel, sample, rix, nr.dir, nr.thr, nr.pdf)) {
-                    if (sp < AUR_MAX_DEPTH + 2) stack[sp++] = nr; else atomicOr(err, 2u);
-                }
-            }
+        const Continuation k =
+            continue_ray<kMis>(sh, b, ray, position, wo, path, depth, maxd, seed, scene, pixel, sample, rix);
+        for (int q = 0; q < k.n; ++q) {
+            if (sp < AUR_MAX_DEPTH + 2) stack[sp++] = k.ray[q]; else atomicOr(err, 2u);
         }
         res.color = res.color + Li * ray.thr;
     }

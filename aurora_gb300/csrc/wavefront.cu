@@ -461,62 +461,24 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
             }
         }
         if (kSpec) {
-            // integrate(): specular splits and the diffuse bounce onto the stack
+            // integrate(): the specular rays and the diffuse bounce onto the stack
             const float4 t4 = a.thr[slot];
-            f3 thr = mk3(t4.x, t4.y, t4.z);
-            float weight = o4.w;
-            const float eta = d4.w;
-            const bool path = kMis || a.mode == AUR_MODE_PATH;
-            const float refl = sh->reflectivity, trans = sh->translucence;
-            uint32_t dep = m.y, sp = a.sp[slot];
-            if (specular) dep++;
-            if (dep <= a.max_depth && refl > 0.0f) {
-                PathRay nr;
-                nr.pos = position;
-                nr.dir = reflect(dir, bs.N);
-                nr.weight = refl;
-                nr.eta = eta;
-                nr.thr = path ? thr * refl : mk3(nr.weight);
-                nr.pdf = 0.0f;
-                weight *= (1.0f - refl);
-                thr = path ? thr * (1.0f - refl) : mk3(weight);
-                wf_push(a, slot, sp, nr, c);
-            }
-            if (dep <= a.max_depth && trans > 0.0f) {
-                f3 rN = bs.N;
-                float etai = eta, etat = sh->refractive_index;
-                if (dot(rN, wo) < 0.0f) { rN = -rN; etai = sh->refractive_index; etat = 1.0f; }
-                f3 tdir;
-                if (refract(tdir, dir, rN, etai, etat)) {
-                    PathRay nr;
-                    nr.pos = position;
-                    nr.dir = tdir;
-                    nr.weight = trans;
-                    nr.eta = etat;
-                    nr.thr = path ? thr * trans : mk3(nr.weight);
-                    nr.pdf = 0.0f;
-                    weight *= (1.0f - trans);
-                    thr = path ? thr * (1.0f - trans) : mk3(weight);
-                    wf_push(a, slot, sp, nr, c);
-                }
-            }
-            if (path && !specular) {
-                dep++;
-                if (dep <= a.max_depth) {
-                    PathRay nr;
-                    nr.pos = position;
-                    nr.weight = 1.0f;
-                    nr.eta = eta;
-                    const bool ok = kMis ? mis_bounce(bs, wo, thr, a.seed, sc.scene_id, pix, sample, rix, nr.dir,
-                                                      nr.thr, nr.pdf)
-                                         : diffuse_bounce(bs, wo, thr, a.seed, sc.scene_id, pix, sample, rix, nr.dir,
-                                                          nr.thr, nr.pdf);
-                    if (ok) wf_push(a, slot, sp, nr, c);
-                }
-            }
+            PathRay ray;
+            ray.pos = pos;
+            ray.dir = dir;
+            ray.thr = mk3(t4.x, t4.y, t4.z);
+            ray.weight = o4.w;
+            ray.eta = d4.w;
+            ray.pdf = t4.w;
+            int dep = (int)m.y;
+            uint32_t sp = a.sp[slot];
+            const Continuation k = continue_ray<kMis>(sh, bs, ray, position, wo, kMis || a.mode == AUR_MODE_PATH, dep,
+                                                      (int)a.max_depth, a.seed, sc.scene_id, pix, sample, rix);
+            for (int q = 0; q < k.n; ++q) wf_push(a, slot, sp, k.ray[q], c);
+            const f3 thr = ray.thr;
             a.thr[slot] = make_float4(thr.x, thr.y, thr.z, 0.0f);   // the colour update's throughput
             a.sp[slot] = sp;
-            a.meta[slot].y = dep;
+            a.meta[slot].y = (uint32_t)dep;
             continue;
         }
         // bounce (BSDF::samplef, bsdf.cuh:222-236)
