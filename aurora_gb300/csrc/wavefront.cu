@@ -1158,6 +1158,10 @@ aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, cons
     // 32M paths in flight ran 16 % faster than 8M. A candidate that does not
     // fit in memory fails in aur_batch_create and is skipped.
     const uint32_t pools[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23, 1u << 24, 1u << 25, 1u << 26};
+    // specular batches carry 864 bytes of ray stack per path: pools up to 8M (7 GB)
+    bool spec = false;
+    for (uint32_t i = 0; i < num_scenes; ++i) spec = spec || (scenes[i] && scenes[i]->has_specular);
+    const uint32_t max_pool = spec ? (1u << 23) : (1u << 26);
     const uint32_t blocks[] = {128, 256};
     const uint32_t per_sm[] = {4, 8, 16};
     cudaEvent_t e0, e1;
@@ -1168,7 +1172,7 @@ aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, cons
     for (uint32_t pool : pools)
         for (uint32_t bs : blocks)
             for (uint32_t bps : per_sm) {
-                if ((uint64_t)bs * bps > 2048) continue;
+                if ((uint64_t)bs * bps > 2048 || pool > max_pool) continue;
                 aur_wavefront_tuning t{pool, 1, bs, bps, 0};
                 aur_batch* bt = nullptr;
                 if (aur_batch_create(ctx, scenes, cameras, p1.data(), num_scenes, &t, &bt) != AUR_OK) {
