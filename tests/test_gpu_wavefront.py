@@ -73,6 +73,19 @@ def test_wavefront_specular_equals_plain(ctx, mode, tuning):
         assert np.array_equal(f.cpu().numpy(), sc.render(p).cpu().numpy())
 
 
+def test_autotune_specular_batch(ctx):
+    """Specular batches carry a ray stack per path: the autotuner keeps their
+    pools at 8M paths or fewer, and its pick renders the plain frame."""
+    scs = [api.Scene(ctx, _specular(scenes.cornell()))]
+    prm = _params(T.MODE_PATH, [(48, 40)])
+    t, ms = api.autotune(ctx, scs, prm)
+    assert ms > 0 and 1024 <= int(t["paths_in_flight"]) <= (1 << 23)
+    b = api.Batch(ctx, scs, prm, tuning=t)
+    fr = b.render()
+    b.status()
+    assert np.array_equal(fr[0].cpu().numpy(), scs[0].render(prm[0]).cpu().numpy())
+
+
 def test_wavefront_needs_a_new_batch_for_new_specular_shaders(ctx):
     sd = scenes.cornell()
     sc = api.Scene(ctx, sd)
