@@ -110,3 +110,17 @@ def test_specular_render_matches_oracle(ctx, mode):
     img = sc.render(p).cpu().numpy()
     ref, _ = oracle.render(oracle.NmhScene(sd2), p)
     assert np.array_equal(img, ref)
+
+
+@pytest.mark.parametrize("W,H,spp,depth,mode", [(1, 1, 1, 0, T.MODE_REFERENCE), (7, 3, 5, 16, T.MODE_PATH),
+                                                (13, 11, 7, 2, T.MODE_PATH_MIS), (16, 16, 2, 16, T.MODE_REFERENCE)])
+def test_edge_sizes_match_oracle(ctx, W, H, spp, depth, mode):
+    """A one-pixel frame, sample counts that are not squares (the reference's
+    (short)sqrtf(spp) grid puts the extra samples below the pixel), depth 0
+    and the maximum depth, in every mode."""
+    sd = scenes.cornell_emissive(area_light=True)
+    sc = api.Scene(ctx, sd)
+    p = T.render_params(W, H, spp, depth, seed=13, mode=mode)
+    img = sc.render(p).cpu().numpy()
+    ref, _ = oracle.render(oracle.NmhScene(sd), p, table=sc.mis_table() if mode == T.MODE_PATH_MIS else None)
+    assert np.array_equal(img, ref)
