@@ -89,6 +89,7 @@ def ref_lib():
         L.ref_power_heuristic.restype = ctypes.c_float
         L.ref_area_hit.argtypes = [P, P, P, P]
         L.ref_area_hit.restype = ctypes.c_int
+        L.ref_triangle_areas.argtypes = [P, U32, P]
         _ref = L
     return _ref
 
@@ -405,3 +406,11 @@ def render_counted(nscene, params, camera=None, nthreads=None):
                                    _ptr(nscene.lights), nscene.lights.shape[0], _ptr(cam), _ptr(p), _ptr(accum),
                                    nthreads or nthreads_default(), _ptr(sp))
     return accum, int(tot), int(sp[0])
+
+
+def ref_triangle_areas(V):
+    """Primitive3::area of each triangle (reference layout, (n, 9))."""
+    V = np.ascontiguousarray(V, np.float32).reshape(-1, 9)
+    out = np.zeros(V.shape[0], np.float32)
+    ref_lib().ref_triangle_areas(_ptr(V), V.shape[0], _ptr(out))
+    return out

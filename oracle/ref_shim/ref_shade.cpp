@@ -252,6 +252,16 @@ void ref_bsdf_hits(const float* V, const float* N, const float* TG, const float*
     delete[] sh;
 }
 
+/* Primitive3::area (primitive.cuh:74-85) of n triangles in the reference
+ * layout (readPoints), the emitter table's area. */
+void ref_triangle_areas(const float* V, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        Primitive3 p;
+        p.readPoints(V + (size_t)i * 9);
+        out[i] = p.area();
+    }
+}
+
 /* powerHeuristic(1, a, 1, b) (sampling.cuh:162-169). */
 float ref_power_heuristic(float a, float b) { return powerHeuristic(1, a, 1, b); }
 

@@ -1,5 +1,6 @@
 """Known answers for the oracle's emitter table (cudaCreateEmitters)."""
 import numpy as np
+import pytest
 
 import oracle
 from aurora_gb300 import scenes, types as T
@@ -34,3 +35,23 @@ def test_cdf_is_monotone_and_ends_at_one():
     sd = _scene(V, list(np.random.default_rng(1).uniform(0, 2, size=37) * (np.arange(37) % 3 > 0)))
     e = oracle.emitters(oracle.NmhScene(sd))
     assert len(e) > 1000 and np.all(np.diff(e["cdf"]) >= 0) and e["cdf"][-1] == np.float32(1.0)
+
+
+def test_areas_match_the_reference_primitive_area():
+    """The emitter table's areas are Primitive3::area (primitive.cuh:74-85),
+    compiled from the reference's own header: bit for bit, on a random soup
+    and on degenerate triangles."""
+    if oracle.ref_lib() is None:
+        pytest.skip("the reference sources are not on this machine")
+    V = scenes.random_soup(3000, seed=9)
+    V[:5] = V[5]                                               # duplicates
+    V[10, 0:3] = V[10, 0]                                      # zero extent in x
+    V[11] = 0.0                                                # a point
+    sh = np.stack([T.lambert((0.5, 0.5, 0.5))])
+    sh["emission"] = 1.0
+    sd = scenes.SceneData("t", V, np.zeros_like(V), np.ones(V.shape[0], np.uint16), sh, np.zeros(0, T.light_dtype),
+                          scenes.cornell_camera())
+    ns = oracle.NmhScene(sd)
+    e = oracle.emitters(ns)
+    ref = oracle.ref_triangle_areas(ns.V)
+    assert np.array_equal(e["area"].view(np.uint32), ref[e["triangle_id"]].view(np.uint32))
