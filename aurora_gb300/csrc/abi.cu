@@ -178,6 +178,7 @@ aur_status aur_ctx_destroy(aur_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+    ::aur::free_build_cache(ctx);
     for (auto& s : ctx->pipe) cudaFree(s.ptr);
     for (auto& s : ctx->out) cudaFree(s.ptr);
     for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);

@@ -57,6 +57,10 @@ constexpr uint32_t kMaxTriangles = 1u << 30;
 // give 30 levels).
 constexpr int kStackDepth = 32;
 
+// A context's cached NMH build (scratch and recorded launch graph), owned
+// by nmh_build.cu; freed with the context.
+struct BuildCache;
+
 }  // namespace aur
 
 struct aur_ctx {
@@ -71,6 +75,7 @@ struct aur_ctx {
     aur::Scratch pipe[2];                // double-buffered device chunks for *_host calls
     aur::Scratch out[2];
     cudaEvent_t ev[8] = {};
+    aur::BuildCache* build = nullptr;    // created by the first aur_nmh_build
 };
 
 struct aur_nmh {
@@ -111,6 +116,8 @@ struct aur_scene {
 namespace aur {
 
 aur_status nmh_build_impl(aur_ctx* ctx, const float* vertices, uint32_t count, aur_nmh** out);
+// Releases the context's cached build scratch and graph (after its last launch).
+void free_build_cache(aur_ctx* ctx);
 aur_status check_params(const aur_render_params* p);
 // Builds the scene's light-selection table for AUR_MODE_PATH_MIS if it is
 // not built (stream-synchronous); free_mis_table drops it.

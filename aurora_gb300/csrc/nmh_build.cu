@@ -22,7 +22,9 @@
 //      (applyIndices, :217-245) and traversal node records are written.
 // Every ordering ties by the lower original prim id.
 #include <cstdio>
+#include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "aur_internal.h"
 #include "aur_math.cuh"
@@ -931,17 +933,149 @@ uint32_t log2i(uint32_t x) {
 // one status word per tile, then the three tile counters.
 constexpr size_t lookback_bytes(size_t ntiles) { return 3 * ntiles * sizeof(unsigned long long) + 16; }
 
+// ------------------------------------------------------------ launch sequence
+//
+// The launches of one build go through a Seq, which either issues them on a
+// stream, or records them as a linear chain of CUDA graph nodes, or replays
+// the same sequence against such a recording and writes into its
+// instantiated graph only the arguments that differ (another vertex array,
+// other output buffers: the next build of the same size). A build of N
+// triangles makes about 4 * levels + 20 launches; recorded once and then
+// launched as one graph they no longer wait on the host's per-launch cost.
+struct NodeRec {
+    cudaGraphNode_t node = nullptr;
+    const void* func = nullptr;          // null for a memset node
+    dim3 grid, block;
+    unsigned smem = 0;
+    std::vector<unsigned char> args;     // packed kernel arguments, or (target, bytes) of a memset
+};
+
+class Seq {
+public:
+    enum Mode { kDirect, kRecord, kPatch };
+
+    static Seq direct(cudaStream_t st) { Seq q; q.mode_ = kDirect; q.st_ = st; return q; }
+    static Seq record(cudaGraph_t g, std::vector<NodeRec>* nodes) {
+        Seq q; q.mode_ = kRecord; q.g_ = g; q.nodes_ = nodes; nodes->clear(); return q;
+    }
+    static Seq patch(cudaGraphExec_t exec, std::vector<NodeRec>* nodes) {
+        Seq q; q.mode_ = kPatch; q.exec_ = exec; q.nodes_ = nodes; return q;
+    }
+
+    template <typename... P, typename... A>
+    void launch(void (*k)(P...), dim3 grid, dim3 block, size_t smem, A... a) {
+        static_assert(sizeof...(P) == sizeof...(A), "kernel argument count");
+        if (err_ != cudaSuccess) return;
+        if (mode_ == kDirect) {
+            k<<<grid, block, smem, st_>>>(static_cast<P>(a)...);
+            return;
+        }
+        std::vector<unsigned char> buf;
+        size_t offs[sizeof...(P) + 1];
+        size_t i = 0;
+        (put<P>(buf, offs[i++], static_cast<P>(a)), ...);
+        void* ptrs[sizeof...(P) + 1];
+        for (size_t j = 0; j < sizeof...(P); ++j) ptrs[j] = buf.data() + offs[j];
+        cudaKernelNodeParams p = {};
+        p.func = (void*)k;
+        p.gridDim = grid;
+        p.blockDim = block;
+        p.sharedMemBytes = (unsigned)smem;
+        p.kernelParams = ptrs;
+        if (mode_ == kRecord) {
+            NodeRec r;
+            err_ = cudaGraphAddKernelNode(&r.node, g_, last_ ? &last_ : nullptr, last_ ? 1 : 0, &p);
+            if (err_ != cudaSuccess) return;
+            last_ = r.node;
+            r.func = p.func; r.grid = grid; r.block = block; r.smem = p.sharedMemBytes;
+            r.args = std::move(buf);
+            nodes_->push_back(std::move(r));
+            return;
+        }
+        if (next_ >= nodes_->size()) { err_ = cudaErrorInvalidValue; return; }
+        NodeRec& r = (*nodes_)[next_++];
+        if (r.func != p.func || !same(r.grid, grid) || !same(r.block, block) || r.smem != p.sharedMemBytes ||
+            r.args.size() != buf.size()) {
+            err_ = cudaErrorInvalidValue;
+            return;
+        }
+        if (r.args != buf) {
+            err_ = cudaGraphExecKernelNodeSetParams(exec_, r.node, &p);
+            if (err_ == cudaSuccess) r.args = std::move(buf);
+        }
+    }
+
+    // Zeroes `bytes` (a multiple of 4) at p.
+    void memset(void* p, size_t bytes) {
+        if (err_ != cudaSuccess) return;
+        if (mode_ == kDirect) {
+            err_ = cudaMemsetAsync(p, 0, bytes, st_);
+            return;
+        }
+        cudaMemsetParams m = {};
+        m.dst = p;
+        m.value = 0;
+        m.elementSize = 4;
+        m.width = bytes / 4;
+        m.height = 1;
+        std::vector<unsigned char> key(sizeof(void*) + sizeof(size_t));
+        std::memcpy(key.data(), &p, sizeof(void*));
+        std::memcpy(key.data() + sizeof(void*), &bytes, sizeof(size_t));
+        if (mode_ == kRecord) {
+            NodeRec r;
+            err_ = cudaGraphAddMemsetNode(&r.node, g_, last_ ? &last_ : nullptr, last_ ? 1 : 0, &m);
+            if (err_ != cudaSuccess) return;
+            last_ = r.node;
+            r.args = std::move(key);
+            nodes_->push_back(std::move(r));
+            return;
+        }
+        if (next_ >= nodes_->size() || (*nodes_)[next_].func != nullptr) { err_ = cudaErrorInvalidValue; return; }
+        NodeRec& r = (*nodes_)[next_++];
+        if (r.args != key) {
+            err_ = cudaGraphExecMemsetNodeSetParams(exec_, r.node, &m);
+            if (err_ == cudaSuccess) r.args = std::move(key);
+        }
+    }
+
+    // First error of the sequence: a failed launch or node call, or (when
+    // patching) a sequence that does not match the recording.
+    cudaError_t finish() {
+        if (err_ == cudaSuccess && mode_ == kDirect) err_ = cudaGetLastError();
+        if (err_ == cudaSuccess && mode_ == kPatch && next_ != nodes_->size()) err_ = cudaErrorInvalidValue;
+        return err_;
+    }
+
+private:
+    template <typename T>
+    static void put(std::vector<unsigned char>& b, size_t& off, const T& v) {
+        off = (b.size() + alignof(T) - 1) & ~(alignof(T) - 1);
+        b.resize(off + sizeof(T));
+        std::memcpy(b.data() + off, &v, sizeof(T));
+    }
+    static bool same(const dim3& a, const dim3& b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+
+    Mode mode_ = kDirect;
+    cudaStream_t st_ = nullptr;
+    cudaGraph_t g_ = nullptr;
+    cudaGraphExec_t exec_ = nullptr;
+    cudaGraphNode_t last_ = nullptr;
+    std::vector<NodeRec>* nodes_ = nullptr;
+    size_t next_ = 0;
+    cudaError_t err_ = cudaSuccess;
+};
+
 // One level's split of the next axis' list and partition of the other two,
 // each a single pass with look-back tile prefixes; the status words and
 // tile counters are cleared first.
-void split_and_partition(const ListSet& sb, const ListSet& sac, uint32_t M, uint32_t mt, uint32_t ntiles,
+void split_and_partition(Seq& q, const ListSet& sb, const ListSet& sac, uint32_t M, uint32_t mt, uint32_t ntiles,
                          uint32_t* node_of, const uint32_t* ns, const uint32_t* nl, const uint32_t* nlb, uint32_t L0,
-                         uint32_t m_next, unsigned long long* lb, uint32_t* err, cudaStream_t st) {
+                         uint32_t m_next, unsigned long long* lb, uint32_t* err) {
     uint32_t* counters = reinterpret_cast<uint32_t*>(lb + 3 * (size_t)ntiles);
-    cudaMemsetAsync(lb, 0, lookback_bytes(ntiles), st);
-    k_split_next<<<mt, kThreads, 0, st>>>(sb, M, node_of, ns, nl, L0, lb, counters, err);
-    k_partition<<<dim3(mt, 2), kThreads, 0, st>>>(sac, M, node_of, ns, nl, nlb, L0, lb + ntiles, ntiles, counters + 1,
-                                                  m_next, err);
+    q.memset(lb, lookback_bytes(ntiles));
+    q.launch(k_split_next, dim3(mt), dim3(kThreads), 0, sb, M, node_of, ns, nl, L0, lb, counters, err);
+    q.launch(k_partition, dim3(mt, 2), dim3(kThreads), 0, sac, M, node_of, ns, nl, nlb, L0, lb + ntiles, ntiles,
+             counters + 1, m_next, err);
 }
 
 // First level whose node segments all fit k_local_finish (the leftmost
@@ -953,17 +1087,12 @@ uint32_t local_level(uint32_t n, uint32_t levels) {
 }
 
 // The remaining levels lv0 .. levels-1, one block per node of level lv0.
-cudaError_t finish_local(const uint32_t* list, size_t S, const float* mn, const float* mx, uint32_t n,
-                         uint32_t lv0, const uint32_t* nstart, uint32_t* node_of, uint32_t* heap, float* sbox,
-                         uint32_t* err, cudaStream_t st) {
+void finish_local(Seq& q, const uint32_t* list, size_t S, const float* mn, const float* mx, uint32_t n, uint32_t lv0,
+                  const uint32_t* nstart, uint32_t* node_of, uint32_t* heap, float* sbox, uint32_t* err) {
     const uint32_t L0 = (1u << lv0) - 1u;
     const uint32_t L1 = ((2u << lv0) - 1u) < n ? ((2u << lv0) - 1u) : n;
-    const cudaError_t e = cudaFuncSetAttribute(k_local_finish, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)sizeof(LocalSmem));
-    if (e != cudaSuccess) return e;
-    k_local_finish<<<L1 - L0, kLocalThreads, sizeof(LocalSmem), st>>>(list, S, mn, mx, n, lv0, L0, nstart, 2 * n,
-                                                                      node_of, heap, sbox, err);
-    return cudaGetLastError();
+    q.launch(k_local_finish, dim3(L1 - L0), dim3(kLocalThreads), sizeof(LocalSmem), list, S, mn, mx, n, lv0, L0,
+             nstart, 2 * n, node_of, heap, sbox, err);
 }
 
 // Node records: pairs and slabs, then the children's subtree boxes. The
@@ -971,16 +1100,253 @@ cudaError_t finish_local(const uint32_t* list, size_t S, const float* mn, const 
 // levels above are unions, level by level from the bottom, of the pair boxes
 // (pbox, written by k_emit_nodes) and the children's subtree boxes.
 // pbox and sbox: 6 floats per node of scratch each.
-void emit_records(const float* V, uint32_t count, const uint32_t* perm, uint32_t n, uint32_t lv0, float* verts,
-                  float4* recs, float* pbox, float* sbox, cudaStream_t st) {
-    k_emit_nodes<<<cdiv(n, 128), 128, 0, st>>>(V, count, perm, n, verts, recs, pbox);
+void emit_records(Seq& q, const float* V, uint32_t count, const uint32_t* perm, uint32_t n, uint32_t lv0,
+                  float* verts, float4* recs, float* pbox, float* sbox) {
+    q.launch(k_emit_nodes, dim3(cdiv(n, 128)), dim3(128), 0, V, count, perm, n, verts, recs, pbox);
     const uint32_t Lb = (1u << lv0) - 1u;   // first node of level lv0
-    if (Lb < n) k_node_boxes<false><<<cdiv(n - Lb, 256), 256, 0, st>>>(Lb, n, n, pbox, sbox, recs);
+    if (Lb < n) q.launch(k_node_boxes<false>, dim3(cdiv(n - Lb, 256)), dim3(256), 0, Lb, n, n, pbox, sbox, recs);
     for (int lv = (int)lv0 - 1; lv >= 0; --lv) {
         const uint32_t L0 = (1u << lv) - 1u;
         const uint32_t L1 = ((2u << lv) - 1u) < n ? ((2u << lv) - 1u) : n;
-        k_node_boxes<true><<<cdiv(L1 - L0, 256), 256, 0, st>>>(L0, L1, n, pbox, sbox, recs);
+        q.launch(k_node_boxes<true>, dim3(cdiv(L1 - L0, 256)), dim3(256), 0, L0, L1, n, pbox, sbox, recs);
     }
+}
+
+constexpr size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Byte offsets of the scratch regions of a build of N (even) triangles; the
+// per-axis arrays use a stride S that keeps every axis 256-byte aligned.
+struct ScratchLayout {
+    size_t S, flags, mn, mx, keys, vals, k2, v2, nodeof, heap, pair0, best, ns, nl, nlb, tiles, hist, tot, end;
+};
+
+constexpr ScratchLayout scratch_layout(size_t N) {
+    ScratchLayout L{};
+    const size_t n = N / 2;
+    const size_t nb = (N + kSortTile - 1) / kSortTile;
+    const size_t ntiles = (N + kTile - 1) / kTile;
+    L.S = (N + 63) & ~(size_t)63;
+    size_t off = 0;
+    L.flags = off; off += round256(4);
+    L.mn = off; off += round256(3 * L.S * 4);
+    L.mx = off; off += round256(3 * L.S * 4);
+    L.keys = off; off += round256(3 * L.S * 4);
+    L.vals = off; off += round256(3 * L.S * 4);
+    L.k2 = off; off += round256(3 * L.S * 4);
+    L.v2 = off; off += round256(3 * L.S * 4);
+    L.nodeof = off; off += round256(N * 4);
+    L.heap = off; off += round256(N * 4);
+    L.pair0 = off; off += round256(n * 4);
+    L.best = off; off += round256(n * 8);
+    L.ns = off; off += round256(n * 4);
+    L.nl = off; off += round256(n * 4);
+    L.nlb = off; off += round256(n * 4);
+    L.tiles = off; off += round256(lookback_bytes(ntiles));
+    L.hist = off; off += round256(3 * 256 * nb * 4);
+    L.tot = off; off += round256(3 * 256 * 4);
+    L.end = off;
+    return L;
+}
+
+// Everything one build reads and writes.
+struct BuildArgs {
+    const float* V;
+    uint32_t count;            // input triangles; N = count rounded up to even
+    float4* recs;
+    uint32_t* perm;
+    float* verts;
+    unsigned char* scratch;    // scratch_layout(N).end bytes
+    uint32_t* flags;           // error bits 4 (internal check), 8 (non-finite vertex), 16 (look-back timeout)
+};
+
+// The whole build of a non-empty soup: bounds and keys, three radix sorts,
+// the global levels, the per-subtree finish, pair order and node records.
+void enqueue_build(Seq& q, const BuildArgs& b) {
+    const uint32_t N = b.count + (b.count & 1u);
+    const uint32_t n = N / 2;
+    const uint32_t levels = log2i(n) + 1;
+    const ScratchLayout L = scratch_layout(N);
+    const size_t S = L.S;
+    unsigned char* base = b.scratch;
+    float* mn = (float*)(base + L.mn);
+    float* mx = (float*)(base + L.mx);
+    uint32_t* keys = (uint32_t*)(base + L.keys);
+    uint32_t* vals = (uint32_t*)(base + L.vals);
+    uint32_t* k2 = (uint32_t*)(base + L.k2);
+    uint32_t* v2 = (uint32_t*)(base + L.v2);
+    uint32_t* node_of = (uint32_t*)(base + L.nodeof);
+    uint32_t* heap = (uint32_t*)(base + L.heap);
+    uint32_t* pair0 = (uint32_t*)(base + L.pair0);
+    unsigned long long* best = (unsigned long long*)(base + L.best);
+    uint32_t* ns = (uint32_t*)(base + L.ns);
+    uint32_t* nl = (uint32_t*)(base + L.nl);
+    uint32_t* nlb = (uint32_t*)(base + L.nlb);
+    unsigned long long* tiles = (unsigned long long*)(base + L.tiles);
+    uint32_t* hist = (uint32_t*)(base + L.hist);
+    uint32_t* tot = (uint32_t*)(base + L.tot);
+    const uint32_t nb = cdiv(N, kSortTile);
+    const uint32_t ntiles = cdiv(N, kTile);
+
+    q.memset(node_of, (size_t)N * 4);
+    q.memset(best, (size_t)n * 8);
+    q.launch(k_bounds, dim3(cdiv(N, 256)), dim3(256), 0, b.V, N, S, b.count, mn, mx, keys, vals, b.flags);
+    // three stable LSD radix sorts of (min-key, prim id); result in keys/vals
+    for (int pass = 0; pass < 4; ++pass) {
+        const int shift = pass * 8;
+        uint32_t* kin = (pass & 1) ? k2 : keys;
+        uint32_t* vin = (pass & 1) ? v2 : vals;
+        uint32_t* kout = (pass & 1) ? keys : k2;
+        uint32_t* vout = (pass & 1) ? vals : v2;
+        q.launch(k_radix_hist, dim3(nb, 3), dim3(kThreads), 0, kin, N, S, shift, hist, nb);
+        q.launch(k_radix_scan_rows, dim3(256, 3), dim3(1024), 0, hist, nb, tot);
+        q.launch(k_radix_scatter, dim3(nb, 3), dim3(kThreads), 0, kin, vin, kout, vout, N, S, shift, hist, tot, nb,
+                 b.flags);
+    }
+    // lists: vals = sorted pids per axis (buffer A), v2 = buffer B
+    uint32_t* listA = vals;
+    uint32_t* listB = v2;
+    q.launch(k_node_table, dim3(cdiv(n, 256)), dim3(256), 0, n, ns, nl, nlb);
+
+    // levels above lv0 over the whole soup, the rest per subtree in shared memory
+    const uint32_t lv0 = local_level(n, levels);
+    for (uint32_t lv = 0; lv < lv0; ++lv) {
+        const uint32_t L0 = (1u << lv) - 1u;
+        const uint32_t L1 = ((2u << lv) - 1u) < n ? ((2u << lv) - 1u) : n;
+        const uint32_t M = N - 2u * L0;
+        const int a = (int)(lv % 3), bx = (int)((lv + 1) % 3), c = (int)((lv + 2) % 3);
+        const uint32_t mt = cdiv(M, kTile);
+        // each node's pair: its segment's first entry and the entry of largest max-key (k_select),
+        // written to the heap (k_emit_pairs)
+        q.launch(k_select, dim3(mt), dim3(kThreads), 0, listA + a * S, M, mx + a * S, node_of, ns, L0, best, pair0);
+        q.launch(k_emit_pairs, dim3(cdiv(L1 - L0, 256)), dim3(256), 0, L0, L1, best, pair0, heap, node_of);
+        if (lv + 1 == levels) break;
+        ListSet sb;
+        sb.in[0] = listA + bx * S; sb.out[0] = listB + bx * S;
+        sb.in[1] = nullptr; sb.out[1] = nullptr;
+        ListSet sac;
+        sac.in[0] = listA + a * S; sac.out[0] = listB + a * S;
+        sac.in[1] = listA + c * S; sac.out[1] = listB + c * S;
+        split_and_partition(q, sb, sac, M, mt, ntiles, node_of, ns, nl, nlb, L0, M - 2u * (L1 - L0), tiles, b.flags);
+        uint32_t* t = listA; listA = listB; listB = t;
+    }
+    if (lv0 < levels) finish_local(q, listA, S, mn, mx, n, lv0, ns, node_of, heap, (float*)k2, b.flags);
+    const int al = (int)((levels - 1) % 3);
+    q.launch(k_pair_order, dim3(cdiv(n, 256)), dim3(256), 0, n, heap, mn + al * S, b.perm);
+    // mx and k2 are free once the levels are placed: 3*S >= 6*n floats each for the boxes
+    emit_records(q, b.V, b.count, b.perm, n, lv0, b.verts, b.recs, mx, (float*)k2);
+}
+
+// Error bits of a finished build, read back on `st`.
+aur_status build_flags(const char* who, uint32_t* d_flags, cudaStream_t st, bool clear) {
+    uint32_t flags = 0;
+    AUR_CUDA(cudaMemcpyAsync(&flags, d_flags, 4, cudaMemcpyDeviceToHost, st));
+    AUR_CUDA(cudaStreamSynchronize(st));
+    if (!(flags & (4u | 8u | 16u))) return AUR_OK;
+    if (clear) {
+        cudaMemsetAsync(d_flags, 0, 4, st);
+        cudaStreamSynchronize(st);
+    }
+    if (flags & 8u) return fail(AUR_ERR_INVALID, "%s: a vertex coordinate is NaN or infinite", who);
+    if (flags & 16u) return fail(AUR_ERR_TIMEOUT, "%s: a tile prefix wait gave up (flags 0x%x)", who, flags);
+    return fail(AUR_ERR_CUDA, "%s: internal partition check failed (flags 0x%x)", who, flags);
+}
+
+cudaError_t set_local_smem() {
+    return cudaFuncSetAttribute(k_local_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LocalSmem));
+}
+
+}  // namespace
+
+// A context's cached build: its scratch, and the launch sequence of the last
+// built size recorded as a CUDA graph. Soups of at most kGraphMaxTriangles
+// use it; larger ones (whose kernels dwarf the launch cost) launch directly
+// with stream-ordered scratch that is released after the build.
+constexpr uint32_t kGraphMaxTriangles = 1u << 24;
+
+struct BuildCache {
+    std::mutex mutex;
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    uint32_t N = 0;                        // size the graph was recorded for
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<NodeRec> nodes;
+    cudaEvent_t done = nullptr;            // recorded after each launch of the graph
+
+    void drop_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        nodes.clear();
+        N = 0;
+    }
+};
+
+void free_build_cache(aur_ctx* ctx) {
+    BuildCache* bc = ctx->build;
+    if (!bc) return;
+    if (bc->done) {
+        cudaEventSynchronize(bc->done);
+        cudaEventDestroy(bc->done);
+    }
+    bc->drop_graph();
+    cudaFree(bc->scratch);
+    delete bc;
+    ctx->build = nullptr;
+}
+
+namespace {
+
+// Runs the build through the context's cached graph: patched when the size
+// matches the recording, recorded and instantiated otherwise.
+aur_status build_with_graph(aur_ctx* ctx, const BuildArgs& a0, uint32_t N, cudaStream_t st) {
+    if (!ctx->build) ctx->build = new BuildCache();
+    BuildCache& bc = *ctx->build;
+    std::lock_guard<std::mutex> lock(bc.mutex);
+    if (!bc.done) AUR_CUDA(cudaEventCreateWithFlags(&bc.done, cudaEventDisableTiming));
+    const size_t need = scratch_layout(N).end;
+    if (bc.scratch_bytes < need) {
+        AUR_CUDA(cudaEventSynchronize(bc.done));   // the last launch may still use the old scratch
+        cudaFree(bc.scratch);
+        bc.scratch = nullptr;
+        bc.scratch_bytes = 0;
+        if (::aur::dev_malloc(&bc.scratch, need) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(AUR_ERR_OOM, "aur_nmh_build: out of device memory for %zu bytes of scratch", need);
+        }
+        bc.scratch_bytes = need;
+    }
+    BuildArgs a = a0;
+    a.scratch = (unsigned char*)bc.scratch;
+    if (bc.exec && bc.N == N) {
+        Seq q = Seq::patch(bc.exec, &bc.nodes);
+        enqueue_build(q, a);
+        if (q.finish() != cudaSuccess) {
+            cudaGetLastError();
+            bc.drop_graph();
+        }
+    } else {
+        bc.drop_graph();
+    }
+    if (!bc.exec) {
+        AUR_CUDA(set_local_smem());
+        AUR_CUDA(cudaGraphCreate(&bc.graph, 0));
+        Seq q = Seq::record(bc.graph, &bc.nodes);
+        enqueue_build(q, a);
+        cudaError_t e = q.finish();
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&bc.exec, bc.graph, 0);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            bc.drop_graph();
+            return cuda_fail(e, "aur_nmh_build (recording the build graph)", __FILE__, __LINE__);
+        }
+        bc.N = N;
+    }
+    AUR_CUDA(cudaStreamWaitEvent(st, bc.done, 0));
+    AUR_CUDA(cudaGraphLaunch(bc.exec, st));
+    AUR_CUDA(cudaEventRecord(bc.done, st));
+    return AUR_OK;
 }
 
 }  // namespace
@@ -1018,114 +1384,37 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
     nmh->verts = (float*)((char*)nmh->mem + b_recs + b_perm);
 
     cudaStream_t st = ctx->stream;
-    const uint32_t nb = cdiv(N, kSortTile);
-    const uint32_t ntiles = cdiv(N, kTile);
-    // scratch layout (4-byte words unless noted)
-    size_t off = 0;
-    auto take = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
-    // per-axis arrays use a stride S that keeps every axis 256-byte aligned
-    const size_t S = ((size_t)N + 63) & ~(size_t)63;
-    const size_t o_mn = take(3 * S * 4), o_mx = take(3 * S * 4);
-    const size_t o_keys = take(3 * S * 4), o_vals = take(3 * S * 4);
-    const size_t o_k2 = take(3 * S * 4), o_v2 = take(3 * S * 4);
-    const size_t o_nodeof = take((size_t)N * 4), o_heap = take((size_t)N * 4);
-    const size_t o_pair0 = take((size_t)n * 4), o_best = take((size_t)n * 8);
-    const size_t o_ns = take((size_t)n * 4), o_nl = take((size_t)n * 4), o_nlb = take((size_t)n * 4);
-    const size_t o_tiles = take(lookback_bytes(ntiles));
-    const size_t o_hist = take((size_t)3 * 256 * nb * 4), o_tot = take((size_t)3 * 256 * 4);
-    char* base = nullptr;
-    if (::aur::dev_malloc_async((void**)&base, off, st) != cudaSuccess) {
-        cudaGetLastError();
-        cleanup();
-        return fail(AUR_ERR_OOM, "aur_nmh_build: out of device memory for %zu bytes of scratch", off);
-    }
-    float* mn = (float*)(base + o_mn);
-    float* mx = (float*)(base + o_mx);
-    uint32_t* keys = (uint32_t*)(base + o_keys);
-    uint32_t* vals = (uint32_t*)(base + o_vals);
-    uint32_t* k2 = (uint32_t*)(base + o_k2);
-    uint32_t* v2 = (uint32_t*)(base + o_v2);
-    uint32_t* node_of = (uint32_t*)(base + o_nodeof);
-    uint32_t* heap = (uint32_t*)(base + o_heap);
-    uint32_t* pair0 = (uint32_t*)(base + o_pair0);
-    unsigned long long* best = (unsigned long long*)(base + o_best);
-    uint32_t* ns = (uint32_t*)(base + o_ns);
-    uint32_t* nl = (uint32_t*)(base + o_nl);
-    uint32_t* nlb = (uint32_t*)(base + o_nlb);
-    unsigned long long* tiles = (unsigned long long*)(base + o_tiles);
-    uint32_t* hist = (uint32_t*)(base + o_hist);
-    uint32_t* tot = (uint32_t*)(base + o_tot);
-
-    k_bounds<<<cdiv(N, 256), 256, 0, st>>>(V, N, S, count, mn, mx, keys, vals, ctx->d_flags);
-    // three stable LSD radix sorts of (min-key, prim id); result in keys/vals
-    for (int pass = 0; pass < 4; ++pass) {
-        const int shift = pass * 8;
-        uint32_t* kin = (pass & 1) ? k2 : keys;
-        uint32_t* vin = (pass & 1) ? v2 : vals;
-        uint32_t* kout = (pass & 1) ? keys : k2;
-        uint32_t* vout = (pass & 1) ? vals : v2;
-        k_radix_hist<<<dim3(nb, 3), kThreads, 0, st>>>(kin, N, S, shift, hist, nb);
-        k_radix_scan_rows<<<dim3(256, 3), 1024, 0, st>>>(hist, nb, tot);
-        k_radix_scatter<<<dim3(nb, 3), kThreads, 0, st>>>(kin, vin, kout, vout, N, S, shift, hist, tot, nb,
-                                                          ctx->d_flags);
-    }
-    // lists: vals = sorted pids per axis (buffer A), v2 = buffer B
-    uint32_t* listA = vals;
-    uint32_t* listB = v2;
-    k_node_table<<<cdiv(n, 256), 256, 0, st>>>(n, ns, nl, nlb);
-    cudaMemsetAsync(node_of, 0, (size_t)N * 4, st);
-    cudaMemsetAsync(best, 0, (size_t)n * 8, st);
-
-    // levels above lv0 over the whole soup, the rest per subtree in shared memory
-    const uint32_t lv0 = local_level(n, nmh->levels);
-    for (uint32_t lv = 0; lv < lv0; ++lv) {
-        const uint32_t L0 = (1u << lv) - 1u;
-        const uint32_t L1 = ((2u << lv) - 1u) < n ? ((2u << lv) - 1u) : n;
-        const uint32_t M = N - 2u * L0;
-        const int a = (int)(lv % 3), b = (int)((lv + 1) % 3), c = (int)((lv + 2) % 3);
-        const uint32_t mt = cdiv(M, kTile);
-        k_select<<<cdiv(M, kTile), kThreads, 0, st>>>(listA + a * S, M, mx + a * S, node_of, ns, L0, best, pair0);
-        k_emit_pairs<<<cdiv(L1 - L0, 256), 256, 0, st>>>(L0, L1, best, pair0, heap, node_of);
-        if (lv + 1 == nmh->levels) break;
-        ListSet sb;
-        sb.in[0] = listA + b * S; sb.out[0] = listB + b * S;
-        sb.in[1] = nullptr; sb.out[1] = nullptr;
-        ListSet sac;
-        sac.in[0] = listA + a * S; sac.out[0] = listB + a * S;
-        sac.in[1] = listA + c * S; sac.out[1] = listB + c * S;
-        split_and_partition(sb, sac, M, mt, ntiles, node_of, ns, nl, nlb, L0, M - 2u * (L1 - L0), tiles,
-                            ctx->d_flags, st);
-        uint32_t* t = listA; listA = listB; listB = t;
-    }
-    if (lv0 < nmh->levels) {
-        const cudaError_t le = finish_local(listA, S, mn, mx, n, lv0, ns, node_of, heap, (float*)k2, ctx->d_flags, st);
-        if (le != cudaSuccess) {
-            cudaFreeAsync(base, st);
+    BuildArgs a{V, count, nmh->node_recs, nmh->perm, nmh->verts, nullptr, ctx->d_flags};
+    if (N <= kGraphMaxTriangles) {
+        const aur_status s = build_with_graph(ctx, a, N, st);
+        if (s != AUR_OK) {
             cleanup();
-            return cuda_fail(le, "aur_nmh_build (subtree finish)", __FILE__, __LINE__);
+            return s;
+        }
+    } else {
+        const size_t need = scratch_layout(N).end;
+        if (::aur::dev_malloc_async((void**)&a.scratch, need, st) != cudaSuccess) {
+            cudaGetLastError();
+            cleanup();
+            return fail(AUR_ERR_OOM, "aur_nmh_build: out of device memory for %zu bytes of scratch", need);
+        }
+        cudaError_t e = set_local_smem();
+        if (e == cudaSuccess) {
+            Seq q = Seq::direct(st);
+            enqueue_build(q, a);
+            e = q.finish();
+        }
+        cudaFreeAsync(a.scratch, st);
+        if (e != cudaSuccess) {
+            cleanup();
+            return cuda_fail(e, "aur_nmh_build kernels", __FILE__, __LINE__);
         }
     }
-    const int al = (int)((nmh->levels - 1) % 3);
-    k_pair_order<<<cdiv(n, 256), 256, 0, st>>>(n, heap, mn + al * S, nmh->perm);
-    // mx and k2 are free once the levels are placed: 3*S >= 6*n floats each for the boxes
-    emit_records(V, count, nmh->perm, n, lv0, nmh->verts, nmh->node_recs, mx, (float*)k2, st);
-    cudaFreeAsync(base, st);
-    cudaError_t e = cudaGetLastError();
-    uint32_t flags = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&flags, ctx->d_flags, 4, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) {
+    const aur_status s = build_flags("aur_nmh_build", ctx->d_flags, st, true);
+    if (s != AUR_OK) {
+        cudaGetLastError();
         cleanup();
-        return cuda_fail(e, "aur_nmh_build kernels", __FILE__, __LINE__);
-    }
-    if (flags & (4u | 8u | 16u)) {
-        cudaMemsetAsync(ctx->d_flags, 0, 4, st);
-        cudaStreamSynchronize(st);
-        cleanup();
-        if (flags & 8u)
-            return fail(AUR_ERR_INVALID, "aur_nmh_build: a vertex coordinate is NaN or infinite");
-        if (flags & 16u) return fail(AUR_ERR_TIMEOUT, "aur_nmh_build: a tile prefix wait gave up (flags 0x%x)", flags);
-        return fail(AUR_ERR_CUDA, "aur_nmh_build: internal partition check failed (flags 0x%x)", flags);
+        return s;
     }
     *out = nmh;
     return AUR_OK;
@@ -1146,44 +1435,7 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
 namespace {
 
 constexpr uint32_t kNoAllocMaxTriangles = 1u << 16;
-
-constexpr size_t na_round(size_t b) { return (b + 255) & ~(size_t)255; }
-
-// Byte offsets of the scratch regions for N (even) triangles; the same
-// regions as aur_nmh_build's stream-ordered scratch, plus the error flag word.
-struct NoAllocLayout {
-    size_t S, flags, mn, mx, keys, vals, k2, v2, nodeof, heap, pair0, best, ns, nl, nlb, tiles, hist, tot, end;
-};
-
-constexpr NoAllocLayout noalloc_layout(size_t N) {
-    NoAllocLayout L{};
-    const size_t n = N / 2;
-    const size_t nb = (N + kSortTile - 1) / kSortTile;
-    const size_t ntiles = (N + kTile - 1) / kTile;
-    L.S = (N + 63) & ~(size_t)63;
-    size_t off = 0;
-    L.flags = off; off += na_round(4);
-    L.mn = off; off += na_round(3 * L.S * 4);
-    L.mx = off; off += na_round(3 * L.S * 4);
-    L.keys = off; off += na_round(3 * L.S * 4);
-    L.vals = off; off += na_round(3 * L.S * 4);
-    L.k2 = off; off += na_round(3 * L.S * 4);
-    L.v2 = off; off += na_round(3 * L.S * 4);
-    L.nodeof = off; off += na_round(N * 4);
-    L.heap = off; off += na_round(N * 4);
-    L.pair0 = off; off += na_round(n * 4);
-    L.best = off; off += na_round(n * 8);
-    L.ns = off; off += na_round(n * 4);
-    L.nl = off; off += na_round(n * 4);
-    L.nlb = off; off += na_round(n * 4);
-    L.tiles = off; off += na_round(lookback_bytes(ntiles));
-    L.hist = off; off += na_round(3 * 256 * nb * 4);
-    L.tot = off; off += na_round(3 * 256 * 4);
-    L.end = off;
-    return L;
-}
-
-constexpr size_t kNoAllocScratchBytes = noalloc_layout(kNoAllocMaxTriangles).end;
+constexpr size_t kNoAllocScratchBytes = scratch_layout(kNoAllocMaxTriangles).end;
 
 // Shared by every call on a device; see aur_nmh_build_noalloc.
 static __device__ __align__(256) unsigned char g_nmh_scratch[kNoAllocScratchBytes];
@@ -1227,80 +1479,15 @@ aur_status nmh_build_noalloc_impl(const float* V, uint32_t count, cudaStream_t s
     unsigned char* base = nullptr;
     aur_status stt = noalloc_scratch(device, &base);
     if (stt != AUR_OK) return stt;
-
-    const NoAllocLayout L = noalloc_layout(N);
-    const size_t S = L.S;
-    uint32_t* flags = (uint32_t*)(base + L.flags);
-    float* mn = (float*)(base + L.mn);
-    float* mx = (float*)(base + L.mx);
-    uint32_t* keys = (uint32_t*)(base + L.keys);
-    uint32_t* vals = (uint32_t*)(base + L.vals);
-    uint32_t* k2 = (uint32_t*)(base + L.k2);
-    uint32_t* v2 = (uint32_t*)(base + L.v2);
-    uint32_t* node_of = (uint32_t*)(base + L.nodeof);
-    uint32_t* heap = (uint32_t*)(base + L.heap);
-    uint32_t* pair0 = (uint32_t*)(base + L.pair0);
-    unsigned long long* best = (unsigned long long*)(base + L.best);
-    uint32_t* ns = (uint32_t*)(base + L.ns);
-    uint32_t* nl = (uint32_t*)(base + L.nl);
-    uint32_t* nlb = (uint32_t*)(base + L.nlb);
-    unsigned long long* tiles = (unsigned long long*)(base + L.tiles);
-    uint32_t* hist = (uint32_t*)(base + L.hist);
-    uint32_t* tot = (uint32_t*)(base + L.tot);
-    const uint32_t nb = cdiv(N, kSortTile);
-    const uint32_t ntiles = cdiv(N, kTile);
-
-    // The array keeps the previous call's contents: clear what must start at zero.
+    uint32_t* flags = (uint32_t*)(base + scratch_layout(N).flags);
+    // The array keeps the previous call's contents: the flags must start at
+    // zero (enqueue_build clears the rest that must).
     AUR_CUDA(cudaMemsetAsync(flags, 0, 4, st));
-    AUR_CUDA(cudaMemsetAsync(node_of, 0, (size_t)N * 4, st));
-    AUR_CUDA(cudaMemsetAsync(best, 0, (size_t)n * 8, st));
-    k_bounds<<<cdiv(N, 256), 256, 0, st>>>(V, N, S, count, mn, mx, keys, vals, flags);
-    for (int pass = 0; pass < 4; ++pass) {
-        const int shift = pass * 8;
-        uint32_t* kin = (pass & 1) ? k2 : keys;
-        uint32_t* vin = (pass & 1) ? v2 : vals;
-        uint32_t* kout = (pass & 1) ? keys : k2;
-        uint32_t* vout = (pass & 1) ? vals : v2;
-        k_radix_hist<<<dim3(nb, 3), kThreads, 0, st>>>(kin, N, S, shift, hist, nb);
-        k_radix_scan_rows<<<dim3(256, 3), 1024, 0, st>>>(hist, nb, tot);
-        k_radix_scatter<<<dim3(nb, 3), kThreads, 0, st>>>(kin, vin, kout, vout, N, S, shift, hist, tot, nb, flags);
-    }
-    uint32_t* listA = vals;
-    uint32_t* listB = v2;
-    k_node_table<<<cdiv(n, 256), 256, 0, st>>>(n, ns, nl, nlb);
-    const uint32_t lv0 = local_level(n, levels);
-    for (uint32_t lv = 0; lv < lv0; ++lv) {
-        const uint32_t L0 = (1u << lv) - 1u;
-        const uint32_t L1 = ((2u << lv) - 1u) < n ? ((2u << lv) - 1u) : n;
-        const uint32_t M = N - 2u * L0;
-        const int a = (int)(lv % 3), b = (int)((lv + 1) % 3), c = (int)((lv + 2) % 3);
-        const uint32_t mt = cdiv(M, kTile);
-        k_select<<<mt, kThreads, 0, st>>>(listA + a * S, M, mx + a * S, node_of, ns, L0, best, pair0);
-        k_emit_pairs<<<cdiv(L1 - L0, 256), 256, 0, st>>>(L0, L1, best, pair0, heap, node_of);
-        if (lv + 1 == levels) break;
-        ListSet sb;
-        sb.in[0] = listA + b * S; sb.out[0] = listB + b * S;
-        sb.in[1] = nullptr; sb.out[1] = nullptr;
-        ListSet sac;
-        sac.in[0] = listA + a * S; sac.out[0] = listB + a * S;
-        sac.in[1] = listA + c * S; sac.out[1] = listB + c * S;
-        split_and_partition(sb, sac, M, mt, ntiles, node_of, ns, nl, nlb, L0, M - 2u * (L1 - L0), tiles, flags, st);
-        uint32_t* t = listA; listA = listB; listB = t;
-    }
-    if (lv0 < levels) AUR_CUDA(finish_local(listA, S, mn, mx, n, lv0, ns, node_of, heap, (float*)k2, flags, st));
-    const int al = (int)((levels - 1) % 3);
-    k_pair_order<<<cdiv(n, 256), 256, 0, st>>>(n, heap, mn + al * S, perm);
-    emit_records(V, count, perm, n, lv0, verts, recs, mx, (float*)k2, st);
-    AUR_CUDA(cudaGetLastError());
-    uint32_t h_flags = 0;
-    AUR_CUDA(cudaMemcpyAsync(&h_flags, flags, 4, cudaMemcpyDeviceToHost, st));
-    AUR_CUDA(cudaStreamSynchronize(st));
-    AUR_CHECK(!(h_flags & 8u), AUR_ERR_INVALID, "aur_nmh_build_noalloc: a vertex coordinate is NaN or infinite");
-    AUR_CHECK(!(h_flags & 16u), AUR_ERR_TIMEOUT, "aur_nmh_build_noalloc: a tile prefix wait gave up (flags 0x%x)",
-              h_flags);
-    AUR_CHECK(!(h_flags & 4u), AUR_ERR_CUDA, "aur_nmh_build_noalloc: internal partition check failed (flags 0x%x)",
-              h_flags);
-    return AUR_OK;
+    AUR_CUDA(set_local_smem());
+    Seq q = Seq::direct(st);
+    enqueue_build(q, BuildArgs{V, count, recs, perm, verts, base, flags});
+    AUR_CUDA(q.finish());
+    return build_flags("aur_nmh_build_noalloc", flags, st, false);
 }
 
 }  // namespace aur

@@ -53,10 +53,16 @@ def test_nmh_build_and_trace(ctx):
     rays = scenes.microbench_rays(1 << 15, seed=3)
 
     def op():
-        nmh = api.Nmh(ctx, Vd, count=V.shape[0])
-        hits = api.hits_to_numpy(api.trace_closest(ctx, nmh, api.rays_tensor(rays)))
-        return [nmh.export()[0], hits.view(np.uint32), np.array(api.count_visits(ctx, nmh, api.rays_tensor(rays)))]
-    assert _sweep(op) >= 3          # NMH arrays, build scratch, trace counters
+        fresh = api.Context(0)      # a fresh context allocates the build's scratch again
+        try:
+            nmh = api.Nmh(fresh, Vd, count=V.shape[0])
+            again = api.Nmh(fresh, Vd, count=V.shape[0])       # the same size: the recorded build graph
+            hits = api.hits_to_numpy(api.trace_closest(fresh, nmh, api.rays_tensor(rays)))
+            return [nmh.export()[0], again.export()[0], hits.view(np.uint32),
+                    np.array(api.count_visits(fresh, nmh, api.rays_tensor(rays)))]
+        finally:
+            fresh.close()
+    assert _sweep(op) >= 5          # context flags, NMH arrays, build scratch, second NMH, trace counters
 
 
 def test_scene_textures_render_emitters_adjoint(ctx):

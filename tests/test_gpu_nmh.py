@@ -37,6 +37,63 @@ def test_build_with_key_ties(ctx, maker):
     assert np.array_equal(perm, oracle.nmh_build(sd.vertices)[0])
 
 
+@pytest.mark.parametrize("n", [4097, 100001])
+def test_build_of_identical_triangles(ctx, n):
+    """Every key tied on every axis: the order comes from the prim ids alone,
+    through the global levels and the per-subtree finish."""
+    V = np.tile(scenes.random_soup(1, seed=5), (n, 1))
+    _, perm, _, _ = _gpu_build(ctx, V)
+    assert np.array_equal(perm, oracle.nmh_build(V)[0])
+
+
+def _subtree_extremes(verts, levels):
+    """Per node: the pair's min of the triangles' minima and max of their
+    maxima on each axis, and the same over the node's whole subtree
+    (bottom-up, one vectorised pass per level)."""
+    mn = np.stack([verts[:, 3 * a:3 * a + 3].min(1) for a in range(3)], 1)
+    mx = np.stack([verts[:, 3 * a:3 * a + 3].max(1) for a in range(3)], 1)
+    pmn, pmx = np.minimum(mn[0::2], mn[1::2]), np.maximum(mx[0::2], mx[1::2])
+    n = pmn.shape[0]
+    smn, smx = pmn.copy(), pmx.copy()
+    for lv in range(levels - 2, -1, -1):
+        k = np.arange((1 << lv) - 1, min((2 << lv) - 1, n))
+        for c in (2 * k + 1, 2 * k + 2):
+            ok = c < n
+            smn[k[ok]] = np.minimum(smn[k[ok]], smn[c[ok]])
+            smx[k[ok]] = np.maximum(smx[k[ok]], smx[c[ok]])
+    return pmn, pmx, smn, smx
+
+
+def test_build_and_trace_beyond_the_largest_workload(ctx):
+    """2^24 + 3 triangles, twice the 8.4M-triangle terrain (the oracle's build
+    would take minutes here, so the tree is checked by its properties): the
+    NMH-ordered soup is the padded input gathered by a permutation; every
+    node's pair holds the extremes of its subtree on the node's axis (the
+    property that makes the pair's slab a bound of the subtree, over all 24
+    levels); and closest and any hits of 2^13 microbench rays equal the
+    oracle's traversal of the exported tree bit for bit."""
+    V = scenes.random_soup((1 << 24) + 3, seed=24)
+    nmh, perm, verts, levels = _gpu_build(ctx, V)
+    N = V.shape[0] + 1
+    n = N // 2
+    assert perm.size == N and levels == n.bit_length()
+    assert np.array_equal(np.bincount(perm, minlength=N), np.ones(N, np.int64))
+    assert np.array_equal(verts, oracle.pad_even(V)[perm])
+    pmn, pmx, smn, smx = _subtree_extremes(verts, levels)
+    axis = np.zeros(n, np.int64)
+    for lv in range(levels):
+        axis[(1 << lv) - 1:min((2 << lv) - 1, n)] = lv % 3
+    k = np.arange(n)
+    assert np.array_equal(pmn[k, axis], smn[k, axis]) and np.array_equal(pmx[k, axis], smx[k, axis])
+    rays = scenes.microbench_rays(1 << 13, seed=25)
+    hits = api.hits_to_numpy(api.trace_closest(ctx, nmh, api.rays_tensor(rays)))
+    ohits, _, _ = oracle.trace_closest(verts, perm, rays)
+    assert np.array_equal(hits.view(np.uint32), ohits.view(np.uint32))
+    assert (ohits["prim"] != 0xFFFFFFFF).mean() > 0.3
+    occ = api.trace_any(ctx, nmh, api.rays_tensor(rays)).cpu().numpy().view(np.uint32)
+    assert np.array_equal(occ, oracle.trace_any(verts, perm, rays)[0])
+
+
 @pytest.mark.parametrize("name", ["soup2048", "cornell"])
 def test_build_matches_golden(ctx, name):
     g = load_golden(name)
@@ -51,6 +108,20 @@ def test_build_is_deterministic(ctx):
     _, p2, _, _ = _gpu_build(ctx, V)
     assert np.array_equal(p1, p2)
     assert np.array_equal(p1, oracle.nmh_build(V)[0])
+
+
+def test_build_graph_reuse(ctx):
+    """Builds of one size after the first replay the context's recorded
+    launch graph with the new vertex and output buffers patched in: soups
+    of the same size from other buffers, and a size in between, each equal
+    the oracle's tree."""
+    Va, Vb = scenes.random_soup(30001, seed=31), scenes.random_soup(30001, seed=32)
+    Vc = scenes.random_soup(777, seed=33)
+    want = {k: oracle.nmh_build(V)[0] for k, V in (("a", Va), ("b", Vb), ("c", Vc))}
+    for k, V in (("a", Va), ("b", Vb), ("a", Va), ("c", Vc), ("b", Vb)):
+        _, perm, verts, _ = _gpu_build(ctx, V)
+        assert np.array_equal(perm, want[k]), k
+        assert np.array_equal(verts, oracle.gather9(oracle.pad_even(V), want[k])), k
 
 
 def test_empty_build(ctx):
