@@ -1257,30 +1257,44 @@ cudaError_t set_local_smem() {
 
 }  // namespace
 
-// A context's cached build: its scratch, and the launch sequence of the last
-// built size recorded as a CUDA graph. Soups of at most kGraphMaxTriangles
-// use it; larger ones (whose kernels dwarf the launch cost) launch directly
+// A context's cached build: its scratch, and the launch sequences of up to
+// kCachedGraphs sizes recorded as CUDA graphs. The first build of a size
+// launches directly; a size built again (as when cudaRebuildNMH runs every
+// frame) is recorded, and later builds of it launch the graph with the
+// changed arguments patched in. Soups of at most kGraphMaxTriangles use the
+// cache; larger ones (whose kernels dwarf the launch cost) launch directly
 // with stream-ordered scratch that is released after the build.
 constexpr uint32_t kGraphMaxTriangles = 1u << 24;
+constexpr int kCachedGraphs = 4;
+constexpr int kSeenSizes = 8;
 
-struct BuildCache {
-    std::mutex mutex;
-    void* scratch = nullptr;
-    size_t scratch_bytes = 0;
+struct BuildGraph {
     uint32_t N = 0;                        // size the graph was recorded for
+    uint64_t used = 0;                     // last use, for eviction
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::vector<NodeRec> nodes;
-    cudaEvent_t done = nullptr;            // recorded after each launch of the graph
 
-    void drop_graph() {
+    void drop() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         exec = nullptr;
         graph = nullptr;
         nodes.clear();
         N = 0;
+        used = 0;
     }
+};
+
+struct BuildCache {
+    std::mutex mutex;
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    BuildGraph graphs[kCachedGraphs];
+    uint32_t seen[kSeenSizes] = {};        // sizes built directly, most recent last written
+    int seen_next = 0;
+    uint64_t clock = 0;
+    cudaEvent_t done = nullptr;            // recorded after each build launched from the cache
 };
 
 void free_build_cache(aur_ctx* ctx) {
@@ -1290,7 +1304,7 @@ void free_build_cache(aur_ctx* ctx) {
         cudaEventSynchronize(bc->done);
         cudaEventDestroy(bc->done);
     }
-    bc->drop_graph();
+    for (BuildGraph& g : bc->graphs) g.drop();
     cudaFree(bc->scratch);
     delete bc;
     ctx->build = nullptr;
@@ -1298,16 +1312,17 @@ void free_build_cache(aur_ctx* ctx) {
 
 namespace {
 
-// Runs the build through the context's cached graph: patched when the size
-// matches the recording, recorded and instantiated otherwise.
-aur_status build_with_graph(aur_ctx* ctx, const BuildArgs& a0, uint32_t N, cudaStream_t st) {
+// Runs the build from the context's cache: the recorded graph of this size,
+// patched; or a new recording, when the size was built before; or direct
+// launches on the cached scratch.
+aur_status build_cached(aur_ctx* ctx, const BuildArgs& a0, uint32_t N, cudaStream_t st) {
     if (!ctx->build) ctx->build = new BuildCache();
     BuildCache& bc = *ctx->build;
     std::lock_guard<std::mutex> lock(bc.mutex);
     if (!bc.done) AUR_CUDA(cudaEventCreateWithFlags(&bc.done, cudaEventDisableTiming));
     const size_t need = scratch_layout(N).end;
     if (bc.scratch_bytes < need) {
-        AUR_CUDA(cudaEventSynchronize(bc.done));   // the last launch may still use the old scratch
+        AUR_CUDA(cudaEventSynchronize(bc.done));   // the last build may still use the old scratch
         cudaFree(bc.scratch);
         bc.scratch = nullptr;
         bc.scratch_bytes = 0;
@@ -1319,32 +1334,51 @@ aur_status build_with_graph(aur_ctx* ctx, const BuildArgs& a0, uint32_t N, cudaS
     }
     BuildArgs a = a0;
     a.scratch = (unsigned char*)bc.scratch;
-    if (bc.exec && bc.N == N) {
-        Seq q = Seq::patch(bc.exec, &bc.nodes);
+    AUR_CUDA(cudaStreamWaitEvent(st, bc.done, 0));
+    AUR_CUDA(set_local_smem());
+    BuildGraph* g = nullptr;
+    for (BuildGraph& c : bc.graphs)
+        if (c.exec && c.N == N) g = &c;
+    if (g) {
+        Seq q = Seq::patch(g->exec, &g->nodes);
         enqueue_build(q, a);
         if (q.finish() != cudaSuccess) {
             cudaGetLastError();
-            bc.drop_graph();
+            g->drop();
+            g = nullptr;
         }
     } else {
-        bc.drop_graph();
+        bool seen = false;
+        for (uint32_t x : bc.seen) seen = seen || x == N;
+        if (!seen) {
+            bc.seen[bc.seen_next] = N;
+            bc.seen_next = (bc.seen_next + 1) % kSeenSizes;
+            Seq q = Seq::direct(st);
+            enqueue_build(q, a);
+            AUR_CUDA(q.finish());
+            AUR_CUDA(cudaEventRecord(bc.done, st));
+            return AUR_OK;
+        }
     }
-    if (!bc.exec) {
-        AUR_CUDA(set_local_smem());
-        AUR_CUDA(cudaGraphCreate(&bc.graph, 0));
-        Seq q = Seq::record(bc.graph, &bc.nodes);
+    if (!g) {
+        g = &bc.graphs[0];
+        for (BuildGraph& c : bc.graphs)
+            if (c.used < g->used) g = &c;
+        g->drop();
+        AUR_CUDA(cudaGraphCreate(&g->graph, 0));
+        Seq q = Seq::record(g->graph, &g->nodes);
         enqueue_build(q, a);
         cudaError_t e = q.finish();
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&bc.exec, bc.graph, 0);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
         if (e != cudaSuccess) {
             cudaGetLastError();
-            bc.drop_graph();
+            g->drop();
             return cuda_fail(e, "aur_nmh_build (recording the build graph)", __FILE__, __LINE__);
         }
-        bc.N = N;
+        g->N = N;
     }
-    AUR_CUDA(cudaStreamWaitEvent(st, bc.done, 0));
-    AUR_CUDA(cudaGraphLaunch(bc.exec, st));
+    g->used = ++bc.clock;
+    AUR_CUDA(cudaGraphLaunch(g->exec, st));
     AUR_CUDA(cudaEventRecord(bc.done, st));
     return AUR_OK;
 }
@@ -1386,7 +1420,7 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
     cudaStream_t st = ctx->stream;
     BuildArgs a{V, count, nmh->node_recs, nmh->perm, nmh->verts, nullptr, ctx->d_flags};
     if (N <= kGraphMaxTriangles) {
-        const aur_status s = build_with_graph(ctx, a, N, st);
+        const aur_status s = build_cached(ctx, a, N, st);
         if (s != AUR_OK) {
             cleanup();
             return s;

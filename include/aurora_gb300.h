@@ -220,14 +220,14 @@ typedef struct aur_nmh aur_nmh;
  * order for NaN).
  * Soups of at most 2^24 triangles (after padding) run from a per-context
  * cache: the build's scratch (about 92 bytes per triangle, kept until the
- * context is destroyed and grown when a larger soup comes) and its launch
- * sequence recorded as one CUDA graph for the last size built. The next
- * build of that size launches the graph with the new vertex and output
- * pointers written into it, which is how cudaRebuildNMH is called per frame;
- * another size records a new graph. Larger soups launch directly with
- * stream-ordered scratch that is released after the build. Builds on one
- * context are serialized on the GPU (each call also waits for its own
- * build before returning). */
+ * context is destroyed and grown when a larger soup comes) and, for up to
+ * four sizes, the launch sequence recorded as one CUDA graph. The first
+ * build of a size launches directly; the second records the graph; later
+ * ones launch it with the new vertex and output pointers written into it
+ * (cudaRebuildNMH runs every frame on the same geometry). Larger soups launch
+ * directly with stream-ordered scratch that is released after the build.
+ * Builds on one context are serialized on the GPU (each call also waits for
+ * its own build before returning). */
 aur_status aur_nmh_build(aur_ctx* ctx, const float* vertices, uint32_t count, aur_nmh** out);
 aur_status aur_nmh_destroy(aur_nmh* nmh);
 /* Triangle count after padding and number of heap levels (log2i(count/2)+1). */

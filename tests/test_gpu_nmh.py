@@ -111,14 +111,20 @@ def test_build_is_deterministic(ctx):
 
 
 def test_build_graph_reuse(ctx):
-    """Builds of one size after the first replay the context's recorded
-    launch graph with the new vertex and output buffers patched in: soups
-    of the same size from other buffers, and a size in between, each equal
-    the oracle's tree."""
-    Va, Vb = scenes.random_soup(30001, seed=31), scenes.random_soup(30001, seed=32)
-    Vc = scenes.random_soup(777, seed=33)
-    want = {k: oracle.nmh_build(V)[0] for k, V in (("a", Va), ("b", Vb), ("c", Vc))}
-    for k, V in (("a", Va), ("b", Vb), ("a", Va), ("c", Vc), ("b", Vb)):
+    """The context's build cache: the first build of a size launches
+    directly, the second records the size's launch graph, later ones replay
+    it with the new vertex and output buffers patched in; up to four sizes
+    keep a graph. Every build, through each of the three ways and across
+    evictions, equals the oracle's tree."""
+    soups = {("a", 30001): scenes.random_soup(30001, seed=31), ("b", 30001): scenes.random_soup(30001, seed=32)}
+    for i, n in enumerate((777, 1500, 2049, 4100, 9001)):
+        soups[("s", n)] = scenes.random_soup(n, seed=40 + i)
+    want = {k: oracle.nmh_build(V)[0] for k, V in soups.items()}
+    order = [("a", 30001), ("b", 30001), ("a", 30001), ("s", 777), ("b", 30001)]
+    sizes = [("s", n) for n in (777, 1500, 2049, 4100, 9001)]
+    order += sizes + sizes + sizes[:2] + [("a", 30001)]
+    for k in order:
+        V = soups[k]
         _, perm, verts, _ = _gpu_build(ctx, V)
         assert np.array_equal(perm, want[k]), k
         assert np.array_equal(verts, oracle.gather9(oracle.pad_even(V), want[k])), k
