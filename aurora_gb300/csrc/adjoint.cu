@@ -100,7 +100,7 @@ __device__ __forceinline__ f3 direct_grad(const SceneView& sc, const aur_shader*
                 }
             }
         } else if (kMis) {
-            // area_light_mis, both strategies
+            // both strategies of every sample, as in direct_light_mis
             f3 acc = mk3(0.0f), accp = mk3(0.0f), accl = mk3(0.0f);
             const AreaLightMis q = area_light_setup(L, f);
             if (q.active) {
@@ -163,7 +163,7 @@ __device__ __forceinline__ f3 direct_grad(const SceneView& sc, const aur_shader*
             atomicAdd(d_light + 3 * i + 2, gl.z);
         }
     }
-    if (kMis) {   // the emitter sample (emitter_sample)
+    if (kMis) {   // the emitter sample (direct_light_mis)
         const ShadowSample ss =
             emitter_shadow_sample(sc, b, f, position, wo, bounce, seed, scene, pixel, sample, rix);
         float du = 0.0f, dv = 0.0f, tt = ss.tmax;

@@ -391,33 +391,6 @@ __device__ __forceinline__ ShadowSample area_bsdf_sample(const AreaLightMis& q, 
     return s;
 }
 
-// One area light, both strategies, averaged over its samples.
-__device__ __forceinline__ f3 area_light_mis(const SceneView& sc, const aur_light& L, uint32_t li, const Bsdf& b,
-                                             const f3& position, const f3& wo, uint32_t seed, uint32_t scene,
-                                             uint32_t pixel, uint32_t sample, uint32_t rix, const StackRef& stk,
-                                             uint32_t& visits, uint32_t* err) {
-    const f3 f = bsdf_f(b);
-    const AreaLightMis q = area_light_setup(L, f);
-    f3 acc = mk3(0.0f);
-    if (q.active) {
-        for (int32_t j = 0; j < L.samples; ++j) {
-            f3 Ls = mk3(0.0f);
-            float du = 0.0f, dv = 0.0f;
-            ShadowSample s = area_light_sample(q, li, (uint32_t)j, b, f, position, wo, seed, scene, pixel, sample, rix);
-            if (s.cand && traverse<true>(sc.recs, sc.nodes, sc.perm, s.o, s.d, s.tmax, du, dv, stk, visits, err) ==
-                              kNoPrim)
-                Ls = Ls + s.c;
-            s = area_bsdf_sample(q, li, (uint32_t)j, b, f, position, wo, seed, scene, pixel, sample, rix);
-            if (s.cand && traverse<true>(sc.recs, sc.nodes, sc.perm, s.o, s.d, s.tmax, du, dv, stk, visits, err) ==
-                              kNoPrim)
-                Ls = Ls + s.c;
-            acc = acc + Ls;
-        }
-    }
-    const float ns = (float)L.samples;
-    return mk3(acc.x / ns, acc.y / ns, acc.z / ns);
-}
-
 // One emitter sample up to its shadow ray: a table entry by its CDF, a
 // uniform point on the triangle (square-root parameterisation); the shadow
 // ray stops short of the emitter.
@@ -464,27 +437,104 @@ __device__ __forceinline__ ShadowSample emitter_shadow_sample(const SceneView& s
     return s;
 }
 
-__device__ __forceinline__ f3 emitter_sample(const SceneView& sc, const Bsdf& b, const f3& position, const f3& wo,
-                                             bool bounce, uint32_t seed, uint32_t scene, uint32_t pixel,
-                                             uint32_t sample, uint32_t rix, const StackRef& stk, uint32_t& visits,
-                                             uint32_t* err) {
-    ShadowSample s = emitter_shadow_sample(sc, b, bsdf_f(b), position, wo, bounce, seed, scene, pixel, sample, rix);
-    float du = 0.0f, dv = 0.0f;
-    if (!s.cand || traverse<true>(sc.recs, sc.nodes, sc.perm, s.o, s.d, s.tmax, du, dv, stk, visits, err) != kNoPrim)
-        return mk3(0.0f);
-    return s.c;
+// Li at a hit in the MIS mode: emission weighted by ew; ambient and delta
+// lights as in the reference; each area light by both strategies
+// (area_light_sample, area_bsdf_sample), the two summed per sample and the
+// samples averaged; then one emitter sample, whose term is always added.
+// Every shadow ray of the hit (a delta light's, the two of each area-light
+// sample, the emitter's) is traced at one call site: the loop walks light
+// i, sample j and the strategy, so the kernel holds one inlined copy of the
+// any-hit traversal for all of them instead of four.
+__device__ __forceinline__ f3 direct_light_mis(const SceneView& sc, const aur_shader* sh, const Bsdf& b,
+                                               const f3& position, const f3& wo, float ew, bool bounce,
+                                               uint32_t seed, uint32_t scene, uint32_t pixel, uint32_t sample,
+                                               uint32_t rix, const StackRef& stk, uint32_t& visits, uint32_t* err) {
+    f3 Li = from(sh->emission_color) * ew;
+    const f3 f = bsdf_f(b);
+    const uint32_t nl = sc.num_lights;
+    uint32_t i = 0;             // light; nl: the emitter sample; nl + 1: done
+    int32_t j = 0;              // area-light sample
+    bool second = false;        // the BSDF strategy of sample j is next
+    f3 acc = mk3(0.0f), Ls = mk3(0.0f);
+    while (i <= nl) {
+        ShadowSample s;
+        s.cand = false;
+        s.c = mk3(0.0f);
+        bool to_ls = false;     // a visible sample adds to Ls (area light) or to Li
+        bool emitter = false;
+        if (i < nl) {
+            const aur_light& L = sc.lights[i];
+            if (L.type != AUR_LIGHT_AREA) {
+                if (L.type == AUR_LIGHT_AMBIENT) Li = Li + f * ((from(L.color) * L.intensity) * L.ambient);
+                // estimateDirectRadianceDelta (radiance.cuh:18-33): no offset
+                f3 wdir;
+                float wt, pdf;
+                const f3 Ld = sample_light(L, position, seed, scene, pixel, sample, rix, 0u, wdir, wt, pdf);
+                if (pdf > 0.0f && !zero(Ld) && !zero(f)) {
+                    s.c = f * Ld * fmaxf(0.0f, dot(wdir, b.N));
+                    s.o = position;
+                    s.d = wdir;
+                    s.tmax = wt;
+                    s.cand = true;
+                }
+                ++i;
+            } else {
+                const AreaLightMis q = area_light_setup(L, f);   // recomputed: nothing held across the trace
+                if (q.active && j < L.samples) {
+                    if (!second) {
+                        Ls = mk3(0.0f);
+                        s = area_light_sample(q, i, (uint32_t)j, b, f, position, wo, seed, scene, pixel, sample, rix);
+                    } else {
+                        s = area_bsdf_sample(q, i, (uint32_t)j, b, f, position, wo, seed, scene, pixel, sample, rix);
+                    }
+                    to_ls = true;
+                } else {
+                    const float ns = (float)L.samples;
+                    Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
+                    acc = mk3(0.0f);
+                    j = 0;
+                    ++i;
+                    continue;
+                }
+            }
+        } else {
+            s = emitter_shadow_sample(sc, b, f, position, wo, bounce, seed, scene, pixel, sample, rix);
+            emitter = true;
+            ++i;
+        }
+        float du = 0.0f, dv = 0.0f;
+        const bool vis =
+            s.cand && traverse<true>(sc.recs, sc.nodes, sc.perm, s.o, s.d, s.tmax, du, dv, stk, visits, err) == kNoPrim;
+        if (to_ls) {
+            if (vis) Ls = Ls + s.c;
+        } else if (emitter) {
+            Li = Li + (vis ? s.c : mk3(0.0f));   // the emitter sample is always added, zero when unseen
+        } else if (vis) {
+            Li = Li + s.c;
+        }
+        if (to_ls) {
+            if (second) {
+                acc = acc + Ls;
+                ++j;
+            }
+            second = !second;
+        }
+    }
+    return Li;
 }
 
 // Li at a hit: emission + ambient + direct light of every light, in the
 // reference's order (monteCarloRaytracer.cu:42-52, radiance.cuh:13-80).
-// kMis: emission weighted by ew, area lights by area_light_mis, plus one
-// emitter sample; `bounce` says whether a diffuse bounce follows this hit.
+// kMis: direct_light_mis; `bounce` says whether a diffuse bounce follows
+// this hit.
 template <bool kMis>
 __device__ __forceinline__ f3 direct_light(const SceneView& sc, const aur_shader* sh, const Bsdf& b, const f3& position,
                                            const f3& wo, float ew, bool bounce, uint32_t seed, uint32_t scene,
                                            uint32_t pixel, uint32_t sample, uint32_t rix, const StackRef& stk,
                                            uint32_t& visits, uint32_t* err) {
-    f3 Li = kMis ? from(sh->emission_color) * ew : from(sh->emission_color);
+    if constexpr (kMis)
+        return direct_light_mis(sc, sh, b, position, wo, ew, bounce, seed, scene, pixel, sample, rix, stk, visits, err);
+    f3 Li = from(sh->emission_color);
     for (uint32_t i = 0; i < sc.num_lights; ++i) {
         const aur_light& L = sc.lights[i];
         if (L.type == AUR_LIGHT_AMBIENT) Li = Li + bsdf_f(b) * ((from(L.color) * L.intensity) * L.ambient);
@@ -499,8 +549,6 @@ __device__ __forceinline__ f3 direct_light(const SceneView& sc, const aur_shader
                     traverse<true>(sc.recs, sc.nodes, sc.perm, position, wdir, wt, du, dv, stk, visits, err) == kNoPrim)
                     Li = Li + f * Ls * fmaxf(0.0f, dot(wdir, b.N));
             }
-        } else if (kMis) {
-            Li = Li + area_light_mis(sc, L, i, b, position, wo, seed, scene, pixel, sample, rix, stk, visits, err);
         } else {
             // estimateDirectRadiance (radiance.cuh:35-80), light-sampling half
             f3 acc = mk3(0.0f);
@@ -528,7 +576,6 @@ __device__ __forceinline__ f3 direct_light(const SceneView& sc, const aur_shader
             Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
         }
     }
-    if (kMis) Li = Li + emitter_sample(sc, b, position, wo, bounce, seed, scene, pixel, sample, rix, stk, visits, err);
     return Li;
 }
 

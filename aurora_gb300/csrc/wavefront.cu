@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
         for (uint32_t li = 0; li < sc.num_lights; ++li) {
             const aur_light& L = sc.lights[li];
             if (mis && L.type == AUR_LIGHT_AREA) {
-                // both strategies of every sample (area_light_mis), two slots each
+                // both strategies of every sample (direct_light_mis), two slots each
                 const AreaLightMis al = area_light_setup(L, f);
                 for (uint32_t j = 0; j < (uint32_t)L.samples; ++j, q += 2) {
                     if (q + 1 >= a.M) {   // lights given more samples since the batch was created
@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
                 }
             }
         }
-        if (mis) {   // the emitter sample (emitter_sample), last slot
+        if (mis) {   // the emitter sample (direct_light_mis), last slot
             if (q >= a.M) {
                 atomicOr(&c->error, kWfErrLightSlots);
             } else {
@@ -581,7 +581,7 @@ __global__ void k_wf_combine(WfArgs a) {
             const aur_light& L = sc.lights[li];
             if (L.type == AUR_LIGHT_AMBIENT) Li = Li + f * ((from(L.color) * L.intensity) * L.ambient);
             if (mis && L.type == AUR_LIGHT_AREA) {
-                // area_light_mis: per sample, the light then the BSDF strategy
+                // direct_light_mis: per sample, the light then the BSDF strategy
                 f3 acc = mk3(0.0f);
                 for (int32_t j = 0; j < L.samples; ++j) {
                     f3 Ls = mk3(0.0f);
@@ -609,7 +609,7 @@ __global__ void k_wf_combine(WfArgs a) {
                 Li = Li + mk3(acc.x / ns, acc.y / ns, acc.z / ns);
             }
         }
-        if (mis) {   // emitter_sample: added whether or not it contributes
+        if (mis) {   // the emitter sample: added whether or not it contributes
             const float4 v = q < a.M ? cj[q] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             Li = Li + ((v.w != 0.0f && ((vis >> q) & 1u)) ? mk3(v.x, v.y, v.z) : mk3(0.0f));
         }

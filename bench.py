@@ -61,9 +61,11 @@ def parse():
                     help="only the large terrain workload (plain vs wavefront, RMSE against 16384 spp)")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling cases only)")
     ap.add_argument("--profile", nargs="?", const="trace", default=None,
-                    choices=["trace", "render", "wavefront", "adjoint", "build", "filter"],
+                    choices=["trace", "render", "mis", "loop", "wavefront", "adjoint", "build", "filter"],
                     help="small profiling case: trace = one closest-hit and one any-hit launch; render = Cornell "
-                         "+ sphere frames; wavefront = stepped 8-scene batch; adjoint = one adjoint; "
+                         "+ sphere frames; mis = one MIS frame of the emissive Cornell box; loop = the "
+                         "reference-structured loop (65,536-ray tiles) on the Cornell + sphere scene; "
+                         "wavefront = stepped 8-scene batch; adjoint = one adjoint; "
                          "build = NMH build of the 1M-triangle soup; filter = pixel filter of a 3840x2160 frame")
     return ap.parse_args()
 
@@ -111,6 +113,29 @@ def run_profile(args):
             sc.render(p)
             torch.cuda.synchronize()
         print(json.dumps({"profile_case": "render"}))
+        return
+    if args.profile == "mis":
+        sc = api.Scene(ctx, scenes.cornell_emissive(area_light=True))
+        sc.render(T.render_params(256, 256, 16, 3, mode=T.MODE_PATH_MIS))
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "mis"}))
+        return
+    if args.profile == "loop":
+        sd = scenes.cornell_sphere(seed=0)
+        sc = api.Scene(ctx, sd)
+        W = H = 256
+        spp = 4
+        p = T.render_params(W, H, spp, 4, mode=T.MODE_PATH)
+        rays = torch.zeros((W * H, 9), dtype=torch.float32, device="cuda")
+        hits = torch.zeros((W * H, 12), dtype=torch.float32, device="cuda")
+        accum = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+        api.clear_pixels(ctx, W, H, accum)
+        for s_ in range(spp):
+            api.generate_rays(ctx, W, H, s_, spp, sd.camera, rays, hits)
+            api.raytrace_monte_carlo(ctx, sc, p, s_, 0, W * H, rays, hits)
+            api.draw_pixels(ctx, W, H, 1.0 / spp, hits, accum)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "loop"}))
         return
     if args.profile == "wavefront":
         sds = [scenes.sphere_scene(i) for i in range(8)]

@@ -130,6 +130,24 @@ def test_build_graph_reuse(ctx):
         assert np.array_equal(verts, oracle.gather9(oracle.pad_even(V), want[k])), k
 
 
+def test_build_cache_across_streams(ctx):
+    """Builds of one size from the context's cache on different launch
+    streams: each waits for the previous one's use of the shared scratch."""
+    import torch
+    V = scenes.random_soup(20001, seed=51)
+    want = oracle.nmh_build(V)[0]
+    Vd = torch.from_numpy(V.reshape(-1)).cuda()
+    streams = [torch.cuda.Stream() for _ in range(3)]
+    try:
+        for i in range(6):
+            with torch.cuda.stream(streams[i % 3]):
+                ctx.use_torch_stream()
+                nmh = api.Nmh(ctx, Vd, count=V.shape[0])
+                assert np.array_equal(nmh.export()[0], want), i
+    finally:
+        ctx.use_torch_stream()
+
+
 def test_empty_build(ctx):
     nmh, perm, verts, levels = _gpu_build(ctx, np.zeros((0, 9), np.float32))
     assert levels == 0 and perm.size == 0
