@@ -1,6 +1,6 @@
 """AUR_MODE_PATH_MIS on the GPU: the light-selection table and the images
 against the oracle, unbiasedness at high sample counts, the tile entry point
-and and the wavefront batch against the fused renderer (the adjoint's
+and the wavefront batch against the fused renderer (the adjoint's
 finite-difference checks are in test_gpu_adjoint.py)."""
 import numpy as np
 import pytest
