@@ -939,9 +939,10 @@ constexpr size_t lookback_bytes(size_t ntiles) { return 3 * ntiles * sizeof(unsi
 // stream, or records them as a linear chain of CUDA graph nodes, or replays
 // the same sequence against such a recording and writes into its
 // instantiated graph only the arguments that differ (another vertex array,
-// other output buffers: the next build of the same size). A build of N
-// triangles makes about 4 * levels + 20 launches; recorded once and then
-// launched as one graph they no longer wait on the host's per-launch cost.
+// other output buffers: the next build of the same size). A build makes six
+// launches per global level plus 20 (74 at 1M triangles); recorded once and
+// then launched as one graph they no longer wait on the host's per-launch
+// cost.
 struct NodeRec {
     cudaGraphNode_t node = nullptr;
     const void* func = nullptr;          // null for a memset node
