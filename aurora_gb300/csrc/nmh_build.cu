@@ -37,6 +37,7 @@ constexpr uint32_t kDone = 0xFFFFFFFFu;
 constexpr int kThreads = 256;
 constexpr int kTileItems = 16;                       // per thread, scan tiles
 constexpr uint32_t kTile = kThreads * kTileItems;     // 4096
+constexpr int kSelectItems = 16;                     // per thread, k_select (a multiple of 4)
 constexpr int kSortItems = 8;
 constexpr uint32_t kSortTile = kThreads * kSortItems; // 2048
 
@@ -266,38 +267,38 @@ __global__ void k_node_table(uint32_t n, uint32_t* __restrict__ nstart, uint32_t
 
 // Segmented arg-max of (max-key, lowest prim id) over each node's segment,
 // excluding the segment's first element, which is recorded as pair[0]
-// (swapMaxTriangleTPS/TPT, rebuilder.cu:93-151). Each thread owns 16
-// consecutive list positions.
+// (swapMaxTriangleTPS/TPT, rebuilder.cu:93-151). Each thread owns
+// kSelectItems consecutive list positions.
 __global__ void __launch_bounds__(kThreads) k_select(const uint32_t* __restrict__ list, uint32_t M,
                                                      const float* __restrict__ mxa,
                                                      const uint32_t* __restrict__ node_of,
                                                      const uint32_t* __restrict__ nstart, uint32_t L0,
                                                      unsigned long long* __restrict__ best,
                                                      uint32_t* __restrict__ pair0) {
-    const uint32_t base = (blockIdx.x * kThreads + threadIdx.x) * kTileItems;
+    const uint32_t base = (blockIdx.x * kThreads + threadIdx.x) * kSelectItems;
     const int lane = threadIdx.x & 31;
     uint32_t cur = kDone;
     unsigned long long cur_key = 0;
     bool first_run = true;
     if (base < M) {
-        const int cnt = (M - base) < (uint32_t)kTileItems ? (int)(M - base) : kTileItems;
-        uint32_t pid[kTileItems];
-        if (cnt == kTileItems) {
+        const int cnt = (M - base) < (uint32_t)kSelectItems ? (int)(M - base) : kSelectItems;
+        uint32_t pid[kSelectItems];
+        if (cnt == kSelectItems) {
             const uint4* p = reinterpret_cast<const uint4*>(list + base);
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < kSelectItems / 4; ++q) {
                 const uint4 v = p[q];
                 pid[4 * q] = v.x; pid[4 * q + 1] = v.y; pid[4 * q + 2] = v.z; pid[4 * q + 3] = v.w;
             }
         } else {
 #pragma unroll
-            for (int i = 0; i < kTileItems; ++i) pid[i] = i < cnt ? list[base + i] : 0u;
+            for (int i = 0; i < kSelectItems; ++i) pid[i] = i < cnt ? list[base + i] : 0u;
         }
-        uint32_t nd[kTileItems];
+        uint32_t nd[kSelectItems];
 #pragma unroll
-        for (int i = 0; i < kTileItems; ++i) nd[i] = i < cnt ? node_of[pid[i]] : kDone;
+        for (int i = 0; i < kSelectItems; ++i) nd[i] = i < cnt ? node_of[pid[i]] : kDone;
 #pragma unroll
-        for (int i = 0; i < kTileItems; ++i) {
+        for (int i = 0; i < kSelectItems; ++i) {
             if (i >= cnt) break;
             const uint32_t k = nd[i];
             unsigned long long key;
@@ -1218,7 +1219,8 @@ void enqueue_build(Seq& q, const BuildArgs& b) {
         const uint32_t mt = cdiv(M, kTile);
         // each node's pair: its segment's first entry and the entry of largest max-key (k_select),
         // written to the heap (k_emit_pairs)
-        q.launch(k_select, dim3(mt), dim3(kThreads), 0, listA + a * S, M, mx + a * S, node_of, ns, L0, best, pair0);
+        q.launch(k_select, dim3(cdiv(M, (uint32_t)kThreads * kSelectItems)), dim3(kThreads), 0, listA + a * S, M,
+                 mx + a * S, node_of, ns, L0, best, pair0);
         q.launch(k_emit_pairs, dim3(cdiv(L1 - L0, 256)), dim3(256), 0, L0, L1, best, pair0, heap, node_of);
         if (lv + 1 == levels) break;
         ListSet sb;
