@@ -23,6 +23,24 @@ def _specular(sd):
     return scenes.SceneData(sd.name + "_specular", sd.vertices, sd.normals, sids, sh, sd.lights, sd.camera)
 
 
+def _all_lights(sd):
+    """Every light type around the emitters, area lights with several samples
+    between the delta lights: the order in which a hit's shadow rays are
+    walked and summed."""
+    lights = np.zeros(5, T.light_dtype)
+    lights[0] = T.area_light((0.2, 0.99, 0.3), (0.3, 0.0, 0.0), (0.0, 0.0, 0.2), (0.0, -1.0, 0.0),
+                             color=(1.0, 0.8, 0.6), intensity=1.5, samples=3)
+    lights[1]["type"], lights[1]["position"], lights[1]["color"], lights[1]["intensity"] = (
+        T.LIGHT_POINT, (0.5, 0.8, 0.5), (0.3, 0.3, 1.0), 0.4)
+    lights[2]["type"], lights[2]["position"], lights[2]["color"] = T.LIGHT_AMBIENT, (0.5, 0.5, 0.5), (1, 1, 1)
+    lights[2]["intensity"], lights[2]["ambient"] = 0.3, 0.25
+    lights[3] = T.area_light((0.6, 0.5, 0.999), (0.2, 0.0, 0.0), (0.0, 0.2, 0.0), (0.0, 0.0, -1.0), samples=2)
+    lights[4]["type"], lights[4]["direction"], lights[4]["color"], lights[4]["intensity"] = (
+        T.LIGHT_DIRECTIONAL, (0.3, -1.0, -0.2), (1.0, 1.0, 1.0), 0.2)
+    return scenes.SceneData(sd.name + "_lights", sd.vertices, sd.normals, sd.shader_ids, sd.shaders, lights,
+                            sd.camera)
+
+
 def test_table_matches_oracle(ctx):
     for sd in (scenes.cornell_emissive(), scenes.cornell_emissive(area_light=True), scenes.cornell()):
         sc = api.Scene(ctx, sd)
@@ -50,11 +68,14 @@ def test_table_of_many_emitters_matches_oracle(ctx):
     assert np.allclose(pa, opa, rtol=2e-3, atol=0)      # cdf differences of an ulp, divided
 
 
-@pytest.mark.parametrize("scene", ["cornell", "emissive", "emissive_area", "emissive_specular"])
+@pytest.mark.parametrize("scene", ["cornell", "emissive", "emissive_area", "emissive_specular", "emissive_all_lights",
+                                   "emissive_all_lights_specular"])
 def test_render_matches_oracle(ctx, scene):
     sd = {"cornell": scenes.cornell, "emissive": scenes.cornell_emissive,
           "emissive_area": lambda: scenes.cornell_emissive(area_light=True),
-          "emissive_specular": lambda: _specular(scenes.cornell_emissive(area_light=True))}[scene]()
+          "emissive_specular": lambda: _specular(scenes.cornell_emissive(area_light=True)),
+          "emissive_all_lights": lambda: _all_lights(scenes.cornell_emissive()),
+          "emissive_all_lights_specular": lambda: _specular(_all_lights(scenes.cornell_emissive()))}[scene]()
     sc = api.Scene(ctx, sd)
     p = T.render_params(40, 40, 4, 4, seed=9, mode=T.MODE_PATH_MIS)
     img = sc.render(p).cpu().numpy()
@@ -109,7 +130,8 @@ def _mis_batch_scenes():
     sph.shaders = sph.shaders.copy()
     sph.shaders["emission"][0] = 1.0          # the first shader's triangles emit (colour set below)
     sph.shaders["emission_color"][0] = (0.5, 0.4, 0.3)
-    return [scenes.cornell_emissive(area_light=True), scenes.cornell_emissive(), scenes.cornell(), sph]
+    return [scenes.cornell_emissive(area_light=True), scenes.cornell_emissive(), scenes.cornell(), sph,
+            _all_lights(scenes.cornell_emissive())]
 
 
 @pytest.mark.parametrize("tuning", [dict(paths_in_flight=1024, samples_per_wave=1, block_size=64, blocks_per_sm=2),
@@ -118,7 +140,7 @@ def test_wavefront_equals_plain(ctx, tuning):
     """The wavefront batch in MIS mode: every frame equals aur_render's."""
     sds = _mis_batch_scenes()
     scs = [api.Scene(ctx, sd) for sd in sds]
-    sizes = [(40, 32), (24, 24), (33, 17), (16, 40)]
+    sizes = [(40, 32), (24, 24), (33, 17), (16, 40), (20, 20)]
     prm = [T.render_params(w, h, 4, 3, seed=7, mode=T.MODE_PATH_MIS, scene_id=i) for i, (w, h) in enumerate(sizes)]
     batch = api.Batch(ctx, scs, prm, tuning=api.make_tuning(**tuning) if tuning else None)
     frames = batch.render()
