@@ -85,6 +85,44 @@ def test_adjoint_matches_finite_differences(ctx, mode, scene):
         assert abs(g - fd) <= 1e-3 * abs(fd) + 1e-6, (kind, idx, ch, g, fd)
 
 
+def _all_lights(sd):
+    """Area lights with several samples between a point, an ambient and a
+    directional light."""
+    lights = np.zeros(5, T.light_dtype)
+    lights[0] = T.area_light((0.2, 0.99, 0.3), (0.3, 0.0, 0.0), (0.0, 0.0, 0.2), (0.0, -1.0, 0.0),
+                             color=(1.0, 0.8, 0.6), intensity=1.5, samples=3)
+    lights[1]["type"], lights[1]["position"], lights[1]["color"], lights[1]["intensity"] = (
+        T.LIGHT_POINT, (0.5, 0.8, 0.5), (0.3, 0.3, 1.0), 0.4)
+    lights[2]["type"], lights[2]["position"], lights[2]["color"] = T.LIGHT_AMBIENT, (0.5, 0.5, 0.5), (1, 1, 1)
+    lights[2]["intensity"], lights[2]["ambient"] = 0.3, 0.25
+    lights[3] = T.area_light((0.6, 0.5, 0.999), (0.2, 0.0, 0.0), (0.0, 0.2, 0.0), (0.0, 0.0, -1.0), samples=2)
+    lights[4]["type"], lights[4]["direction"], lights[4]["color"], lights[4]["intensity"] = (
+        T.LIGHT_DIRECTIONAL, (0.3, -1.0, -0.2), (1.0, 1.0, 1.0), 0.2)
+    return scenes.SceneData(sd.name + "_lights", sd.vertices, sd.normals, sd.shader_ids, sd.shaders, lights,
+                            sd.camera)
+
+
+@pytest.mark.parametrize("mode", [T.MODE_PATH, T.MODE_PATH_MIS])
+def test_adjoint_with_every_light_type(ctx, mode):
+    """Every light type around emissive triangles: the largest shader
+    gradients and the colour gradient of each light (those above 1 % of the
+    largest) against central differences."""
+    sd, sc, p, target = _setup(ctx, mode, sd=_all_lights(scenes.cornell_emissive()))
+    img = sc.render(p)
+    d_image = (2.0 * (img - target)).contiguous()
+    d_image[..., 3] = 0.0
+    g_sh, g_lt = sc.adjoint(p, d_image)
+    g_sh, g_lt = g_sh.cpu().numpy(), g_lt.cpu().numpy()
+    order = np.argsort(-np.abs(g_sh).ravel())[:4]
+    checks = [("shader", int(k // 3), int(k % 3), g_sh.ravel()[k]) for k in order]
+    big = np.abs(g_lt).max()
+    checks += [("light", i, c, g_lt[i, c]) for i in range(5) for c in range(3) if abs(g_lt[i, c]) > 0.01 * big]
+    assert len({c[1] for c in checks if c[0] == "light"}) >= 4
+    for kind, idx, ch, g in checks:
+        fd = _fd(sc, sd, p, target, kind, idx, ch)
+        assert abs(g - fd) <= 1e-3 * abs(fd) + 1e-6, (kind, idx, ch, g, fd)
+
+
 def test_adjoint_through_torch_autograd(ctx):
     import torch
     sd, sc, p, target = _setup(ctx, T.MODE_PATH, W=32, spp=4)
