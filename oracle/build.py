@@ -4,7 +4,10 @@ build_oracle() compiles aur_oracle.cpp, the CPU restatement of the reference
 algorithms, into oracle/_build/liboracle.so. build_ref() compiles the
 reference's own traversal headers, read in place from the reference source
 tree, through the shim in ref_shim/ into oracle/_ref/libaurora_ref.so; it is
-skipped when that tree is absent. Both use -ffp-contract=off so that no
+skipped when that tree is absent. The tree is found at $AURORA_REFERENCE,
+else at DEFAULT_REFERENCE, the directory where the build container mounts
+the reference checkout (read only); on a machine without it (the GPU host)
+build_ref() does nothing and the tests that need it skip. Both use -ffp-contract=off so that no
 multiply-add is fused, like the -fmad=false CUDA build they are compared with.
 """
 import os
@@ -14,6 +17,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libaurora_ref.so")
+DEFAULT_REFERENCE = "/root/reference"
 FLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-pthread"]
 
 
@@ -34,7 +38,7 @@ def build_oracle(force=False):
 
 
 def build_ref(reference=None, force=False):
-    ref = reference or os.environ.get("AURORA_REFERENCE", "/root/reference")
+    ref = reference or os.environ.get("AURORA_REFERENCE", DEFAULT_REFERENCE)
     if not os.path.isdir(os.path.join(ref, "src")):
         return None
     srcs = [os.path.join(HERE, "ref_shim", "ref_traverse.cpp"), os.path.join(HERE, "ref_shim", "ref_shade.cpp")]

@@ -1,8 +1,8 @@
 /*
  * ref_traverse.cpp — the reference's own traversal code compiled as host C++.
  *
- * TEST INFRASTRUCTURE ONLY. Built by oracle/build_ref.sh into oracle/_ref/
- * from the unmodified Nadrin/aurora headers (include path = the reference's
+ * TEST INFRASTRUCTURE ONLY. Built by build_ref() in oracle/build.py into
+ * oracle/_ref/ from the unmodified Nadrin/aurora headers (include path = the reference's
  * src/ directory); nothing of the reference is copied here. It exists to pin
  * the oracle's traversal (oracle/aur_oracle.cpp) to the reference's code:
  *   util/math.h, util/ray.h, util/hitpoint.h, data/geometry.h,
