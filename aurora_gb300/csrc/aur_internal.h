@@ -76,6 +76,7 @@ struct aur_ctx {
     aur::Scratch out[2];
     cudaEvent_t ev[8] = {};
     aur::BuildCache* build = nullptr;    // created by the first aur_nmh_build
+    uint32_t lookback_test = 0;          // test hook for the next build (aur_debug_lookback_timeout)
 };
 
 struct aur_nmh {

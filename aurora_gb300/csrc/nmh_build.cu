@@ -265,6 +265,15 @@ __global__ void k_node_table(uint32_t n, uint32_t* __restrict__ nstart, uint32_t
     nlbase[k] = (uint32_t)left_base(k, L0, n);
 }
 
+// Bit 16 of the error word: a look-back wait gave up. The lists of that
+// level then have positions nobody wrote, so every later kernel of the build
+// returns at once instead of reading ids out of them; the build reports
+// AUR_ERR_TIMEOUT and its outputs are not used.
+constexpr uint32_t kErrLookback = 16u;
+__device__ __forceinline__ bool build_aborted(const uint32_t* err) {
+    return (*reinterpret_cast<const volatile uint32_t*>(err) & kErrLookback) != 0u;
+}
+
 // Segmented arg-max of (max-key, lowest prim id) over each node's segment,
 // excluding the segment's first element, which is recorded as pair[0]
 // (swapMaxTriangleTPS/TPT, rebuilder.cu:93-151). Each thread owns
@@ -274,7 +283,8 @@ __global__ void __launch_bounds__(kThreads) k_select(const uint32_t* __restrict_
                                                      const uint32_t* __restrict__ node_of,
                                                      const uint32_t* __restrict__ nstart, uint32_t L0,
                                                      unsigned long long* __restrict__ best,
-                                                     uint32_t* __restrict__ pair0) {
+                                                     uint32_t* __restrict__ pair0, const uint32_t* err) {
+    if (build_aborted(err)) return;       // whole blocks: the word does not change during this launch
     const uint32_t base = (blockIdx.x * kThreads + threadIdx.x) * kSelectItems;
     const int lane = threadIdx.x & 31;
     uint32_t cur = kDone;
@@ -338,9 +348,9 @@ __global__ void __launch_bounds__(kThreads) k_select(const uint32_t* __restrict_
 // Writes each level node's pair into the heap and retires its triangles.
 __global__ void k_emit_pairs(uint32_t L0, uint32_t L1, unsigned long long* __restrict__ best,
                              const uint32_t* __restrict__ pair0, uint32_t* __restrict__ heap,
-                             uint32_t* __restrict__ node_of) {
+                             uint32_t* __restrict__ node_of, const uint32_t* err) {
     const uint32_t k = L0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= L1) return;
+    if (k >= L1 || build_aborted(err)) return;
     const uint32_t p0 = pair0[k - L0];
     const uint32_t p1 = 0xFFFFFFFFu - (uint32_t)(best[k - L0] & 0xFFFFFFFFull);
     best[k - L0] = 0ull;
@@ -371,7 +381,10 @@ __device__ __forceinline__ void flags_of(uint32_t nd, bool& D, bool& Lf) {
 // 0-30), so one 64-bit store publishes all of it. Tiles are taken in launch
 // order from a counter, so every tile a block waits for belongs to a block
 // that is already running; the wait is still bounded, and a block that gives
-// up sets bit 16 of *err and publishes what it has.
+// up sets bit 16 of *err and publishes what it has. `test` != 0 is a test
+// hook (aur_debug_lookback_timeout): every tile after the first then waits
+// on its predecessor as on a word that nothing sets, for `test` spins, so
+// that the give-up path runs on purpose.
 constexpr unsigned long long kStTile = 1ull << 62, kStPrefix = 2ull << 62;
 constexpr uint32_t kLookbackSpins = 1u << 22;
 
@@ -381,7 +394,7 @@ __device__ __forceinline__ unsigned long long st_word(unsigned long long state, 
 
 // One thread: exclusive (D, L) prefix of `tile` given its own counts.
 __device__ uint2 tile_lookback(unsigned long long* status, uint32_t tile, uint32_t cd, uint32_t cl,
-                               uint32_t* err) {
+                               uint32_t* err, uint32_t test) {
     if (tile == 0) {
         atomicExch(status, st_word(kStPrefix, cd, cl));
         return make_uint2(0u, 0u);
@@ -389,12 +402,13 @@ __device__ uint2 tile_lookback(unsigned long long* status, uint32_t tile, uint32
     atomicExch(status + tile, st_word(kStTile, cd, cl));
     uint64_t ed = 0, el = 0;
     uint32_t spins = 0;
+    const uint32_t limit = test ? test : kLookbackSpins;
     for (int64_t p = (int64_t)tile - 1; p >= 0;) {
         const unsigned long long w = atomicAdd(status + p, 0ull);   // coherent read
-        const unsigned long long state = w >> 62;
+        const unsigned long long state = test ? 0ull : w >> 62;
         if (state == 0) {
-            if (++spins > kLookbackSpins) {
-                atomicOr(err, 16u);
+            if (++spins > limit) {
+                atomicOr(err, kErrLookback);
                 break;
             }
             __nanosleep(32);
@@ -424,7 +438,8 @@ struct TileScan {
 template <bool kPart>
 __device__ __forceinline__ void tile_scan(const uint32_t* __restrict__ list, uint32_t M,
                                           const uint32_t* __restrict__ node_of, unsigned long long* status,
-                                          uint32_t* tile_counter, uint32_t* err, TileScan<kPart>& s) {
+                                          uint32_t* tile_counter, uint32_t* err, uint32_t test,
+                                          TileScan<kPart>& s) {
     __shared__ uint32_t s_d[kThreads / 32], s_l[kThreads / 32];
     __shared__ uint32_t s_tile;
     __shared__ uint2 s_pre;
@@ -455,7 +470,7 @@ __device__ __forceinline__ void tile_scan(const uint32_t* __restrict__ list, uin
     if (threadIdx.x == 0) {
         uint32_t td = 0, tl = 0;
         for (int w = 0; w < kThreads / 32; ++w) { td += s_d[w]; tl += s_l[w]; }
-        s_pre = tile_lookback(status, s.tile, td, tl, err);
+        s_pre = tile_lookback(status, s.tile, td, tl, err, test);
     }
     __syncthreads();
     uint32_t od = s_pre.x, ol = s_pre.y;
@@ -471,9 +486,13 @@ __global__ void __launch_bounds__(kThreads) k_split_next(ListSet ls, uint32_t M,
                                                          const uint32_t* __restrict__ nnuml, uint32_t L0,
                                                          unsigned long long* __restrict__ status,
                                                          uint32_t* __restrict__ tile_counter,
-                                                         uint32_t* __restrict__ err) {
+                                                         uint32_t* __restrict__ err, uint32_t test) {
+    // Blocks of this launch may see the word change (a tile that gives up),
+    // so the decision is made block-wide. A block that leaves takes no tile;
+    // the tiles after it then give up too, within their bounded wait.
+    if (__syncthreads_or(build_aborted(err))) return;
     TileScan<false> s;
-    tile_scan<false>(ls.in[0], M, node_of, status, tile_counter, err, s);
+    tile_scan<false>(ls.in[0], M, node_of, status, tile_counter, err, test, s);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t wbase = s.tile * kTile + warp * 32 * kTileItems;
     const uint32_t lt = lanemask_lt();
@@ -500,10 +519,11 @@ __global__ void __launch_bounds__(kThreads) k_partition(ListSet ls, uint32_t M, 
                                                         const uint32_t* __restrict__ nlbase, uint32_t L0,
                                                         unsigned long long* __restrict__ status, uint32_t ntiles,
                                                         uint32_t* __restrict__ tile_counter, uint32_t m_next,
-                                                        uint32_t* __restrict__ err) {
+                                                        uint32_t* __restrict__ err, uint32_t test) {
+    if (__syncthreads_or(build_aborted(err))) return;      // see k_split_next
     TileScan<true> s;
     tile_scan<true>(ls.in[blockIdx.y], M, node_of, status + (size_t)blockIdx.y * ntiles, tile_counter + blockIdx.y,
-                    err, s);
+                    err, test, s);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t wbase = s.tile * kTile + warp * 32 * kTileItems;
     const uint32_t lt = lanemask_lt();
@@ -626,6 +646,7 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_finish(const uint32_t* 
                                                                  uint32_t* __restrict__ err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     LocalSmem& s = *reinterpret_cast<LocalSmem*>(smem_raw);
+    if (build_aborted(err)) return;       // whole blocks: the word does not change during this launch
     const uint32_t k = L0 + blockIdx.x;
     const int t = threadIdx.x;
     const uint32_t seg0 = nstart[k];
@@ -816,9 +837,9 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_finish(const uint32_t* 
 
 // Orders each pair by (min-key on the last level's axis, prim id).
 __global__ void k_pair_order(uint32_t n, const uint32_t* __restrict__ heap, const float* __restrict__ mn_last,
-                             uint32_t* __restrict__ perm) {
+                             uint32_t* __restrict__ perm, const uint32_t* err) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    if (k >= n || build_aborted(err)) return;
     uint32_t p = heap[2 * k], q = heap[2 * k + 1];
     const float kp = mn_last[p], kq = mn_last[q];
     if (kq < kp || (kq == kp && q < p)) { const uint32_t t = p; p = q; q = t; }
@@ -832,9 +853,9 @@ __global__ void k_pair_order(uint32_t n, const uint32_t* __restrict__ heap, cons
 // box of the pair goes to box[6k..6k+5] (lo.xyz, hi.xyz) for k_node_boxes.
 __global__ void k_emit_nodes(const float* __restrict__ V, uint32_t count_in, const uint32_t* __restrict__ perm,
                              uint32_t n, float* __restrict__ verts, float4* __restrict__ recs,
-                             float* __restrict__ box) {
+                             float* __restrict__ box, const uint32_t* err) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    if (k >= n || build_aborted(err)) return;
     const int a = (int)(level_of(k) % 3u);
     float c[2][9];
 #pragma unroll
@@ -887,9 +908,9 @@ __device__ __forceinline__ void pad_interval(float lo, float hi, float& plo, flo
 // node k (an empty box where a child does not exist).
 template <bool kUnion>
 __global__ void k_node_boxes(uint32_t L0, uint32_t L1, uint32_t n, const float* __restrict__ pbox,
-                             float* __restrict__ box, float4* __restrict__ recs) {
+                             float* __restrict__ box, float4* __restrict__ recs, const uint32_t* err) {
     const uint32_t k = L0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= L1) return;
+    if (k >= L1 || build_aborted(err)) return;
     float b[6];
     if (kUnion) {
 #pragma unroll
@@ -1072,12 +1093,12 @@ private:
 // tile counters are cleared first.
 void split_and_partition(Seq& q, const ListSet& sb, const ListSet& sac, uint32_t M, uint32_t mt, uint32_t ntiles,
                          uint32_t* node_of, const uint32_t* ns, const uint32_t* nl, const uint32_t* nlb, uint32_t L0,
-                         uint32_t m_next, unsigned long long* lb, uint32_t* err) {
+                         uint32_t m_next, unsigned long long* lb, uint32_t* err, uint32_t test) {
     uint32_t* counters = reinterpret_cast<uint32_t*>(lb + 3 * (size_t)ntiles);
     q.memset(lb, lookback_bytes(ntiles));
-    q.launch(k_split_next, dim3(mt), dim3(kThreads), 0, sb, M, node_of, ns, nl, L0, lb, counters, err);
+    q.launch(k_split_next, dim3(mt), dim3(kThreads), 0, sb, M, node_of, ns, nl, L0, lb, counters, err, test);
     q.launch(k_partition, dim3(mt, 2), dim3(kThreads), 0, sac, M, node_of, ns, nl, nlb, L0, lb + ntiles, ntiles,
-             counters + 1, m_next, err);
+             counters + 1, m_next, err, test);
 }
 
 // First level whose node segments all fit k_local_finish (the leftmost
@@ -1103,14 +1124,15 @@ void finish_local(Seq& q, const uint32_t* list, size_t S, const float* mn, const
 // (pbox, written by k_emit_nodes) and the children's subtree boxes.
 // pbox and sbox: 6 floats per node of scratch each.
 void emit_records(Seq& q, const float* V, uint32_t count, const uint32_t* perm, uint32_t n, uint32_t lv0,
-                  float* verts, float4* recs, float* pbox, float* sbox) {
-    q.launch(k_emit_nodes, dim3(cdiv(n, 128)), dim3(128), 0, V, count, perm, n, verts, recs, pbox);
+                  float* verts, float4* recs, float* pbox, float* sbox, const uint32_t* err) {
+    q.launch(k_emit_nodes, dim3(cdiv(n, 128)), dim3(128), 0, V, count, perm, n, verts, recs, pbox, err);
     const uint32_t Lb = (1u << lv0) - 1u;   // first node of level lv0
-    if (Lb < n) q.launch(k_node_boxes<false>, dim3(cdiv(n - Lb, 256)), dim3(256), 0, Lb, n, n, pbox, sbox, recs);
+    if (Lb < n)
+        q.launch(k_node_boxes<false>, dim3(cdiv(n - Lb, 256)), dim3(256), 0, Lb, n, n, pbox, sbox, recs, err);
     for (int lv = (int)lv0 - 1; lv >= 0; --lv) {
         const uint32_t L0 = (1u << lv) - 1u;
         const uint32_t L1 = ((2u << lv) - 1u) < n ? ((2u << lv) - 1u) : n;
-        q.launch(k_node_boxes<true>, dim3(cdiv(L1 - L0, 256)), dim3(256), 0, L0, L1, n, pbox, sbox, recs);
+        q.launch(k_node_boxes<true>, dim3(cdiv(L1 - L0, 256)), dim3(256), 0, L0, L1, n, pbox, sbox, recs, err);
     }
 }
 
@@ -1159,6 +1181,7 @@ struct BuildArgs {
     float* verts;
     unsigned char* scratch;    // scratch_layout(N).end bytes
     uint32_t* flags;           // error bits 4 (internal check), 8 (non-finite vertex), 16 (look-back timeout)
+    uint32_t lookback_test = 0;  // test hook: nonzero makes the look-back waits run out (see tile_lookback)
 };
 
 // The whole build of a non-empty soup: bounds and keys, three radix sorts,
@@ -1220,8 +1243,8 @@ void enqueue_build(Seq& q, const BuildArgs& b) {
         // each node's pair: its segment's first entry and the entry of largest max-key (k_select),
         // written to the heap (k_emit_pairs)
         q.launch(k_select, dim3(cdiv(M, (uint32_t)kThreads * kSelectItems)), dim3(kThreads), 0, listA + a * S, M,
-                 mx + a * S, node_of, ns, L0, best, pair0);
-        q.launch(k_emit_pairs, dim3(cdiv(L1 - L0, 256)), dim3(256), 0, L0, L1, best, pair0, heap, node_of);
+                 mx + a * S, node_of, ns, L0, best, pair0, b.flags);
+        q.launch(k_emit_pairs, dim3(cdiv(L1 - L0, 256)), dim3(256), 0, L0, L1, best, pair0, heap, node_of, b.flags);
         if (lv + 1 == levels) break;
         ListSet sb;
         sb.in[0] = listA + bx * S; sb.out[0] = listB + bx * S;
@@ -1229,14 +1252,15 @@ void enqueue_build(Seq& q, const BuildArgs& b) {
         ListSet sac;
         sac.in[0] = listA + a * S; sac.out[0] = listB + a * S;
         sac.in[1] = listA + c * S; sac.out[1] = listB + c * S;
-        split_and_partition(q, sb, sac, M, mt, ntiles, node_of, ns, nl, nlb, L0, M - 2u * (L1 - L0), tiles, b.flags);
+        split_and_partition(q, sb, sac, M, mt, ntiles, node_of, ns, nl, nlb, L0, M - 2u * (L1 - L0), tiles, b.flags,
+                            b.lookback_test);
         uint32_t* t = listA; listA = listB; listB = t;
     }
     if (lv0 < levels) finish_local(q, listA, S, mn, mx, n, lv0, ns, node_of, heap, (float*)k2, b.flags);
     const int al = (int)((levels - 1) % 3);
-    q.launch(k_pair_order, dim3(cdiv(n, 256)), dim3(256), 0, n, heap, mn + al * S, b.perm);
+    q.launch(k_pair_order, dim3(cdiv(n, 256)), dim3(256), 0, n, heap, mn + al * S, b.perm, b.flags);
     // mx and k2 are free once the levels are placed: 3*S >= 6*n floats each for the boxes
-    emit_records(q, b.V, b.count, b.perm, n, lv0, b.verts, b.recs, mx, (float*)k2);
+    emit_records(q, b.V, b.count, b.perm, n, lv0, b.verts, b.recs, mx, (float*)k2, b.flags);
 }
 
 // Error bits of a finished build, read back on `st`.
@@ -1422,6 +1446,8 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
 
     cudaStream_t st = ctx->stream;
     BuildArgs a{V, count, nmh->node_recs, nmh->perm, nmh->verts, nullptr, ctx->d_flags};
+    a.lookback_test = ctx->lookback_test;     // armed for this one build only
+    ctx->lookback_test = 0;
     if (N <= kGraphMaxTriangles) {
         const aur_status s = build_cached(ctx, a, N, st);
         if (s != AUR_OK) {
@@ -1478,7 +1504,9 @@ constexpr size_t kNoAllocScratchBytes = scratch_layout(kNoAllocMaxTriangles).end
 static __device__ __align__(256) unsigned char g_nmh_scratch[kNoAllocScratchBytes];
 
 // Device address of g_nmh_scratch per device, looked up once per device with
-// that device current (the host-side name of the array is not a device address).
+// that device current (the host-side name of the array is not a device
+// address). A cudaDeviceReset of the device makes the kept address stale; the
+// header tells callers not to use this entry point on a device after a reset.
 constexpr int kMaxDevices = 64;
 unsigned char* g_scratch_addr[kMaxDevices] = {};
 std::mutex g_scratch_mutex;
@@ -1523,7 +1551,11 @@ aur_status nmh_build_noalloc_impl(const float* V, uint32_t count, cudaStream_t s
     AUR_CUDA(set_local_smem());
     Seq q = Seq::direct(st);
     enqueue_build(q, BuildArgs{V, count, recs, perm, verts, base, flags});
-    AUR_CUDA(q.finish());
+    const cudaError_t e = q.finish();
+    if (e != cudaSuccess) {
+        cudaGetLastError();     // a failed launch leaves a non-sticky error behind, as in aur_nmh_build
+        return cuda_fail(e, "aur_nmh_build_noalloc kernels", __FILE__, __LINE__);
+    }
     return build_flags("aur_nmh_build_noalloc", flags, st, false);
 }
 
@@ -1540,6 +1572,14 @@ aur_status aur_debug_nmh_layout(uint32_t n, uint32_t k, uint32_t out[3]) {
     out[0] = (uint32_t)aur::segment_start(k, L0, n);
     out[1] = (2u * k + 1u < n) ? (uint32_t)(2 * aur::subtree_nodes(2u * k + 1u, n)) : 0u;
     out[2] = (uint32_t)aur::left_base(k, L0, n);
+    return AUR_OK;
+}
+
+/* Test hook: the next aur_nmh_build on ctx makes its look-back waits run out. */
+aur_status aur_debug_lookback_timeout(aur_ctx* ctx, uint32_t spins) {
+    aur::clear_error();
+    AUR_CHECK(ctx, AUR_ERR_INVALID, "aur_debug_lookback_timeout: null context");
+    ctx->lookback_test = spins;
     return AUR_OK;
 }
 

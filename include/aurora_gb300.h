@@ -229,6 +229,17 @@ typedef struct aur_nmh aur_nmh;
  * Builds on one context are serialized on the GPU (each call also waits for
  * its own build before returning). */
 aur_status aur_nmh_build(aur_ctx* ctx, const float* vertices, uint32_t count, aur_nmh** out);
+/* Test hook for the bounded waits of the build (no counterpart in the
+ * reference, whose build waits on nothing on the device). The build's split
+ * and partition passes are single-pass scans whose tiles wait for their
+ * predecessors' prefixes (decoupled look-back); each wait gives up after a
+ * bounded number of spins and the build then returns AUR_ERR_TIMEOUT, with
+ * the context still usable. With spins != 0, the next aur_nmh_build on ctx
+ * (and only that one) makes every tile after the first wait for `spins`
+ * spins on a prefix that nothing publishes, so the give-up path runs on
+ * purpose: that build returns AUR_ERR_TIMEOUT and creates no NMH. Soups of
+ * at most 4,096 triangles have no such wait and build normally. */
+aur_status aur_debug_lookback_timeout(aur_ctx* ctx, uint32_t spins);
 aur_status aur_nmh_destroy(aur_nmh* nmh);
 /* Triangle count after padding and number of heap levels (log2i(count/2)+1). */
 aur_status aur_nmh_info(const aur_nmh* nmh, uint32_t* count, uint32_t* levels);
@@ -254,7 +265,8 @@ aur_status aur_nmh_perm_device(const aur_nmh* nmh, const uint32_t** perm);
  *                 read with 256-bit loads)
  *   perm:         count + (count & 1) uint32 (NMH position -> original prim id)
  *   nmh_vertices: (count + (count & 1)) * 9 floats (NMH-ordered soup)
- *   levels:       host, nullable; receives log2i(count/2)+1
+ *   levels:       host, nullable; receives 0 for count == 0, else
+ *                 log2i((count+1)/2)+1 (the heap's level count)
  * Runs on `cuda_stream` (NULL = the legacy default stream) of the current
  * device and returns after the build has finished on that stream.
  * Limit: at most 65,536 triangles; larger counts return AUR_ERR_INVALID. The
@@ -262,9 +274,11 @@ aur_status aur_nmh_perm_device(const aur_nmh* nmh, const uint32_t** perm);
  * every GPU that loads the library holds until the process exits. The first
  * call on a device looks up that array's device address
  * (cudaGetSymbolAddress) with the device current; make that first call before
- * any stream capture. All calls share the array: calls whose work overlaps on
- * the GPU (other streams, other host threads) race and must be serialized by
- * the caller. */
+ * any stream capture. The address is kept per device ordinal for the life of
+ * the process: a cudaDeviceReset of that device invalidates it, so do not
+ * call this entry point again on a device after resetting it. All calls share
+ * the array: calls whose work overlaps on the GPU (other streams, other host
+ * threads) race and must be serialized by the caller. */
 aur_status aur_nmh_build_noalloc(const float* vertices, uint32_t count, void* cuda_stream, float* node_records,
                                  uint32_t* perm, float* nmh_vertices, uint32_t* levels);
 

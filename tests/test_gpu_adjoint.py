@@ -85,6 +85,26 @@ def test_adjoint_matches_finite_differences(ctx, mode, scene):
         assert abs(g - fd) <= 1e-3 * abs(fd) + 1e-6, (kind, idx, ch, g, fd)
 
 
+def test_adjoint_at_the_differentiable_workload_size(ctx):
+    """The differentiable workload as stated: Cornell box + 4096-triangle
+    sphere with one shader per triangle, 256x256, 64 spp, depth 4, path mode,
+    L2 loss against the frame at albedo + N(0, 0.05); the two largest albedo
+    gradients and the light colour gradient against central differences."""
+    sd = scenes.cornell_sphere(seed=0)
+    sd, sc, p, target = _setup(ctx, T.MODE_PATH, W=256, spp=64, depth=4, sd=sd)
+    img = sc.render(p)
+    d_image = (2.0 * (img - target)).contiguous()
+    d_image[..., 3] = 0.0
+    g_sh, g_lt = sc.adjoint(p, d_image)
+    g_sh, g_lt = g_sh.cpu().numpy(), g_lt.cpu().numpy()
+    order = np.argsort(-np.abs(g_sh).ravel())[:2]
+    checks = [("shader", int(k // 3), int(k % 3), g_sh.ravel()[k]) for k in order]
+    checks.append(("light", 0, int(np.argmax(np.abs(g_lt[0]))), float(g_lt[0].flat[np.argmax(np.abs(g_lt[0]))])))
+    for kind, idx, ch, g in checks:
+        fd = _fd(sc, sd, p, target, kind, idx, ch)
+        assert abs(g - fd) <= 1e-3 * abs(fd) + 1e-6, (kind, idx, ch, g, fd)
+
+
 def _all_lights(sd):
     """Area lights with several samples between a point, an ambient and a
     directional light."""

@@ -29,6 +29,18 @@ def test_build_matches_oracle(ctx, n):
     assert np.array_equal(verts, oracle.gather9(oracle.pad_even(V), operm))
 
 
+def test_build_matches_oracle_on_the_traversal_benchmark_soup(ctx):
+    """The 1,000,000-triangle soup the traversal benchmark builds and traces
+    (random_soup(1_000_000, seed=0)), with its 19 levels: topology and the
+    NMH-ordered vertices equal the oracle's."""
+    V = scenes.random_soup(1_000_000, seed=0)
+    nmh, perm, verts, levels = _gpu_build(ctx, V)
+    operm, olv = oracle.nmh_build(V)
+    assert levels == olv == 19
+    assert np.array_equal(perm, operm)
+    assert np.array_equal(verts.view(np.uint32), oracle.gather9(V, operm).view(np.uint32))
+
+
 @pytest.mark.parametrize("maker", ["cornell", "cornell_sphere", "terrain64", "spheres"])
 def test_build_with_key_ties(ctx, maker):
     sd = {"cornell": scenes.cornell, "cornell_sphere": scenes.cornell_sphere,

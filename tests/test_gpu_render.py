@@ -26,6 +26,18 @@ def test_cornell_render_matches_oracle(ctx, mode):
     assert np.array_equal(img, ref)      # same arithmetic, same order: bit-exact
 
 
+@pytest.mark.parametrize("mode", [T.MODE_REFERENCE, T.MODE_PATH])
+def test_cornell_full_frame_matches_oracle(ctx, mode):
+    """The Cornell workload at its stated size: 256x256, 16 spp, depth 4, seed 0."""
+    sd = scenes.cornell()
+    sc = api.Scene(ctx, sd)
+    p = T.render_params(256, 256, 16, 4, seed=0, mode=mode)
+    img = sc.render(p).cpu().numpy()
+    ref, _ = oracle.render(oracle.NmhScene(sd), p)
+    assert _close(img, ref)
+    assert np.array_equal(img, ref)
+
+
 def test_cornell_sphere_render_matches_oracle(ctx):
     sd = scenes.cornell_sphere(seed=1)
     sc = api.Scene(ctx, sd)

@@ -39,6 +39,27 @@ def test_wavefront_equals_plain(ctx, mode, tuning):
         assert np.array_equal(f.cpu().numpy(), twice.cpu().numpy())
 
 
+@pytest.mark.parametrize("mode", [T.MODE_PATH, T.MODE_PATH_MIS, T.MODE_REFERENCE])
+def test_wavefront_frames_match_oracle(ctx, mode):
+    """Batch frames against the oracle directly (not through aur_render, which
+    shares the device helpers): a sphere scene, the Cornell box with a sphere,
+    and emissive triangles plus an area light, in one batch whose pool is small
+    enough to refill several times."""
+    import oracle
+    sds = [scenes.sphere_scene(5, max_tris=20000), scenes.cornell_sphere(seed=2),
+           scenes.cornell_emissive(area_light=True)]
+    scs = [api.Scene(ctx, sd) for sd in sds]
+    sizes = [(32, 24), (24, 24), (20, 28)]
+    prm = [T.render_params(w, h, 4, 4, seed=11, mode=mode, scene_id=i) for i, (w, h) in enumerate(sizes)]
+    batch = api.Batch(ctx, scs, prm, tuning=api.make_tuning(1024, 1, 64, 2))
+    frames = batch.render()
+    assert batch.status() > 0
+    for sd, sc, p, f in zip(sds, scs, prm, frames):
+        table = sc.mis_table() if mode == T.MODE_PATH_MIS else None
+        ref, _ = oracle.render(oracle.NmhScene(sd), p, table=table)
+        assert np.array_equal(f.cpu().numpy(), ref), sd.name
+
+
 def _specular(sd, k0=10, k1=22, k2=34):
     """The scene with a mirror-like block (reflectivity 0.6) and a glass-like
     one (translucence 0.7, index 1.5)."""

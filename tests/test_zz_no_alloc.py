@@ -95,6 +95,37 @@ def test_noalloc_build_matches_regular_build_twice_in_a_row(ctx):
         assert np.array_equal(recs.view(np.uint32), exp.view(np.uint32))
 
 
+@pytest.mark.parametrize("count", [LIMIT, LIMIT - 1])
+def test_noalloc_build_at_its_limit(ctx, count):
+    """65,536 triangles, and 65,535 (which pads to 65,536): the scratch layout
+    then ends exactly at the end of the fixed array."""
+    V = scenes.random_soup(count, seed=3)
+    recs, perm, verts, levels = _noalloc_build(V)
+    rperm, rverts, rlevels = _regular_build(ctx, V)
+    assert levels == rlevels
+    assert np.array_equal(perm, rperm)
+    assert np.array_equal(verts.view(np.uint32), rverts.view(np.uint32))
+    exp = _expected_records(rverts)
+    assert np.array_equal(recs.view(np.uint32), exp.view(np.uint32))
+
+
+def test_noalloc_build_allocates_nothing(ctx):
+    """Every device or pinned allocation the library makes goes through one
+    helper, which the fault injector can make fail; armed to fail the very
+    next allocation, the allocation-free build must still succeed."""
+    V = scenes.random_soup(5000, seed=4)
+    _noalloc_build(V)                            # device set-up (the array's address) done beforehand
+    lib = api.lib()
+    try:
+        lib.aur_debug_fail_allocation(1)
+        recs, perm, verts, levels = _noalloc_build(V)
+    finally:
+        lib.aur_debug_fail_allocation(0)
+    rperm, rverts, _ = _regular_build(ctx, V)
+    assert np.array_equal(perm, rperm)
+    assert np.array_equal(verts.view(np.uint32), rverts.view(np.uint32))
+
+
 def test_noalloc_build_rejects_soups_above_its_limit(ctx):
     import torch
     V = torch.zeros(9 * (LIMIT + 1), dtype=torch.float32, device="cuda")
