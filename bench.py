@@ -11,17 +11,25 @@ the metric is Mrays/s closest-hit. Inputs are seeded synthetic data.
 Prints one JSON line. `e2e` measures the same metric through the C ABI's
 host-buffer call (aur_trace_closest_host: rays copied in from pinned host
 memory and hits copied back inside the timed region). `roofline` divides the
-algorithmic bytes of a launch by the kernel's CUDA-event duration: 28 B ray
-in + 16 B hit out + per node record fetched 16 B (slab), per slab crossed
-64 B (two triangles) and per crossing of a node with children 48 B (the
-children's subtree boxes), the reads of this traversal as counted by
-aur_trace_stats. The reference algorithm's own figure (72 B per node it
-visits, counted by the unpruned traversal) is reported beside it.
-`cpu_baseline` times the oracle's C++ restatement of the reference traversal
-on a sample of the same rays on all host cores. With --gpus N > 1 (under
-torchrun) every rank runs an independent replica of the workload.
+algorithmic bytes of a launch by the kernel's CUDA-event duration, with the
+reference algorithm's bytes: 24 B ray in + 16 B hit out + 72 B per node that
+the reference's intersect() visits (two triangles of 36 B), the visits
+counted by the same traversal without box pruning. This traversal's own
+reads (fewer nodes, 128-byte records) are reported beside it, and the DRAM
+traffic of one launch from the committed ncu summary when that summary was
+captured from the current traversal sources. `cpu_baseline` times the
+oracle's C++ restatement of the reference traversal on a sample of the same
+rays on all host cores. With --gpus N > 1 (under torchrun) every rank runs
+an independent replica of the workload.
+
+The same line carries the other workloads (Cornell, MIS, pixel filter, the
+64-scene wavefront batch at all 64 spp, the adjoint, the terrain at
+1920x1080), each with its correctness checks against the oracle or central
+differences; bench.py prints the line and exits with status 1 when any
+check fails (the failures are listed under "parity").
 """
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -37,12 +45,14 @@ sys.path.insert(0, ROOT)
 
 N_TRIS = 1_000_000
 N_RAYS = 1 << 24
-RAY_IN_BYTES = 28      # origin, direction, tmax
+RAY_IN_BYTES = 28      # origin, direction, tmax (this traversal's own reads)
+REF_RAY_IN_BYTES = 24  # origin, direction: the reference algorithm's ray
 HIT_OUT_BYTES = 16     # t, u, v, prim
 NODE_BYTES = 72        # two triangles, as the reference fetches per visited node
 SLAB_BYTES = 16        # first word of a node record: slab lo/hi (+ 8 B of triangle)
 TRI_BYTES = 64         # rest of the two triangles, read when the slab is crossed
 BOX_BYTES = 48         # children's subtree boxes, read before descending
+NMH_LEVEL_BYTES = 32   # NMH build, per triangle per level: 16 B read + 16 B written
 METRIC = "Mrays/s closest-hit"
 WORKLOAD = ("traversal microbench: 1M triangles (centroid U[0,1]^3, edges LogNormal(-4,0.5)), 2^24 rays "
             "(half coherent pinhole 4096x4096 even rows, half random origin/direction), closest hit")
@@ -58,7 +68,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-extras", action="store_true", help="headline traversal only")
     ap.add_argument("--terrain", action="store_true",
-                    help="only the large terrain workload (plain vs wavefront, RMSE against 16384 spp)")
+                    help="only the large terrain workload (plain vs wavefront, full frame)")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling cases only)")
     ap.add_argument("--profile", nargs="?", const="trace", default=None,
                     choices=["trace", "render", "mis", "loop", "wavefront", "adjoint", "build", "filter"],
@@ -191,19 +201,44 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+TRAVERSAL_SOURCES = ("aurora_gb300/csrc/trace.cu", "aurora_gb300/csrc/aur_traverse.cuh",
+                     "aurora_gb300/csrc/aur_math.cuh")
+TRAFFIC_PROFILE = "profiles/k_trace_microbench_full.md"
+
+
+def traversal_source_sha():
+    """First 16 hex digits of the SHA-256 of the closest-hit kernel's sources."""
+    h = hashlib.sha256()
+    for rel in TRAVERSAL_SOURCES:
+        with open(os.path.join(ROOT, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
 def load_traffic():
-    """Per-launch DRAM bytes of the closest-hit kernel from the committed ncu
-    summary, if present (a line 'traffic_bytes_per_launch: N')."""
-    p = os.path.join(ROOT, "profiles", "k_trace_microbench_full.md")
+    """(per-launch DRAM bytes of the closest-hit kernel, where they come from).
+
+    The committed ncu summary holds 'traffic_bytes_per_launch: N' and
+    'source_sha256_16: H', H being traversal_source_sha() of the sources it
+    was captured from. The figure is used only when H equals the hash of the
+    sources now; otherwise traffic is None and the source says why."""
+    p = os.path.join(ROOT, TRAFFIC_PROFILE)
     if not os.path.exists(p):
-        return None
+        return None, "no ncu summary (%s)" % TRAFFIC_PROFILE
+    vals = {}
     for line in open(p):
-        if line.strip().startswith("traffic_bytes_per_launch:"):
-            try:
-                return int(line.split(":", 1)[1].strip())
-            except ValueError:
-                return None
-    return None
+        k, sep, v = line.strip().partition(":")
+        if sep and k in ("traffic_bytes_per_launch", "source_sha256_16"):
+            vals[k] = v.strip()
+    now = traversal_source_sha()
+    if vals.get("source_sha256_16") != now:
+        return None, ("stale: %s was captured from traversal sources %s, the current ones hash to %s"
+                      % (TRAFFIC_PROFILE, vals.get("source_sha256_16", "(unrecorded)"), now))
+    try:
+        return int(vals["traffic_bytes_per_launch"]), "%s (ncu dram__bytes_read.sum + dram__bytes_write.sum, " \
+            "traversal sources %s)" % (TRAFFIC_PROFILE, now)
+    except (KeyError, ValueError):
+        return None, "no traffic_bytes_per_launch line in %s" % TRAFFIC_PROFILE
 
 
 class ClockSampler:
@@ -277,71 +312,111 @@ def cpu_baseline(verts, perm, rays, sample, seed=7):
                       "intersect(), %d host threads, %.1f s" % (sub.shape[0], seed, nth, dt)}
 
 
-def bench_batched(ctx, n_scenes=64, size=512, spp=64, depth=6, samples=8):
+class Checks:
+    """Correctness checks of the workloads: every check is recorded, and a
+    failed one makes bench.py exit with status 1 after printing its line."""
+
+    def __init__(self):
+        self.names, self.failures = [], []
+
+    def add(self, name, ok):
+        self.names.append(name)
+        if not bool(ok):
+            self.failures.append(name)
+        return bool(ok)
+
+    def summary(self):
+        return {"checks": len(self.names), "passed": len(self.names) - len(self.failures),
+                "failures": self.failures}
+
+
+def cpu_build_baseline(V, gpu_perm):
+    """The oracle's NMH build (C++ restatement of rebuilder.cu's algorithm,
+    one host thread) of the whole soup, timed; its permutation must equal the
+    GPU's."""
+    import oracle
+    t0 = time.perf_counter()
+    perm, levels = oracle.nmh_build(V)
+    dt = time.perf_counter() - t0
+    return {"ms": dt * 1e3, "mtris_per_s": V.shape[0] / dt / 1e6, "cores": 1, "kind": "port",
+            "sample": "the whole %d-triangle soup, %d levels, oracle C++ restatement, 1 host thread" % (V.shape[0], levels),
+            "equal": bool(np.array_equal(perm, gpu_perm))}
+
+
+def _render_rate(n_samples, ms):
+    return n_samples / (ms * 1e-3)
+
+
+def _rmse(a, ref):
+    return float(((a[..., :3].double() - ref[..., :3].double()) ** 2).mean().sqrt())
+
+
+def bench_batched(ctx, checks, n_scenes=64, size=512, spp=64, depth=6, loop_samples=8, rmse_scene=0,
+                  ref_spp=4096):
     """Batched workload: 64 sphere scenes (1k-500k triangles each), 512x512,
-    64 spp, depth 6, path mode; samples [0, 8) of the 64 are rendered three
-    ways, timed with CUDA events, and the frames must be identical:
-      * the plain path as the reference structures it
-        (render/monteCarloRaytracer.cpp:81-120): per scene and sample,
-        generate rays, the megakernel over 65,536-ray tiles, draw pixels;
+    64 spp, depth 6, path mode, all 64 samples of every scene timed with CUDA
+    events in two forms whose frames must be identical:
       * this library's fused plain renderer (one aur_render per scene, all
-        samples of a scene in one launch);
-      * the wavefront batch (one graph launch for all scenes)."""
+        samples of a scene in one launch), the plain GPU path;
+      * the wavefront batch (one graph launch for all scenes).
+    `speedup` is wavefront over fused plain. Beside them, the plain path as
+    the reference structures it (render/monteCarloRaytracer.cpp:81-120: per
+    scene and sample, generate rays, the megakernel over 65,536-ray tiles,
+    draw pixels) on samples [0, loop_samples), with its frames checked
+    against the fused renderer's at that sample count. RMSE: the 64-spp
+    frames of scene `rmse_scene` from both forms against a `ref_spp`-spp
+    render of that scene (seed 1)."""
     import torch
     from aurora_gb300 import api, scenes, types as T
     sds = [scenes.sphere_scene(i) for i in range(n_scenes)]
     scs = [api.Scene(ctx, sd) for sd in sds]
-    prm = [T.render_params(size, size, spp, depth, seed=0, mode=T.MODE_PATH, sample_end=samples, scene_id=i)
-           for i in range(n_scenes)]
-    n_samples = n_scenes * size * size * samples
+    prm = [T.render_params(size, size, spp, depth, seed=0, mode=T.MODE_PATH, scene_id=i) for i in range(n_scenes)]
+    n_samples = n_scenes * size * size * spp
     stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     frames = [torch.zeros((size, size, 4), dtype=torch.float32, device="cuda") for _ in range(n_scenes)]
 
-    def plain():
-        for sc, p, f in zip(scs, prm, frames):
-            sc.render(p, accum=f)
-
-    plain()                                   # warm-up
+    scs[0].render(T.render_params(size, size, spp, depth, seed=0, mode=T.MODE_PATH, sample_end=1))   # warm-up
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for f in frames:
-        f.zero_()
     e0.record(stream)
-    plain()
+    for sc, p, f in zip(scs, prm, frames):
+        sc.render(p, accum=f)
     e1.record(stream)
     torch.cuda.synchronize()
     plain_ms = e0.elapsed_time(e1)
-    plain_img = [f.clone() for f in frames]
+    plain_img = frames
 
+    # the reference-structured loop on samples [0, loop_samples)
     tile = 65536
     rays_b = torch.empty((size * size * 9,), dtype=torch.float32, device="cuda")     # aur_path_ray, 36 B
     hits_b = torch.empty((size * size * 12,), dtype=torch.float32, device="cuda")    # aur_hitpoint, 48 B
-
-    def plain_tiles(k):
-        for sc, p, f in zip(scs[:k], prm[:k], frames[:k]):
-            for smp in range(samples):
-                api.generate_rays(ctx, size, size, smp, spp, sc.data.camera, rays_b, hits_b)
-                for off in range(0, size * size, tile):
-                    api.raytrace_monte_carlo(ctx, sc, p, smp, off, min(tile, size * size - off), rays_b, hits_b)
-                api.draw_pixels(ctx, size, size, 1.0 / spp, hits_b, f)
-
-    plain_tiles(1)                            # warm-up
+    loop_frames = [torch.zeros((size, size, 4), dtype=torch.float32, device="cuda") for _ in range(n_scenes)]
     torch.cuda.synchronize()
-    for f in frames:
-        f.zero_()
     e0.record(stream)
-    plain_tiles(n_scenes)
+    for sc, p, f in zip(scs, prm, loop_frames):
+        for smp in range(loop_samples):
+            api.generate_rays(ctx, size, size, smp, spp, sc.data.camera, rays_b, hits_b)
+            for off in range(0, size * size, tile):
+                api.raytrace_monte_carlo(ctx, sc, p, smp, off, min(tile, size * size - off), rays_b, hits_b)
+            api.draw_pixels(ctx, size, size, 1.0 / spp, hits_b, f)
     e1.record(stream)
     torch.cuda.synchronize()
-    tiles_ms = e0.elapsed_time(e1)
-    tiles_same = all(torch.equal(a, b) for a, b in zip(frames, plain_img))
+    loop_ms = e0.elapsed_time(e1)
     del rays_b, hits_b
+    loop_same = True
+    for i in (0, n_scenes - 1):
+        part = scs[i].render(T.render_params(size, size, spp, depth, seed=0, mode=T.MODE_PATH, scene_id=i,
+                                             sample_end=loop_samples))
+        loop_same = loop_same and bool(torch.equal(part, loop_frames[i]))
+    del loop_frames
+    checks.add("batch: the reference-structured loop's frames equal the fused renderer's", loop_same)
+
     t0 = time.perf_counter()
     tuning, tune_ms = api.autotune(ctx, scs, prm)
     tune_s = time.perf_counter() - t0
     batch = api.Batch(ctx, scs, prm, tuning=tuning)
     wf = [torch.zeros_like(f) for f in frames]
-    batch.render(wf)
+    batch.render(wf)                                     # warm-up (graph upload)
     batch.status()
     for f in wf:
         f.zero_()
@@ -351,24 +426,45 @@ def bench_batched(ctx, n_scenes=64, size=512, spp=64, depth=6, samples=8):
     iters = batch.status()
     wf_ms = e0.elapsed_time(e1)
     ext, shadow, _ = batch.counters()
+    batch.close()
     same = all(torch.equal(a, b) for a, b in zip(wf, plain_img))
+    checks.add("batch: wavefront frames equal the fused renderer's (64 scenes, 64 spp)", same)
+
+    # RMSE against a high-spp frame of one scene
+    rp = T.render_params(size, size, ref_spp, depth, seed=1, mode=T.MODE_PATH, scene_id=rmse_scene)
+    rb = api.Batch(ctx, [scs[rmse_scene]], [rp], tuning=tuning)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ref = rb.render()[0]
+    rb.status()
+    ref_s = time.perf_counter() - t0
+    rb.close()
+    rmse_plain, rmse_wf = _rmse(plain_img[rmse_scene], ref), _rmse(wf[rmse_scene], ref)
+    checks.add("batch: equal RMSE of plain and wavefront", rmse_plain == rmse_wf)
     tris = [sd.count for sd in sds]
-    return {"workload": "%d sphere scenes (%d-%d triangles, %d total), %dx%d, %d spp, depth %d, path mode; "
-                        "samples [0, %d) timed" % (n_scenes, min(tris), max(tris), sum(tris), size, size, spp, depth,
-                                                   samples),
-            "plain_reference_loop_samples_per_s": n_samples / (tiles_ms * 1e-3), "plain_reference_loop_ms": tiles_ms,
-            "plain_reference_loop_launches": n_scenes * samples * (2 + (size * size + tile - 1) // tile),
-            "plain_samples_per_s": n_samples / (plain_ms * 1e-3), "plain_ms": plain_ms,
-            "wavefront_samples_per_s": n_samples / (wf_ms * 1e-3), "wavefront_ms": wf_ms,
-            "speedup_vs_reference_loop": tiles_ms / wf_ms, "speedup": plain_ms / wf_ms,
-            "frames_identical": bool(same and tiles_same), "equal_rmse": bool(same and tiles_same),
+    return {"workload": "%d sphere scenes (%d-%d triangles, %d total), %dx%d, %d spp, depth %d, path mode; all "
+                        "samples timed" % (n_scenes, min(tris), max(tris), sum(tris), size, size, spp, depth),
+            "plain_samples_per_s": _render_rate(n_samples, plain_ms), "plain_ms": plain_ms,
+            "wavefront_samples_per_s": _render_rate(n_samples, wf_ms), "wavefront_ms": wf_ms,
+            "speedup": plain_ms / wf_ms,
+            "target": "wavefront >= 5x the plain GPU path (fused renderer)",
+            "target_met": plain_ms / wf_ms >= 5.0,
+            "plain_reference_loop": {"samples": "[0, %d) of %d" % (loop_samples, spp),
+                                     "samples_per_s": _render_rate(n_scenes * size * size * loop_samples, loop_ms),
+                                     "ms": loop_ms, "launches": n_scenes * loop_samples *
+                                     (2 + (size * size + tile - 1) // tile)},
+            "speedup_vs_reference_loop": _render_rate(n_samples, wf_ms) /
+                                         _render_rate(n_scenes * size * size * loop_samples, loop_ms),
+            "frames_identical": bool(same),
+            "rmse": {"scene": rmse_scene, "reference": "%dx%d at %d spp (seed 1, wavefront, %.1f s)"
+                     % (size, size, ref_spp, ref_s), "spp": spp, "plain": rmse_plain, "wavefront": rmse_wf},
             "wavefront_graph_launches": 1, "wavefront_iterations": iters,
             "wavefront_rays": {"closest": ext, "shadow": shadow,
                                "mrays_per_s": (ext + shadow) / (wf_ms * 1e-3) / 1e6},
             "tuning": {k: int(tuning[k]) for k in tuning.dtype.names}, "autotune_s": tune_s}
 
 
-def bench_cornell(ctx, cpu=True, textured=False):
+def bench_cornell(ctx, checks, cpu=True, textured=False):
     """Cornell workload: 34 triangles, 256x256, 16 spp, depth 4, seed 0, path
     mode: plain GPU render vs the oracle on all host cores. textured: the
     floor, back wall and short box use textured shaders (two RGBA8 images,
@@ -406,8 +502,10 @@ def bench_cornell(ctx, cpu=True, textured=False):
         out["cpu_samples_per_s"] = 256 * 256 * 16 / dt
         out["cpu_cores"] = os.cpu_count()
         g = img.cpu().numpy()
-        out["matches_oracle"] = bool(np.all(np.abs(g - ref) <= 1e-4 * np.abs(ref) + 1e-7))
-        out["bit_exact"] = bool(np.array_equal(g, ref))
+        out["matches_oracle"] = checks.add("Cornell%s frame within 1e-4 of the oracle" % (" textured" if textured else ""),
+                                           np.all(np.abs(g - ref) <= 1e-4 * np.abs(ref) + 1e-7))
+        out["bit_exact"] = checks.add("Cornell%s frame bit-exact with the oracle" % (" textured" if textured else ""),
+                                      np.array_equal(g, ref))
         if not textured:
             # path-sampling roofline: per sample, 72 B per node fetch of the
             # reference algorithm (closest and any hit), 36 B of normals and an
@@ -486,7 +584,7 @@ def bench_filter(ctx, width=3840, height=2160, reps=20):
             "frac_of_hbm_peak": gbs / peak}
 
 
-def bench_adjoint(ctx, size=256, spp=64, depth=4):
+def bench_adjoint(ctx, checks, size=256, spp=64, depth=4):
     """Differentiable workload: Cornell box + 4096-triangle sphere, one shader
     per triangle (albedo U[0.2, 0.8]), 256x256, 64 spp, depth 4; L2 loss
     against the frame rendered at albedo + N(0, 0.05). grad/fwd = adjoint
@@ -526,7 +624,7 @@ def bench_adjoint(ctx, size=256, spp=64, depth=4):
         d = sc.render(p).double() - target.double()
         return float((d[..., :3] ** 2).sum())
 
-    checks = []
+    fd_checks = []
     for k in list(np.argsort(-np.abs(g).ravel())[:2]):
         i, c = int(k // 3), int(k % 3)
         vals = []
@@ -537,20 +635,29 @@ def bench_adjoint(ctx, size=256, spp=64, depth=4):
             vals.append(loss())
         sc.set_shaders(sd.shaders)
         fd = (vals[0] - vals[1]) / 2e-3
-        checks.append({"shader": i, "channel": c, "adjoint": float(g[i, c]), "fd": fd,
-                       "rel_err": abs(float(g[i, c]) - fd) / abs(fd)})
+        fd_checks.append({"shader": i, "channel": c, "adjoint": float(g[i, c]), "fd": fd,
+                          "rel_err": abs(float(g[i, c]) - fd) / abs(fd)})
+        checks.add("adjoint d/d(albedo[%d][%d]) within 1e-3 of central differences" % (i, c),
+                   abs(float(g[i, c]) - fd) <= 1e-3 * abs(fd) + 1e-6)
     return {"workload": "Cornell box + 4096-triangle sphere (4130 per-triangle shaders), %dx%d, %d spp, depth %d, "
                         "path mode, L2 loss" % (size, size, spp, depth),
-            "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "grad_over_fwd": adj_ms / fwd_ms, "fd_checks": checks}
+            "forward_ms": fwd_ms, "adjoint_ms": adj_ms, "grad_over_fwd": adj_ms / fwd_ms, "fd_checks": fd_checks}
 
 
-def bench_terrain(ctx, res=2048, samples=1, ref_spp=16384, small=(64, 36), small_spp=64):
+def bench_terrain(ctx, checks, res=2048, samples=16, ref_seed=1, crop=(64, 36), cpu=True):
     """Large workload: 2048x2048-vertex fBm heightfield (8,380,418 triangles),
-    16 area lights, 1920x1080, 256 spp, depth 8, path mode. Times the NMH
-    build, then plain vs wavefront on samples [0, `samples`) of the 256 (the
-    frames must be identical). RMSE: both forms render a small (64x36) crop
-    of the same camera at 64 spp and are compared with a 16384-spp render of
-    that crop."""
+    16 area lights, 1920x1080, 256 spp, depth 8, path mode, full frame.
+      * NMH build of the terrain (warm, CUDA events);
+      * plain GPU path (fused renderer) and wavefront on samples [0, `samples`)
+        of the 256, timed; the frames must be identical;
+      * the wavefront renders all 256 samples of the frame with seed
+        `ref_seed` (independent of the timed seed 0), timed: the workload at
+        its full sample count, and the reference image for the RMSE of the
+        timed frames;
+      * the reference-structured loop (65,536-ray megakernel tiles) on sample 0;
+      * CPU baseline: the oracle renders a `crop` of the same camera at 1 spp
+        on all host cores (a bounded sample of the workload), and the GPU's
+        render of that crop must equal it bit for bit."""
     import torch
     from aurora_gb300 import api, scenes, types as T
     t0 = time.perf_counter()
@@ -561,44 +668,47 @@ def bench_terrain(ctx, res=2048, samples=1, ref_spp=16384, small=(64, 36), small
     sc = api.Scene(ctx, sd)
     torch.cuda.synchronize()
     scene_s = time.perf_counter() - t0
-    Vd = torch.from_numpy(sd.vertices.reshape(-1)).cuda()
-    api.Nmh(ctx, Vd, count=sd.count)
-    torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    api.Nmh(ctx, Vd, count=sd.count)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    build_ms = e0.elapsed_time(e1)
+    Vd = torch.from_numpy(sd.vertices.reshape(-1)).cuda()
+    build = []
+    for _ in range(3):                                 # the third build replays the recorded graph
+        e0.record(stream)
+        api.Nmh(ctx, Vd, count=sd.count).close()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        build.append(e0.elapsed_time(e1))
     del Vd
-    W, H = 1920, 1080
-    p = T.render_params(W, H, 256, 8, seed=0, mode=T.MODE_PATH, sample_end=samples)
-    sc.render(T.render_params(W, H, 256, 8, seed=0, mode=T.MODE_PATH, sample_end=1))     # warm-up
+    W, H, spp, depth = 1920, 1080, 256, 8
+    p = T.render_params(W, H, spp, depth, seed=0, mode=T.MODE_PATH, sample_end=samples)
+    sc.render(T.render_params(W, H, spp, depth, seed=0, mode=T.MODE_PATH, sample_end=1))     # warm-up
     torch.cuda.synchronize()
     e0.record(stream)
     plain = sc.render(p)
     e1.record(stream)
     torch.cuda.synchronize()
     plain_ms = e0.elapsed_time(e1)
-    # the plain path as the reference structures it: generate, 65,536-ray
-    # megakernel tiles, draw (render/monteCarloRaytracer.cpp:81-120)
+    # the plain path as the reference structures it, sample 0: generate,
+    # 65,536-ray megakernel tiles, draw (render/monteCarloRaytracer.cpp:81-120)
     tile = 65536
     rays_b = torch.empty((W * H * 9,), dtype=torch.float32, device="cuda")
     hits_b = torch.empty((W * H * 12,), dtype=torch.float32, device="cuda")
     loop_img = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
     e0.record(stream)
-    for smp in range(samples):
-        api.generate_rays(ctx, W, H, smp, 256, sd.camera, rays_b, hits_b)
-        for off in range(0, W * H, tile):
-            api.raytrace_monte_carlo(ctx, sc, p, smp, off, min(tile, W * H - off), rays_b, hits_b)
-        api.draw_pixels(ctx, W, H, 1.0 / 256, hits_b, loop_img)
+    api.generate_rays(ctx, W, H, 0, spp, sd.camera, rays_b, hits_b)
+    for off in range(0, W * H, tile):
+        api.raytrace_monte_carlo(ctx, sc, p, 0, off, min(tile, W * H - off), rays_b, hits_b)
+    api.draw_pixels(ctx, W, H, 1.0 / spp, hits_b, loop_img)
     e1.record(stream)
     torch.cuda.synchronize()
     loop_ms = e0.elapsed_time(e1)
-    loop_same = bool(torch.equal(loop_img, plain))
+    p1 = T.render_params(W, H, spp, depth, seed=0, mode=T.MODE_PATH, sample_end=1)
+    checks.add("terrain: the reference-structured loop's frame equals the fused renderer's",
+               torch.equal(loop_img, sc.render(p1)))
     del rays_b, hits_b, loop_img
+    t0 = time.perf_counter()
     tuning, _ = api.autotune(ctx, [sc], [p])
+    tune_s = time.perf_counter() - t0
     batch = api.Batch(ctx, [sc], [p], tuning=tuning)
     batch.render()
     batch.status()
@@ -608,51 +718,59 @@ def bench_terrain(ctx, res=2048, samples=1, ref_spp=16384, small=(64, 36), small
     batch.status()
     wf_ms = e0.elapsed_time(e1)
     ext, shadow, iters = batch.counters()
-    same = bool(torch.equal(wf, plain))
     batch.close()
-    # RMSE at equal spp against a 16384-spp reference of a small frame
-    sw, sh = small
-    cam = sd.camera
-    ref = sc.render(T.render_params(sw, sh, ref_spp, 8, seed=1, mode=T.MODE_PATH), camera=cam)
-    ps = T.render_params(sw, sh, small_spp, 8, seed=0, mode=T.MODE_PATH)
-    pl = sc.render(ps, camera=cam)
-    b2 = api.Batch(ctx, [sc], [ps], cameras=[cam])
-    wfs = b2.render()[0]
-    b2.status()
-
-    def rmse(a):
-        return float(torch.sqrt(((a[..., :3].double() - ref[..., :3].double()) ** 2).mean()))
-
-    # CPU baseline on a bounded sample of the workload: the oracle renders the
-    # small crop at 1 spp on all host cores (the GPU's NMH permutation, equal
-    # to the oracle's own build, saves the host build of 8.4M triangles); the
-    # GPU's image of the same crop must be bit-identical
-    import oracle
-    ns = oracle.NmhScene(sd, perm=sc.nmh.export(with_vertices=False)[0])
-    pc = T.render_params(sw, sh, 1, 8, seed=0, mode=T.MODE_PATH)
-    nth = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    cimg, _ = oracle.render(ns, pc, camera=cam, nthreads=nth)
-    cpu_s = time.perf_counter() - t0
-    cpu_exact = bool(np.array_equal(sc.render(pc, camera=cam).cpu().numpy(), cimg))
-
+    same = checks.add("terrain: wavefront frame equals the fused renderer's (1920x1080, %d spp)" % samples,
+                      torch.equal(wf, plain))
+    # all 256 samples, seed ref_seed: the full workload, and the RMSE reference
+    pf = T.render_params(W, H, spp, depth, seed=ref_seed, mode=T.MODE_PATH)
+    fb = api.Batch(ctx, [sc], [pf], tuning=tuning)
+    e0.record(stream)
+    ref = fb.render()[0]
+    e1.record(stream)
+    fb.status()
+    full_ms = e0.elapsed_time(e1)
+    full_rays = fb.counters()
+    fb.close()
+    rmse_plain, rmse_wf = _rmse(plain, ref), _rmse(wf, ref)
+    checks.add("terrain: equal RMSE of plain and wavefront", rmse_plain == rmse_wf)
     n_samples = W * H * samples
-    return {"workload": "fBm terrain %dx%d vertices (%d triangles), 16 area lights, %dx%d, 256 spp, depth 8, path mode; "
-                        "samples [0, %d) timed" % (res, res, sd.count, W, H, samples),
-            "generate_s": gen_s, "scene_upload_and_build_s": scene_s, "nmh_build_ms": build_ms,
-            "plain_reference_loop_samples_per_s": n_samples / (loop_ms * 1e-3), "plain_reference_loop_ms": loop_ms,
-            "plain_samples_per_s": n_samples / (plain_ms * 1e-3), "plain_ms": plain_ms,
-            "wavefront_samples_per_s": n_samples / (wf_ms * 1e-3), "wavefront_ms": wf_ms,
-            "speedup_vs_reference_loop": loop_ms / wf_ms, "speedup": plain_ms / wf_ms,
-            "frames_identical": same and loop_same,
-            "tuning": {k: int(tuning[k]) for k in tuning.dtype.names},
-            "wavefront_rays": {"closest": ext, "shadow": shadow, "iterations": iters,
-                               "mrays_per_s": (ext + shadow) / (wf_ms * 1e-3) / 1e6},
-            "rmse": {"reference": "%dx%d at %d spp (seed 1)" % (sw, sh, ref_spp), "spp": small_spp,
-                     "plain": rmse(pl), "wavefront": rmse(wfs)},
-            "cpu_baseline": {"samples_per_s": sw * sh / cpu_s, "cores": nth, "kind": "port",
-                             "sample": "%dx%d crop of the same camera, 1 spp, depth 8, oracle C++ restatement" % (sw, sh),
-                             "gpu_bit_exact": cpu_exact}}
+    out = {"workload": "fBm terrain %dx%d vertices (%d triangles), 16 area lights, %dx%d, %d spp, depth %d, path mode, "
+                       "full frame; plain and wavefront timed on samples [0, %d), the wavefront also on all %d"
+                       % (res, res, sd.count, W, H, spp, depth, samples, spp),
+           "generate_s": gen_s, "scene_upload_and_build_s": scene_s, "nmh_build_ms": build[-1],
+           "nmh_build_mtris_per_s": sd.count / (build[-1] * 1e-3) / 1e6,
+           "plain_samples_per_s": _render_rate(n_samples, plain_ms), "plain_ms": plain_ms,
+           "wavefront_samples_per_s": _render_rate(n_samples, wf_ms), "wavefront_ms": wf_ms,
+           "speedup": plain_ms / wf_ms, "target": "wavefront >= 5x the plain GPU path (fused renderer)",
+           "target_met": plain_ms / wf_ms >= 5.0,
+           "wavefront_full_spp": {"spp": spp, "ms": full_ms, "samples_per_s": _render_rate(W * H * spp, full_ms),
+                                  "closest_rays": full_rays[0], "shadow_rays": full_rays[1]},
+           "plain_reference_loop": {"samples": "[0, 1) of %d" % spp, "ms": loop_ms,
+                                    "samples_per_s": _render_rate(W * H, loop_ms)},
+           "speedup_vs_reference_loop": _render_rate(n_samples, wf_ms) / _render_rate(W * H, loop_ms),
+           "frames_identical": same,
+           "tuning": {k: int(tuning[k]) for k in tuning.dtype.names}, "autotune_s": tune_s,
+           "wavefront_rays": {"closest": ext, "shadow": shadow, "iterations": iters,
+                              "mrays_per_s": (ext + shadow) / (wf_ms * 1e-3) / 1e6},
+           "rmse": {"reference": "the full %dx%d frame at %d spp, seed %d (wavefront)" % (W, H, spp, ref_seed),
+                    "spp": samples, "plain": rmse_plain, "wavefront": rmse_wf}}
+    if cpu:
+        import oracle
+        sw, sh = crop
+        cam = sd.camera
+        ns = oracle.NmhScene(sd, perm=sc.nmh.export(with_vertices=False)[0])
+        pc = T.render_params(sw, sh, 1, depth, seed=0, mode=T.MODE_PATH)
+        nth = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        cimg, _ = oracle.render(ns, pc, camera=cam, nthreads=nth)
+        cpu_s = time.perf_counter() - t0
+        exact = checks.add("terrain: GPU crop bit-exact with the oracle",
+                           np.array_equal(sc.render(pc, camera=cam).cpu().numpy(), cimg))
+        out["cpu_baseline"] = {"samples_per_s": sw * sh / cpu_s, "cores": nth, "kind": "port",
+                               "sample": "%dx%d frame of the same camera, 1 spp, depth 8, oracle C++ restatement "
+                                         "(the GPU's NMH permutation, equal to the oracle's build)" % (sw, sh),
+                               "gpu_bit_exact": exact}
+    return out
 
 
 def run_reference(args):
@@ -701,8 +819,9 @@ def main():
     if args.terrain:
         from aurora_gb300 import api, build as abuild
         abuild.build()
-        print(json.dumps({"terrain": bench_terrain(api.Context(0))}), flush=True)
-        return
+        checks = Checks()
+        print(json.dumps({"terrain": bench_terrain(api.Context(0), checks), "parity": checks.summary()}), flush=True)
+        sys.exit(1 if checks.failures else 0)
     import torch
     rank, world, local = dist_env()
     if world > 1:
@@ -785,28 +904,38 @@ def main():
 
     peak, peak_kind = load_peaks()
     wc = work["closest"]
-    alg_bytes = (N_RAYS * (RAY_IN_BYTES + HIT_OUT_BYTES) + SLAB_BYTES * wc["node_fetches"] +
+    own_bytes = (N_RAYS * (RAY_IN_BYTES + HIT_OUT_BYTES) + SLAB_BYTES * wc["node_fetches"] +
                  TRI_BYTES * wc["slab_crossings"] + BOX_BYTES * wc["box_loads"])
-    ref_bytes = N_RAYS * (RAY_IN_BYTES + HIT_OUT_BYTES) + NODE_BYTES * visits_closest
+    ref_bytes = N_RAYS * (REF_RAY_IN_BYTES + HIT_OUT_BYTES) + NODE_BYTES * visits_closest
     avg_launch_s = statistics.mean(launch_ms) * 1e-3
-    achieved = alg_bytes / avg_launch_s / 1e9
+    achieved = ref_bytes / avg_launch_s / 1e9
+    traffic, traffic_source = load_traffic()
     clocks = clk.summary()
     out = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "triangles": N_TRIS, "rays": N_RAYS, "nmh_levels": nmh.info()[1],
-                   "l2": "inputs larger than L2: 512 MiB of rays streamed per step; the 40 MB of node records "
+                   "l2": "inputs larger than L2: 512 MiB of rays streamed per step; the 64 MB of node records "
                          "stay L2-resident as in any traversal",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": load_traffic(), "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                     "algorithmic_bytes_per_launch": alg_bytes,
-                     "node_fetches_per_ray": wc["node_fetches"] / N_RAYS,
-                     "slab_crossings_per_ray": wc["slab_crossings"] / N_RAYS,
+                     "traffic": traffic, "traffic_source": traffic_source,
+                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "definition": "reference algorithm bytes per launch: 24 B ray in + 16 B hit out + 72 B per node "
+                                   "the reference's intersect() visits (counted by this traversal without box "
+                                   "pruning), divided by the average CUDA-event time of a launch",
+                     "algorithmic_bytes_per_launch": ref_bytes,
                      "reference_node_visits_per_ray": visits_closest / N_RAYS,
-                     "reference_algorithm_bytes_per_launch": ref_bytes,
-                     "reference_algorithm_GBps": ref_bytes / avg_launch_s / 1e9},
+                     "dram_GBps": traffic / avg_launch_s / 1e9 if traffic else None,
+                     "dram_frac": traffic / avg_launch_s / 1e9 / peak if traffic else None,
+                     "limiter": "instruction issue and the L1 data pipe, not DRAM (see the ncu summary): the 64 MB "
+                                "of node records stay in the 129 MB L2, so the algorithmic bytes are served by "
+                                "L1/L2 and their rate can exceed the HBM copy peak",
+                     "traversal_reads_bytes_per_launch": own_bytes,
+                     "traversal_reads_GBps": own_bytes / avg_launch_s / 1e9,
+                     "node_fetches_per_ray": wc["node_fetches"] / N_RAYS,
+                     "slab_crossings_per_ray": wc["slab_crossings"] / N_RAYS},
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 32,
                 "d2h_bytes_per_step": N_RAYS * 16, "matches_device_result": bool(same)},
         "gpu_launches": args.steps,
@@ -814,23 +943,40 @@ def main():
         "any_hit": {"value": world * N_RAYS / (any_ms * 1e-3) / 1e6, "unit": "Mrays/s", "ms_per_step": any_ms,
                     "node_fetches_per_ray": work["any"]["node_fetches"] / N_RAYS,
                     "reference_node_visits_per_ray": visits_any / N_RAYS},
-        "nmh_build_ms": build_ms, "nmh_build_mtris_per_s": N_TRIS / (build_ms * 1e-3) / 1e6,
     }
+    checks = Checks()
+    checks.add("e2e hits equal the device-resident hits", same)
+    levels = nmh.info()[1]
+    build_bytes = NMH_LEVEL_BYTES * V.shape[0] * levels
+    out["nmh_build"] = {
+        "workload": "NMH build of the same 1M-triangle soup (%d levels), warm (graph replay), host wall time of "
+                    "the whole aur_nmh_build call, median of 5" % levels,
+        "ms": build_ms, "mtris_per_s": N_TRIS / (build_ms * 1e-3) / 1e6,
+        "roofline": {"bound": "hbm", "achieved": build_bytes / (build_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": build_bytes / (build_ms * 1e-3) / 1e9 / peak, "algorithmic_bytes_per_build": build_bytes,
+                     "definition": "16 B read + 16 B written per triangle per level (key, id, node, permutation)"}}
     if rank == 0 and not args.no_cpu_baseline:
         perm, verts = nmh.export()
         out["cpu_baseline"] = cpu_baseline(verts, perm, rays, args.cpu_sample)
+        out["nmh_build"]["cpu_baseline"] = cpu_build_baseline(V, perm)
+        checks.add("NMH build of the 1M soup equals the oracle's", out["nmh_build"]["cpu_baseline"].pop("equal"))
     if not args.skip_extras:
         del rays_d, hits_d, occ_d
-        out["cornell_plain"] = bench_cornell(ctx, cpu=rank == 0 and not args.no_cpu_baseline)
-        out["cornell_textured"] = bench_cornell(ctx, cpu=rank == 0 and not args.no_cpu_baseline, textured=True)
+        cpu = rank == 0 and not args.no_cpu_baseline
+        out["cornell_plain"] = bench_cornell(ctx, checks, cpu=cpu)
+        out["cornell_textured"] = bench_cornell(ctx, checks, cpu=cpu, textured=True)
         out["filter_pixels"] = bench_filter(ctx)
         out["mis"] = bench_mis(ctx)
-        out["batched_wavefront"] = bench_batched(ctx)
-        out["adjoint"] = bench_adjoint(ctx)
+        out["batched_wavefront"] = bench_batched(ctx, checks)
+        out["adjoint"] = bench_adjoint(ctx, checks)
+        out["terrain"] = bench_terrain(ctx, checks, cpu=cpu)
+    out["parity"] = checks.summary()
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+    if checks.failures:
+        sys.exit(1)
 
 
 if __name__ == "__main__":
