@@ -42,6 +42,34 @@ __device__ __forceinline__ f3 box_inv(const f3& d) {
                1.0f / copysignf(fmaxf(fabsf(d.z), 1e-30f), d.z));
 }
 
+// The two slab distances (a0 / d, a1 / d) of the slab test (ray.cuh:225-237),
+// equal bit for bit to the IEEE divisions. y is the ray's box reciprocal on
+// the axis, which is RN(1/d) whenever |d| >= 1e-30 (box_inv). With
+// y = RN(1/d), q = RN(a * y) is within an ulp of a / d, the remainder
+// a - q * d is exact in one fused multiply-add, and RN(q + remainder * y) is
+// the correctly rounded quotient (P. Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
+// 1990), provided nothing overflows or underflows: that holds when |y| is in
+// [2^-40, 2^40] and the quotient's magnitude is in [2^-59, 2^100], which
+// bounds |a| to [2^-100, 2^140]. Anything else (a zero or NaN quotient, a
+// tiny or huge one, a near axis-parallel ray) takes the IEEE division.
+// Checked against IEEE division on 6e8 pairs spanning subnormal to
+// near-overflow numerators, and by the traversal parity tests.
+__device__ __forceinline__ void slab_div(float a0, float a1, float d, float y, float& q0, float& q1) {
+    float f0 = a0 * y, f1 = a1 * y;
+    f0 = __fmaf_rn(__fmaf_rn(-f0, d, a0), y, f0);
+    f1 = __fmaf_rn(__fmaf_rn(-f1, d, a1), y, f1);
+    const float my = fabsf(y), m0 = fabsf(f0), m1 = fabsf(f1);
+    if (my >= 0x1p-40f && my <= 0x1p40f && m0 >= 0x1p-59f && m0 <= 0x1p100f && m1 >= 0x1p-59f &&
+        m1 <= 0x1p100f) {
+        q0 = f0;
+        q1 = f1;
+    } else {
+        q0 = a0 / d;
+        q1 = a1 / d;
+    }
+}
+
 // Conservative ray/box overlap over (0, tlimit]. poi = pos * inv per axis, so
 // each slab distance is one fused multiply-add, (lo * inv - poi); its
 // rounding, like that of (lo - pos) * inv, is far inside the box padding and
@@ -105,8 +133,8 @@ __device__ __forceinline__ void trav_init(TravState& s) {
 // traversal is exhausted; otherwise s0 holds the node's first record sector
 // (words 0 and 1) and nlo/nhi its clipped range.
 __device__ __forceinline__ bool trav_next(TravState& s, const float4* __restrict__ recs, uint32_t nodes, const f3& pos,
-                                          const f3& dir, float best_t, const StackRef& stk, Sector& s0, float& nlo,
-                                          float& nhi, uint32_t& visits) {
+                                          const f3& dir, const f3& inv, float best_t, const StackRef& stk, Sector& s0,
+                                          float& nlo, float& nhi, uint32_t& visits) {
     for (;;) {
         if (s.k < nodes) {
             ++visits;
@@ -114,8 +142,8 @@ __device__ __forceinline__ bool trav_next(TravState& s, const float4* __restrict
             const float4& q0 = s0.a;
             const float p = sel3(s.a, pos.x, pos.y, pos.z);
             const float d = sel3(s.a, dir.x, dir.y, dir.z);
-            const float d0 = (q0.x - p) / d;
-            const float d1 = (q0.y - p) / d;
+            float d0, d1;
+            slab_div(q0.x - p, q0.y - p, d, sel3(s.a, inv.x, inv.y, inv.z), d0, d1);
             nlo = fmaxf(fminf(d0, d1), s.lo);
             nhi = fminf(fmaxf(d0, d1), s.hi);
             if (nlo <= nhi && nlo <= best_t) return true;
@@ -224,7 +252,7 @@ __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ recs, ui
     Sector s0;
     float4 q5;
     float nlo, nhi;
-    while (trav_next(s, recs, nodes, pos, dir, best_t, stk, s0, nlo, nhi, visits)) {
+    while (trav_next(s, recs, nodes, pos, dir, inv, best_t, stk, s0, nlo, nhi, visits)) {
         if (node_triangles<kAny>(recs, s.k, s0, perm, pos, dir, best_t, bu, bv, best, q5)) return best;
         trav_descend(s, recs, q5, pos, dir, inv, best_t, nodes, stk, nlo, nhi);
     }

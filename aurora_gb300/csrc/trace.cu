@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restric
         float4 q5;
         float nlo, nhi;
         bool done;
-        if (trav_next(s, recs, nodes, pos, dir, best_t, stk, s0, nlo, nhi, visits)) {
+        if (trav_next(s, recs, nodes, pos, dir, inv, best_t, stk, s0, nlo, nhi, visits)) {
             if (kCount) {
                 ++crossings;
                 inner += 2 * s.k + 1 < nodes;

@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_extend(WfArgs a) {
         Sector s0;
         float4 q5;
         float nlo, nhi;
-        if (trav_next(s, recs, nodes, pos, dir, best_t, stk, s0, nlo, nhi, visits)) {
+        if (trav_next(s, recs, nodes, pos, dir, inv, best_t, stk, s0, nlo, nhi, visits)) {
             node_triangles<false>(recs, s.k, s0, perm, pos, dir, best_t, bu, bv, best, q5);
             trav_descend(s, recs, q5, pos, dir, inv, best_t, nodes, stk, nlo, nhi);
         } else {
@@ -544,7 +544,7 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shadow(WfArgs a) {
         float4 q5;
         float nlo, nhi;
         bool done;
-        if (trav_next(s, recs, nodes, pos, dir, tmax, stk, s0, nlo, nhi, visits)) {
+        if (trav_next(s, recs, nodes, pos, dir, inv, tmax, stk, s0, nlo, nhi, visits)) {
             done = node_triangles<true>(recs, s.k, s0, perm, pos, dir, tmax, bu, bv, best, q5);
             if (!done) trav_descend(s, recs, q5, pos, dir, inv, tmax, nodes, stk, nlo, nhi);
         } else {
