@@ -80,7 +80,7 @@ SIGNATURES = {
     "aur_batch_tuning": ([P, P], ctypes.c_int),
     "aur_batch_destroy": ([P], ctypes.c_int),
     "aur_batch_autotune": ([P, P, P, P, U32, P, P], ctypes.c_int),
-    "aur_render_adjoint": ([P, P, P, P, P, P, P], ctypes.c_int),
+    "aur_render_adjoint": ([P, P, P, P, P, P, P, P], ctypes.c_int),
     "aur_batch_profile": ([P, P, P, P], ctypes.c_int),
     "aur_batch_counters": ([P, P, P], ctypes.c_int),
     "aur_transform": ([P, P, P, U32, P, U32, P, P], ctypes.c_int),
@@ -341,18 +341,24 @@ class Scene:
         check(lib().aur_render(self.ctx.handle, self.handle, _ptr(cam), _ptr(p), _ptr(accum)))
         return accum
 
-    def adjoint(self, params, d_image, d_diffuse=None, d_light=None, camera=None):
-        """Adds dLoss/d(diffuse_color) and dLoss/d(light color) for dLoss/d(image)."""
+    def adjoint(self, params, d_image, d_diffuse=None, d_light=None, camera=None, d_emission=None,
+                emission=False):
+        """Adds dLoss/d(diffuse_color) and dLoss/d(light color) for
+        dLoss/d(image); with emission=True (or a d_emission buffer) also
+        dLoss/d(emission_color), returned third."""
         torch = _torch()
         p = np.asarray(params, T.params_dtype).reshape(())
         if d_diffuse is None:
             d_diffuse = torch.zeros((self.data.shaders.shape[0], 3), dtype=torch.float32, device="cuda")
         if d_light is None:
             d_light = torch.zeros((max(1, self.data.lights.shape[0]), 3), dtype=torch.float32, device="cuda")
+        if emission and d_emission is None:
+            d_emission = torch.zeros((self.data.shaders.shape[0], 3), dtype=torch.float32, device="cuda")
         cam = np.asarray(self.data.camera if camera is None else camera, T.camera_dtype).reshape(())
         check(lib().aur_render_adjoint(self.ctx.handle, self.handle, _ptr(cam), _ptr(p),
-                                       _ptr(_dense(d_image)), _ptr(d_diffuse), _ptr(d_light)))
-        return d_diffuse, d_light
+                                       _ptr(_dense(d_image)), _ptr(d_diffuse), _ptr(d_light),
+                                       _ptr(d_emission) if d_emission is not None else None))
+        return (d_diffuse, d_light, d_emission) if d_emission is not None else (d_diffuse, d_light)
 
     def close(self):
         if self.handle:

@@ -1,7 +1,8 @@
 // adjoint.cu — path-replay backpropagation through the integrator.
 //
-// Gradients of a loss L(image) with respect to every shader's diffuse colour
-// and every light's colour, given dL/dimage. No counterpart in the
+// Gradients of a loss L(image) with respect to every shader's diffuse colour,
+// every shader's emission colour and every light's colour, given dL/dimage.
+// No counterpart in the
 // reference. Method: path replay backpropagation (D. Vicini, S. Speierer,
 // W. Jakob, "Path Replay Backpropagation", ACM TOG 40(4), 2021). For each
 // camera sample the primal pass (aur_integrate.cuh, the same estimator as
@@ -17,6 +18,15 @@
 // D_k / c_k is evaluated directly (f replaced by 1/pi), so the direct part
 // needs no division; the later-vertex part divides by c_k and is skipped for
 // colour channels that are exactly zero.
+// Emission E_s of shader s enters linearly: at every vertex on s as T_k * E_s
+// (times the emission's MIS weight in AUR_MODE_PATH_MIS,
+// monteCarloRaytracer.cu:42), and in AUR_MODE_PATH_MIS through the emitter
+// sample of every vertex, f * E_s * G with G the sample's geometric factor
+// over its density. So
+//   dL/dE_s += g * T_k * w_k  (vertex on s),  g * T_k * f_k * G  (emitter on s, visible).
+// Neither the MIS weights nor the light-selection table depend on E_s: the
+// table weighs triangles by the shader's scalar `emission` times area
+// (emitter.cu's weight), not by its emission colour.
 #include <algorithm>
 #include <vector>
 
@@ -64,18 +74,38 @@ __device__ __forceinline__ void add_diffuse_grad(float* __restrict__ d_diffuse, 
     }
 }
 
+// Adds g to shader si's entry of a per-shader gradient (emission), summed per
+// warp over the lanes that hit the same shader first.
+__device__ __forceinline__ void add_shader_grad(float* __restrict__ d, uint32_t si, const f3& gs) {
+    namespace cg = cooperative_groups;
+    const cg::coalesced_group active = cg::coalesced_threads();
+    const cg::coalesced_group same = cg::labeled_partition(active, si);
+    const float sx = cg::reduce(same, gs.x, cg::plus<float>());
+    const float sy = cg::reduce(same, gs.y, cg::plus<float>());
+    const float sz = cg::reduce(same, gs.z, cg::plus<float>());
+    if (same.thread_rank() == 0 && (sx != 0.0f || sy != 0.0f || sz != 0.0f)) {
+        atomicAdd(d + 3 * si + 0, sx);
+        atomicAdd(d + 3 * si + 1, sy);
+        atomicAdd(d + 3 * si + 2, sz);
+    }
+}
+
 // Direct light at a hit as the primal computes it (direct_light), with its
 // derivatives: Dp receives the direct light per unit Lambert colour, and the
 // light-colour gradients g * thr * d(direct)/d(colour_l) are added (light 0
 // into gl0, the others to d_light). ew: the emission's MIS weight; bounce:
 // whether a diffuse bounce follows the hit (both for AUR_MODE_PATH_MIS).
+// With d_emission, the emission gradients of the hit's own shader si and of
+// the emitter sample's shader are added too.
 template <bool kMis>
 __device__ __forceinline__ f3 direct_grad(const SceneView& sc, const aur_shader* sh, const Bsdf& b, const f3& f,
                                           const f3& position, const f3& wo, float ew, bool bounce, uint32_t seed,
                                           uint32_t scene, uint32_t pixel, uint32_t sample, uint32_t rix, const f3& thr,
                                           const f3& g, float* __restrict__ d_light, f3& gl0, f3& Dp,
-                                          const StackRef& stk, uint32_t& visits, uint32_t* err) {
+                                          float* __restrict__ d_emission, uint32_t si, const StackRef& stk,
+                                          uint32_t& visits, uint32_t* err) {
     f3 Li = kMis ? from(sh->emission_color) * ew : from(sh->emission_color);
+    if (d_emission) add_shader_grad(d_emission, si, kMis ? (g * thr) * ew : g * thr);
     Dp = mk3(0.0f);   // direct light per unit Lambert colour
     for (uint32_t i = 0; i < sc.num_lights; ++i) {
         const aur_light& L = sc.lights[i];
@@ -171,6 +201,7 @@ __device__ __forceinline__ f3 direct_grad(const SceneView& sc, const aur_shader*
                                                    visits, err) == kNoPrim;
         Li = Li + (vis ? ss.c : mk3(0.0f));
         if (vis) Dp = Dp + ss.e * (ss.geo * kInvPi);
+        if (d_emission && vis) add_shader_grad(d_emission, ss.esi, (g * thr) * (f * ss.geo));
     }
     return Li;
 }
@@ -185,8 +216,8 @@ __device__ __forceinline__ f3 direct_grad(const SceneView& sc, const aur_shader*
 template <bool kMis>
 __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, uint32_t seed, uint32_t scene,
                        uint32_t pixel, uint32_t sample, PathRay ray, const StackRef& stk, const f3& C, const f3& g,
-                       float* __restrict__ d_diffuse, float* __restrict__ d_light, f3& gl0, uint32_t& visits,
-                       uint32_t* err) {
+                       float* __restrict__ d_diffuse, float* __restrict__ d_light, float* __restrict__ d_emission,
+                       f3& gl0, uint32_t& visits, uint32_t* err) {
     f3 Lrem = C;
     uint32_t depth = 0;
     for (uint32_t rix = 0;; ++rix) {
@@ -204,7 +235,7 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
         const float ew = kMis ? emission_weight(sc, tri, ray.dir, t, ray.pdf) : 1.0f;
         f3 Dp;
         const f3 Li = direct_grad<kMis>(sc, sh, b, f, position, wo, ew, depth + 1 <= max_depth, seed, scene, pixel,
-                                        sample, rix, thr, g, d_light, gl0, Dp, stk, visits, err);
+                                        sample, rix, thr, g, d_light, gl0, Dp, d_emission, si, stk, visits, err);
         Lrem = Lrem - Li * thr;
         // bounce, as in the primal
         bool cont = false;
@@ -269,8 +300,8 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
 template <bool kMis>
 __device__ void replay_stack(const SceneView& sc, uint32_t max_depth, uint32_t mode, uint32_t seed, uint32_t scene,
                              uint32_t pixel, uint32_t sample, const PathRay& primary, const StackRef& stk,
-                             const f3& g, float* __restrict__ d_diffuse, float* __restrict__ d_light, f3& gl0,
-                             uint32_t& visits, uint32_t* err) {
+                             const f3& g, float* __restrict__ d_diffuse, float* __restrict__ d_light,
+                             float* __restrict__ d_emission, f3& gl0, uint32_t& visits, uint32_t* err) {
     struct Marker {
         f3 col0, c1;          // colour before the subtree, the bouncing vertex's Lambert colour
         const aur_shader* sh;
@@ -320,7 +351,7 @@ __device__ void replay_stack(const SceneView& sc, uint32_t max_depth, uint32_t m
             continue_ray<kMis>(sh, b, cur, position, wo, path, depth, maxd, seed, scene, pixel, sample, rix);
         f3 Dp;
         const f3 Li = direct_grad<kMis>(sc, sh, b, f, position, wo, ew, bounce_follows, seed, scene, pixel, sample, rix,
-                                        cur.thr, g, d_light, gl0, Dp, stk, visits, err);
+                                        cur.thr, g, d_light, gl0, Dp, d_emission, si, stk, visits, err);
         add_diffuse_grad(d_diffuse, si, sh, g * (cur.thr * Dp));
         col = col + Li * cur.thr;
         for (int q = 0; q < kc.n; ++q) {
@@ -375,6 +406,7 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_replay(Sce
                                                             uint32_t nb, const float4* __restrict__ prim,
                                                             const float4* __restrict__ d_image,
                                                             float* __restrict__ d_diffuse, float* __restrict__ d_light,
+                                                            float* __restrict__ d_emission,
                                                             uint32_t* __restrict__ err, int cap) {
     extern __shared__ uint32_t smem[];
     const StackRef stk = adj_stack(smem, cap);
@@ -396,7 +428,7 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_replay(Sce
         const f3 g = mk3(di.x * w, di.y * w, di.z * w);
         uint32_t visits = 0;
         replay_stack<kMis>(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, g, d_diffuse,
-                           shared_lights ? s_light : d_light, gl0, visits, err);
+                           shared_lights ? s_light : d_light, d_emission, gl0, visits, err);
     } else if (!kGeneric && t < P * nb) {
         const float4 c = prim[t];
         if (c.w != 0.0f) {
@@ -408,7 +440,7 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_replay(Sce
             const f3 g = mk3(di.x * w, di.y * w, di.z * w);
             uint32_t visits = 0;
             replay<kMis>(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, mk3(c.x, c.y, c.z), g, d_diffuse,
-                   shared_lights ? s_light : d_light, gl0, visits, err);
+                   shared_lights ? s_light : d_light, d_emission, gl0, visits, err);
         }
     }
     // light 0: warp sum, then one shared atomic per warp
@@ -443,7 +475,7 @@ extern "C" {
 
 aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_camera* camera,
                               const aur_render_params* params, const float* d_image, float* d_diffuse,
-                              float* d_light_color) {
+                              float* d_light_color, float* d_emission) {
     AUR_RANGE("aur_render_adjoint");
     clear_error();
     AUR_CHECK(ctx && scene && camera && d_image && d_diffuse && (d_light_color || scene->num_lights == 0),
@@ -483,20 +515,20 @@ aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_ca
         if (generic) {   // the stack replay needs no primal radiance
             if (mis)
                 k_adj_replay<true, true><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
-                    sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, ctx->d_flags, cap);
+                    sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, d_emission, ctx->d_flags, cap);
             else
                 k_adj_replay<false, true><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
-                    sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, ctx->d_flags, cap);
+                    sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, d_emission, ctx->d_flags, cap);
         } else if (mis) {
             k_adj_primal<true><<<grid, kAdjThreads, smem_p, ctx->stream>>>(sv, *camera, p, s, nb, prim, ctx->d_flags,
                                                                            cap);
             k_adj_replay<true, false><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
-                sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, ctx->d_flags, cap);
+                sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, d_emission, ctx->d_flags, cap);
         } else {
             k_adj_primal<false><<<grid, kAdjThreads, smem_p, ctx->stream>>>(sv, *camera, p, s, nb, prim, ctx->d_flags,
                                                                             cap);
             k_adj_replay<false, false><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
-                sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, ctx->d_flags, cap);
+                sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, d_emission, ctx->d_flags, cap);
         }
     }
     cudaFreeAsync(prim, ctx->stream);

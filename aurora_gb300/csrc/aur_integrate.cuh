@@ -302,6 +302,7 @@ struct ShadowSample {
     f3 c, o, d, e;
     float tmax, geo;
     bool cand;
+    uint32_t esi;   // emitter sample only: the shader index of the sampled triangle
 };
 
 __device__ __forceinline__ f3 offset_origin(const f3& position, const f3& dir) {
@@ -426,7 +427,8 @@ __device__ __forceinline__ ShadowSample emitter_shadow_sample(const SceneView& s
     const float epdf = (__ldg(sc.mis_pa + tri) * (t * t)) / (det / len);
     const float w = bounce ? mis_weight(epdf, bsdf_pdf(b, wo, wdir)) : 1.0f;
     const uint32_t sid = sc.sids[tri];
-    const aur_shader* sh = sc.shaders + (sid > 0 ? sid - 1 : 0);
+    s.esi = sid > 0 ? sid - 1 : 0;
+    const aur_shader* sh = sc.shaders + s.esi;
     s.c = f * from(sh->emission_color) * ((cs * w) / epdf);
     s.e = from(sh->emission_color);
     s.geo = (cs * w) / epdf;

@@ -477,19 +477,24 @@ aur_status aur_filter_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, cons
 
 /* ----------------------------------------------------------------- adjoint */
 
-/* Gradients of a loss with respect to every shader's diffuse_color and every
- * light's color, by path replay backpropagation. No counterpart in the
- * reference. d_image: device, width*height float4 = dLoss/d(accum) of
- * aur_render with the same parameters (alpha ignored). d_diffuse
- * (num_shaders*3) and d_light_color (num_lights*3), device: gradients are
- * ADDED. Same estimator and RNG streams as aur_render, in every mode
- * (AUR_MODE_PATH_MIS included: its weights do not depend on the colours)
- * and for every material (scenes with specular shaders are replayed
- * through the integrator's ray stack). A textured shader's colour is not
- * its diffuse_color: its gradient entries stay zero. */
+/* Gradients of a loss with respect to every shader's diffuse_color, every
+ * shader's emission_color and every light's color, by path replay
+ * backpropagation. No counterpart in the reference. d_image: device,
+ * width*height float4 = dLoss/d(accum) of aur_render with the same
+ * parameters (alpha ignored). d_diffuse (num_shaders*3), d_light_color
+ * (num_lights*3) and d_emission (num_shaders*3, nullable: no emission
+ * gradients), device: gradients are ADDED. Same estimator and RNG streams
+ * as aur_render, in every mode and for every material (scenes with specular
+ * shaders are replayed through the integrator's ray stack). In
+ * AUR_MODE_PATH_MIS neither the MIS weights nor the light-selection table
+ * depend on the differentiated colours (the table weighs emitters by the
+ * scalar `emission` times area). A textured shader's colour is not its
+ * diffuse_color: its diffuse entries stay zero. Emission colour is found at
+ * every hit (monteCarloRaytracer.cu:42) and, in AUR_MODE_PATH_MIS, by the
+ * emitter sample of every hit. */
 aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_camera* camera,
                               const aur_render_params* params, const float* d_image, float* d_diffuse,
-                              float* d_light_color);
+                              float* d_light_color, float* d_emission);
 
 /* ------------------------------------------------------ batched wavefront */
 
