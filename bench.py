@@ -71,12 +71,15 @@ def parse():
                     help="only the large terrain workload (plain vs wavefront, full frame)")
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling cases only)")
     ap.add_argument("--profile", nargs="?", const="trace", default=None,
-                    choices=["trace", "render", "mis", "loop", "wavefront", "adjoint", "build", "filter"],
+                    choices=["trace", "render", "mis", "loop", "wavefront", "adjoint", "build", "filter", "emitters",
+                             "prep"],
                     help="small profiling case: trace = one closest-hit and one any-hit launch; render = Cornell "
                          "+ sphere frames; mis = one MIS frame of the emissive Cornell box; loop = the "
                          "reference-structured loop (65,536-ray tiles) on the Cornell + sphere scene; "
                          "wavefront = stepped 8-scene batch; adjoint = one adjoint; "
-                         "build = NMH build of the 1M-triangle soup; filter = pixel filter of a 3840x2160 frame")
+                         "build = NMH build of the 1M-triangle soup; filter = pixel filter of a 3840x2160 frame; "
+                         "emitters = emitter table and MIS light-selection table of a 1M-triangle soup whose "
+                         "triangles all emit; prep = object-to-world transform and tangent frames of 4M triangles")
     return ap.parse_args()
 
 
@@ -171,6 +174,40 @@ def run_profile(args):
             api.filter_pixels(ctx, 3840, 2160, src, out)
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": "filter"}))
+        return
+    if args.profile == "emitters":
+        V = scenes.random_soup(1_000_000, seed=0)
+        n = V.shape[0]
+        sh = np.stack([T.lambert((0.5, 0.5, 0.5), emission=(1.0, 0.8, 0.6))])
+        sh["emission"] = 1.0
+        corners = [np.stack([V[:, k], V[:, 3 + k], V[:, 6 + k]], 1) for k in range(3)]   # p1, p2, p3
+        fn = scenes.face_normals(*corners)
+        sd = scenes.SceneData("emissive_soup", V, scenes.normals_to_aos(fn, fn, fn), np.ones(n, np.uint16), sh,
+                              np.zeros(0, T.light_dtype), scenes.cornell_camera())
+        sc = api.Scene(ctx, sd)
+        for _ in range(2):
+            sc.emitters()
+            sc.mis_table()
+            sc.set_shaders(sh)                    # a shader change rebuilds the light-selection table
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "emitters", "triangles": n}))
+        return
+    if args.profile == "prep":
+        n = 1 << 22
+        src = torch.rand((n * 9,), device="cuda")
+        nrm = torch.rand((n * 9,), device="cuda")
+        dv, dn = torch.empty_like(src), torch.empty_like(src)
+        tb, bt = torch.empty_like(src), torch.empty_like(src)
+        xf = np.zeros(4, T.object_transform_dtype)
+        for i in range(4):
+            xf[i]["offset"], xf[i]["size"] = i * (n // 4), n // 4
+            xf[i]["world_matrix"] = np.eye(4) * (1.0 + i)
+            xf[i]["normal_matrix"] = np.eye(4) / (1.0 + i)
+        for _ in range(2):
+            api.transform(ctx, src, nrm, xf, dv, dn)
+            api.generate_tb(ctx, dn, tb, bt)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "prep", "triangles": n}))
         return
     if args.profile == "build":
         V, _ = workload(16)
