@@ -72,14 +72,16 @@ def parse():
     ap.add_argument("--rays", type=int, default=N_RAYS, help="rays per step (profiling cases only)")
     ap.add_argument("--profile", nargs="?", const="trace", default=None,
                     choices=["trace", "render", "mis", "loop", "wavefront", "adjoint", "build", "filter", "emitters",
-                             "prep"],
+                             "prep", "stages"],
                     help="small profiling case: trace = one closest-hit and one any-hit launch; render = Cornell "
                          "+ sphere frames; mis = one MIS frame of the emissive Cornell box; loop = the "
                          "reference-structured loop (65,536-ray tiles) on the Cornell + sphere scene; "
                          "wavefront = stepped 8-scene batch; adjoint = one adjoint; "
                          "build = NMH build of the 1M-triangle soup; filter = pixel filter of a 3840x2160 frame; "
                          "emitters = emitter table and MIS light-selection table of a 1M-triangle soup whose "
-                         "triangles all emit; prep = object-to-world transform and tangent frames of 4M triangles")
+                         "triangles all emit; prep = object-to-world transform and tangent frames of 4M triangles; "
+                         "stages = per-stage time split of the 64-scene batch (samples [0, 2) of 64) and of the "
+                         "terrain (sample 0 of 256), the wavefront's kernels launched stepped")
     return ap.parse_args()
 
 
@@ -174,6 +176,28 @@ def run_profile(args):
             api.filter_pixels(ctx, 3840, 2160, src, out)
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": "filter"}))
+        return
+    if args.profile == "stages":
+        out = {"profile_case": "stages"}
+        sds = [scenes.sphere_scene(i) for i in range(64)]
+        scs = [api.Scene(ctx, sd) for sd in sds]
+        prm = [T.render_params(512, 512, 64, 6, seed=0, mode=T.MODE_PATH, sample_end=2, scene_id=i)
+               for i in range(64)]
+        b = api.Batch(ctx, scs, prm, tuning=api.make_tuning(1 << 25, 0, 256, 4))
+        frames = [torch.zeros((512, 512, 4), device="cuda") for _ in range(64)]
+        b.profile(frames)                              # warm-up
+        out["spheres_64_scenes_2spp_ms"] = b.profile(frames)
+        b.close()
+        del scs, frames
+        sd = scenes.terrain(res=2048, seed=0)
+        sc = api.Scene(ctx, sd)
+        p = T.render_params(1920, 1080, 256, 8, seed=0, mode=T.MODE_PATH, sample_end=1)
+        b = api.Batch(ctx, [sc], [p], tuning=api.make_tuning(1 << 21, 0, 128, 16))
+        f = [torch.zeros((1080, 1920, 4), device="cuda")]
+        b.profile(f)
+        out["terrain_1spp_ms"] = b.profile(f)
+        b.close()
+        print(json.dumps(out))
         return
     if args.profile == "emitters":
         V = scenes.random_soup(1_000_000, seed=0)
