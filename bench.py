@@ -412,6 +412,27 @@ def _rmse(a, ref):
     return float(((a[..., :3].double() - ref[..., :3].double()) ** 2).mean().sqrt())
 
 
+def _rmse_16384(ctx, sc, p, tuning):
+    """RMSE at the workload's spp of a small view of the same camera, plain
+    renderer and wavefront, against a 16384-spp render of that view (seed 1)."""
+    from aurora_gb300 import api, types as T
+    pr = np.array(p, copy=True)
+    pr["spp"], pr["seed"] = 16384, 1
+    rb = api.Batch(ctx, [sc], [pr], tuning=tuning)
+    t0 = time.perf_counter()
+    ref = rb.render()[0]
+    rb.status()
+    ref_s = time.perf_counter() - t0
+    rb.close()
+    plain = sc.render(p)
+    wb = api.Batch(ctx, [sc], [p], tuning=tuning)
+    wf = wb.render()[0]
+    wb.status()
+    wb.close()
+    return {"view": "%dx%d" % (int(p["width"]), int(p["height"])), "spp": int(p["spp"]),
+            "reference": "16384 spp, seed 1 (%.1f s)" % ref_s, "plain": _rmse(plain, ref), "wavefront": _rmse(wf, ref)}
+
+
 def bench_batched(ctx, checks, n_scenes=64, size=512, spp=64, depth=6, loop_samples=8, rmse_scene=0,
                   ref_spp=4096):
     """Batched workload: 64 sphere scenes (1k-500k triangles each), 512x512,
@@ -502,6 +523,9 @@ def bench_batched(ctx, checks, n_scenes=64, size=512, spp=64, depth=6, loop_samp
     rb.close()
     rmse_plain, rmse_wf = _rmse(plain_img[rmse_scene], ref), _rmse(wf[rmse_scene], ref)
     checks.add("batch: equal RMSE of plain and wavefront", rmse_plain == rmse_wf)
+    small = _rmse_16384(ctx, scs[rmse_scene], T.render_params(128, 128, spp, depth, seed=0, mode=T.MODE_PATH,
+                                                              scene_id=rmse_scene), tuning)
+    checks.add("batch: equal RMSE against the 16384-spp view", small["plain"] == small["wavefront"])
     tris = [sd.count for sd in sds]
     return {"workload": "%d sphere scenes (%d-%d triangles, %d total), %dx%d, %d spp, depth %d, path mode; all "
                         "samples timed" % (n_scenes, min(tris), max(tris), sum(tris), size, size, spp, depth),
@@ -519,6 +543,7 @@ def bench_batched(ctx, checks, n_scenes=64, size=512, spp=64, depth=6, loop_samp
             "frames_identical": bool(same),
             "rmse": {"scene": rmse_scene, "reference": "%dx%d at %d spp (seed 1, wavefront, %.1f s)"
                      % (size, size, ref_spp, ref_s), "spp": spp, "plain": rmse_plain, "wavefront": rmse_wf},
+            "rmse_16384": small,
             "wavefront_graph_launches": 1, "wavefront_iterations": iters,
             "wavefront_rays": {"closest": ext, "shadow": shadow,
                                "mrays_per_s": (ext + shadow) / (wf_ms * 1e-3) / 1e6},
@@ -794,6 +819,8 @@ def bench_terrain(ctx, checks, res=2048, samples=16, ref_seed=1, crop=(64, 36), 
     fb.close()
     rmse_plain, rmse_wf = _rmse(plain, ref), _rmse(wf, ref)
     checks.add("terrain: equal RMSE of plain and wavefront", rmse_plain == rmse_wf)
+    small = _rmse_16384(ctx, sc, T.render_params(64, 36, spp, depth, seed=0, mode=T.MODE_PATH), tuning)
+    checks.add("terrain: equal RMSE against the 16384-spp view", small["plain"] == small["wavefront"])
     n_samples = W * H * samples
     out = {"workload": "fBm terrain %dx%d vertices (%d triangles), 16 area lights, %dx%d, %d spp, depth %d, path mode, "
                        "full frame; plain and wavefront timed on samples [0, %d), the wavefront also on all %d"
@@ -814,7 +841,8 @@ def bench_terrain(ctx, checks, res=2048, samples=16, ref_seed=1, crop=(64, 36), 
            "wavefront_rays": {"closest": ext, "shadow": shadow, "iterations": iters,
                               "mrays_per_s": (ext + shadow) / (wf_ms * 1e-3) / 1e6},
            "rmse": {"reference": "the full %dx%d frame at %d spp, seed %d (wavefront)" % (W, H, spp, ref_seed),
-                    "spp": samples, "plain": rmse_plain, "wavefront": rmse_wf}}
+                    "spp": samples, "plain": rmse_plain, "wavefront": rmse_wf},
+           "rmse_16384": small}
     if cpu:
         import oracle
         sw, sh = crop
