@@ -1145,11 +1145,20 @@ aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, cons
     AUR_CHECK(ctx && scenes && cameras && params && best && num_scenes > 0, AUR_ERR_INVALID,
               "aur_batch_autotune: null argument");
     AUR_CUDA(cudaSetDevice(ctx->device));
-    // one sample per pixel of the real batch, into scratch frames
+    // up to two samples per pixel of the real batch (fewer if it asks for
+    // fewer), into scratch frames. A pool larger than the probe's work would
+    // run it in one wave, like any other such pool, and tie with them within
+    // noise, so those pools are not timed.
     std::vector<aur_render_params> p1(params, params + num_scenes);
-    for (auto& p : p1) { p.sample_end = p.sample_begin + 1; }
+    uint32_t probe = 2;
+    for (const auto& p : p1) {
+        const uint32_t s1 = p.sample_end ? p.sample_end : p.spp;
+        probe = std::min(probe, s1 > p.sample_begin ? s1 - p.sample_begin : 1u);
+    }
+    for (auto& p : p1) { p.sample_end = p.sample_begin + probe; }
     size_t pixels = 0;
     for (uint32_t i = 0; i < num_scenes; ++i) pixels += (size_t)p1[i].width * p1[i].height;
+    const uint64_t probe_items = (uint64_t)pixels * probe;
     float4* frames = nullptr;
     AUR_CHECK(::aur::dev_malloc(&frames, pixels * sizeof(float4)) == cudaSuccess, AUR_ERR_OOM, "aur_batch_autotune: out of memory");
     std::vector<float*> acc(num_scenes);
@@ -1173,6 +1182,7 @@ aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, cons
         for (uint32_t bs : blocks)
             for (uint32_t bps : per_sm) {
                 if ((uint64_t)bs * bps > 2048 || pool > max_pool) continue;
+                if (pool > probe_items && pool != pools[0]) continue;
                 aur_wavefront_tuning t{pool, 1, bs, bps, 0};
                 aur_batch* bt = nullptr;
                 if (aur_batch_create(ctx, scenes, cameras, p1.data(), num_scenes, &t, &bt) != AUR_OK) {

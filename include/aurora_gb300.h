@@ -546,8 +546,10 @@ aur_status aur_batch_counters(aur_ctx* ctx, aur_batch* batch, unsigned long long
  * set-up, generate, extend, shade, shadow, combine, accumulate. */
 aur_status aur_batch_profile(aur_ctx* ctx, aur_batch* batch, float* const* accum, float stage_ms[7]);
 aur_status aur_batch_destroy(aur_batch* batch);
-/* Autotuner: times one-sample renders of the batch for a set of candidate
- * tunings (pool size, block size, blocks per SM) and returns the fastest. */
+/* Autotuner: times renders of the batch's first two samples (one if it
+ * renders one) for a set of candidate tunings (pool size, block size, blocks
+ * per SM) and returns the fastest; pools larger than that probe's paths are
+ * not timed (they would all run it in one wave). best_ms: the probe's time. */
 aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, const aur_camera* cameras,
                               const aur_render_params* params, uint32_t num_scenes,
                               aur_wavefront_tuning* best, float* best_ms);
