@@ -89,6 +89,9 @@ struct aur_nmh {
     float4* node_recs = nullptr;  // nodes * 8 float4 (slab, 2 x (v1, e1, e2), children's boxes)
     uint32_t* perm = nullptr;     // NMH position -> original prim id
     float* verts = nullptr;       // count * 9, NMH order, reference layout
+    // node_recs as a linear texture of float4 texels: k_trace reads one of a
+    // node's four sectors through the texture path (0: none, plain loads)
+    cudaTextureObject_t rec_tex = 0;
 };
 
 struct aur_scene {

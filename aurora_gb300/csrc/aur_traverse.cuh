@@ -112,6 +112,15 @@ __device__ __forceinline__ Sector ld_sector(const float4* __restrict__ p) {
     return s;
 }
 
+// The same sector through the texture path: two float4 texels of the records
+// bound as a linear texture (texel index = float4 index in the records).
+__device__ __forceinline__ Sector tex_sector(cudaTextureObject_t tex, size_t texel) {
+    Sector s;
+    s.a = tex1Dfetch<float4>(tex, (int)texel);
+    s.b = tex1Dfetch<float4>(tex, (int)texel + 1);
+    return s;
+}
+
 // Traversal state of one ray. The heap is implicit, so a pending far child
 // needs no stored index: it is the sibling of the current node's ancestor on
 // the far child's level, ((k+1) >> (lvl - L) ^ 1) - 1 in 0-based heap
@@ -199,13 +208,18 @@ __device__ __forceinline__ void trav_descend(TravState& s, const float4* __restr
 // ray.cuh:198-223) in order. Closest hit: ties in t go to the lower original
 // prim id. Any hit: returns true on the first hit with Epsilon < t < best_t.
 // s0: record sector 0 (from trav_next); sectors 1 and 2 are read here, and
-// word 5 (the tail of sector 2) is handed back in q5 for trav_descend.
-template <bool kAny>
+// word 5 (the tail of sector 2) is handed back in q5 for trav_descend. With
+// kTex, sector 2 comes through the texture path (tex: the records as float4
+// texels): with one of a node's four sectors there, the L1 load pipe, which
+// bounds the traversal, and the texture pipe share the node's reads (+2.3 %
+// on the traversal microbench; more sectors there, or others, measured slower).
+template <bool kAny, bool kTex = false>
 __device__ __forceinline__ bool node_triangles(const float4* __restrict__ recs, uint32_t k, const Sector& s0,
                                                const uint32_t* __restrict__ perm, const f3& pos, const f3& dir,
-                                               float& best_t, float& bu, float& bv, uint32_t& best, float4& q5) {
+                                               float& best_t, float& bu, float& bv, uint32_t& best, float4& q5,
+                                               cudaTextureObject_t tex = 0) {
     const Sector s1 = ld_sector(recs + (size_t)k * kRecStride + 2);
-    const Sector s2 = ld_sector(recs + (size_t)k * kRecStride + 4);
+    const Sector s2 = kTex ? tex_sector(tex, (size_t)k * kRecStride + 4) : ld_sector(recs + (size_t)k * kRecStride + 4);
     const float4& q0 = s0.a;
     const float4& q1 = s0.b;
     const float4& q2 = s1.a;

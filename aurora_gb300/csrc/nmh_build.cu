@@ -1479,6 +1479,23 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
         cleanup();
         return s;
     }
+    // the records as a linear float4 texture for k_trace (when they fit one);
+    // without it k_trace reads every sector with plain loads
+    int max_linear = 0;
+    if (cudaDeviceGetAttribute(&max_linear, cudaDevAttrMaxTexture1DLinearWidth, ctx->device) == cudaSuccess &&
+        (uint64_t)n * kRecStride <= (uint64_t)max_linear) {
+        cudaResourceDesc rd = {};
+        rd.resType = cudaResourceTypeLinear;
+        rd.res.linear.devPtr = nmh->node_recs;
+        rd.res.linear.desc = cudaCreateChannelDesc<float4>();
+        rd.res.linear.sizeInBytes = (size_t)n * kRecStride * sizeof(float4);
+        cudaTextureDesc td = {};
+        td.readMode = cudaReadModeElementType;
+        if (cudaCreateTextureObject(&nmh->rec_tex, &rd, &td, nullptr) != cudaSuccess) {
+            cudaGetLastError();
+            nmh->rec_tex = 0;
+        }
+    }
     *out = nmh;
     return AUR_OK;
 }

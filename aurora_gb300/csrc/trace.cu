@@ -37,13 +37,15 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // the subtree-box pruning (off only to count the reference's own node visits).
 // kCount adds up node fetches, slab crossings (triangle tests) and crossings
 // of nodes with children (box loads) into counters[0..2].
-template <bool kAny, bool kCount, bool kBoxes>
+// kTex: one sector of each node through the texture path (node_triangles).
+template <bool kAny, bool kCount, bool kBoxes, bool kTex>
 __global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restrict__ recs, uint32_t nodes,
                                                          const uint32_t* __restrict__ perm,
                                                          const float4* __restrict__ rays, uint32_t n,
                                                          float4* __restrict__ hits, uint32_t* __restrict__ occ,
                                                          unsigned long long* __restrict__ counters,
-                                                         uint32_t* __restrict__ ray_counter, int cap) {
+                                                         uint32_t* __restrict__ ray_counter, int cap,
+                                                         cudaTextureObject_t tex) {
     extern __shared__ uint32_t smem[];
     const int tid = threadIdx.x;
     StackRef stk;
@@ -86,7 +88,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restric
                 ++crossings;
                 inner += 2 * s.k + 1 < nodes;
             }
-            done = node_triangles<kAny>(recs, s.k, s0, perm, pos, dir, best_t, bu, bv, best, q5);
+            done = node_triangles<kAny, kTex>(recs, s.k, s0, perm, pos, dir, best_t, bu, bv, best, q5, tex);
             if (!done) trav_descend<kBoxes>(s, recs, q5, pos, dir, inv, best_t, nodes, stk, nlo, nhi);
         } else {
             done = true;
@@ -116,20 +118,30 @@ inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b
 
 }  // namespace
 
-template <bool kAny, bool kCount, bool kBoxes = true>
-aur_status launch_one(aur_ctx* ctx, const aur_nmh* nmh, const float4* r, uint32_t n, float4* h, uint32_t* occ,
-                      unsigned long long* counters, cudaStream_t stream, uint32_t* ray_counter) {
+template <bool kAny, bool kCount, bool kBoxes, bool kTex>
+aur_status launch_kernel(aur_ctx* ctx, const aur_nmh* nmh, const float4* r, uint32_t n, float4* h, uint32_t* occ,
+                         unsigned long long* counters, cudaStream_t stream, uint32_t* ray_counter) {
     const int cap = (int)nmh->levels + 1;
     const size_t smem = (size_t)2 * cap * kTraceThreads * sizeof(uint32_t);
     int per_sm = 0;
-    AUR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<kAny, kCount, kBoxes>, kTraceThreads,
-                                                           smem));
+    AUR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<kAny, kCount, kBoxes, kTex>,
+                                                           kTraceThreads, smem));
     const uint32_t grid = std::max(1u, std::min<uint32_t>(cdiv(n, kTraceThreads), (uint32_t)(ctx->sm_count * per_sm)));
     AUR_CUDA(cudaMemsetAsync(ray_counter, 0, sizeof(uint32_t), stream));
-    k_trace<kAny, kCount, kBoxes><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r,
-                                                                        n, h, occ, counters, ray_counter, cap);
+    k_trace<kAny, kCount, kBoxes, kTex><<<grid, kTraceThreads, smem, stream>>>(
+        nmh->node_recs, nmh->nodes, nmh->perm, r, n, h, occ, counters, ray_counter, cap, nmh->rec_tex);
     AUR_CUDA(cudaGetLastError());
     return AUR_OK;
+}
+
+// The shipped kernels read through the texture path when the NMH has its
+// record texture; the counting kernels (roofline accounting) never do.
+template <bool kAny, bool kCount, bool kBoxes = true>
+aur_status launch_one(aur_ctx* ctx, const aur_nmh* nmh, const float4* r, uint32_t n, float4* h, uint32_t* occ,
+                      unsigned long long* counters, cudaStream_t stream, uint32_t* ray_counter) {
+    if (!kCount && nmh->rec_tex)
+        return launch_kernel<kAny, kCount, kBoxes, true>(ctx, nmh, r, n, h, occ, counters, stream, ray_counter);
+    return launch_kernel<kAny, kCount, kBoxes, false>(ctx, nmh, r, n, h, occ, counters, stream, ray_counter);
 }
 
 aur_status launch_trace(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits,
