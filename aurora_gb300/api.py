@@ -38,6 +38,7 @@ SIGNATURES = {
     "aur_ctx_sm_count": ([P, P], ctypes.c_int),
     "aur_nmh_build": ([P, P, U32, P], ctypes.c_int),
     "aur_debug_lookback_timeout": ([P, U32], ctypes.c_int),
+    "aur_debug_nmh_drop_texture": ([P], ctypes.c_int),
     "aur_nmh_destroy": ([P], ctypes.c_int),
     "aur_nmh_info": ([P, P, P], ctypes.c_int),
     "aur_nmh_export": ([P, P, P, P], ctypes.c_int),

@@ -239,6 +239,17 @@ aur_status aur_nmh_destroy(aur_nmh* nmh) {
     return AUR_OK;
 }
 
+aur_status aur_debug_nmh_drop_texture(aur_nmh* nmh) {
+    AUR_CHECK(nmh, AUR_ERR_INVALID, "aur_debug_nmh_drop_texture: null NMH");
+    AUR_CUDA(cudaSetDevice(nmh->device));
+    if (nmh->rec_tex) {
+        AUR_CUDA(cudaDeviceSynchronize());   // no launch may still read through it
+        AUR_CUDA(cudaDestroyTextureObject(nmh->rec_tex));
+        nmh->rec_tex = 0;
+    }
+    return AUR_OK;
+}
+
 aur_status aur_nmh_info(const aur_nmh* nmh, uint32_t* count, uint32_t* levels) {
     AUR_CHECK(nmh, AUR_ERR_INVALID, "aur_nmh_info: null NMH");
     if (count) *count = nmh->count;

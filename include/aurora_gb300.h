@@ -240,6 +240,13 @@ aur_status aur_nmh_build(aur_ctx* ctx, const float* vertices, uint32_t count, au
  * purpose: that build returns AUR_ERR_TIMEOUT and creates no NMH. Soups of
  * at most 4,096 triangles have no such wait and build normally. */
 aur_status aur_debug_lookback_timeout(aur_ctx* ctx, uint32_t spins);
+/* Test hook (no counterpart in the reference): the NMH's node records are
+ * bound as a texture at build, and the traversal entry points read part of
+ * each node through it; an NMH too large for a texture (over about 33M
+ * triangles) is traversed with plain loads only. This drops the texture of
+ * `nmh` (after synchronizing its device), so that tests can compare both
+ * paths on small soups. */
+aur_status aur_debug_nmh_drop_texture(aur_nmh* nmh);
 aur_status aur_nmh_destroy(aur_nmh* nmh);
 /* Triangle count after padding and number of heap levels (log2i(count/2)+1). */
 aur_status aur_nmh_info(const aur_nmh* nmh, uint32_t* count, uint32_t* levels);

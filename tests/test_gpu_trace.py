@@ -49,6 +49,23 @@ def test_trace_matches_oracle(ctx, n_tris, n_rays):
     assert api.count_visits(ctx, nmh, api.rays_tensor(rays)) == (otot, atot)
 
 
+@pytest.mark.parametrize("n_tris", [3000, 1000000])
+def test_trace_texture_and_plain_loads_agree(ctx, n_tris):
+    """The traversal entry points read part of each node through the records'
+    texture; an NMH without one (too large for a texture) is read with plain
+    loads. Both give the same hits, bit for bit, in closest and any hit."""
+    V = scenes.random_soup(n_tris, seed=n_tris + 7)
+    nmh, perm, verts = _setup(ctx, V)
+    rays = scenes.microbench_rays(1 << 16, seed=5)
+    hits_tex, occ_tex = _gpu_trace(ctx, nmh, rays)
+    api.check(api.lib().aur_debug_nmh_drop_texture(nmh.handle))
+    hits_plain, occ_plain = _gpu_trace(ctx, nmh, rays)
+    assert hits_equal(hits_tex, hits_plain)
+    assert np.array_equal(occ_tex, occ_plain)
+    ohits, _, _ = oracle.trace_closest(verts, perm, rays)
+    assert hits_equal(hits_plain, ohits)
+
+
 def test_trace_tie_rule_on_duplicates(ctx):
     V = scenes.random_soup(4000, seed=5)
     V[3000:3100] = V[100:200]           # coincident copies: exact ties in t
