@@ -233,7 +233,10 @@ aur_status aur_nmh_build(aur_ctx* ctx, const float* vertices, uint32_t count, au
 aur_status aur_nmh_destroy(aur_nmh* nmh) {
     if (!nmh) return AUR_OK;
     cudaSetDevice(nmh->device);
-    if (nmh->rec_tex) cudaDestroyTextureObject(nmh->rec_tex);
+    if (nmh->rec_tex) {
+        cudaDeviceSynchronize();   // no traversal may still read through the texture
+        cudaDestroyTextureObject(nmh->rec_tex);
+    }
     cudaFree(nmh->mem);
     delete nmh;
     return AUR_OK;
