@@ -247,6 +247,9 @@ aur_status aur_debug_lookback_timeout(aur_ctx* ctx, uint32_t spins);
  * `nmh` (after synchronizing its device), so that tests can compare both
  * paths on small soups. */
 aur_status aur_debug_nmh_drop_texture(aur_nmh* nmh);
+/* Frees the NMH (its records, permutation and vertices, and the records'
+ * texture). Synchronizes the NMH's device first: no launch may still be
+ * reading it. */
 aur_status aur_nmh_destroy(aur_nmh* nmh);
 /* Triangle count after padding and number of heap levels (log2i(count/2)+1). */
 aur_status aur_nmh_info(const aur_nmh* nmh, uint32_t* count, uint32_t* levels);
