@@ -1146,9 +1146,9 @@ aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, cons
               "aur_batch_autotune: null argument");
     AUR_CUDA(cudaSetDevice(ctx->device));
     // up to two samples per pixel of the real batch (fewer if it asks for
-    // fewer), into scratch frames. A pool larger than the probe's work would
-    // run it in one wave, like any other such pool, and tie with them within
-    // noise, so those pools are not timed.
+    // fewer), into scratch frames. Pools up to 4x the probe's paths are timed
+    // (they run it in one wave and tie within noise; larger ones would only
+    // hold memory).
     std::vector<aur_render_params> p1(params, params + num_scenes);
     uint32_t probe = 2;
     for (const auto& p : p1) {
@@ -1187,7 +1187,7 @@ aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, cons
         for (uint32_t bs : blocks)
             for (uint32_t bps : per_sm) {
                 if ((uint64_t)bs * bps > 2048 || pool > max_pool) continue;
-                if (pool > probe_items && pool != pools[0]) continue;
+                if (pool > 4 * probe_items && pool != pools[0]) continue;
                 aur_wavefront_tuning t{pool, 1, bs, bps, 0};
                 aur_batch* bt = nullptr;
                 if (aur_batch_create(ctx, scenes, cameras, p1.data(), num_scenes, &t, &bt) != AUR_OK) {
@@ -1215,8 +1215,9 @@ aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, cons
     if (timed.empty()) return st != AUR_OK ? st : fail(AUR_ERR_CUDA, "aur_batch_autotune: no candidate ran");
     // Of the candidates within 3 % of the fastest probe, the largest pool (then
     // the fastest): the probe is short, and a render of many samples runs
-    // fewer, fuller iterations with a larger pool (the 64-scene sphere batch:
-    // 32M paths 10 % faster than 16M over 64 samples, equal on the probe).
+    // fewer, fuller iterations with a larger pool (over all 64 samples of the
+    // 64-scene sphere batch: 16M 3.56 s, 32M 3.31 s, 64M 3.04 s, equal on
+    // the probe; the terrain's 16 samples: 2M 1.70 s, 16M 1.67 s).
     const Timed* pick = nullptr;
     for (const Timed& c : timed) {
         if (c.ms > best_t * 1.03f) continue;

@@ -560,8 +560,8 @@ aur_status aur_batch_destroy(aur_batch* batch);
  * renders one) for a set of candidate tunings (pool size, block size, blocks
  * per SM) and returns the fastest, preferring the largest pool among the
  * candidates within 3 % of the fastest (longer renders run fewer, fuller
- * iterations with it); pools larger than the probe's paths are not timed
- * (they would all run it in one wave). best_ms: the pick's probe time. */
+ * iterations with it); pools above 4x the probe's paths are not timed.
+ * best_ms: the pick's probe time. */
 aur_status aur_batch_autotune(aur_ctx* ctx, const aur_scene* const* scenes, const aur_camera* cameras,
                               const aur_render_params* params, uint32_t num_scenes,
                               aur_wavefront_tuning* best, float* best_ms);
