@@ -4,20 +4,24 @@
 // every shader's emission colour and every light's colour, given dL/dimage.
 // No counterpart in the
 // reference. Method: path replay backpropagation (D. Vicini, S. Speierer,
-// W. Jakob, "Path Replay Backpropagation", ACM TOG 40(4), 2021). For each
-// camera sample the primal pass (aur_integrate.cuh, the same estimator as
-// aur_render) gives the sample's radiance C; the replay walks the same path
-// again with the same counter-RNG draws, keeps the radiance still to come
-// L_rem = C - sum of the contributions already passed, and at vertex k with
-// throughput T_k and Lambert colour c_k = diffuse_color * diffuse adds
-//   dL/dc_k  += g * (T_k * D_k / c_k + L_rem_after_k / c_k)
+// W. Jakob, "Path Replay Backpropagation", ACM TOG 40(4), 2021), in one pass
+// per camera sample: the integrator's ray stack (monteCarloRaytracer.cu:26-88,
+// the same estimator and counter-RNG draws as aur_render) is walked again,
+// and at vertex k with throughput T_k and Lambert colour
+// c_k = diffuse_color * diffuse the replay adds
+//   dL/dc_k  += g * (T_k * D_k / c_k + L_after_k / c_k)
 //   dL/dcolor_l += g * T_k * dD_k/dcolor_l
 // where D_k is the direct light at k (ambient, delta and area terms,
-// radiance.cuh:13-80), g = dL/dpixel / spp, and c_k enters the bounce
-// throughput f*|cos|/pdf of every later vertex (BSDF::samplef, bsdf.cuh:222-236).
-// D_k / c_k is evaluated directly (f replaced by 1/pi), so the direct part
-// needs no division; the later-vertex part divides by c_k and is skipped for
-// colour channels that are exactly zero.
+// radiance.cuh:13-80), g = dL/dpixel / spp, and L_after_k the radiance of
+// the rays that descend from k's diffuse bounce (c_k enters the throughput
+// f*|cos|/pdf of every later vertex, BSDF::samplef, bsdf.cuh:222-236). The
+// rays that descend from a bounce are exactly those traced between its pop
+// and the stack's return to its height before the push (depth first), so a
+// marker per pending bounce sums that radiance and hands it over when the
+// subtree ends; no primal pass is needed. D_k / c_k is evaluated directly
+// (f replaced by 1/pi), so the direct part needs no division; the
+// later-vertex part divides by c_k and is skipped for colour channels that
+// are exactly zero.
 // Emission E_s of shader s enters linearly: at every vertex on s as T_k * E_s
 // (times the emission's MIS weight in AUR_MODE_PATH_MIS,
 // monteCarloRaytracer.cu:42), and in AUR_MODE_PATH_MIS through the emitter
@@ -40,8 +44,8 @@ namespace aur {
 namespace {
 
 constexpr int kAdjThreads = 128;
-// Primal and replay kernels compiled for 8 resident blocks per SM (at most 64
-// registers): 24 % faster than their free 150-160 registers (3 blocks).
+// The replay kernel is compiled for 8 resident blocks per SM (at most 64
+// registers): 24 % faster than its free 150-160 registers (3 blocks).
 constexpr int kAdjBlocksPerSm = 8;
 constexpr uint32_t kSharedLights = 64;
 
@@ -206,89 +210,7 @@ __device__ __forceinline__ f3 direct_grad(const SceneView& sc, const aur_shader*
     return Li;
 }
 
-// Replays one camera sample whose primal radiance is C and adds its
-// gradient contributions (scaled by g per colour channel).
-// Gradients of light 0 are summed in `gl0` (reduced once per block by the
-// caller); those of further lights go to d_light with atomics.
-// kMis: AUR_MODE_PATH_MIS, whose MIS weights do not depend on the colours
-// (Lambert densities are |cos| / pi), so every direct term stays linear in
-// the vertex colour and in the light colour.
-template <bool kMis>
-__device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, uint32_t seed, uint32_t scene,
-                       uint32_t pixel, uint32_t sample, PathRay ray, const StackRef& stk, const f3& C, const f3& g,
-                       float* __restrict__ d_diffuse, float* __restrict__ d_light, float* __restrict__ d_emission,
-                       f3& gl0, uint32_t& visits, uint32_t* err) {
-    f3 Lrem = C;
-    uint32_t depth = 0;
-    for (uint32_t rix = 0;; ++rix) {
-        float t = kInfinity, u = 0.0f, v = 0.0f;
-        const uint32_t tri = traverse<false>(sc.recs, sc.nodes, sc.perm, ray.pos, ray.dir, t, u, v, stk, visits, err);
-        if (tri == kNoPrim) return;
-        const f3 position = ray.pos + (ray.dir * t);
-        const f3 wo = -ray.dir;
-        const uint32_t sid = sc.sids[tri];
-        const uint32_t si = sid > 0 ? sid - 1 : 0;
-        const aur_shader* sh = sc.shaders + si;
-        const Bsdf b = get_bsdf(sc, sh, tri, u, v);
-        const f3 f = bsdf_f(b);
-        const f3 thr = ray.thr;
-        const float ew = kMis ? emission_weight(sc, tri, ray.dir, t, ray.pdf) : 1.0f;
-        f3 Dp;
-        const f3 Li = direct_grad<kMis>(sc, sh, b, f, position, wo, ew, depth + 1 <= max_depth, seed, scene, pixel,
-                                        sample, rix, thr, g, d_light, gl0, Dp, d_emission, si, stk, visits, err);
-        Lrem = Lrem - Li * thr;
-        // bounce, as in the primal
-        bool cont = false;
-        PathRay nr;
-        if (kMis) {
-            depth++;
-            f3 wi, nt;
-            float pdf;
-            if (depth <= max_depth && mis_bounce(b, wo, thr, seed, scene, pixel, sample, rix, wi, nt, pdf)) {
-                nr.pos = position;
-                nr.dir = wi;
-                nr.weight = 1.0f;
-                nr.eta = ray.eta;
-                nr.thr = nt;
-                nr.pdf = pdf;
-                cont = true;
-            }
-        } else if (mode == AUR_MODE_PATH) {
-            depth++;
-            if (depth <= max_depth) {
-                float u1, u2;
-                draw2(seed, scene, pixel, sample, rix, 0u, u1, u2);
-                const f3 lwo = world_to_local(wo, b.N, b.S, b.T);
-                f3 lwi = sample_hemisphere_cosine(u1, u2);
-                if (lwo.z < 0.0f) lwi.z *= -1.0f;
-                const float pdf = (lwo.z * lwi.z > 0.0f) ? fabsf(lwi.z) * kInvPi : 0.0f;
-                const f3 wi = local_to_world(lwi, b.N, b.S, b.T);
-                if (pdf > 0.0f && !zero(f)) {
-                    nr.pos = position;
-                    nr.dir = wi;
-                    nr.weight = 1.0f;
-                    nr.eta = ray.eta;
-                    nr.thr = thr * (f * (fabsf(dot(wi, b.N)) / pdf));
-                    nr.pdf = pdf;
-                    cont = true;
-                }
-            }
-        }
-        const f3 c1 = b.color1;
-        f3 dc = thr * Dp;
-        if (cont) {
-            dc.x += c1.x != 0.0f ? Lrem.x / c1.x : 0.0f;
-            dc.y += c1.y != 0.0f ? Lrem.y / c1.y : 0.0f;
-            dc.z += c1.z != 0.0f ? Lrem.z / c1.z : 0.0f;
-        }
-        add_diffuse_grad(d_diffuse, si, sh, g * dc);
-        if (!cont) return;
-        ray = nr;
-    }
-}
-
-
-// The replay for scenes with specular shaders: integrate()'s ray stack
+// The replay of one camera sample: integrate()'s ray stack
 // (monteCarloRaytracer.cu:26-88) walked again with the same draws. A hit's
 // colour Li * thr depends on its own vertex's colour through the direct
 // light, and on the colour of every vertex whose diffuse bounce lies on its
@@ -297,6 +219,13 @@ __device__ void replay(const SceneView& sc, uint32_t max_depth, uint32_t mode, u
 // the stack to the height it had before the bounce was pushed (depth first),
 // so a marker per pending bounce sums its subtree's radiance; when the
 // subtree ends, g * subtree / c_k goes to the bouncing vertex's shader.
+// Gradients of light 0 are summed in `gl0` (reduced once per block by the
+// caller); those of further lights go to d_light with atomics. kMis:
+// AUR_MODE_PATH_MIS, whose MIS weights do not depend on the colours (Lambert
+// densities are |cos| / pi), so every direct term stays linear in the vertex
+// colour and in the light colour. One pass replaces a primal pass (each
+// sample's radiance) plus a replay: 29.3 -> 21.1 ms on the differentiable
+// workload (256x256, 64 spp, path mode).
 template <bool kMis>
 __device__ void replay_stack(const SceneView& sc, uint32_t max_depth, uint32_t mode, uint32_t seed, uint32_t scene,
                              uint32_t pixel, uint32_t sample, const PathRay& primary, const StackRef& stk,
@@ -379,35 +308,16 @@ __device__ __forceinline__ StackRef adj_stack(uint32_t* smem, int cap) {
     return stk;
 }
 
-// Primal pass: the radiance C of every camera sample (the estimator of
-// aur_render), w = 1 when the sample hit something.
+// Replay kernel: one thread per camera sample of samples [s0, s0 + nb).
 template <bool kMis>
-__global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_primal(SceneView sc, aur_camera cam, aur_render_params p, uint32_t s0,
-                                                            uint32_t nb, float4* __restrict__ prim,
-                                                            uint32_t* __restrict__ err, int cap) {
-    extern __shared__ uint32_t smem[];
-    const StackRef stk = adj_stack(smem, cap);
-    const uint64_t P = (uint64_t)p.width * p.height;
-    const uint64_t t = (uint64_t)blockIdx.x * kAdjThreads + threadIdx.x;
-    if (t >= P * nb) return;
-    const uint32_t pix = (uint32_t)(t % P);
-    const uint32_t s = s0 + (uint32_t)(t / P);
-    const PathRay r = camera_ray(cam, p.width, p.height, pix % p.width, pix / p.width, s, p.spp);
-    uint32_t visits = 0;
-    const SampleResult res =
-        integrate_diffuse<kMis>(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, visits, err);
-    prim[t] = make_float4(res.color.x, res.color.y, res.color.z, res.any_hit ? 1.0f : 0.0f);
-}
-
-// Replay pass. kGeneric: scenes with specular shaders, replayed through the
-// ray stack (replay_stack) without the primal pass.
-template <bool kMis, bool kGeneric>
-__global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_replay(SceneView sc, aur_camera cam, aur_render_params p, uint32_t s0,
-                                                            uint32_t nb, const float4* __restrict__ prim,
-                                                            const float4* __restrict__ d_image,
-                                                            float* __restrict__ d_diffuse, float* __restrict__ d_light,
-                                                            float* __restrict__ d_emission,
-                                                            uint32_t* __restrict__ err, int cap) {
+__global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_replay(SceneView sc, aur_camera cam,
+                                                                            aur_render_params p, uint32_t s0,
+                                                                            uint32_t nb,
+                                                                            const float4* __restrict__ d_image,
+                                                                            float* __restrict__ d_diffuse,
+                                                                            float* __restrict__ d_light,
+                                                                            float* __restrict__ d_emission,
+                                                                            uint32_t* __restrict__ err, int cap) {
     extern __shared__ uint32_t smem[];
     const StackRef stk = adj_stack(smem, cap);
     // light gradients are reduced in shared memory first (one light is hit by every sample)
@@ -419,7 +329,7 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_replay(Sce
     const uint64_t P = (uint64_t)p.width * p.height;
     const uint64_t t = (uint64_t)blockIdx.x * kAdjThreads + threadIdx.x;
     f3 gl0 = mk3(0.0f);
-    if (kGeneric && t < P * nb) {
+    if (t < P * nb) {
         const uint32_t pix = (uint32_t)(t % P);
         const uint32_t s = s0 + (uint32_t)(t / P);
         const PathRay r = camera_ray(cam, p.width, p.height, pix % p.width, pix / p.width, s, p.spp);
@@ -429,19 +339,6 @@ __global__ void __launch_bounds__(kAdjThreads, kAdjBlocksPerSm) k_adj_replay(Sce
         uint32_t visits = 0;
         replay_stack<kMis>(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, g, d_diffuse,
                            shared_lights ? s_light : d_light, d_emission, gl0, visits, err);
-    } else if (!kGeneric && t < P * nb) {
-        const float4 c = prim[t];
-        if (c.w != 0.0f) {
-            const uint32_t pix = (uint32_t)(t % P);
-            const uint32_t s = s0 + (uint32_t)(t / P);
-            const PathRay r = camera_ray(cam, p.width, p.height, pix % p.width, pix / p.width, s, p.spp);
-            const float4 di = d_image[pix];
-            const float w = 1.0f / (float)p.spp;
-            const f3 g = mk3(di.x * w, di.y * w, di.z * w);
-            uint32_t visits = 0;
-            replay<kMis>(sc, p.max_depth, p.mode, p.seed, p.scene_id, pix, s, r, stk, mk3(c.x, c.y, c.z), g, d_diffuse,
-                   shared_lights ? s_light : d_light, d_emission, gl0, visits, err);
-        }
     }
     // light 0: warp sum, then one shared atomic per warp
 #pragma unroll
@@ -491,47 +388,27 @@ aur_status aur_render_adjoint(aur_ctx* ctx, const aur_scene* scene, const aur_ca
         st = build_mis_table(ctx, scene);
         if (st != AUR_OK) return st;
     }
-    const bool generic = scene->has_specular;
     const aur_render_params p = *params;
     const uint32_t s0 = p.sample_begin, s1 = p.sample_end ? p.sample_end : p.spp;
     if (s1 == s0) return AUR_OK;
     const uint64_t P = (uint64_t)p.width * p.height;
     const uint32_t batch = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(s1 - s0, (1ull << 24) / P));
     const int cap = (int)scene->nmh->levels + 1;
-    const size_t smem_p = (size_t)2 * cap * kAdjThreads * sizeof(uint32_t);
-    const size_t smem_r = smem_p + 3 * kSharedLights * sizeof(float);
-    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
-    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
-    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
-    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
-    float4* prim = nullptr;
-    AUR_CHECK(::aur::dev_malloc_async(&prim, P * batch * sizeof(float4), ctx->stream) == cudaSuccess, AUR_ERR_OOM,
-              "aur_render_adjoint: out of device memory");
+    const size_t smem = (size_t)2 * cap * kAdjThreads * sizeof(uint32_t) + 3 * kSharedLights * sizeof(float);
+    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    AUR_CUDA(cudaFuncSetAttribute(k_adj_replay<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const SceneView sv = scene_view(scene);
+    const float4* di = (const float4*)d_image;
     for (uint32_t s = s0; s < s1; s += batch) {
         const uint32_t nb = std::min(batch, s1 - s);
         const uint32_t grid = cdiv(P * nb, kAdjThreads);
-        const float4* di = (const float4*)d_image;
-        if (generic) {   // the stack replay needs no primal radiance
-            if (mis)
-                k_adj_replay<true, true><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
-                    sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, d_emission, ctx->d_flags, cap);
-            else
-                k_adj_replay<false, true><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
-                    sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, d_emission, ctx->d_flags, cap);
-        } else if (mis) {
-            k_adj_primal<true><<<grid, kAdjThreads, smem_p, ctx->stream>>>(sv, *camera, p, s, nb, prim, ctx->d_flags,
-                                                                           cap);
-            k_adj_replay<true, false><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
-                sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, d_emission, ctx->d_flags, cap);
-        } else {
-            k_adj_primal<false><<<grid, kAdjThreads, smem_p, ctx->stream>>>(sv, *camera, p, s, nb, prim, ctx->d_flags,
-                                                                            cap);
-            k_adj_replay<false, false><<<grid, kAdjThreads, smem_r, ctx->stream>>>(
-                sv, *camera, p, s, nb, prim, di, d_diffuse, d_light_color, d_emission, ctx->d_flags, cap);
-        }
+        if (mis)
+            k_adj_replay<true><<<grid, kAdjThreads, smem, ctx->stream>>>(sv, *camera, p, s, nb, di, d_diffuse,
+                                                                        d_light_color, d_emission, ctx->d_flags, cap);
+        else
+            k_adj_replay<false><<<grid, kAdjThreads, smem, ctx->stream>>>(sv, *camera, p, s, nb, di, d_diffuse,
+                                                                         d_light_color, d_emission, ctx->d_flags, cap);
     }
-    cudaFreeAsync(prim, ctx->stream);
     AUR_CUDA(cudaGetLastError());
     return AUR_OK;
 }

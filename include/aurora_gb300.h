@@ -494,8 +494,8 @@ aur_status aur_filter_pixels(aur_ctx* ctx, uint32_t width, uint32_t height, cons
  * parameters (alpha ignored). d_diffuse (num_shaders*3), d_light_color
  * (num_lights*3) and d_emission (num_shaders*3, nullable: no emission
  * gradients), device: gradients are ADDED. Same estimator and RNG streams
- * as aur_render, in every mode and for every material (scenes with specular
- * shaders are replayed through the integrator's ray stack). In
+ * as aur_render, in every mode and for every material (each sample's path is
+ * replayed once through the integrator's ray stack; nothing is allocated). In
  * AUR_MODE_PATH_MIS neither the MIS weights nor the light-selection table
  * depend on the differentiated colours (the table weighs emitters by the
  * scalar `emission` times area). A textured shader's colour is not its
