@@ -39,6 +39,7 @@ SIGNATURES = {
     "aur_nmh_build": ([P, P, U32, P], ctypes.c_int),
     "aur_debug_lookback_timeout": ([P, U32], ctypes.c_int),
     "aur_debug_nmh_drop_texture": ([P], ctypes.c_int),
+    "aur_debug_trace_deferred": ([P, P], ctypes.c_int),
     "aur_nmh_destroy": ([P], ctypes.c_int),
     "aur_nmh_info": ([P, P, P], ctypes.c_int),
     "aur_nmh_export": ([P, P, P, P], ctypes.c_int),
@@ -238,6 +239,14 @@ def trace_any(ctx, nmh, rays_dev, occ_dev=None):
 
 def hits_to_numpy(hits_dev):
     return hits_dev.cpu().numpy().view(T.hit_dtype).reshape(-1)
+
+
+def trace_deferred(ctx):
+    """Chunks of 32 rays that the context's last device trace left to the
+    one-ray-per-thread kernel (test hook)."""
+    c = ctypes.c_uint32()
+    check(lib().aur_debug_trace_deferred(ctx.handle, ctypes.byref(c)))
+    return c.value
 
 
 def trace_closest_host(ctx, nmh, rays_host, hits_host):

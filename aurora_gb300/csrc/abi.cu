@@ -181,6 +181,7 @@ aur_status aur_ctx_destroy(aur_ctx* ctx) {
     ::aur::free_build_cache(ctx);
     for (auto& s : ctx->pipe) cudaFree(s.ptr);
     for (auto& s : ctx->out) cudaFree(s.ptr);
+    for (auto& s : ctx->defer) cudaFree(s.ptr);
     for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
     cudaFree(ctx->d_flags);
     if (ctx->copy_in) cudaStreamDestroy(ctx->copy_in);

@@ -74,6 +74,7 @@ struct aur_ctx {
     uint32_t* d_flags = nullptr;         // small device scratch: counters, error flags
     aur::Scratch pipe[2];                // double-buffered device chunks for *_host calls
     aur::Scratch out[2];
+    aur::Scratch defer[2];               // per trace slot: ray chunks left to the per-lane kernel
     cudaEvent_t ev[8] = {};
     aur::BuildCache* build = nullptr;    // created by the first aur_nmh_build
     uint32_t lookback_test = 0;          // test hook for the next build (aur_debug_lookback_timeout)
@@ -129,10 +130,11 @@ aur_status build_mis_table(aur_ctx* ctx, const aur_scene* sc);
 void free_mis_table(const aur_scene* sc);
 // Every texture the scene's shaders name exists (and texcoords were given).
 aur_status check_scene_textures(const aur_scene* sc);
-// ray_counter: the persistent kernel's work counter (default d_flags[8]);
-// launches that may run concurrently need distinct counters.
+// slot: the work counters (d_flags[16 + 4 * slot ...]) and deferred-chunk
+// list (defer[slot]) of the launch; launches that may run concurrently need
+// distinct slots (0 or 1).
 aur_status launch_trace(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits,
                         uint32_t* occluder, unsigned long long* counters, cudaStream_t stream, bool pruned,
-                        uint32_t* ray_counter = nullptr);
+                        int slot = 0);
 
 }  // namespace aur

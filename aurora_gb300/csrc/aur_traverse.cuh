@@ -273,4 +273,99 @@ __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ recs, ui
     return best;
 }
 
+// ------------------------------------------------------------ warp packets
+// The 3-bit direction octant of a ray (bit a: dir[a] < 0, the comparison
+// that picks the near child).
+__device__ __forceinline__ uint32_t dir_octant(const f3& dir) {
+    return (dir.x < 0.0f ? 1u : 0u) | (dir.y < 0.0f ? 2u : 0u) | (dir.z < 0.0f ? 4u : 0u);
+}
+
+// All 32 lanes of a warp traverse together, one node at a time: the node
+// sequence (k, level, axis) is the warp's, each lane keeps its own range,
+// best hit and pending far children, and takes part in a node only where
+// its own traversal would visit it. The rays must share their direction
+// octant (`oct`): then every node's near child is the same for all lanes,
+// the warp walks the depth-first, near-first order of intersect() over the
+// union of the lanes' nodes, and each lane meets its own nodes in its own
+// order with its own decisions (slab range, prune by best t, child boxes):
+// its result is that of `traverse`, bit for bit. Node records are read at
+// one address per warp (one L1 wavefront instead of one per lane), and
+// lanes of coherent rays share most of their nodes. `valid`: the lane has a
+// ray (false lanes never take part). Call with all 32 lanes.
+template <bool kAny>
+__device__ __forceinline__ uint32_t traverse_packet(const float4* __restrict__ recs, uint32_t nodes,
+                                                    const uint32_t* __restrict__ perm, bool valid, uint32_t oct,
+                                                    const f3& pos, const f3& dir, float& best_t, float& bu,
+                                                    float& bv, const StackRef& stk) {
+    const f3 inv = box_inv(dir);
+    uint32_t best = kNoPrim;
+    uint32_t k = 0, lvl = 0, ax = 0;   // the warp's node
+    uint32_t trail = 0;                // this lane's pending far children, bit per level
+    bool act = valid;                  // this lane visits node k
+    float lo = kEpsilon, hi = kInfinity;
+    for (;;) {
+        if (__any_sync(0xffffffffu, act) && k < nodes) {
+            const Sector s0 = ld_sector(recs + (size_t)k * kRecStride);
+            bool crossed = false;
+            float nlo = 0.0f, nhi = 0.0f;
+            if (act) {
+                const float p = sel3(ax, pos.x, pos.y, pos.z);
+                const float d = sel3(ax, dir.x, dir.y, dir.z);
+                float d0, d1;
+                slab_div(s0.a.x - p, s0.a.y - p, d, sel3(ax, inv.x, inv.y, inv.z), d0, d1);
+                nlo = fmaxf(fminf(d0, d1), lo);
+                nhi = fminf(fmaxf(d0, d1), hi);
+                crossed = nlo <= nhi && nlo <= best_t;
+            }
+            float4 q5 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (crossed && node_triangles<kAny>(recs, k, s0, perm, pos, dir, best_t, bu, bv, best, q5)) {
+                crossed = false;   // any hit: this lane is done
+                trail = 0;
+            }
+            const uint32_t c1 = 2 * k + 1;
+            if (__any_sync(0xffffffffu, crossed) && c1 < nodes) {
+                bool h1 = false, h2 = false;
+                if (crossed) {
+                    const Sector s3 = ld_sector(recs + (size_t)k * kRecStride + 6);
+                    const f3 poi = mk3(pos.x * inv.x, pos.y * inv.y, pos.z * inv.z);
+                    h1 = box_hit(q5.x, q5.y, q5.z, q5.w, s3.a.x, s3.a.y, poi, inv, best_t);
+                    if (c1 + 1 < nodes)
+                        h2 = box_hit(s3.a.z, s3.a.w, s3.b.x, s3.b.y, s3.b.z, s3.b.w, poi, inv, best_t);
+                }
+                const uint32_t na = ax == 2 ? 0 : ax + 1;
+                const bool neg = (oct >> na) & 1u;
+                const bool near_ok = neg ? h2 : h1;
+                const bool far_ok = neg ? h1 : h2;
+                const uint32_t L = lvl + 1;
+                if (far_ok) {
+                    stk.lo[L * stk.stride] = nlo;
+                    stk.hi[L * stk.stride] = nhi;
+                    trail |= 1u << L;
+                }
+                if (near_ok) { lo = nlo; hi = nhi; }
+                act = near_ok;
+                k = neg ? c1 + 1 : c1;
+                lvl = L;
+                ax = na;
+                if (__any_sync(0xffffffffu, act)) continue;
+            }
+        }
+        // Next: the deepest level where some lane has a pending far child
+        // (the sibling of the warp's ancestor on that level).
+        const uint32_t wt = __reduce_or_sync(0xffffffffu, trail);
+        if (wt == 0) break;
+        const uint32_t L = 31u - (uint32_t)__clz(wt);
+        k = (((k + 1u) >> (lvl - L)) ^ 1u) - 1u;
+        lvl = L;
+        ax = L % 3u;
+        act = (trail >> L) & 1u;
+        if (act) {
+            trail &= ~(1u << L);
+            lo = stk.lo[L * stk.stride];
+            hi = stk.hi[L * stk.stride];
+        }
+    }
+    return best;
+}
+
 }  // namespace aur

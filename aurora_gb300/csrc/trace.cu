@@ -11,6 +11,13 @@
 // for the children's boxes before descending. The traversal stack lives in
 // shared memory: the near child is visited next, only the far child is
 // pushed, so the stack never holds more entries than the heap has levels.
+//
+// A trace is two launches. k_trace_packets takes the rays in chunks of 32
+// consecutive rays and traverses each chunk whose rays share a direction
+// octant as one warp packet (one node at a time for the whole warp, each
+// lane with its own decisions: coherent rays share the node fetches); the
+// other chunks go to k_trace, which traverses one ray per lane. Results are
+// the same bit for bit either way.
 #include <algorithm>
 
 #include "aur_internal.h"
@@ -29,6 +36,74 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
+// Stores a ray's result (hits: t, u, v, original prim id; occ: the
+// occluder's original prim id) as intersect()/intersectAny() report it.
+template <bool kAny>
+__device__ __forceinline__ void store_result(uint32_t i, uint32_t best, float tmax, float best_t, float bu, float bv,
+                                             const uint32_t* __restrict__ perm, float4* __restrict__ hits,
+                                             uint32_t* __restrict__ occ) {
+    if (kAny) {
+        occ[i] = best == kNoPrim ? AUR_NO_HIT : perm[best];
+    } else {
+        float4 h;
+        h.x = best == kNoPrim ? tmax : best_t;
+        h.y = best == kNoPrim ? 0.0f : bu;
+        h.z = best == kNoPrim ? 0.0f : bv;
+        h.w = __uint_as_float(best == kNoPrim ? AUR_NO_HIT : perm[best]);
+        hits[i] = h;
+    }
+}
+
+// First pass of a trace: persistent warps take the rays in chunks of 32
+// consecutive rays (one atomic per warp). A chunk whose rays share their
+// direction octant is traversed as a warp packet (traverse_packet: coherent
+// rays, such as a camera's, share node fetches and lanes); any other chunk
+// goes to the deferred list for k_trace.
+template <bool kAny>
+__global__ void __launch_bounds__(kTraceThreads) k_trace_packets(const float4* __restrict__ recs, uint32_t nodes,
+                                                                 const uint32_t* __restrict__ perm,
+                                                                 const float4* __restrict__ rays, uint32_t n,
+                                                                 float4* __restrict__ hits,
+                                                                 uint32_t* __restrict__ occ,
+                                                                 uint32_t* __restrict__ ctr,
+                                                                 uint32_t* __restrict__ defer, int cap) {
+    extern __shared__ uint32_t smem[];
+    const int tid = threadIdx.x;
+    const uint32_t lane = tid & 31;
+    StackRef stk;
+    stk.lo = reinterpret_cast<float*>(smem) + tid;
+    stk.hi = reinterpret_cast<float*>(smem + cap * kTraceThreads) + tid;
+    stk.stride = kTraceThreads;
+    stk.cap = cap;
+    const uint32_t chunks = (uint32_t)(((uint64_t)n + 31) >> 5);
+    for (;;) {
+        uint32_t c = 0;
+        if (lane == 0) c = atomicAdd(ctr + 1, 1u);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (c >= chunks) break;
+        const uint32_t i = c * 32u + lane;
+        const bool valid = i < n;       // lane 0 always has a ray
+        f3 pos = mk3(0.0f), dir = mk3(0.0f);
+        float tmax = 0.0f;
+        if (valid) {
+            const float4 r0 = rays[2 * (size_t)i];
+            const float4 r1 = rays[2 * (size_t)i + 1];
+            pos = mk3(r0.x, r0.y, r0.z);
+            dir = mk3(r1.x, r1.y, r1.z);
+            tmax = r0.w;
+        }
+        const uint32_t oct = dir_octant(dir);
+        const uint32_t oct0 = __shfl_sync(0xffffffffu, oct, 0);
+        if (!__all_sync(0xffffffffu, !valid || oct == oct0)) {
+            if (lane == 0) defer[atomicAdd(ctr + 2, 1u)] = c;
+            continue;
+        }
+        float best_t = tmax, bu = 0.0f, bv = 0.0f;
+        const uint32_t best = traverse_packet<kAny>(recs, nodes, perm, valid, oct0, pos, dir, best_t, bu, bv, stk);
+        if (valid) store_result<kAny>(i, best, tmax, best_t, bu, bv, perm, hits, occ);
+    }
+}
+
 // Persistent traversal kernel with dynamic ray fetch: a lane whose ray is
 // done takes the next unprocessed ray at once (one atomic per warp for all
 // lanes asking together), so warps stay full until the ray pool is drained
@@ -38,14 +113,20 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // kCount adds up node fetches, slab crossings (triangle tests) and crossings
 // of nodes with children (box loads) into counters[0..2].
 // kTex: one sector of each node through the texture path (node_triangles).
-template <bool kAny, bool kCount, bool kBoxes, bool kTex>
-__global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restrict__ recs, uint32_t nodes,
+// kDefer: the rays are those of the chunks k_trace_packets deferred
+// (defer[0 .. ctr[2]), 32 consecutive rays each), else rays [0, n).
+// ctr[0] is the ray fetch counter. Compiled for 9 blocks of 128 per SM (56
+// registers): the deferred form otherwise takes 62 registers and 8 blocks,
+// which measured slower.
+template <bool kAny, bool kCount, bool kBoxes, bool kTex, bool kDefer>
+__global__ void __launch_bounds__(kTraceThreads, 9) k_trace(const float4* __restrict__ recs, uint32_t nodes,
                                                          const uint32_t* __restrict__ perm,
                                                          const float4* __restrict__ rays, uint32_t n,
                                                          float4* __restrict__ hits, uint32_t* __restrict__ occ,
                                                          unsigned long long* __restrict__ counters,
-                                                         uint32_t* __restrict__ ray_counter, int cap,
-                                                         cudaTextureObject_t tex) {
+                                                         uint32_t* __restrict__ ctr, int cap,
+                                                         cudaTextureObject_t tex,
+                                                         const uint32_t* __restrict__ defer) {
     extern __shared__ uint32_t smem[];
     const int tid = threadIdx.x;
     StackRef stk;
@@ -54,6 +135,8 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restric
     stk.stride = kTraceThreads;
     stk.cap = cap;
     uint32_t visits = 0, crossings = 0, inner = 0;
+    // work items: the rays, or 32 per deferred chunk
+    const uint32_t m = kDefer ? (uint32_t)min((unsigned long long)ctr[2] * 32ull, 0xFFFFFFFFull) : n;
     uint32_t i = kNoRay;
     f3 pos = mk3(0.0f), dir = mk3(0.0f), inv = mk3(0.0f);
     float tmax = 0.0f, best_t = 0.0f, bu = 0.0f, bv = 0.0f;
@@ -62,13 +145,16 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restric
     trav_init(s);
     for (;;) {
         if (i == kNoRay) {
-            const uint32_t m = __activemask();
-            const int leader = __ffs(m) - 1;
+            const uint32_t am = __activemask();
+            const int leader = __ffs(am) - 1;
             uint32_t base = 0;
-            if ((tid & 31) == leader) base = atomicAdd(ray_counter, (uint32_t)__popc(m));
-            base = __shfl_sync(m, base, leader);
-            i = base + __popc(m & lanemask_lt());
-            if (i >= n) break;
+            if ((tid & 31) == leader) base = atomicAdd(ctr, (uint32_t)__popc(am));
+            base = __shfl_sync(am, base, leader);
+            i = base + __popc(am & lanemask_lt());
+            if (i >= m) break;
+            // A deferred chunk's positions past the last ray trace the last
+            // ray again (the same result, stored twice).
+            if (kDefer) i = min(defer[i >> 5] * 32u + (i & 31u), n - 1u);
             const float4 r0 = rays[2 * (size_t)i];
             const float4 r1 = rays[2 * (size_t)i + 1];
             pos = mk3(r0.x, r0.y, r0.z);
@@ -94,16 +180,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace(const float4* __restric
             done = true;
         }
         if (done) {
-            if (kAny) {
-                occ[i] = best == kNoPrim ? AUR_NO_HIT : perm[best];
-            } else {
-                float4 h;
-                h.x = best == kNoPrim ? tmax : best_t;
-                h.y = best == kNoPrim ? 0.0f : bu;
-                h.z = best == kNoPrim ? 0.0f : bv;
-                h.w = __uint_as_float(best == kNoPrim ? AUR_NO_HIT : perm[best]);
-                hits[i] = h;
-            }
+            store_result<kAny>(i, best, tmax, best_t, bu, bv, perm, hits, occ);
             i = kNoRay;
         }
     }
@@ -118,18 +195,53 @@ inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b
 
 }  // namespace
 
+template <typename K>
+aur_status persistent_grid(aur_ctx* ctx, K kernel, size_t smem, uint32_t n, uint32_t& grid) {
+    int per_sm = 0;
+    AUR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTraceThreads, smem));
+    grid = std::max(1u, std::min<uint32_t>(cdiv(n, kTraceThreads), (uint32_t)(ctx->sm_count * per_sm)));
+    return AUR_OK;
+}
+
+// The counting kernels (roofline accounting) trace every ray per lane and
+// never read through the texture path; the shipped trace is two launches:
+// k_trace_packets over all rays, then k_trace over the chunks it deferred.
 template <bool kAny, bool kCount, bool kBoxes, bool kTex>
 aur_status launch_kernel(aur_ctx* ctx, const aur_nmh* nmh, const float4* r, uint32_t n, float4* h, uint32_t* occ,
-                         unsigned long long* counters, cudaStream_t stream, uint32_t* ray_counter) {
+                         unsigned long long* counters, cudaStream_t stream, int slot) {
     const int cap = (int)nmh->levels + 1;
     const size_t smem = (size_t)2 * cap * kTraceThreads * sizeof(uint32_t);
-    int per_sm = 0;
-    AUR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<kAny, kCount, kBoxes, kTex>,
-                                                           kTraceThreads, smem));
-    const uint32_t grid = std::max(1u, std::min<uint32_t>(cdiv(n, kTraceThreads), (uint32_t)(ctx->sm_count * per_sm)));
-    AUR_CUDA(cudaMemsetAsync(ray_counter, 0, sizeof(uint32_t), stream));
-    k_trace<kAny, kCount, kBoxes, kTex><<<grid, kTraceThreads, smem, stream>>>(
-        nmh->node_recs, nmh->nodes, nmh->perm, r, n, h, occ, counters, ray_counter, cap, nmh->rec_tex);
+    uint32_t* ctr = ctx->d_flags + 16 + 4 * slot;
+    AUR_CUDA(cudaMemsetAsync(ctr, 0, 3 * sizeof(uint32_t), stream));
+    uint32_t grid = 0;
+    if constexpr (kCount) {
+        aur_status st = persistent_grid(ctx, k_trace<kAny, kCount, kBoxes, kTex, false>, smem, n, grid);
+        if (st != AUR_OK) return st;
+        k_trace<kAny, kCount, kBoxes, kTex, false><<<grid, kTraceThreads, smem, stream>>>(
+            nmh->node_recs, nmh->nodes, nmh->perm, r, n, h, occ, counters, ctr, cap, nmh->rec_tex, nullptr);
+        AUR_CUDA(cudaGetLastError());
+        return AUR_OK;
+    }
+    Scratch& d = ctx->defer[slot];
+    const size_t need = (size_t)cdiv(n, 32) * sizeof(uint32_t);
+    if (d.bytes < need) {
+        if (d.ptr) cudaFreeAsync(d.ptr, stream);
+        d.ptr = nullptr;
+        d.bytes = 0;
+        AUR_CHECK(::aur::dev_malloc_async(&d.ptr, need, stream) == cudaSuccess, AUR_ERR_OOM,
+                  "trace: out of device memory for %u rays", n);
+        d.bytes = need;
+    }
+    uint32_t* defer = static_cast<uint32_t*>(d.ptr);
+    aur_status st = persistent_grid(ctx, k_trace_packets<kAny>, smem, n, grid);
+    if (st != AUR_OK) return st;
+    k_trace_packets<kAny><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r, n, h, occ,
+                                                                  ctr, defer, cap);
+    AUR_CUDA(cudaGetLastError());
+    st = persistent_grid(ctx, k_trace<kAny, false, kBoxes, kTex, true>, smem, n, grid);
+    if (st != AUR_OK) return st;
+    k_trace<kAny, false, kBoxes, kTex, true><<<grid, kTraceThreads, smem, stream>>>(
+        nmh->node_recs, nmh->nodes, nmh->perm, r, n, h, occ, nullptr, ctr, cap, nmh->rec_tex, defer);
     AUR_CUDA(cudaGetLastError());
     return AUR_OK;
 }
@@ -138,27 +250,26 @@ aur_status launch_kernel(aur_ctx* ctx, const aur_nmh* nmh, const float4* r, uint
 // record texture; the counting kernels (roofline accounting) never do.
 template <bool kAny, bool kCount, bool kBoxes = true>
 aur_status launch_one(aur_ctx* ctx, const aur_nmh* nmh, const float4* r, uint32_t n, float4* h, uint32_t* occ,
-                      unsigned long long* counters, cudaStream_t stream, uint32_t* ray_counter) {
+                      unsigned long long* counters, cudaStream_t stream, int slot) {
     if (!kCount && nmh->rec_tex)
-        return launch_kernel<kAny, kCount, kBoxes, true>(ctx, nmh, r, n, h, occ, counters, stream, ray_counter);
-    return launch_kernel<kAny, kCount, kBoxes, false>(ctx, nmh, r, n, h, occ, counters, stream, ray_counter);
+        return launch_kernel<kAny, kCount, kBoxes, true>(ctx, nmh, r, n, h, occ, counters, stream, slot);
+    return launch_kernel<kAny, kCount, kBoxes, false>(ctx, nmh, r, n, h, occ, counters, stream, slot);
 }
 
 aur_status launch_trace(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits,
                         uint32_t* occluder, unsigned long long* counters, cudaStream_t stream, bool pruned,
-                        uint32_t* rc) {
+                        int slot) {
     if (n == 0) return AUR_OK;
-    if (!rc) rc = ctx->d_flags + 8;
     const float4* r = reinterpret_cast<const float4*>(rays);
     float4* h = reinterpret_cast<float4*>(hits);
     if (counters && !pruned)
-        return occluder ? launch_one<true, true, false>(ctx, nmh, r, n, nullptr, occluder, counters, stream, rc)
-                        : launch_one<false, true, false>(ctx, nmh, r, n, h, nullptr, counters, stream, rc);
+        return occluder ? launch_one<true, true, false>(ctx, nmh, r, n, nullptr, occluder, counters, stream, slot)
+                        : launch_one<false, true, false>(ctx, nmh, r, n, h, nullptr, counters, stream, slot);
     if (counters)
-        return occluder ? launch_one<true, true>(ctx, nmh, r, n, nullptr, occluder, counters, stream, rc)
-                        : launch_one<false, true>(ctx, nmh, r, n, h, nullptr, counters, stream, rc);
-    return occluder ? launch_one<true, false>(ctx, nmh, r, n, nullptr, occluder, nullptr, stream, rc)
-                    : launch_one<false, false>(ctx, nmh, r, n, h, nullptr, nullptr, stream, rc);
+        return occluder ? launch_one<true, true>(ctx, nmh, r, n, nullptr, occluder, counters, stream, slot)
+                        : launch_one<false, true>(ctx, nmh, r, n, h, nullptr, counters, stream, slot);
+    return occluder ? launch_one<true, false>(ctx, nmh, r, n, nullptr, occluder, nullptr, stream, slot)
+                    : launch_one<false, false>(ctx, nmh, r, n, h, nullptr, nullptr, stream, slot);
 }
 
 }  // namespace aur
@@ -222,7 +333,7 @@ aur_status trace_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uin
         AUR_CUDA(cudaEventRecord(in_done[s], ctx->copy_in));
         AUR_CUDA(cudaStreamWaitEvent(launch[s], in_done[s], 0));
         st = launch_trace(ctx, nmh, (const aur_ray*)ctx->pipe[s].ptr, m, any ? nullptr : (aur_hit*)ctx->out[s].ptr,
-                          any ? (uint32_t*)ctx->out[s].ptr : nullptr, nullptr, launch[s], true, ctx->d_flags + 8 + s);
+                          any ? (uint32_t*)ctx->out[s].ptr : nullptr, nullptr, launch[s], true, s);
         if (st != AUR_OK) return st;
         AUR_CUDA(cudaEventRecord(comp_done[s], launch[s]));
         AUR_CUDA(cudaStreamWaitEvent(ctx->copy_out, comp_done[s], 0));
@@ -307,6 +418,14 @@ aur_status aur_trace_count_visits(aur_ctx* ctx, const aur_nmh* nmh, const aur_ra
     node_visits[0] = c[0];
     node_visits[1] = c[3];
     return st;
+}
+
+aur_status aur_debug_trace_deferred(aur_ctx* ctx, uint32_t* chunks) {
+    AUR_CHECK(ctx && chunks, AUR_ERR_INVALID, "aur_debug_trace_deferred: null argument");
+    AUR_CUDA(cudaSetDevice(ctx->device));
+    AUR_CUDA(cudaMemcpyAsync(chunks, ctx->d_flags + 16 + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    AUR_CUDA(cudaStreamSynchronize(ctx->stream));
+    return AUR_OK;
 }
 
 aur_status aur_trace_stats(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n,

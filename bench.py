@@ -10,14 +10,16 @@ the metric is Mrays/s closest-hit. Inputs are seeded synthetic data.
 
 Prints one JSON line. `e2e` measures the same metric through the C ABI's
 host-buffer call (aur_trace_closest_host: rays copied in from pinned host
-memory and hits copied back inside the timed region). `roofline` divides the
-algorithmic bytes of a launch by the kernel's CUDA-event duration, with the
+memory and hits copied back inside the timed region). A trace is two
+launches: warp packets for the 32-ray chunks of one direction octant (the
+pinhole half), then one ray per thread for the other chunks. `roofline`
+divides the algorithmic bytes of a trace by its CUDA-event duration, with the
 reference algorithm's bytes: 24 B ray in + 16 B hit out + 72 B per node that
 the reference's intersect() visits (two triangles of 36 B), the visits
 counted by the same traversal without box pruning. This traversal's own
-reads (fewer nodes, 128-byte records) are reported beside it, and the DRAM
-traffic of one launch from the committed ncu summary when that summary was
-captured from the current traversal sources. `cpu_baseline` times the
+reads per ray (fewer nodes, 128-byte records) are reported beside it, and
+the DRAM traffic of one trace (both launches) from the committed ncu summary
+when that summary was captured from the current traversal sources. `cpu_baseline` times the
 oracle's C++ restatement of the reference traversal on a sample of the same
 rays on all host cores. With --gpus N > 1 (under torchrun) every rank runs
 an independent replica of the workload.
@@ -277,9 +279,9 @@ def traversal_source_sha():
 
 
 def load_traffic():
-    """(per-launch DRAM bytes of the closest-hit kernel, where they come from).
+    """(DRAM bytes of one closest-hit trace, both launches; where they come from).
 
-    The committed ncu summary holds 'traffic_bytes_per_launch: N' and
+    The committed ncu summary holds 'traffic_bytes_per_trace: N' and
     'source_sha256_16: H', H being traversal_source_sha() of the sources it
     was captured from. The figure is used only when H equals the hash of the
     sources now; otherwise traffic is None and the source says why."""
@@ -289,17 +291,17 @@ def load_traffic():
     vals = {}
     for line in open(p):
         k, sep, v = line.strip().partition(":")
-        if sep and k in ("traffic_bytes_per_launch", "source_sha256_16"):
+        if sep and k in ("traffic_bytes_per_trace", "source_sha256_16"):
             vals[k] = v.strip()
     now = traversal_source_sha()
     if vals.get("source_sha256_16") != now:
         return None, ("stale: %s was captured from traversal sources %s, the current ones hash to %s"
                       % (TRAFFIC_PROFILE, vals.get("source_sha256_16", "(unrecorded)"), now))
     try:
-        return int(vals["traffic_bytes_per_launch"]), "%s (ncu dram__bytes_read.sum + dram__bytes_write.sum, " \
-            "traversal sources %s)" % (TRAFFIC_PROFILE, now)
+        return int(vals["traffic_bytes_per_trace"]), "%s (ncu dram__bytes_read.sum + dram__bytes_write.sum of " \
+            "both launches of a trace, traversal sources %s)" % (TRAFFIC_PROFILE, now)
     except (KeyError, ValueError):
-        return None, "no traffic_bytes_per_launch line in %s" % TRAFFIC_PROFILE
+        return None, "no traffic_bytes_per_trace line in %s" % TRAFFIC_PROFILE
 
 
 class ClockSampler:
@@ -1011,9 +1013,11 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "traffic_source": traffic_source,
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                     "definition": "reference algorithm bytes per launch: 24 B ray in + 16 B hit out + 72 B per node "
+                     "definition": "reference algorithm bytes per trace: 24 B ray in + 16 B hit out + 72 B per node "
                                    "the reference's intersect() visits (counted by this traversal without box "
-                                   "pruning), divided by the average CUDA-event time of a launch",
+                                   "pruning), divided by the average CUDA-event time of a trace call (its two "
+                                   "launches: the warp-packet pass and the one-ray-per-thread pass over the "
+                                   "chunks it deferred)",
                      "algorithmic_bytes_per_launch": ref_bytes,
                      "reference_node_visits_per_ray": visits_closest / N_RAYS,
                      "dram_GBps": traffic / avg_launch_s / 1e9 if traffic else None,
@@ -1027,7 +1031,7 @@ def main():
                      "slab_crossings_per_ray": wc["slab_crossings"] / N_RAYS},
         "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 32,
                 "d2h_bytes_per_step": N_RAYS * 16, "matches_device_result": bool(same)},
-        "gpu_launches": args.steps,
+        "gpu_launches": 2 * args.steps,    # k_trace_packets + k_trace per step
         "clocks": clocks,
         "any_hit": {"value": world * N_RAYS / (any_ms * 1e-3) / 1e6, "unit": "Mrays/s", "ms_per_step": any_ms,
                     "node_fetches_per_ray": work["any"]["node_fetches"] / N_RAYS,

@@ -321,11 +321,17 @@ aur_status aur_generate_tb(aur_ctx* ctx, const float* normals, uint32_t count, f
 /* --------------------------------------------------------------- traversal */
 
 /* Closest hit for n rays (intersect(), kernels/lib/intersect.cuh:95-152).
- * rays, hits: device. Ties in t go to the lower original prim id. */
+ * rays, hits: device. Ties in t go to the lower original prim id. Rays are
+ * taken in chunks of 32 consecutive rays: a chunk whose directions share
+ * their octant (signs of x, y, z) is traversed by one warp together, which
+ * is fastest for coherent rays (a camera's, rays toward one light); the
+ * other chunks are traversed one ray per thread. Results are the same. The
+ * first call with more rays than before allocates 4 bytes per 32 rays. */
 aur_status aur_trace_closest(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits);
 /* Any hit (shadow ray, intersectAny(), intersect.cuh:36-86): occluder[i] is
  * the original prim id of the first hit found in traversal order with
- * Epsilon < t < tmax, or AUR_NO_HIT. rays, occluder: device. */
+ * Epsilon < t < tmax, or AUR_NO_HIT. rays, occluder: device. Chunks of
+ * one octant go to warp packets as in aur_trace_closest. */
 aur_status aur_trace_any(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, uint32_t* occluder);
 /* Same as above with HOST buffers: rays go in chunks of 4M, traced on the
  * context's stream and one internal launch stream in turn, with two internal
@@ -338,6 +344,11 @@ aur_status aur_trace_any_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* r
  * counted by running the traversal without subtree-box pruning. */
 aur_status aur_trace_count_visits(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n,
                                   unsigned long long node_visits[2]);
+
+/* Test hook: the number of 32-ray chunks that the last aur_trace_closest /
+ * aur_trace_any on this context left to the one-ray-per-thread kernel
+ * (directions of more than one octant). Synchronizes the context's stream. */
+aur_status aur_debug_trace_deferred(aur_ctx* ctx, uint32_t* chunks);
 
 /* Work of this library's traversal (with subtree-box pruning) over n rays:
  * node records fetched (16-byte slab load), slabs crossed (two triangles,

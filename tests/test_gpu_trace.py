@@ -138,3 +138,76 @@ def test_trace_non_finite_rays(ctx):
     assert np.all(hits["prim"][nan_rays] == T.NO_HIT)
     good = np.setdiff1d(np.arange(4096), bad)
     assert (hits["prim"][good] != T.NO_HIT).mean() > 0.05
+
+
+def _octant_rays(n, seed, octant_of_chunk):
+    """Random origins in the unit cube, random directions whose signs are
+    set per chunk of 32 rays by octant_of_chunk(chunk index) (bit a: dir[a] < 0)."""
+    rng = np.random.default_rng(seed)
+    rays = np.zeros(n, T.ray_dtype)
+    o = rng.random((n, 3)).astype(np.float32)
+    d = np.abs(rng.normal(size=(n, 3)))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    oct_ = np.array([octant_of_chunk(i // 32) for i in range(n)])
+    for a in range(3):
+        d[:, a] = np.where((oct_ >> a) & 1, -d[:, a], d[:, a])
+    rays["ox"], rays["oy"], rays["oz"] = o.T
+    rays["dx"], rays["dy"], rays["dz"] = d.astype(np.float32).T
+    rays["tmax"] = 1e6
+    return rays
+
+
+def _check_against_oracle(ctx, nmh, perm, verts, rays):
+    hits, occ = _gpu_trace(ctx, nmh, rays)
+    ohits, _, _ = oracle.trace_closest(verts, perm, rays)
+    oocc, _, _ = oracle.trace_any(verts, perm, rays)
+    assert hits_equal(hits, ohits)
+    assert np.array_equal(occ, oocc)
+    return hits
+
+
+def test_packets_of_one_octant_match_oracle(ctx):
+    """Chunks of incoherent rays that share an octant (a different one per
+    chunk) all run as warp packets, where the lanes' node sets differ the
+    most; the last chunk is partial. Closest and any hit equal the oracle."""
+    V = scenes.random_soup(100000, seed=21)
+    nmh, perm, verts = _setup(ctx, V)
+    rays = _octant_rays(32 * 700 + 13, 4, lambda c: c % 8)
+    hits = _check_against_oracle(ctx, nmh, perm, verts, rays)
+    assert api.trace_deferred(ctx) == 0
+    assert (hits["prim"] != T.NO_HIT).mean() > 0.5
+
+
+def test_packets_and_deferred_chunks_mixed(ctx):
+    """Uniform and mixed-octant chunks in one launch, a partial mixed last
+    chunk (its missing rays trace the last ray again), and packets of
+    axis-parallel rays with +0 and -0 direction components (-0 is not
+    negative: the same near child as +0, in packets and per lane)."""
+    V = scenes.random_soup(20000, seed=22)
+    nmh, perm, verts = _setup(ctx, V)
+    n = 32 * 64 + 20
+    rays = _octant_rays(n, 5, lambda c: (c * 5) % 8)
+    rng = np.random.default_rng(6)
+    mixed = sorted({c for c in range(65) if c % 3 == 1} | {64})
+    for c in mixed:                                   # flip one lane's x sign
+        j = min(32 * c + 7, n - 1)
+        rays["dx"][j] = -rays["dx"][j]
+    ax = np.arange(32 * 3, 32 * 4)                    # a uniform chunk of axis-parallel rays
+    rays["dx"][ax], rays["dy"][ax] = np.where(np.arange(32) % 2, -0.0, 0.0), 0.0
+    rays["dz"][ax] = 1.0
+    rays["ox"][ax], rays["oy"][ax] = rng.random(32), rng.random(32)
+    rays["oz"][ax] = -1.0
+    _check_against_oracle(ctx, nmh, perm, verts, rays)
+    assert 3 not in mixed and 64 in mixed
+    assert api.trace_deferred(ctx) == len(mixed)
+
+
+def test_camera_rays_run_as_packets(ctx):
+    """The microbench's pinhole half (rows of 4096 rays, no chunk across the
+    image's centre column) is all packets; its random half all deferred."""
+    V = scenes.random_soup(50000, seed=23)
+    nmh, perm, verts = _setup(ctx, V)
+    rays = scenes.microbench_rays(1 << 15, seed=7)
+    _check_against_oracle(ctx, nmh, perm, verts, rays)
+    deferred = api.trace_deferred(ctx)
+    assert deferred <= (1 << 14) // 32 and deferred > (1 << 14) // 32 - 8
