@@ -93,6 +93,10 @@ struct aur_nmh {
     // node_recs as a linear texture of float4 texels: k_trace reads one of a
     // node's four sectors through the texture path (0: none, plain loads)
     cudaTextureObject_t rec_tex = 0;
+    // Largest side of the bounding box of all triangles (from the root node's
+    // record): the scale for deciding when a warp's rays are close enough
+    // together to traverse as a packet.
+    float extent = 0.0f;
 };
 
 struct aur_scene {

@@ -280,6 +280,25 @@ __device__ __forceinline__ uint32_t dir_octant(const f3& dir) {
     return (dir.x < 0.0f ? 1u : 0u) | (dir.y < 0.0f ? 2u : 0u) | (dir.z < 0.0f ? 4u : 0u);
 }
 
+// Largest side of the box around the valid lanes' ray origins (call with
+// all 32 lanes). A packet pays for the union of its lanes' nodes, so it is
+// only worth taking when the rays start close together (a camera's, or
+// neighbouring points toward one light); this is that test's measure.
+__device__ __forceinline__ float warp_origin_span(const f3& pos, bool valid) {
+    float lx = valid ? pos.x : INFINITY, ly = valid ? pos.y : INFINITY, lz = valid ? pos.z : INFINITY;
+    float hx = valid ? pos.x : -INFINITY, hy = valid ? pos.y : -INFINITY, hz = valid ? pos.z : -INFINITY;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        lx = fminf(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+        ly = fminf(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+        lz = fminf(lz, __shfl_xor_sync(0xffffffffu, lz, o));
+        hx = fmaxf(hx, __shfl_xor_sync(0xffffffffu, hx, o));
+        hy = fmaxf(hy, __shfl_xor_sync(0xffffffffu, hy, o));
+        hz = fmaxf(hz, __shfl_xor_sync(0xffffffffu, hz, o));
+    }
+    return fmaxf(fmaxf(hx - lx, hy - ly), hz - lz);
+}
+
 // All 32 lanes of a warp traverse together, one node at a time: the node
 // sequence (k, level, axis) is the warp's, each lane keeps its own range,
 // best hit and pending far children, and takes part in a node only where

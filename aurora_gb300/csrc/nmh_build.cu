@@ -21,6 +21,8 @@
 //      final sort, :381-385), then vertices are gathered into NMH order
 //      (applyIndices, :217-245) and traversal node records are written.
 // Every ordering ties by the lower original prim id.
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -1412,6 +1414,34 @@ aur_status build_cached(aur_ctx* ctx, const BuildArgs& a0, uint32_t N, cudaStrea
 
 }  // namespace
 
+// Largest side of the box around the root's two triangles (v1, v1 + e1,
+// v1 + e2) and its children's padded subtree boxes: the whole soup's bounds,
+// up to the padding and the rounding of v1 + e.
+static float record_extent(const float* r, uint32_t nodes) {
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    auto add = [&](int a, float v) {
+        if (v == v) { lo[a] = std::min(lo[a], v); hi[a] = std::max(hi[a], v); }
+    };
+    for (int t = 0; t < 2; ++t) {
+        const float* q = r + 2 + 9 * t;    // v1, e1, e2
+        for (int a = 0; a < 3; ++a) {
+            add(a, q[a]);
+            add(a, q[a] + q[3 + a]);
+            add(a, q[a] + q[6 + a]);
+        }
+    }
+    for (uint32_t j = 0; j < 2; ++j)
+        if (1 + j < nodes)
+            for (int a = 0; a < 3; ++a) {
+                add(a, r[20 + 6 * j + a]);
+                add(a, r[20 + 6 * j + 3 + a]);
+            }
+    float e = 0.0f;
+    for (int a = 0; a < 3; ++a)
+        if (hi[a] >= lo[a]) e = std::max(e, hi[a] - lo[a]);
+    return std::isfinite(e) ? e : 0.0f;
+}
+
 aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh** out) {
     AUR_CHECK(ctx && out, AUR_ERR_INVALID, "aur_nmh_build: null context or output pointer");
     AUR_CHECK(count == 0 || V, AUR_ERR_INVALID, "aur_nmh_build: null vertices for %u triangles", count);
@@ -1473,12 +1503,15 @@ aur_status nmh_build_impl(aur_ctx* ctx, const float* V, uint32_t count, aur_nmh*
             return cuda_fail(e, "aur_nmh_build kernels", __FILE__, __LINE__);
         }
     }
+    float root[32];    // the root's record, read back with the flags (build_flags synchronizes the stream)
+    AUR_CUDA(cudaMemcpyAsync(root, nmh->node_recs, sizeof(root), cudaMemcpyDeviceToHost, st));
     const aur_status s = build_flags("aur_nmh_build", ctx->d_flags, st, true);
     if (s != AUR_OK) {
         cudaGetLastError();
         cleanup();
         return s;
     }
+    nmh->extent = record_extent(root, n);
     // the records as a linear float4 texture for k_trace (when they fit one);
     // without it k_trace reads every sector with plain loads
     int max_linear = 0;

@@ -56,9 +56,10 @@ __device__ __forceinline__ void store_result(uint32_t i, uint32_t best, float tm
 
 // First pass of a trace: persistent warps take the rays in chunks of 32
 // consecutive rays (one atomic per warp). A chunk whose rays share their
-// direction octant is traversed as a warp packet (traverse_packet: coherent
-// rays, such as a camera's, share node fetches and lanes); any other chunk
-// goes to the deferred list for k_trace.
+// direction octant and start within `packet_span` of each other is
+// traversed as a warp packet (traverse_packet: coherent rays, such as a
+// camera's, share node fetches and lanes); any other chunk goes to the
+// deferred list for k_trace.
 template <bool kAny>
 __global__ void __launch_bounds__(kTraceThreads) k_trace_packets(const float4* __restrict__ recs, uint32_t nodes,
                                                                  const uint32_t* __restrict__ perm,
@@ -66,7 +67,8 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_packets(const float4* _
                                                                  float4* __restrict__ hits,
                                                                  uint32_t* __restrict__ occ,
                                                                  uint32_t* __restrict__ ctr,
-                                                                 uint32_t* __restrict__ defer, int cap) {
+                                                                 uint32_t* __restrict__ defer, int cap,
+                                                                 float packet_span) {
     extern __shared__ uint32_t smem[];
     const int tid = threadIdx.x;
     const uint32_t lane = tid & 31;
@@ -94,7 +96,7 @@ __global__ void __launch_bounds__(kTraceThreads) k_trace_packets(const float4* _
         }
         const uint32_t oct = dir_octant(dir);
         const uint32_t oct0 = __shfl_sync(0xffffffffu, oct, 0);
-        if (!__all_sync(0xffffffffu, !valid || oct == oct0)) {
+        if (!__all_sync(0xffffffffu, !valid || oct == oct0) || !(warp_origin_span(pos, valid) <= packet_span)) {
             if (lane == 0) defer[atomicAdd(ctr + 2, 1u)] = c;
             continue;
         }
@@ -195,6 +197,11 @@ inline uint32_t cdiv(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b
 
 }  // namespace
 
+// Largest origin spread of a warp packet: 1/64 of the soup's extent. Rays
+// that start further apart visit mostly different nodes near their origins,
+// and one ray per lane is faster for them.
+inline float packet_span(const aur_nmh* nmh) { return nmh->extent * (1.0f / 64.0f); }
+
 template <typename K>
 aur_status persistent_grid(aur_ctx* ctx, K kernel, size_t smem, uint32_t n, uint32_t& grid) {
     int per_sm = 0;
@@ -236,7 +243,7 @@ aur_status launch_kernel(aur_ctx* ctx, const aur_nmh* nmh, const float4* r, uint
     aur_status st = persistent_grid(ctx, k_trace_packets<kAny>, smem, n, grid);
     if (st != AUR_OK) return st;
     k_trace_packets<kAny><<<grid, kTraceThreads, smem, stream>>>(nmh->node_recs, nmh->nodes, nmh->perm, r, n, h, occ,
-                                                                  ctr, defer, cap);
+                                                                  ctr, defer, cap, packet_span(nmh));
     AUR_CUDA(cudaGetLastError());
     st = persistent_grid(ctx, k_trace<kAny, false, kBoxes, kTex, true>, smem, n, grid);
     if (st != AUR_OK) return st;

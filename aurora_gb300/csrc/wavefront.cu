@@ -69,6 +69,7 @@ struct WfScene {
     const float* mis_pa;
     uint32_t mis_count;
     uint32_t nodes;
+    float packet_span;   // largest origin spread of a warp packet (1/64 of the soup's extent)
     uint32_t num_lights;
     uint32_t width, height;
     uint32_t pix_off;
@@ -89,6 +90,8 @@ struct WfCtl {
     uint32_t free_count;
     uint32_t iter, iter_limit;
     uint32_t ext_fetch, shadow_fetch;   // dynamic-fetch cursors of the extend / shadow kernels
+    uint32_t ext_chunk;                 // chunk cursor of k_wf_extend_packets
+    uint32_t ext_defer;                 // chunks it left to k_wf_extend
 };
 
 struct WfArgs {
@@ -120,6 +123,7 @@ struct WfArgs {
     uint32_t* free_list;
     float4* sh_o;   // shadow ray origin, w = tmax
     float4* sh_d;   // shadow ray direction, w = (slot << 5 | light slot) bits
+    uint32_t* defer;   // chunks of 32 extend-queue entries left to k_wf_extend
     float4* out;    // per wave: nb * P_tot sample colours, indexed by item
     // specular batches: per slot a stack of kWfStack pending rays, entry e
     // component k (pos + weight, dir + eta, thr + pdf) at stk[(e * 3 + k) * Q + slot]
@@ -259,19 +263,82 @@ __global__ void k_wf_generate_commit(WfArgs a) {
     c->ext_count[cur] += n_new;
     c->ext_fetch = 0;
     c->shadow_fetch = 0;
+    c->ext_chunk = 0;
+    c->ext_defer = 0;
 }
 
 // Next queue position for a lane that needs work (one atomic per warp).
 __device__ __forceinline__ uint32_t fetch_next(uint32_t* cursor) { return agg_inc(cursor); }
 
-// Closest hit for every queued path: persistent lanes fetch queue entries
-// dynamically, so a lane whose ray finished takes the next one at once.
+// Takes the next chunk of 32 queue entries for the whole warp (one atomic);
+// returns false when the n entries are exhausted.
+__device__ __forceinline__ bool next_chunk(uint32_t* cursor, uint32_t n, uint32_t& chunk) {
+    uint32_t ch = 0;
+    if (lane_id() == 0) ch = atomicAdd(cursor, 1u);
+    chunk = __shfl_sync(0xffffffffu, ch, 0);
+    return chunk < ((n + 31u) >> 5);
+}
+
+// True when every valid lane's ray has lane 0's scene and direction octant
+// (lane 0 is valid) and the origins lie within the scene's packet span;
+// otherwise lane 0 appends the chunk to the deferred list.
+__device__ __forceinline__ bool packet_or_defer(const WfArgs& a, uint32_t* defer_count, uint32_t chunk, bool valid,
+                                                uint32_t scene, const f3& pos, const f3& dir, uint32_t& scene0,
+                                                uint32_t& oct0) {
+    const uint32_t oct = dir_octant(dir);
+    scene0 = __shfl_sync(0xffffffffu, scene, 0);
+    oct0 = __shfl_sync(0xffffffffu, oct, 0);
+    if (__all_sync(0xffffffffu, !valid || (scene == scene0 && oct == oct0)) &&
+        warp_origin_span(pos, valid) <= a.scenes[scene0].packet_span)
+        return true;
+    if (lane_id() == 0) a.defer[atomicAdd(defer_count, 1u)] = chunk;
+    return false;
+}
+
+// Closest hit, first pass: chunks of 32 queued paths of one scene and one
+// direction octant (the camera rays of an 8x4 pixel tile, say) are
+// traversed as warp packets (traverse_packet); the other chunks are left to
+// k_wf_extend. Same results either way.
+__global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_extend_packets(WfArgs a) {
+    extern __shared__ uint32_t smem[];
+    const StackRef stk = wf_stack(smem, a.cap);
+    WfCtl* c = a.ctl;
+    const uint32_t cur = c->iter & 1u;
+    const uint32_t n = c->ext_count[cur];
+    uint32_t chunk;
+    while (next_chunk(&c->ext_chunk, n, chunk)) {
+        const uint32_t i = chunk * 32u + lane_id();
+        const bool valid = i < n;
+        uint32_t slot = 0, scene = 0;
+        f3 pos = mk3(0.0f), dir = mk3(0.0f);
+        if (valid) {
+            slot = a.ext_q[cur][i];
+            scene = a.meta[slot].w;
+            const float4 o = a.o[slot], d = a.d[slot];
+            pos = mk3(o.x, o.y, o.z);
+            dir = mk3(d.x, d.y, d.z);
+        }
+        uint32_t scene0, oct0;
+        if (!packet_or_defer(a, &c->ext_defer, chunk, valid, scene, pos, dir, scene0, oct0)) continue;
+        const WfScene& sc = a.scenes[scene0];
+        float best_t = kInfinity, bu = 0.0f, bv = 0.0f;
+        const uint32_t best = traverse_packet<false>(sc.recs, sc.nodes, sc.perm, valid, oct0, pos, dir, best_t, bu, bv,
+                                                     stk);
+        if (valid) a.hit[slot] = make_float4(best_t, bu, bv, __uint_as_float(best));
+    }
+}
+
+// Closest hit for the queued paths of the deferred chunks: persistent lanes
+// fetch them dynamically, so a lane whose ray finished takes the next one at
+// once. Positions past the queue's end in the last chunk trace the last
+// entry again (the same hit, written twice).
 __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_extend(WfArgs a) {
     extern __shared__ uint32_t smem[];
     const StackRef stk = wf_stack(smem, a.cap);
     WfCtl* c = a.ctl;
     const uint32_t cur = c->iter & 1u;
     const uint32_t n = c->ext_count[cur];
+    const uint32_t m = c->ext_defer * 32u;
     uint32_t visits = 0;
     uint32_t slot = 0xFFFFFFFFu;
     const float4* recs = nullptr;
@@ -284,9 +351,9 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_extend(WfArgs a) {
     trav_init(s);
     for (;;) {
         if (slot == 0xFFFFFFFFu) {
-            const uint32_t i = fetch_next(&c->ext_fetch);
-            if (i >= n) break;
-            slot = a.ext_q[cur][i];
+            const uint32_t j = fetch_next(&c->ext_fetch);
+            if (j >= m) break;
+            slot = a.ext_q[cur][min(a.defer[j >> 5] * 32u + (j & 31u), n - 1u)];
             const WfScene& sc = a.scenes[a.meta[slot].w];
             recs = sc.recs; perm = sc.perm; nodes = sc.nodes;
             const float4 o = a.o[slot], d = a.d[slot];
@@ -509,7 +576,9 @@ __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shade(WfArgs a) {
 }
 
 // Any hit for every queued shadow ray; unoccluded rays set their bit.
-// Persistent lanes with dynamic fetch, as in k_wf_extend.
+// Persistent lanes with dynamic fetch, as in k_wf_extend. (Warp packets, as
+// in the extend stage, made this stage slower: the rays of a chunk start at
+// different surface points and share few nodes.)
 __global__ void __launch_bounds__(kWfMaxBlock, 4) k_wf_shadow(WfArgs a) {
     extern __shared__ uint32_t smem[];
     const StackRef stk = wf_stack(smem, a.cap);
@@ -770,6 +839,7 @@ aur_status make_graph(aur_batch* bt) {
     AUR_CUDA(cudaStreamBeginCaptureToGraph(s, iter_body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     k_wf_generate<<<g, bs, 0, s>>>(a);
     k_wf_generate_commit<<<1, 1, 0, s>>>(a);
+    k_wf_extend_packets<<<g, bs, bt->smem, s>>>(a);
     k_wf_extend<<<g, bs, bt->smem, s>>>(a);
     launch_shade(a, g, bs, s);
     k_wf_shadow<<<g, bs, bt->smem, s>>>(a);
@@ -888,6 +958,7 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
         w.mis_pa = sc->mis_pa;
         w.mis_count = sc->mis_count;
         w.nodes = sc->nmh->nodes;
+        w.packet_span = sc->nmh->extent * (1.0f / 64.0f);
         w.num_lights = sc->num_lights;
         w.width = p.width;
         w.height = p.height;
@@ -943,6 +1014,7 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     const size_t o_fsh = take(16 * Q), o_emi = take(16 * Q), o_cj = take(16 * Q * M), o_vis = take(4 * Q);
     const size_t o_q0 = take(4 * Q), o_q1 = take(4 * Q), o_free = take(4 * Q);
     const size_t o_sho = take(16 * Q * M), o_shd = take(16 * Q * M), o_out = take(16 * out_items);
+    const size_t o_def = take(4 * ((Q + 31) / 32));
     const size_t o_stk = spec ? take(16 * 3 * (size_t)kWfStack * Q) : 0, o_sp = spec ? take(4 * Q) : 0;
     if (::aur::dev_malloc(&bt->mem, off) != cudaSuccess) {
         cudaGetLastError();
@@ -971,6 +1043,7 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     a.ext_q[0] = (uint32_t*)(base + o_q0); a.ext_q[1] = (uint32_t*)(base + o_q1);
     a.free_list = (uint32_t*)(base + o_free);
     a.sh_o = (float4*)(base + o_sho); a.sh_d = (float4*)(base + o_shd); a.out = (float4*)(base + o_out);
+    a.defer = (uint32_t*)(base + o_def);
     a.stk = spec ? (float4*)(base + o_stk) : nullptr;
     a.sp = spec ? (uint32_t*)(base + o_sp) : nullptr;
     cudaMemcpy(base + o_tab, table.data(), sizeof(WfScene) * num_scenes, cudaMemcpyHostToDevice);
@@ -985,9 +1058,9 @@ aur_status aur_batch_create(aur_ctx* ctx, const aur_scene* const* scenes, const 
     ctl.iter_limit = (uint32_t)std::min<uint64_t>(0x7FFFFFFFull, 4 * waves_of_pool * (p0.max_depth + 2) + 64);
     if (tn.max_iterations) ctl.iter_limit = tn.max_iterations;
     cudaMemcpy(a.ctl, &ctl, sizeof(ctl), cudaMemcpyHostToDevice);
-    cudaError_t e = cudaFuncSetAttribute(k_wf_extend, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_wf_shadow, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem);
+    cudaError_t e = cudaSuccess;
+    for (const void* k : {(const void*)k_wf_extend_packets, (const void*)k_wf_extend, (const void*)k_wf_shadow})
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bt->smem);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&bt->cap_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -1110,6 +1183,7 @@ aur_status aur_batch_profile(aur_ctx* ctx, aur_batch* bt, float* const* accum, f
             k_wf_generate<<<g, bs, 0, st>>>(a);
             k_wf_generate_commit<<<1, 1, 0, st>>>(a);
             cudaEventRecord(ev[1], st);
+            k_wf_extend_packets<<<g, bs, bt->smem, st>>>(a);
             k_wf_extend<<<g, bs, bt->smem, st>>>(a);
             cudaEventRecord(ev[2], st);
             launch_shade(a, g, bs, st);

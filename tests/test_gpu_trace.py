@@ -140,12 +140,14 @@ def test_trace_non_finite_rays(ctx):
     assert (hits["prim"][good] != T.NO_HIT).mean() > 0.05
 
 
-def _octant_rays(n, seed, octant_of_chunk):
-    """Random origins in the unit cube, random directions whose signs are
-    set per chunk of 32 rays by octant_of_chunk(chunk index) (bit a: dir[a] < 0)."""
+def _octant_rays(n, seed, octant_of_chunk, spread=1.0):
+    """Random directions whose signs are set per chunk of 32 rays by
+    octant_of_chunk(chunk index) (bit a: dir[a] < 0); origins at a random
+    point of the unit cube per chunk, plus U[0, spread)^3 per ray."""
     rng = np.random.default_rng(seed)
     rays = np.zeros(n, T.ray_dtype)
-    o = rng.random((n, 3)).astype(np.float32)
+    centre = np.repeat(rng.random(((n + 31) // 32, 3)), 32, axis=0)[:n]
+    o = (centre * (1.0 - spread) + rng.random((n, 3)) * spread).astype(np.float32)
     d = np.abs(rng.normal(size=(n, 3)))
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     oct_ = np.array([octant_of_chunk(i // 32) for i in range(n)])
@@ -167,15 +169,21 @@ def _check_against_oracle(ctx, nmh, perm, verts, rays):
 
 
 def test_packets_of_one_octant_match_oracle(ctx):
-    """Chunks of incoherent rays that share an octant (a different one per
-    chunk) all run as warp packets, where the lanes' node sets differ the
-    most; the last chunk is partial. Closest and any hit equal the oracle."""
+    """Chunks of rays from nearby origins with random directions of one
+    octant (a different one per chunk) run as warp packets whose lanes' node
+    sets differ widely; the last chunk is partial. The same directions from
+    origins spread over the soup go one ray per lane (the packet test also
+    asks for nearby origins). Closest and any hit equal the oracle."""
     V = scenes.random_soup(100000, seed=21)
     nmh, perm, verts = _setup(ctx, V)
-    rays = _octant_rays(32 * 700 + 13, 4, lambda c: c % 8)
+    n = 32 * 700 + 13
+    rays = _octant_rays(n, 4, lambda c: c % 8, spread=0.004)
     hits = _check_against_oracle(ctx, nmh, perm, verts, rays)
     assert api.trace_deferred(ctx) == 0
     assert (hits["prim"] != T.NO_HIT).mean() > 0.5
+    spread = _octant_rays(n, 4, lambda c: c % 8)
+    _check_against_oracle(ctx, nmh, perm, verts, spread)
+    assert api.trace_deferred(ctx) == (n + 31) // 32
 
 
 def test_packets_and_deferred_chunks_mixed(ctx):
@@ -186,7 +194,7 @@ def test_packets_and_deferred_chunks_mixed(ctx):
     V = scenes.random_soup(20000, seed=22)
     nmh, perm, verts = _setup(ctx, V)
     n = 32 * 64 + 20
-    rays = _octant_rays(n, 5, lambda c: (c * 5) % 8)
+    rays = _octant_rays(n, 5, lambda c: (c * 5) % 8, spread=0.004)
     rng = np.random.default_rng(6)
     mixed = sorted({c for c in range(65) if c % 3 == 1} | {64})
     for c in mixed:                                   # flip one lane's x sign
@@ -195,7 +203,7 @@ def test_packets_and_deferred_chunks_mixed(ctx):
     ax = np.arange(32 * 3, 32 * 4)                    # a uniform chunk of axis-parallel rays
     rays["dx"][ax], rays["dy"][ax] = np.where(np.arange(32) % 2, -0.0, 0.0), 0.0
     rays["dz"][ax] = 1.0
-    rays["ox"][ax], rays["oy"][ax] = rng.random(32), rng.random(32)
+    rays["ox"][ax], rays["oy"][ax] = 0.3 + 0.004 * rng.random(32), 0.6 + 0.004 * rng.random(32)
     rays["oz"][ax] = -1.0
     _check_against_oracle(ctx, nmh, perm, verts, rays)
     assert 3 not in mixed and 64 in mixed
