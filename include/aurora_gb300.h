@@ -333,9 +333,12 @@ aur_status aur_trace_closest(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* ra
  * Epsilon < t < tmax, or AUR_NO_HIT. rays, occluder: device. Chunks of
  * one octant go to warp packets as in aur_trace_closest. */
 aur_status aur_trace_any(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, uint32_t* occluder);
-/* Same as above with HOST buffers: rays go in chunks of 4M, traced on the
- * context's stream and one internal launch stream in turn, with two internal
- * copy streams overlapping the copies; returns when all hits are back. */
+/* Same as above with HOST buffers: rays go in chunks of up to 8M (a 2M
+ * chunk first and, where the count allows, last), traced on the context's
+ * stream and one internal launch stream in turn, with two internal copy
+ * streams overlapping the copies; returns when all hits are back. The
+ * context keeps two 8M-ray slots of device memory (384 MiB each) after the
+ * first call. */
 aur_status aur_trace_closest_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, aur_hit* hits);
 aur_status aur_trace_any_host(aur_ctx* ctx, const aur_nmh* nmh, const aur_ray* rays, uint32_t n, uint32_t* occluder);
 /* Counts the reference algorithm's traversal work for n device rays:

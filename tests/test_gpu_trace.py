@@ -91,7 +91,7 @@ def test_trace_tie_rule_on_duplicates(ctx):
 def test_trace_host_buffers_match_device(ctx):
     V = scenes.random_soup(50000, seed=9)
     nmh, perm, verts = _setup(ctx, V)
-    # three pipeline chunks of 4M rays: both launch streams, and slot 0 reused
+    # three pipeline chunks (2M, 4M + 12345, 2M): both launch streams, and slot 0 reused
     rays = scenes.microbench_rays((2 << 22) + 12345, seed=4)
     hits_d, occ_d = _gpu_trace(ctx, nmh, rays)
     hits_h = np.zeros(rays.shape[0], T.hit_dtype)
